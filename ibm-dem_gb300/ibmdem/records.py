@@ -1,0 +1,57 @@
+"""Record layouts of the C ABI (include/ibmdem.h) as numpy dtypes.
+
+`PARCEL` mirrors `type Parcel` (ZJS_VARS.F90:6-12) and `MULTISPHERE` mirrors
+`type MultiSphere` (ZJS_VARS.F90:97-102); `PARAMS` carries the constants the
+reference hard-codes in source.  Sizes are checked against the C structs when
+the library loads.
+"""
+import numpy as np
+
+PARCEL = np.dtype([
+    ("globalIdx", "<i4"), ("localIdx", "<i4"), ("cellIdx", "<i4"), ("pType", "<i4"),
+    ("MSIdx", "<i4"), ("pad_", "<i4"),
+    ("radeff", "<f8"), ("rad", "<f8"), ("rho", "<f8"), ("vol", "<f8"), ("m", "<f8"),
+    ("x", "<f8", 3), ("v", "<f8", 3), ("fcol", "<f8", 3), ("fdrag", "<f8", 3), ("vgap", "<f8", 3),
+    ("wdrag", "<f8"), ("wsum", "<f8"),
+])
+assert PARCEL.itemsize == 200
+
+MULTISPHERE = np.dtype([
+    ("globalIdx", "<i4"), ("cpuIdx", "<i4"),
+    ("rotMat", "<f8", 9), ("rotMatGlo", "<f8", 9), ("rotMatGloOld", "<f8", 9), ("InertiaTensor", "<f8", 9),
+    ("x", "<f8", 3), ("xold", "<f8", 3), ("v", "<f8", 3), ("vold", "<f8", 3), ("omega", "<f8", 3),
+    ("omegaold", "<f8", 3), ("fcol", "<f8", 3), ("fmom", "<f8", 3), ("fdrag", "<f8", 3),
+    ("AngMom", "<f8", 3), ("AngMomOld", "<f8", 3), ("fhydro", "<f8", 3), ("fmomHydro", "<f8", 3),
+    ("fmomCol", "<f8", 3),
+    ("I", "<f8"), ("rad", "<f8"), ("rho", "<f8"), ("vol", "<f8"), ("m", "<f8"),
+])
+assert MULTISPHERE.itemsize == 672
+
+PARAMS = np.dtype([
+    ("nx", "<i4"), ("ny", "<i4"), ("nz", "<i4"), ("coupleInterval", "<i4"), ("Ns", "<i4"),
+    ("bType", "<i4", 6), ("pad_", "<i4"),
+    ("dx", "<f8"), ("dy", "<f8"), ("dz", "<f8"), ("dt", "<f8"), ("rhof", "<f8"),
+    ("knCoeff", "<f8"), ("ResistCoeff", "<f8"), ("collisionDist", "<f8"), ("collisionBuffer", "<f8"),
+    ("gravity", "<f8", 3),
+])
+assert PARAMS.itemsize == 144
+
+
+def make_params(nx, ny, nz, h=1.0, dt=1e-3, coupleInterval=1, Ns=5, rhof=1e3, knCoeff=1e4,
+                ResistCoeff=0.9, collisionBuffer=0.1, gravity=(0.0, 0.0, -9.81), collisionDist=None):
+    """Case parameters; collisionDist defaults to dx*0.75*2 (ZJS_INIT_DEM.F90:413)."""
+    p = np.zeros((), PARAMS)
+    p["nx"], p["ny"], p["nz"] = nx, ny, nz
+    p["coupleInterval"], p["Ns"] = coupleInterval, Ns
+    p["bType"] = 0
+    p["dx"] = p["dy"] = p["dz"] = h
+    p["dt"], p["rhof"], p["knCoeff"], p["ResistCoeff"] = dt, rhof, knCoeff, ResistCoeff
+    p["collisionDist"] = h * 0.75 * 2 if collisionDist is None else collisionDist
+    p["collisionBuffer"] = collisionBuffer
+    p["gravity"] = gravity
+    return p
+
+
+def field_shape(p):
+    """(nk, nj, ni) C-order view of a Fortran (lg1:ug1, lg2:ug2, lg3:ug3) array."""
+    return (int(p["nz"]) + 4, int(p["ny"]) + 4, int(p["nx"]) + 4)

@@ -1,0 +1,181 @@
+"""Seeded synthetic cases for the resolved IBM-DEM path.
+
+The reference builds its cases from marker template files (ZJS_INIT_DEM.F90:
+350-494 for cylinders; :233-348 for spheres, whose template file is not in the
+repository).  These generators produce the same records from formulas:
+
+* spheres: a Fibonacci lattice of n = round(pi d^2) markers per sphere at radius
+  radSphere = R - 0.3 dx, with the marker volume, mass and effective radius of
+  the sphere initialiser (ZJS_INIT_DEM.F90:250, 311-314) and the body mass and
+  moment of inertia of ZJS_INIT_DEM.F90:327-331;
+* centres by random sequential addition (minimum-image distance > d);
+* a periodic fluid field made of random Fourier modes with amplitude vectors
+  perpendicular to their wave vectors, sampled on the MAC faces that the
+  interpolation addresses (u at x=(i-1)h, y=(j-1/2)h, z=(k-1/2)h and the
+  analogous v, w faces) with a periodic 2-cell halo.
+
+Two choices differ from the reference initialiser because the reference only
+starts bodies at rest and in one sub-domain: markers of a body that crosses a
+periodic face are stored at their periodic image (x -/+ L), and bodies start
+with vold = v and markers with v = V so that the first step sees no spurious
+acceleration.  The sphere initialiser never fills InertiaTensor; the generator
+sets it to diag(I, I, I), which EvolutionMS needs.
+"""
+import math
+
+import numpy as np
+
+from .records import MULTISPHERE, PARCEL, field_shape, make_params
+
+PI32 = float(np.float32(3.1415926536))  # default-real literal of ZJS_INIT_DEM.F90:312
+
+
+def fibonacci_sphere(n):
+    i = np.arange(n, dtype=np.float64) + 0.5
+    z = 1.0 - 2.0 * i / n
+    r = np.sqrt(np.maximum(0.0, 1.0 - z * z))
+    phi = i * (math.pi * (3.0 - math.sqrt(5.0)))
+    return np.stack([r * np.cos(phi), r * np.sin(phi), z], axis=1)
+
+
+def rsa_centres(L, nb, d, rng, max_tries=2_000_000):
+    """Random sequential addition with minimum-image centre distance > d."""
+    L = np.asarray(L, dtype=np.float64)
+    out = np.empty((0, 3))
+    tries = 0
+    batch = 256
+    while out.shape[0] < nb:
+        cand = rng.random((batch, 3)) * L
+        for c in cand:
+            tries += 1
+            if tries > max_tries:
+                raise RuntimeError(f"RSA could not place {nb} spheres of diameter {d}")
+            if out.shape[0]:
+                dv = out - c
+                dv -= L * np.round(dv / L)
+                if np.min(np.einsum("ij,ij->i", dv, dv)) <= d * d:
+                    continue
+            out = np.vstack([out, c])
+            if out.shape[0] == nb:
+                break
+    return out
+
+
+def wrap_coord(x, L):
+    """Periodic image of a coordinate as the reference forms it: one add of +/-L."""
+    x = np.array(x, dtype=np.float64)
+    for d in range(3):
+        lo = x[..., d] < 0.0
+        hi = x[..., d] >= L[d]
+        x[..., d] = np.where(lo, x[..., d] + L[d], np.where(hi, x[..., d] + (-L[d]), x[..., d]))
+    return x
+
+
+def sphere_bodies(centres, d, h, rho_p, vel, n_markers=None):
+    """Parcels and bodies for spheres of diameter d (in length units)."""
+    nb = centres.shape[0]
+    R = 0.5 * d
+    rad_sphere = R - 0.3 * h
+    n = int(round(math.pi * (d / h) ** 2)) if n_markers is None else int(n_markers)
+    tpl = fibonacci_sphere(n)
+    parts = np.zeros(nb * n, PARCEL)
+    bodies = np.zeros(nb, MULTISPHERE)
+    vol_p = PI32 * h / 3 / n * (12 * rad_sphere * rad_sphere + h * h)
+    eye = np.eye(3).reshape(9)
+    for b in range(nb):
+        sl = slice(b * n, (b + 1) * n)
+        parts["x"][sl] = rad_sphere * tpl + centres[b]
+        parts["v"][sl] = vel[b]
+        parts["MSIdx"][sl] = b + 1
+        parts["globalIdx"][sl] = np.arange(1, n + 1)
+    parts["radeff"] = h * 0.75
+    parts["rad"] = 0.0
+    parts["rho"] = rho_p
+    parts["vol"] = vol_p
+    parts["m"] = rho_p * vol_p
+    parts["pType"] = -1
+    rad = rad_sphere + 0.3 * h
+    vol = 4.0 / 3 * math.pi * (rad * rad * rad)
+    m = vol * rho_p
+    inertia = 0.4 * m * (rad * rad)
+    bodies["globalIdx"] = np.arange(1, nb + 1)
+    bodies["x"] = centres
+    bodies["v"] = vel
+    bodies["vold"] = vel
+    bodies["rad"] = rad
+    bodies["rho"] = rho_p
+    bodies["vol"] = vol
+    bodies["m"] = m
+    bodies["I"] = inertia
+    bodies["InertiaTensor"] = np.diag([inertia] * 3).reshape(9)
+    bodies["rotMat"] = eye
+    bodies["rotMatGlo"] = eye
+    bodies["rotMatGloOld"] = eye
+    return parts, bodies
+
+
+def fourier_field(p, n_modes, amp, seed, kmax=4, device="cpu"):
+    """u, v, w on the MAC faces (Fortran layout incl. halo) as float64 numpy arrays."""
+    import torch
+
+    rng = np.random.default_rng(seed + 7919)
+    nx, ny, nz = int(p["nx"]), int(p["ny"]), int(p["nz"])
+    h = float(p["dx"])
+    L = np.array([nx * h, ny * h, nz * h])
+    ks, amps, phases = [], [], []
+    while len(ks) < n_modes:
+        kv = rng.integers(-kmax, kmax + 1, size=3)
+        if not kv.any() or np.linalg.norm(kv) > kmax:
+            continue
+        k = 2 * math.pi * kv / L
+        a = rng.standard_normal(3)
+        a -= k * (a @ k) / (k @ k)
+        a /= np.linalg.norm(a)
+        ks.append(k)
+        amps.append(a)
+        phases.append(rng.random() * 2 * math.pi)
+    w = rng.random(n_modes) + 0.5
+    w *= amp / w.sum()
+    shape = field_shape(p)
+    out = []
+    dev = torch.device(device)
+    # face positions: component c is staggered by -h/2 along axis c
+    for comp in range(3):
+        coords = []
+        for ax, n in enumerate((nx, ny, nz)):
+            idx = torch.arange(1, n + 1, dtype=torch.float64, device=dev)
+            coords.append((idx - 1.0) * h if ax == comp else (idx - 0.5) * h)
+        acc = torch.zeros((nz, ny, nx), dtype=torch.float64, device=dev)
+        for m in range(n_modes):
+            k = ks[m]
+            ex = torch.exp(1j * (k[0] * coords[0]))
+            ey = torch.exp(1j * (k[1] * coords[1]))
+            ez = torch.exp(1j * (k[2] * coords[2]) + 1j * phases[m])
+            plane = (ez[:, None] * ey[None, :])  # (nz, ny)
+            acc += (w[m] * amps[m][comp]) * (plane[:, :, None] * ex[None, None, :]).real
+        full = torch.zeros(shape, dtype=torch.float64, device=dev)
+        full[2:-2, 2:-2, 2:-2] = acc
+        # periodic halo, as FillGhostRegionForFluid leaves it
+        iz = (torch.arange(shape[0], device=dev) - 2) % nz + 2
+        iy = (torch.arange(shape[1], device=dev) - 2) % ny + 2
+        ix = (torch.arange(shape[2], device=dev) - 2) % nx + 2
+        full = full[iz][:, iy][:, :, ix]
+        out.append(np.ascontiguousarray(full.cpu().numpy()))
+    return out
+
+
+def resolved_case(nx, ny, nz, nbodies, d, seed=0, h=1.0, vel_std=0.01, n_modes=32, amp=0.05,
+                  rho_p=1.14e3, field_device="cpu", n_markers=None, **param_kw):
+    """A triply periodic case of monodisperse spheres in a frozen Fourier field.
+
+    Returns (params, parcels, bodies, (u, v, w))."""
+    p = make_params(nx, ny, nz, h=h, **param_kw)
+    rng = np.random.default_rng(seed)
+    L = np.array([nx * h, ny * h, nz * h])
+    centres = rsa_centres(L, nbodies, d * h, rng)
+    vel = rng.standard_normal((nbodies, 3)) * vel_std
+    parts, bodies = sphere_bodies(centres, d * h, h, rho_p, vel, n_markers=n_markers)
+    parts["x"] = wrap_coord(parts["x"], L)
+    field = fourier_field(p, n_modes, amp, seed, device=field_device) if n_modes > 0 else \
+        [np.zeros(field_shape(p)) for _ in range(3)]
+    return p, parts, bodies, field

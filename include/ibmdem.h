@@ -1,0 +1,181 @@
+/*
+ * ibmdem.h — C ABI of the GB300 particle-side hot path of IBM-DEM.
+ *
+ * The reference (zengjs1993/IBM-DEM, Fortran 90 + MPI) exposes this path as
+ * argument-less subroutines that act on the module globals `vars` and `ZjsVar`.
+ * This header replaces them one-for-one: every reference subroutine on the path
+ * has an `ibmdem_<SubroutineName>` entry point acting on a context that owns the
+ * device-resident state.  A Fortran caller binds these with ISO_C_BINDING (the
+ * record types below are `bind(C)`-compatible mirrors of the reference's derived
+ * types); a Python or C caller uses them directly.
+ *
+ * Conventions
+ *   - Every function returns an int status: IBMDEM_OK (0) or a negative error
+ *     code; ibmdem_last_error() gives a one-line message for the last failure.
+ *   - Host pointers are borrowed for the duration of the call only.
+ *   - Work is issued on the context's CUDA stream and is stream-ordered; getters
+ *     synchronise that stream before returning.
+ *   - One context per host thread; there is no global mutable state.
+ *   - Indices in records are 1-based where the reference's are (MSIdx,
+ *     globalIdx, localIdx); cell ids are map3Dto1D ids (1-based, Fortran order
+ *     over the grid including its 2-cell halo).
+ */
+#ifndef IBMDEM_H
+#define IBMDEM_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define IBMDEM_ABI_VERSION 1
+
+/* status codes */
+#define IBMDEM_OK 0
+#define IBMDEM_EINVAL (-1)     /* bad argument, size or handle            */
+#define IBMDEM_ECUDA (-2)      /* a CUDA runtime call failed              */
+#define IBMDEM_ENOMEM (-3)     /* device allocation failed / over budget  */
+#define IBMDEM_ERANGE (-4)     /* a parcel left the grid+halo region      */
+#define IBMDEM_ECAPACITY (-5)  /* a fixed capacity was exceeded           */
+#define IBMDEM_EUNSUPPORTED (-6) /* configuration not supported            */
+#define IBMDEM_ESTATE (-7)     /* call out of order (e.g. no lists yet)   */
+
+/* Marker record: mirrors `type Parcel` (ZJS_VARS.F90:6-12) with a fixed
+ * C layout (a Fortran shim declares the same fields with bind(C)). 200 bytes. */
+typedef struct ibmdem_parcel {
+  int32_t globalIdx, localIdx, cellIdx, pType, MSIdx;
+  int32_t pad_;
+  double radeff, rad, rho, vol, m;
+  double x[3], v[3], fcol[3], fdrag[3], vgap[3];
+  double wdrag, wsum;
+} ibmdem_parcel;
+
+/* Rigid-body record: mirrors `type MultiSphere` (ZJS_VARS.F90:97-102). */
+typedef struct ibmdem_multisphere {
+  int32_t globalIdx, cpuIdx;
+  double rotMat[9], rotMatGlo[9], rotMatGloOld[9], InertiaTensor[9];
+  double x[3], xold[3], v[3], vold[3], omega[3], omegaold[3];
+  double fcol[3], fmom[3], fdrag[3], AngMom[3], AngMomOld[3];
+  double fhydro[3], fmomHydro[3], fmomCol[3];
+  double I, rad, rho, vol, m;
+} ibmdem_multisphere;
+
+/* Case parameters: the reference hard-codes these in source
+ * (vars.F90, ZJS_VARS.F90:48-50, ZJS_INIT_DEM.F90:187-194,
+ *  initialization.F90:251-259, fluid.F90:257, couplesolverCylinder.F90:12-13). */
+typedef struct ibmdem_params {
+  int32_t nx, ny, nz;        /* interior cells of the (single-rank) domain   */
+  int32_t coupleInterval;    /* DEM sub-steps per fluid step                 */
+  int32_t Ns;                /* multi-direct-forcing iterations (ref: 5)     */
+  int32_t bType[6];          /* face types -x,+x,-y,+y,-z,+z: 0 = periodic   */
+  int32_t pad_;
+  double dx, dy, dz;         /* cell sizes                                   */
+  double dt;                 /* fluid time step                              */
+  double rhof;               /* fluid density                                */
+  double knCoeff;            /* spring coefficient                           */
+  double ResistCoeff;        /* restitution coefficient e                    */
+  double collisionDist;      /* contact distance (ref: 1.5 dx)               */
+  double collisionBuffer;    /* list buffer fraction (ref: 0.1)              */
+  double gravity[3];         /* (0,0,-9.81) in the reference                 */
+} ibmdem_params;
+
+typedef struct ibmdem_ctx ibmdem_ctx;
+
+/* ---- lifetime --------------------------------------------------------- */
+/* New context on CUDA device `device`; replaces InitParameters /
+ * CopyGridInformationDEM / AllocateDEM / SetCellIndexMapDEM /
+ * SetNeighCellIndexForCellsDEM / SetMirrorAndShiftCoords
+ * (ZJS_INIT_DEM.F90:67-214) — the tables they build are implicit here. */
+int ibmdem_create(const ibmdem_params* p, int32_t device, ibmdem_ctx** out);
+int ibmdem_destroy(ibmdem_ctx* ctx);
+const char* ibmdem_last_error(const ibmdem_ctx* ctx);
+int ibmdem_abi_version(void);
+/* Issue work on this CUDA stream (a cudaStream_t passed as void*). */
+int ibmdem_set_stream(ibmdem_ctx* ctx, void* stream);
+int ibmdem_synchronize(ibmdem_ctx* ctx);
+
+/* ---- state in / out --------------------------------------------------- */
+/* Fluid velocity u,v,w in the reference layout: Fortran order
+ * (lg1:ug1, lg2:ug2, lg3:ug3), i fastest, 2-cell halo (vars.F90:44,
+ * allocate.F90:16-18): (nx+4)*(ny+4)*(nz+4) doubles each.  Also stored as the
+ * frozen field that ibmdem_step() restores at the start of every step. */
+int ibmdem_set_fluid(ibmdem_ctx* ctx, const double* u, const double* v, const double* w);
+/* Copy out u,v,w and the momentum source fx,fy,fz (vars.F90:63), same layout.
+ * Any pointer may be NULL. */
+int ibmdem_get_fluid(ibmdem_ctx* ctx, double* u, double* v, double* w,
+                     double* fx, double* fy, double* fz);
+/* Local parcels part(1:npLocal) (ZJS_VARS.F90:20); pType is set to -1. */
+int ibmdem_set_parcels(ibmdem_ctx* ctx, int32_t np, const ibmdem_parcel* parts);
+/* Copy out part(1:np): locals first, then periodic images (np_out gets np,
+ * nlocal_out gets npLocal).  cap = capacity of `parts` in records. */
+int ibmdem_get_parcels(ibmdem_ctx* ctx, ibmdem_parcel* parts, int32_t cap,
+                       int32_t* np_out, int32_t* nlocal_out);
+/* Bodies MS(1:nMS) == MSGlo on one rank (ZJS_VARS.F90:106). */
+int ibmdem_set_bodies(ibmdem_ctx* ctx, int32_t nMS, const ibmdem_multisphere* ms);
+int ibmdem_get_bodies(ibmdem_ctx* ctx, ibmdem_multisphere* ms, int32_t cap, int32_t* nMS_out);
+
+/* ---- list inspection (parity) ----------------------------------------- */
+/* Cell lists npPartInCell / partIdxInCell (ZJS_VARS.F90:38-39) as CSR over all
+ * ni*nj*nk cells: cell_start[ncell+1] (0-based offsets), items = 1-based part
+ * indices.  Pass NULL to query sizes into *ncell_out / *nitems_out. */
+int ibmdem_get_cell_lists(ibmdem_ctx* ctx, int32_t* cell_start, int32_t* items,
+                          int64_t* ncell_out, int32_t* nitems_out);
+/* Contact lists neighPartNo / neighPartIdx (ZJS_VARS.F90:30-31) as CSR over
+ * local parcels: start[npLocal+1], idx = 1-based part indices. */
+int ibmdem_get_collision_lists(ibmdem_ctx* ctx, int32_t* start, int32_t* idx,
+                               int32_t* nlocal_out, int32_t* npairs_out);
+
+/* ---- the hot path: one entry per reference subroutine ----------------- */
+/* RebuildParcelInCellListDEM + RebuildParcelCollisionListDEM +
+ * RebuildNeighborCellListForParcelsDEM (ZJS_EVOLUTION_DEM.F90:34-41). */
+int ibmdem_RebuildAllListOrNot(ibmdem_ctx* ctx);
+/* ZJS_UPDATE_LIST_DEM.F90:323-370: delta weights of local parcels. */
+int ibmdem_UpdateLocalCellWeightListDEM(ibmdem_ctx* ctx);
+/* ZJS_UPDATE_LIST_DEM.F90:372-416: delta weights of periodic images. */
+int ibmdem_UpdateGhostCellWeightListDEM(ibmdem_ctx* ctx);
+/* ZJS_UPDATE_LIST_DEM.F90:179-246: refresh image copies (x + shift, v, fdrag). */
+int ibmdem_UpdateParcelInfoInGhostRegion(ibmdem_ctx* ctx);
+/* ZJS_COLLISION_DEM.F90:21-74: spring-dashpot contact force fcol. */
+int ibmdem_CalculateCollisionForce(ibmdem_ctx* ctx);
+/* ZJS_VOLUMEFRACTION_DEM.F90:2-36: interpolation and direct forcing. */
+int ibmdem_UpdateFluidVelocityOnLagrangianPoints(ibmdem_ctx* ctx);
+/* ZJS_VOLUMEFRACTION_DEM.F90:38-67: deterministic spreading into fx,fy,fz. */
+int ibmdem_UpdateMomentumSourceTerm(ibmdem_ctx* ctx);
+/* fluid.F90:135-153 + the periodic halo refill of u,v,w (boundary.F90:122-147). */
+int ibmdem_VelocityPostGuess(ibmdem_ctx* ctx);
+/* ZJS_MS_DEM.F90:494-519 (== AssembleForceMS on one rank, :385-432). */
+int ibmdem_AssembleLocalForceMS(ibmdem_ctx* ctx);
+/* couplesolverCylinder.F90:2-42 (rigid-body update with Rodrigues rotation). */
+int ibmdem_EvolutionMS(ibmdem_ctx* ctx);
+/* couplesolverCylinder.F90:44-60 (marker translation, rotation, velocity). */
+int ibmdem_ResetVelocityAndPositionLagrangianPoints(ibmdem_ctx* ctx);
+/* ZJS_EVOLUTION_DEM.F90:121-150. */
+int ibmdem_AdjustParcelPosition(ibmdem_ctx* ctx);
+
+/* ---- fused drivers ---------------------------------------------------- */
+/* The list-building tail of InitializationDEM (ZJS_INIT_DEM.F90:24-35). */
+int ibmdem_InitializationDEM(ibmdem_ctx* ctx);
+/* Particle side of FirstOrderForwardEuler (fluid.F90:252-285): fdrag=0,
+ * fx=fy=fz=0, then Ns x {interpolate, image update, spread, post-guess}. */
+int ibmdem_MultiDirectForcing(ibmdem_ctx* ctx);
+/* couplesolverCylinder.F90:99-187. */
+int ibmdem_CloudEvolutionStepMS(ibmdem_ctx* ctx);
+/* couplesolverCylinder.F90:189-217. */
+int ibmdem_CloudEvolutionMS(ibmdem_ctx* ctx);
+/* `nsteps` frozen-fluid steps: restore the fluid set by ibmdem_set_fluid,
+ * then ibmdem_MultiDirectForcing + ibmdem_CloudEvolutionMS. */
+int ibmdem_step(ibmdem_ctx* ctx, int32_t nsteps);
+
+/* ---- instrumentation -------------------------------------------------- */
+/* Number of kernel launches this context has issued so far. */
+int64_t ibmdem_launch_count(const ibmdem_ctx* ctx);
+/* Counters of the current lists: [0]=npLocal [1]=np [2]=pairs
+ * [3]=touched u nodes [4]=touched v nodes [5]=touched w nodes
+ * [6]=spread contributions. */
+int ibmdem_get_counters(ibmdem_ctx* ctx, int64_t* out, int32_t n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* IBMDEM_H */

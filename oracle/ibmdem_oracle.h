@@ -1,0 +1,75 @@
+/*
+ * ibmdem_oracle.h — CPU restatement of the IBM-DEM particle-side hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the parity checker for the GPU
+ * library (libibmdem) and the timed CPU baseline; nothing in the product links
+ * or calls it.  Only tests/, __graft_entry__.smoke() and bench.py's CPU legs
+ * load it.
+ *
+ * PARITY UNPINNED: the reference (Fortran 90 + MPI + PETSc) cannot be compiled
+ * or run here (no Fortran compiler, no MPI) and ships no tests, golden vectors
+ * or known-answer fixtures for this path.  The restatement follows the
+ * reference source line by line (file:line cited at each function) and is
+ * pinned only by analytic and self-consistency checks (tests/test_oracle_*.py).
+ *
+ * The entry points mirror the reference subroutines one-for-one and operate on
+ * one single-rank, triply periodic case.  Record layouts are the C-ABI ones
+ * from include/ibmdem.h.
+ */
+#ifndef IBMDEM_ORACLE_H
+#define IBMDEM_ORACLE_H
+#include "../include/ibmdem.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct orc_case orc_case;
+
+orc_case* orc_create(const ibmdem_params* p);
+void orc_destroy(orc_case* c);
+const char* orc_last_error(const orc_case* c);
+void orc_set_threads(int n);
+int orc_get_threads(void);
+
+int orc_set_fluid(orc_case* c, const double* u, const double* v, const double* w);
+int orc_get_fluid(orc_case* c, double* u, double* v, double* w, double* fx, double* fy, double* fz);
+int orc_set_parcels(orc_case* c, int32_t np, const ibmdem_parcel* parts);
+int orc_get_parcels(orc_case* c, ibmdem_parcel* parts, int32_t cap, int32_t* np_out, int32_t* nlocal_out);
+int orc_set_bodies(orc_case* c, int32_t n, const ibmdem_multisphere* ms);
+int orc_get_bodies(orc_case* c, ibmdem_multisphere* ms, int32_t cap, int32_t* n_out);
+int orc_get_cell_lists(orc_case* c, int32_t* cell_start, int32_t* items, int64_t* ncell_out, int32_t* nitems_out);
+int orc_get_collision_lists(orc_case* c, int32_t* start, int32_t* idx, int32_t* nlocal_out, int32_t* npairs_out);
+/* Per-marker delta weights of the 125 stencil cells (3 components), for the
+ * first `n` parcels: w[(p*125 + j)*3 + comp]; cells[p*125 + j] (0 = absent). */
+int orc_get_weights(orc_case* c, int32_t n, double* w, int32_t* cells);
+
+int orc_RebuildAllListOrNot(orc_case* c);
+int orc_UpdateLocalCellWeightListDEM(orc_case* c);
+int orc_UpdateGhostCellWeightListDEM(orc_case* c);
+int orc_UpdateParcelInfoInGhostRegion(orc_case* c);
+int orc_CalculateCollisionForce(orc_case* c);
+int orc_UpdateFluidVelocityOnLagrangianPoints(orc_case* c);
+int orc_UpdateMomentumSourceTerm(orc_case* c);
+int orc_VelocityPostGuess(orc_case* c);
+int orc_AssembleLocalForceMS(orc_case* c);
+int orc_EvolutionMS(orc_case* c);
+int orc_ResetVelocityAndPositionLagrangianPoints(orc_case* c);
+int orc_AdjustParcelPosition(orc_case* c);
+
+int orc_InitializationDEM(orc_case* c);
+int orc_MultiDirectForcing(orc_case* c);
+int orc_CloudEvolutionStepMS(orc_case* c);
+int orc_CloudEvolutionMS(orc_case* c);
+int orc_step(orc_case* c, int32_t nsteps);
+
+/* Drag coefficient of ZJS_DRAGFORCE_DEM.F90:2-35 for one parcel. */
+void orc_CalculateDragForce(double rho_p, double rad_p, const double* v_p, double denf,
+                            double alphaf_local, const double* velf, double* beta);
+/* eta of ZJS_COLLISION_DEM.F90:30 (single-precision pi literal reproduced). */
+double orc_eta(double ResistCoeff);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
