@@ -1,0 +1,696 @@
+// api.cu — the C ABI of include/ibmdem.h: context lifetime, device allocation,
+// record conversion, and the reference-named entry points and drivers.
+//
+// Work is stream-ordered and issued without host round trips; errors raised
+// on the device (capacity, range) are latched in a device word and reported by
+// the next call that synchronises (getters, ibmdem_synchronize).
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "common.cuh"
+#include "kernels.cuh"
+#include "prims.cuh"
+
+using namespace ibmdem;
+
+struct ibmdem_ctx {
+  Ctx c;
+};
+
+namespace {
+
+int set_error(ibmdem_ctx* h, int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  if (h) h->c.err = buf;
+  return code;
+}
+
+#define CU(call)                                                                                \
+  do {                                                                                          \
+    cudaError_t e_ = (call);                                                                    \
+    if (e_ != cudaSuccess)                                                                      \
+      return set_error(h, IBMDEM_ECUDA, "%s failed: %s", #call, cudaGetErrorString(e_));       \
+  } while (0)
+
+template <typename T>
+cudaError_t dalloc(T*& p, size_t n) {
+  p = nullptr;
+  return cudaMalloc(reinterpret_cast<void**>(&p), std::max<size_t>(n, 1) * sizeof(T));
+}
+
+void dfree(void* p) {
+  if (p) cudaFree(p);
+}
+
+double eta_of(double e) {
+  // ZJS_COLLISION_DEM.F90:30: 3.1415926536 is a single-precision literal
+  float pi32 = 3.1415926536f;
+  float pi2 = pi32 * pi32;
+  return -2 * std::log(e) / std::sqrt((double)pi2 + std::log(e));
+}
+
+void free_parcel_buffers(Ctx& c) {
+  void* ps[] = {c.recD[0], c.recD[1], c.recI[0], c.recI[1], c.imgSrc, c.imgShift, c.cellItems, c.bodyItems,
+                c.iTmpA, c.iTmpB, c.scanScratch, c.sortHist, c.kA, c.vA, c.kB, c.vB, c.activeList, c.pairCnt,
+                c.pairStart, c.pairIdx, c.W, c.win, c.cntInt, c.fv, c.runStart, c.runKey, c.fCur, c.fPrev,
+                c.lastNodes};
+  for (void* p : ps) dfree(p);
+  c.recD[0] = c.recD[1] = nullptr;
+  c.recI[0] = c.recI[1] = nullptr;
+  c.imgSrc = c.imgShift = c.cellItems = c.bodyItems = c.iTmpA = c.iTmpB = c.scanScratch = c.sortHist = nullptr;
+  c.kA = c.vA = c.kB = c.vB = nullptr;
+  c.activeList = c.pairCnt = c.pairStart = c.pairIdx = nullptr;
+  c.W = nullptr;
+  c.win = nullptr;
+  c.cntInt = nullptr;
+  c.fv = nullptr;
+  c.runStart = nullptr;
+  c.runKey = nullptr;
+  c.fCur = c.fPrev = nullptr;
+  c.lastNodes = nullptr;
+  c.cap = c.capLocal = c.capImg = 0;
+}
+
+// images the configuration needs right now (host estimate for the capacity)
+long long count_images(const Geom& g, int np, const ibmdem_parcel* parts) {
+  long long n = 0;
+  for (int i = 0; i < np; ++i) {
+    long long f = 1;
+    for (int d = 0; d < 3; ++d) {
+      int a = (int)std::floor((parts[i].x[d] - g.start[d]) / g.h[d]) + 1;
+      int opts = 1 + ((a >= 1 && a <= kHalo) ? 1 : 0) + ((a >= g.n[d] - kHalo + 1 && a <= g.n[d]) ? 1 : 0);
+      f *= opts;
+    }
+    n += f - 1;
+  }
+  return n;
+}
+
+int alloc_parcels(ibmdem_ctx* h, int np, long long nimg_est) {
+  Ctx& c = h->c;
+  free_parcel_buffers(c);
+  c.capLocal = std::max(np, 1);
+  long long ci = nimg_est + nimg_est / 2 + 4096;
+  c.capImg = (int)std::min<long long>(ci, 7ll * c.capLocal + 64);
+  c.cap = c.capLocal + c.capImg;
+  c.capPairs = 4ll * c.capLocal + 65536;
+  c.capContrib = (long long)kSlots * c.cap;
+  c.capRuns = c.capContrib;
+  long long tmpInts = std::max<long long>(c.cap + 1, 26ll * nblocks(c.capLocal) + 1);
+  long long scanInts = std::max({scan_scratch_ints(c.capContrib), scan_scratch_ints(sort_hist_ints(c.capContrib)),
+                                 scan_scratch_ints(c.g.ncell + 1), scan_scratch_ints(26ll * nblocks(c.capLocal))});
+  CU(dalloc(c.recD[0], (size_t)ND * c.cap));
+  CU(dalloc(c.recD[1], (size_t)ND * c.cap));
+  CU(dalloc(c.recI[0], (size_t)NI * c.cap));
+  CU(dalloc(c.recI[1], (size_t)NI * c.cap));
+  CU(dalloc(c.imgSrc, c.capImg));
+  CU(dalloc(c.imgShift, c.capImg));
+  CU(dalloc(c.cellItems, c.cap));
+  CU(dalloc(c.bodyItems, c.capLocal));
+  CU(dalloc(c.iTmpA, tmpInts));
+  CU(dalloc(c.iTmpB, tmpInts));
+  CU(dalloc(c.scanScratch, scanInts));
+  CU(dalloc(c.sortHist, sort_hist_ints(c.capContrib)));
+  CU(dalloc(c.kA, c.capContrib));
+  CU(dalloc(c.vA, c.capContrib));
+  CU(dalloc(c.kB, c.capContrib));
+  CU(dalloc(c.vB, c.capContrib));
+  CU(dalloc(c.activeList, c.capLocal));
+  CU(dalloc(c.pairCnt, c.capLocal + 1));
+  CU(dalloc(c.pairStart, c.capLocal + 1));
+  CU(dalloc(c.pairIdx, c.capPairs));
+  CU(dalloc(c.W, (size_t)kSlots * c.cap));
+  CU(dalloc(c.win, c.cap));
+  CU(dalloc(c.cntInt, c.cap));
+  CU(dalloc(c.fv, 3 * (size_t)c.cap));
+  CU(dalloc(c.runStart, c.capRuns + 1));
+  CU(dalloc(c.runKey, c.capRuns));
+  CU(dalloc(c.fCur, c.capRuns));
+  CU(dalloc(c.fPrev, c.capRuns));
+  CU(dalloc(c.lastNodes, c.capRuns));
+  CU(cudaMemsetAsync(c.cntInt, 0, sizeof(int) * c.cap, c.stream));
+  CU(cudaMemsetAsync(c.pairStart, 0, sizeof(int) * (c.capLocal + 1), c.stream));
+  CU(cudaMemsetAsync(c.recD[0], 0, sizeof(double) * ND * (size_t)c.cap, c.stream));
+  CU(cudaMemsetAsync(c.recI[0], 0, sizeof(int) * NI * (size_t)c.cap, c.stream));
+  return IBMDEM_OK;
+}
+
+// latch device errors into a status (after a stream synchronise)
+int check_device(ibmdem_ctx* h) {
+  Ctx& c = h->c;
+  CU(cudaMemcpyAsync(c.hCnt, c.dCnt, sizeof(Counters), cudaMemcpyDeviceToHost, c.stream));
+  CU(cudaStreamSynchronize(c.stream));
+  int e = c.hCnt->err;
+  if (!e) return IBMDEM_OK;
+  int info = c.hCnt->errInfo;
+  // clear so that the context stays usable after the report
+  CU(cudaMemsetAsync(&c.dCnt->err, 0, sizeof(int), c.stream));
+  if (e & E_RANGE) return set_error(h, IBMDEM_ERANGE, "parcel %d left the grid and its halo", info);
+  if (e & E_IMGCAP) return set_error(h, IBMDEM_ECAPACITY, "periodic images exceed capacity %d (%d)", c.capImg, info);
+  if (e & E_PAIRCAP)
+    return set_error(h, IBMDEM_ECAPACITY, "contact pairs exceed capacity %lld (%d)", c.capPairs, info);
+  if (e & E_PARTNER) return set_error(h, IBMDEM_ECAPACITY, "body %d has more than %d near bodies", info, c.maxPartners);
+  if (e & E_WINDOW) return set_error(h, IBMDEM_EUNSUPPORTED, "parcel %d needs a 4-node delta window", info);
+  if (e & E_MSIDX) return set_error(h, IBMDEM_EINVAL, "parcel %d has a body index outside 1..nMS", info);
+  return set_error(h, IBMDEM_ECUDA, "device error bits 0x%x", e);
+}
+
+int launch_status(ibmdem_ctx* h) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return set_error(h, IBMDEM_ECUDA, "kernel launch failed: %s", cudaGetErrorString(e));
+  return IBMDEM_OK;
+}
+
+#define CHECK_CTX()                              \
+  do {                                           \
+    if (!h) return IBMDEM_EINVAL;                \
+    cudaError_t se_ = cudaSetDevice(h->c.device);\
+    if (se_ != cudaSuccess)                      \
+      return set_error(h, IBMDEM_ECUDA, "cudaSetDevice: %s", cudaGetErrorString(se_)); \
+  } while (0)
+
+#define REQUIRE(cond, msg)                                  \
+  do {                                                      \
+    if (!(cond)) return set_error(h, IBMDEM_ESTATE, msg);   \
+  } while (0)
+
+}  // namespace
+
+extern "C" {
+
+int ibmdem_abi_version(void) { return IBMDEM_ABI_VERSION; }
+
+const char* ibmdem_last_error(const ibmdem_ctx* h) { return h ? h->c.err.c_str() : "null context"; }
+
+int64_t ibmdem_launch_count(const ibmdem_ctx* h) { return h ? h->c.launches : 0; }
+
+int ibmdem_create(const ibmdem_params* p, int32_t device, ibmdem_ctx** out) {
+  if (!p || !out) return IBMDEM_EINVAL;
+  *out = nullptr;
+  if (p->nx < 4 || p->ny < 4 || p->nz < 4 || p->coupleInterval < 1 || p->Ns < 0 || !(p->dx > 0) || !(p->dy > 0) ||
+      !(p->dz > 0) || !(p->dt > 0))
+    return IBMDEM_EINVAL;
+  for (int f = 0; f < 6; ++f)
+    if (p->bType[f] != 0) return IBMDEM_EUNSUPPORTED;  // periodic faces only
+  long long ncell = (long long)(p->nx + 4) * (p->ny + 4) * (p->nz + 4);
+  long long nint = (long long)p->nx * p->ny * p->nz;
+  if (ncell >= (1ll << 31) || 3 * nint >= (1ll << 32)) return IBMDEM_EUNSUPPORTED;
+  ibmdem_ctx* h = new (std::nothrow) ibmdem_ctx();
+  if (!h) return IBMDEM_ENOMEM;
+  Ctx& c = h->c;
+  c.p = *p;
+  c.device = device;
+  if (cudaSetDevice(device) != cudaSuccess) {
+    delete h;
+    return IBMDEM_ECUDA;
+  }
+  Geom& g = c.g;
+  g.n[0] = p->nx;
+  g.n[1] = p->ny;
+  g.n[2] = p->nz;
+  g.ni = p->nx + 4;
+  g.nj = p->ny + 4;
+  g.nk = p->nz + 4;
+  g.ncell = ncell;
+  g.nint = nint;
+  double hh[3] = {p->dx, p->dy, p->dz};
+  for (int d = 0; d < 3; ++d) {
+    g.h[d] = hh[d];
+    g.start[d] = (1 - 1) * hh[d];
+    g.end[d] = (g.n[d] - 1 + 1) * hh[d];
+    g.len[d] = hh[d] * g.n[d];
+    g.halfh[d] = 0.5 * hh[d];
+    g.err[d] = hh[d] * 1e-20;
+  }
+  g.hprod = p->dx * p->dy * p->dz;
+  g.unit_h = (p->dx == 1.0 && p->dy == 1.0 && p->dz == 1.0) ? 1 : 0;
+  g.dt = p->dt;
+  g.dtDEM = p->dt / p->coupleInterval;
+  g.rhof = p->rhof;
+  g.eta = eta_of(p->ResistCoeff);
+  double cd = p->collisionDist * (1.0 + p->collisionBuffer);
+  g.cut2 = cd * cd;
+  g.knCoeff = p->knCoeff;
+  g.di = p->dx;
+  for (int k = 0; k < 3; ++k) g.g[k] = p->gravity[k];
+
+  int rc = IBMDEM_OK;
+  size_t nf = (size_t)ncell;
+  double** f[] = {&c.u, &c.v, &c.w, &c.u0, &c.v0, &c.w0, &c.fx, &c.fy, &c.fz};
+  for (double** q : f)
+    if (dalloc(*q, nf) != cudaSuccess) rc = IBMDEM_ENOMEM;
+  if (rc == IBMDEM_OK && dalloc(c.cellStart, (size_t)ncell + 1) != cudaSuccess) rc = IBMDEM_ENOMEM;
+  if (rc == IBMDEM_OK && dalloc(c.dCnt, 1) != cudaSuccess) rc = IBMDEM_ENOMEM;
+  if (rc == IBMDEM_OK && dalloc(c.dTotal, 4) != cudaSuccess) rc = IBMDEM_ENOMEM;
+  if (rc == IBMDEM_OK && cudaMallocHost(reinterpret_cast<void**>(&c.hCnt), sizeof(Counters)) != cudaSuccess)
+    rc = IBMDEM_ENOMEM;
+  if (rc != IBMDEM_OK) {
+    ibmdem_destroy(h);
+    return rc;
+  }
+  for (double** q : f) cudaMemset(*q, 0, nf * sizeof(double));
+  cudaMemset(c.dCnt, 0, sizeof(Counters));
+  cudaMemset(c.cellStart, 0, sizeof(int) * (nf + 1));
+  if (cudaDeviceSynchronize() != cudaSuccess) {
+    ibmdem_destroy(h);
+    return IBMDEM_ECUDA;
+  }
+  *out = h;
+  return IBMDEM_OK;
+}
+
+int ibmdem_destroy(ibmdem_ctx* h) {
+  if (!h) return IBMDEM_EINVAL;
+  Ctx& c = h->c;
+  cudaSetDevice(c.device);
+  if (c.stream) cudaStreamSynchronize(c.stream);
+  free_parcel_buffers(c);
+  void* ps[] = {c.u, c.v, c.w, c.u0, c.v0, c.w0, c.fx, c.fy, c.fz, c.cellStart, c.dCnt, c.dTotal, c.dBodies,
+                c.bodyStart, c.bodyR2, c.partnerCnt, c.partners};
+  for (void* p : ps) dfree(p);
+  if (c.hCnt) cudaFreeHost(c.hCnt);
+  delete h;
+  return IBMDEM_OK;
+}
+
+int ibmdem_set_stream(ibmdem_ctx* h, void* stream) {
+  CHECK_CTX();
+  h->c.stream = reinterpret_cast<cudaStream_t>(stream);
+  return IBMDEM_OK;
+}
+
+int ibmdem_synchronize(ibmdem_ctx* h) {
+  CHECK_CTX();
+  int rc = launch_status(h);
+  if (rc) return rc;
+  return check_device(h);
+}
+
+int ibmdem_set_fluid(ibmdem_ctx* h, const double* u, const double* v, const double* w) {
+  CHECK_CTX();
+  if (!u || !v || !w) return set_error(h, IBMDEM_EINVAL, "null field");
+  Ctx& c = h->c;
+  size_t nb = sizeof(double) * (size_t)c.g.ncell;
+  CU(cudaMemcpyAsync(c.u, u, nb, cudaMemcpyHostToDevice, c.stream));
+  CU(cudaMemcpyAsync(c.v, v, nb, cudaMemcpyHostToDevice, c.stream));
+  CU(cudaMemcpyAsync(c.w, w, nb, cudaMemcpyHostToDevice, c.stream));
+  CU(cudaMemcpyAsync(c.u0, c.u, nb, cudaMemcpyDeviceToDevice, c.stream));
+  CU(cudaMemcpyAsync(c.v0, c.v, nb, cudaMemcpyDeviceToDevice, c.stream));
+  CU(cudaMemcpyAsync(c.w0, c.w, nb, cudaMemcpyDeviceToDevice, c.stream));
+  CU(cudaMemsetAsync(c.fx, 0, nb, c.stream));
+  CU(cudaMemsetAsync(c.fy, 0, nb, c.stream));
+  CU(cudaMemsetAsync(c.fz, 0, nb, c.stream));
+  CU(cudaMemsetAsync(&c.dCnt->nLast, 0, sizeof(int), c.stream));
+  c.haveFluid = true;
+  // synchronous for pageable host memory semantics: the caller may reuse u,v,w
+  CU(cudaStreamSynchronize(c.stream));
+  return IBMDEM_OK;
+}
+
+int ibmdem_get_fluid(ibmdem_ctx* h, double* u, double* v, double* w, double* fx, double* fy, double* fz) {
+  CHECK_CTX();
+  Ctx& c = h->c;
+  size_t nb = sizeof(double) * (size_t)c.g.ncell;
+  double* dst[6] = {u, v, w, fx, fy, fz};
+  double* src[6] = {c.u, c.v, c.w, c.fx, c.fy, c.fz};
+  for (int q = 0; q < 6; ++q)
+    if (dst[q]) CU(cudaMemcpyAsync(dst[q], src[q], nb, cudaMemcpyDeviceToHost, c.stream));
+  return check_device(h);
+}
+
+int ibmdem_set_parcels(ibmdem_ctx* h, int32_t np, const ibmdem_parcel* parts) {
+  CHECK_CTX();
+  if (np < 0 || (np > 0 && !parts)) return set_error(h, IBMDEM_EINVAL, "bad parcel array");
+  if ((long long)np * kSlots >= (1ll << 32)) return set_error(h, IBMDEM_EUNSUPPORTED, "too many parcels");
+  Ctx& c = h->c;
+  CU(cudaStreamSynchronize(c.stream));
+  long long nimg = count_images(c.g, np, parts);
+  int rc = alloc_parcels(h, np, nimg);
+  if (rc) return rc;
+  std::vector<double> hd((size_t)ND * c.cap, 0.0);
+  std::vector<int> hi((size_t)NI * c.cap, 0);
+  for (int i = 0; i < np; ++i) {
+    const ibmdem_parcel& p = parts[i];
+    const double* src[ND];
+    for (int k = 0; k < 3; ++k) {
+      src[D_X + k] = &p.x[k];
+      src[D_V + k] = &p.v[k];
+      src[D_FCOL + k] = &p.fcol[k];
+      src[D_FDRAG + k] = &p.fdrag[k];
+      src[D_VGAP + k] = &p.vgap[k];
+    }
+    src[D_RADEFF] = &p.radeff;
+    src[D_RAD] = &p.rad;
+    src[D_RHO] = &p.rho;
+    src[D_VOL] = &p.vol;
+    src[D_M] = &p.m;
+    src[D_WDRAG] = &p.wdrag;
+    src[D_WSUM] = &p.wsum;
+    for (int f = 0; f < ND; ++f) hd[(size_t)f * c.cap + i] = *src[f];
+    hi[(size_t)I_GIDX * c.cap + i] = p.globalIdx;
+    hi[(size_t)I_MSIDX * c.cap + i] = p.MSIdx;
+    int a[3];
+    for (int d = 0; d < 3; ++d) a[d] = (int)std::floor((p.x[d] - c.g.start[d]) / c.g.h[d]) + 1;
+    bool in = true;
+    for (int d = 0; d < 3; ++d) in = in && a[d] >= -1 && a[d] <= c.g.n[d] + 2;
+    if (!in) return set_error(h, IBMDEM_ERANGE, "parcel %d at (%g,%g,%g) exceeds the region", i + 1, p.x[0], p.x[1], p.x[2]);
+    hi[(size_t)I_CELL * c.cap + i] = cell_id(c.g, a[0], a[1], a[2]);
+  }
+  CU(cudaMemcpy(c.recD[c.cur], hd.data(), sizeof(double) * hd.size(), cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(c.recI[c.cur], hi.data(), sizeof(int) * hi.size(), cudaMemcpyHostToDevice));
+  Counters hc{};
+  hc.npLocal = hc.np = np;
+  CU(cudaMemcpy(c.dCnt, &hc, sizeof hc, cudaMemcpyHostToDevice));
+  c.haveParcels = true;
+  c.listsBuilt = c.weightsLocal = c.weightsGhost = c.planReady = c.spreadValid = false;
+  return IBMDEM_OK;
+}
+
+int ibmdem_get_parcels(ibmdem_ctx* h, ibmdem_parcel* parts, int32_t cap, int32_t* np_out, int32_t* nlocal_out) {
+  CHECK_CTX();
+  Ctx& c = h->c;
+  int rc = check_device(h);
+  if (rc) return rc;
+  int np = c.hCnt->np, nl = c.hCnt->npLocal;
+  if (np_out) *np_out = np;
+  if (nlocal_out) *nlocal_out = nl;
+  if (!parts || np == 0) return IBMDEM_OK;
+  int n = std::min(np, cap);
+  std::vector<double> hd((size_t)ND * c.cap);
+  std::vector<int> hi((size_t)NI * c.cap);
+  CU(cudaMemcpy(hd.data(), c.recD[c.cur], sizeof(double) * hd.size(), cudaMemcpyDeviceToHost));
+  CU(cudaMemcpy(hi.data(), c.recI[c.cur], sizeof(int) * hi.size(), cudaMemcpyDeviceToHost));
+  for (int i = 0; i < n; ++i) {
+    ibmdem_parcel& p = parts[i];
+    std::memset(&p, 0, sizeof p);
+    auto D = [&](int f) { return hd[(size_t)f * c.cap + i]; };
+    for (int k = 0; k < 3; ++k) {
+      p.x[k] = D(D_X + k);
+      p.v[k] = D(D_V + k);
+      p.fcol[k] = D(D_FCOL + k);
+      p.fdrag[k] = D(D_FDRAG + k);
+      p.vgap[k] = D(D_VGAP + k);
+    }
+    p.radeff = D(D_RADEFF);
+    p.rad = D(D_RAD);
+    p.rho = D(D_RHO);
+    p.vol = D(D_VOL);
+    p.m = D(D_M);
+    p.wdrag = D(D_WDRAG);
+    p.wsum = D(D_WSUM);
+    p.globalIdx = hi[(size_t)I_GIDX * c.cap + i];
+    p.MSIdx = hi[(size_t)I_MSIDX * c.cap + i];
+    p.cellIdx = hi[(size_t)I_CELL * c.cap + i];
+    p.localIdx = i + 1;
+    p.pType = -1;
+  }
+  return IBMDEM_OK;
+}
+
+int ibmdem_set_bodies(ibmdem_ctx* h, int32_t nMS, const ibmdem_multisphere* ms) {
+  CHECK_CTX();
+  if (nMS < 0 || (nMS > 0 && !ms)) return set_error(h, IBMDEM_EINVAL, "bad body array");
+  Ctx& c = h->c;
+  CU(cudaStreamSynchronize(c.stream));
+  if (nMS > c.capMS) {
+    dfree(c.dBodies);
+    dfree(c.bodyStart);
+    dfree(c.bodyR2);
+    dfree(c.partnerCnt);
+    dfree(c.partners);
+    c.dBodies = nullptr;
+    c.bodyStart = nullptr;
+    c.bodyR2 = nullptr;
+    c.partnerCnt = c.partners = nullptr;
+    CU(dalloc(c.dBodies, nMS));
+    CU(dalloc(c.bodyStart, nMS + 1));
+    CU(dalloc(c.bodyR2, nMS));
+    CU(dalloc(c.partnerCnt, nMS));
+    CU(dalloc(c.partners, (size_t)nMS * c.maxPartners));
+    c.capMS = nMS;
+  }
+  if (nMS > 0) CU(cudaMemcpy(c.dBodies, ms, sizeof(ibmdem_multisphere) * nMS, cudaMemcpyHostToDevice));
+  c.nMS = nMS;
+  c.listsBuilt = false;  // body lists are built with the cell lists
+  return IBMDEM_OK;
+}
+
+int ibmdem_get_bodies(ibmdem_ctx* h, ibmdem_multisphere* ms, int32_t cap, int32_t* nMS_out) {
+  CHECK_CTX();
+  Ctx& c = h->c;
+  int rc = check_device(h);
+  if (rc) return rc;
+  if (nMS_out) *nMS_out = c.nMS;
+  if (ms && c.nMS > 0)
+    CU(cudaMemcpy(ms, c.dBodies, sizeof(ibmdem_multisphere) * std::min(c.nMS, cap), cudaMemcpyDeviceToHost));
+  return IBMDEM_OK;
+}
+
+int ibmdem_get_cell_lists(ibmdem_ctx* h, int32_t* cell_start, int32_t* items, int64_t* ncell_out,
+                          int32_t* nitems_out) {
+  CHECK_CTX();
+  Ctx& c = h->c;
+  int rc = check_device(h);
+  if (rc) return rc;
+  if (ncell_out) *ncell_out = c.g.ncell;
+  if (nitems_out) *nitems_out = c.hCnt->np;
+  REQUIRE(c.listsBuilt, "cell lists are not built");
+  if (cell_start) CU(cudaMemcpy(cell_start, c.cellStart, sizeof(int) * (c.g.ncell + 1), cudaMemcpyDeviceToHost));
+  if (items) {
+    int n = c.hCnt->np;
+    CU(cudaMemcpy(items, c.cellItems, sizeof(int) * n, cudaMemcpyDeviceToHost));
+    for (int i = 0; i < n; ++i) items[i] += 1;
+  }
+  return IBMDEM_OK;
+}
+
+int ibmdem_get_collision_lists(ibmdem_ctx* h, int32_t* start, int32_t* idx, int32_t* nlocal_out,
+                               int32_t* npairs_out) {
+  CHECK_CTX();
+  Ctx& c = h->c;
+  int rc = check_device(h);
+  if (rc) return rc;
+  REQUIRE(c.listsBuilt, "collision lists are not built");
+  int nl = c.hCnt->npLocal, npairs = c.hCnt->nPairs;
+  if (nlocal_out) *nlocal_out = nl;
+  if (npairs_out) *npairs_out = npairs;
+  if (start) CU(cudaMemcpy(start, c.pairStart, sizeof(int) * (nl + 1), cudaMemcpyDeviceToHost));
+  if (idx) {
+    CU(cudaMemcpy(idx, c.pairIdx, sizeof(int) * npairs, cudaMemcpyDeviceToHost));
+    for (int i = 0; i < npairs; ++i) idx[i] += 1;
+  }
+  return IBMDEM_OK;
+}
+
+int ibmdem_get_counters(ibmdem_ctx* h, int64_t* out, int32_t n) {
+  CHECK_CTX();
+  Ctx& c = h->c;
+  int rc = check_device(h);
+  if (rc) return rc;
+  int64_t v[7] = {c.hCnt->npLocal, c.hCnt->np, c.hCnt->nPairs, 0, 0, 0, c.hCnt->nContrib};
+  // touched nodes per component from the run keys
+  if (c.planReady && c.hCnt->nRuns > 0) {
+    std::vector<uint32_t> keys(c.hCnt->nRuns);
+    CU(cudaMemcpy(keys.data(), c.runKey, sizeof(uint32_t) * keys.size(), cudaMemcpyDeviceToHost));
+    for (uint32_t k : keys) v[3 + (int)(k / (uint32_t)c.g.nint)]++;
+  }
+  for (int q = 0; q < n && q < 7; ++q) out[q] = v[q];
+  return IBMDEM_OK;
+}
+
+// ---- reference subroutines ------------------------------------------------
+
+int ibmdem_RebuildAllListOrNot(ibmdem_ctx* h) {
+  CHECK_CTX();
+  Ctx& c = h->c;
+  REQUIRE(c.haveParcels, "no parcels");
+  rebuild_cell_lists(c);
+  rebuild_collision_lists(c);
+  c.listsBuilt = true;
+  c.weightsLocal = c.weightsGhost = c.planReady = c.spreadValid = false;
+  return launch_status(h);
+}
+
+int ibmdem_UpdateLocalCellWeightListDEM(ibmdem_ctx* h) {
+  CHECK_CTX();
+  Ctx& c = h->c;
+  REQUIRE(c.listsBuilt, "lists are not built");
+  launch_weights(c, true);
+  c.weightsLocal = true;
+  c.planReady = false;
+  return launch_status(h);
+}
+
+int ibmdem_UpdateGhostCellWeightListDEM(ibmdem_ctx* h) {
+  CHECK_CTX();
+  Ctx& c = h->c;
+  REQUIRE(c.listsBuilt, "lists are not built");
+  launch_weights(c, false);
+  c.weightsGhost = true;
+  c.planReady = false;
+  if (c.weightsLocal) build_spread_plan(c);
+  return launch_status(h);
+}
+
+int ibmdem_UpdateParcelInfoInGhostRegion(ibmdem_ctx* h) {
+  CHECK_CTX();
+  Ctx& c = h->c;
+  REQUIRE(c.haveParcels, "no parcels");
+  launch_img_update(c);
+  return launch_status(h);
+}
+
+int ibmdem_CalculateCollisionForce(ibmdem_ctx* h) {
+  CHECK_CTX();
+  Ctx& c = h->c;
+  REQUIRE(c.listsBuilt, "lists are not built");
+  launch_collision_force(c);
+  return launch_status(h);
+}
+
+int ibmdem_UpdateFluidVelocityOnLagrangianPoints(ibmdem_ctx* h) {
+  CHECK_CTX();
+  Ctx& c = h->c;
+  REQUIRE(c.weightsLocal, "local weights are not computed");
+  REQUIRE(c.haveFluid, "no fluid field");
+  launch_interp(c);
+  return launch_status(h);
+}
+
+static int ensure_plan(ibmdem_ctx* h) {
+  Ctx& c = h->c;
+  REQUIRE(c.weightsLocal && c.weightsGhost, "weights are not computed");
+  if (!c.planReady) build_spread_plan(c);
+  return IBMDEM_OK;
+}
+
+int ibmdem_UpdateMomentumSourceTerm(ibmdem_ctx* h) {
+  CHECK_CTX();
+  Ctx& c = h->c;
+  int rc = ensure_plan(h);
+  if (rc) return rc;
+  REQUIRE(c.spreadValid, "spreading needs MultiDirectForcing's reset after the weights change");
+  launch_spread(c, false);
+  return launch_status(h);
+}
+
+int ibmdem_VelocityPostGuess(ibmdem_ctx* h) {
+  CHECK_CTX();
+  Ctx& c = h->c;
+  REQUIRE(c.planReady && c.spreadValid, "no spread to apply");
+  launch_post_guess(c);
+  return launch_status(h);
+}
+
+int ibmdem_AssembleLocalForceMS(ibmdem_ctx* h) {
+  CHECK_CTX();
+  Ctx& c = h->c;
+  REQUIRE(c.listsBuilt, "body lists are not built");
+  launch_body_sums(c);
+  return launch_status(h);
+}
+
+int ibmdem_EvolutionMS(ibmdem_ctx* h) {
+  CHECK_CTX();
+  launch_evolution(h->c);
+  return launch_status(h);
+}
+
+int ibmdem_ResetVelocityAndPositionLagrangianPoints(ibmdem_ctx* h) {
+  CHECK_CTX();
+  REQUIRE(h->c.haveParcels, "no parcels");
+  launch_marker_update(h->c, true, false);
+  return launch_status(h);
+}
+
+int ibmdem_AdjustParcelPosition(ibmdem_ctx* h) {
+  CHECK_CTX();
+  REQUIRE(h->c.haveParcels, "no parcels");
+  launch_marker_update(h->c, false, true);
+  return launch_status(h);
+}
+
+// ---- drivers -----------------------------------------------------------------
+
+int ibmdem_InitializationDEM(ibmdem_ctx* h) {
+  int rc = ibmdem_RebuildAllListOrNot(h);
+  if (!rc) rc = ibmdem_UpdateLocalCellWeightListDEM(h);
+  if (!rc) rc = ibmdem_UpdateParcelInfoInGhostRegion(h);
+  if (!rc) rc = ibmdem_UpdateGhostCellWeightListDEM(h);
+  return rc;
+}
+
+static int mdf(ibmdem_ctx* h, bool frozen) {
+  Ctx& c = h->c;
+  REQUIRE(c.haveFluid, "no fluid field");
+  int rc = ensure_plan(h);
+  if (rc) return rc;
+  launch_mdf_reset(c, frozen);
+  for (int it = 0; it < c.p.Ns; ++it) {
+    launch_interp(c);
+    launch_img_update(c);
+    launch_spread(c, true);
+  }
+  record_written_nodes(c);
+  return launch_status(h);
+}
+
+int ibmdem_MultiDirectForcing(ibmdem_ctx* h) {
+  CHECK_CTX();
+  return mdf(h, false);
+}
+
+int ibmdem_CloudEvolutionStepMS(ibmdem_ctx* h) {
+  CHECK_CTX();
+  Ctx& c = h->c;
+  REQUIRE(c.listsBuilt && c.weightsLocal && c.weightsGhost, "lists and weights are not built");
+  launch_collision_force(c);
+  launch_body_sums(c);
+  launch_evolution(c);
+  launch_marker_update(c, true, true);
+  launch_img_update(c);
+  rebuild_cell_lists(c);
+  rebuild_collision_lists(c);
+  launch_weights(c, true);
+  launch_img_update(c);
+  launch_weights(c, false);
+  build_spread_plan(c);
+  c.listsBuilt = c.weightsLocal = c.weightsGhost = true;
+  return launch_status(h);
+}
+
+int ibmdem_CloudEvolutionMS(ibmdem_ctx* h) {
+  CHECK_CTX();
+  Ctx& c = h->c;
+  REQUIRE(c.listsBuilt, "lists are not built");
+  launch_cloud_pre(c);
+  launch_body_sums(c);
+  launch_cloud_post(c);
+  for (int s = 0; s < c.p.coupleInterval; ++s) {
+    int rc = ibmdem_CloudEvolutionStepMS(h);
+    if (rc) return rc;
+  }
+  return launch_status(h);
+}
+
+int ibmdem_step(ibmdem_ctx* h, int32_t nsteps) {
+  CHECK_CTX();
+  for (int s = 0; s < nsteps; ++s) {
+    int rc = mdf(h, true);
+    if (rc) return rc;
+    rc = ibmdem_CloudEvolutionMS(h);
+    if (rc) return rc;
+  }
+  return IBMDEM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,120 @@
+// common.cuh — shared definitions of the GB300 IBM-DEM particle hot path.
+//
+// Device data layout
+//   parcels   structure of arrays, field-major: recD[f*cap + i] (22 doubles per
+//             parcel) and recI[f*cap + i] (3 ints).  Index i is the reference's
+//             part(i+1): locals first (0..npLocal), then periodic images.
+//   fields    u,v,w,fx,fy,fz in the reference's Fortran layout with the 2-cell
+//             halo: offset = ((k+1)*nj + (j+1))*ni + (i+1) for i in -1..nx+2.
+//   weights   W[slot*cap + i], slot = comp*27 + kz*9 + ky*3 + kx: the 27
+//             non-zero delta weights per component in stencil order.
+//   plan      the spread order: (node, contribution) pairs sorted by node with
+//             the reference's part order inside each node.
+// All FP64 arithmetic on the parity path is compiled with -fmad=false and keeps
+// the reference's operation order, so results are bit-identical to the CPU
+// restatement (libm-dependent cos/sin of the body rotation excepted).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/ibmdem.h"
+
+namespace ibmdem {
+
+constexpr int kHalo = 2;
+constexpr int kSlots = 81;  // 3 components x 27 nodes
+constexpr int kBlock = 256;
+
+// double fields of a parcel record
+enum : int {
+  D_X = 0, D_V = 3, D_FCOL = 6, D_FDRAG = 9, D_VGAP = 12,
+  D_RADEFF = 15, D_RAD, D_RHO, D_VOL, D_M, D_WDRAG, D_WSUM, ND
+};
+// int fields
+enum : int { I_GIDX = 0, I_MSIDX, I_CELL, NI };
+
+// device error bits (Counters::err)
+enum : int {
+  E_RANGE = 1,     // a parcel left the grid + halo region
+  E_IMGCAP = 2,    // periodic images exceed their capacity
+  E_PAIRCAP = 4,   // contact pairs exceed their capacity
+  E_WINDOW = 8,    // a delta stencil needed 4 nodes on one axis
+  E_MSIDX = 16,    // parcel body index out of range
+  E_PARTNER = 32,  // body partner list overflow
+};
+
+struct Geom {
+  int n[3];
+  int ni, nj, nk;
+  long long ncell;  // ni*nj*nk
+  long long nint;   // nx*ny*nz
+  double h[3];      // dx, dy, dz
+  double start[3], end[3], len[3];
+  double halfh[3];  // 0.5*di etc. (GetWeight)
+  double err[3];    // di*1e-20 (AdjustParcelPosition)
+  double hprod;     // dx*dy*dz
+  int unit_h;       // dx == dy == dz == 1: /h, *dx*dy*dz are exact identities
+  double dt, dtDEM, rhof, eta, cut2, knCoeff, di;
+  double g[3];
+};
+
+struct Counters {
+  int npLocal, np, nImg, nActive, nPairs, nRuns, nContrib, nLast;
+  int err, errInfo;
+  int pad[6];
+};
+
+struct Recs {
+  double* d;
+  int* i;
+  int cap;
+  __host__ __device__ double& D(int f, int idx) const { return d[(size_t)f * cap + idx]; }
+  __host__ __device__ int& I(int f, int idx) const { return i[(size_t)f * cap + idx]; }
+};
+
+// ---- index helpers -------------------------------------------------------
+__host__ __device__ inline long long field_off(const Geom& g, int i, int j, int k) {
+  return ((long long)(k + 1) * g.nj + (j + 1)) * g.ni + (i + 1);
+}
+// map3Dto1D (ZJS_INIT_DEM.F90:286), 1-based
+__host__ __device__ inline int cell_id(const Geom& g, int i, int j, int k) {
+  return (int)(field_off(g, i, j, k) + 1);
+}
+__host__ __device__ inline void cell_coords(const Geom& g, int id, int& i, int& j, int& k) {
+  int t = id - 1;
+  i = t % g.ni - 1;
+  t /= g.ni;
+  j = t % g.nj - 1;
+  k = t / g.nj - 1;
+}
+// floor((x-xStart)/di)+SG (ZJS_UPDATE_LIST_DEM.F90:41-43)
+__device__ inline int cell_of(const Geom& g, int d, double x) {
+  return (int)floor((x - g.start[d]) / g.h[d]) + 1;
+}
+__device__ inline bool interior(const Geom& g, int i, int j, int k) {
+  return i >= 1 && i <= g.n[0] && j >= 1 && j <= g.n[1] && k >= 1 && k <= g.n[2];
+}
+__device__ inline void set_err(Counters* c, int bit, int info) {
+  atomicOr(&c->err, bit);
+  atomicExch(&c->errInfo, info);
+}
+// periodic image of the body centre nearest to a marker coordinate
+__device__ inline double body_ref(const Geom& g, int d, double xm, double X) {
+  double L = g.len[d];
+  double diff = xm - X;
+  if (diff > 0.5 * L) return X + L;
+  if (diff < -0.5 * L) return X - L;
+  return X;
+}
+
+// launch helpers
+inline int nblocks(long long n, int bs = kBlock) { return (int)((n + bs - 1) / bs); }
+// grid for a grid-stride loop over up to n items: at most 16 blocks per SM
+inline int gs_blocks(long long n, int bs = kBlock) {
+  long long b = (n + bs - 1) / bs;
+  return (int)(b < 152 * 16 ? (b < 1 ? 1 : b) : 152 * 16);
+}
+#define GRID_STRIDE(i, n) \
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < (n); i += (long long)gridDim.x * blockDim.x)
+
+}  // namespace ibmdem

@@ -1,0 +1,226 @@
+// contact.cu — RebuildParcelCollisionListDEM (ZJS_UPDATE_LIST_DEM.F90:248-286)
+// and CalculateCollisionForce (ZJS_COLLISION_DEM.F90:21-74).
+//
+// The reference scans, for every local parcel, the 125 cells around its cell
+// and every parcel in them.  Parcels of one body never pair (MSIdx test), so a
+// body-level broad phase removes almost all of that work: a parcel can only
+// have a partner when some other body's bounding sphere, grown by the contact
+// cut-off plus a margin far above FP32 rounding, reaches it.  Parcels that pass
+// this conservative filter run the reference scan unchanged (same cells, same
+// order, same FP64 predicate), so the lists are identical, in order, to the
+// reference's; the others provably have empty lists.
+#include "common.cuh"
+#include "kernels.cuh"
+#include "prims.cuh"
+
+namespace ibmdem {
+
+namespace {
+
+__device__ inline float min_image_f(float d, float L) {
+  if (d > 0.5f * L) return d - L;
+  if (d < -0.5f * L) return d + L;
+  return d;
+}
+
+__global__ void k_body_bound(Recs R, Geom g, const Counters* cnt, const ibmdem_multisphere* B, int nMS,
+                             unsigned* r2bits) {
+  int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= cnt->npLocal) return;
+  int b = R.I(I_MSIDX, m) - 1;
+  if (b < 0 || b >= nMS) return;
+  float d2 = 0.f;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    float dd = min_image_f((float)R.D(D_X + d, m) - (float)B[b].x[d], (float)g.len[d]);
+    d2 += dd * dd;
+  }
+  atomicMax(&r2bits[b], __float_as_uint(d2));
+}
+
+__global__ void k_body_pairs(const ibmdem_multisphere* B, int nMS, Geom g, const unsigned* r2bits, float reach,
+                             int* partnerCnt, int* partners, int maxPartners, Counters* cnt) {
+  int a = blockIdx.y;
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= nMS || b >= nMS || b <= a) return;
+  float d2 = 0.f;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    float dd = min_image_f((float)B[a].x[d] - (float)B[b].x[d], (float)g.len[d]);
+    d2 += dd * dd;
+  }
+  float lim = sqrtf(__uint_as_float(r2bits[a])) + sqrtf(__uint_as_float(r2bits[b])) + reach;
+  if (d2 < lim * lim) {
+    int qa = atomicAdd(&partnerCnt[a], 1);
+    int qb = atomicAdd(&partnerCnt[b], 1);
+    if (qa < maxPartners) partners[a * maxPartners + qa] = b;
+    else set_err(cnt, E_PARTNER, a);
+    if (qb < maxPartners) partners[b * maxPartners + qb] = a;
+    else set_err(cnt, E_PARTNER, b);
+  }
+}
+
+__global__ void k_marker_active(Recs R, Geom g, const Counters* cnt, const ibmdem_multisphere* B, int nMS,
+                                const unsigned* r2bits, const int* partnerCnt, const int* partners,
+                                int maxPartners, float reach, int* flag) {
+  int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= cnt->npLocal) return;
+  int b = R.I(I_MSIDX, m) - 1;
+  int act = 0;
+  if (b >= 0 && b < nMS) {
+    int np = min(partnerCnt[b], maxPartners);
+    float x[3] = {(float)R.D(D_X, m), (float)R.D(D_X + 1, m), (float)R.D(D_X + 2, m)};
+    for (int q = 0; q < np && !act; ++q) {
+      int o = partners[b * maxPartners + q];
+      float d2 = 0.f;
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        float dd = min_image_f(x[d] - (float)B[o].x[d], (float)g.len[d]);
+        d2 += dd * dd;
+      }
+      float lim = sqrtf(__uint_as_float(r2bits[o])) + reach;
+      act = d2 < lim * lim;
+    }
+  }
+  flag[m] = act;
+}
+
+__global__ void k_compact_active(const Counters* cnt, const int* flag, const int* pos, int* list) {
+  int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= cnt->npLocal || !flag[m]) return;
+  list[pos[m]] = m;
+}
+
+// Collision (ZJS_COLLISION_DEM.F90:2-19) inside the 125-cell scan of
+// RebuildParcelCollisionListDEM; FILL = false counts, true writes.
+template <bool FILL>
+__global__ void k_pair_scan(Recs R, Geom g, const Counters* cnt, const int* activeList, const int* nActive,
+                            const int* cellStart, const int* cellItems, int* pairCnt, const int* pairStart,
+                            int* pairIdx, long long capPairs, Counters* cntw) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= *nActive) return;
+  int ii = activeList[q];
+  int ci, cj, ck;
+  cell_coords(g, R.I(I_CELL, ii), ci, cj, ck);
+  const int msi = R.I(I_MSIDX, ii);
+  const double xi0 = R.D(D_X, ii), xi1 = R.D(D_X + 1, ii), xi2 = R.D(D_X + 2, ii);
+  int count = 0;
+  long long base = FILL ? pairStart[ii] : 0;
+  for (int kk = -2; kk <= 2; ++kk)
+    for (int jj = -2; jj <= 2; ++jj)
+      for (int i2 = -2; i2 <= 2; ++i2) {
+        int a = ci + i2, b = cj + jj, c = ck + kk;
+        if (a < -1 || a > g.n[0] + 2 || b < -1 || b > g.n[1] + 2 || c < -1 || c > g.n[2] + 2) continue;
+        int cell = cell_id(g, a, b, c);
+        int s = cellStart[cell - 1], e = cellStart[cell];
+        for (int k = s; k < e; ++k) {
+          int jjx = cellItems[k];
+          if (R.I(I_MSIDX, jjx) == msi) continue;
+          double xij1 = xi0 - R.D(D_X, jjx);
+          double xij2 = xi1 - R.D(D_X + 1, jjx);
+          double xij3 = xi2 - R.D(D_X + 2, jjx);
+          double distSqr = xij1 * xij1 + xij2 * xij2 + xij3 * xij3;
+          if (distSqr < g.cut2 && jjx != ii) {
+            if (FILL) {
+              long long at = base + count;
+              if (at < capPairs) pairIdx[at] = jjx;
+              else set_err(cntw, E_PAIRCAP, (int)at);
+            }
+            ++count;
+          }
+        }
+      }
+  if (!FILL) pairCnt[ii] = count;
+}
+
+__global__ void k_set_pair_total(Counters* cnt, const int* total, long long capPairs) {
+  int n = *total;
+  if (n > capPairs) {
+    atomicOr(&cnt->err, E_PAIRCAP);
+    cnt->errInfo = n;
+  }
+  cnt->nPairs = n;
+}
+
+// CalculateCollisionForce (ZJS_COLLISION_DEM.F90:21-74), one thread per local
+__global__ void k_collision_force(Recs R, Geom g, const Counters* cnt, const int* pairStart, const int* pairIdx,
+                                  long long capPairs) {
+  int ii = blockIdx.x * blockDim.x + threadIdx.x;
+  if (ii >= cnt->npLocal) return;
+  double fc1 = 0, fc2 = 0, fc3 = 0;
+  int s = pairStart[ii], e = pairStart[ii + 1];
+  if (e > capPairs) e = (int)capPairs;
+  if (s < e) {
+    const double xi0 = R.D(D_X, ii), xi1 = R.D(D_X + 1, ii), xi2 = R.D(D_X + 2, ii);
+    const double vi0 = R.D(D_V, ii), vi1 = R.D(D_V + 1, ii), vi2 = R.D(D_V + 2, ii);
+    const double mi = R.D(D_M, ii), ri = R.D(D_RADEFF, ii);
+    for (int q = s; q < e; ++q) {
+      int j = pairIdx[q];
+      double r1 = xi0 - R.D(D_X, j);
+      double r2 = xi1 - R.D(D_X + 1, j);
+      double r3 = xi2 - R.D(D_X + 2, j);
+      double dist = sqrt(r1 * r1 + r2 * r2 + r3 * r3);
+      double n1 = r1 / dist, n2 = r2 / dist, n3 = r3 / dist;
+      double mj = R.D(D_M, j);
+      double meff = 2 * mi * mj / (mi + mj);
+      double rij = ri + R.D(D_RADEFF, j);
+      double deltan = rij - dist;
+      double kn = g.knCoeff / (0.1 * g.di) * meff;
+      double etan = g.eta * sqrt(meff * kn);
+      double f1 = 0, f2 = 0, f3 = 0;
+      double vnij = n1 * (vi0 - R.D(D_V, j)) + n2 * (vi1 - R.D(D_V + 1, j)) + n3 * (vi2 - R.D(D_V + 2, j));
+      if (deltan > 0) {
+        f1 = n1 * (kn * deltan - etan * vnij);
+        f2 = n2 * (kn * deltan - etan * vnij);
+        f3 = n3 * (kn * deltan - etan * vnij);
+      }
+      fc1 = fc1 + f1;
+      fc2 = fc2 + f2;
+      fc3 = fc3 + f3;
+    }
+  }
+  R.D(D_FCOL, ii) = fc1;
+  R.D(D_FCOL + 1, ii) = fc2;
+  R.D(D_FCOL + 2, ii) = fc3;
+}
+
+}  // namespace
+
+void rebuild_collision_lists(Ctx& c) {
+  cudaStream_t s = c.stream;
+  const int nbl = nblocks(c.capLocal);
+  // conservative reach: contact cut-off plus a margin far above FP32 error
+  float hmax = (float)fmax(c.g.h[0], fmax(c.g.h[1], c.g.h[2]));
+  float reach = (float)sqrt(c.g.cut2) + 0.05f * hmax + 1e-5f * (float)fmax(c.g.len[0], fmax(c.g.len[1], c.g.len[2]));
+  if (c.nMS > 0) {
+    cudaMemsetAsync(c.bodyR2, 0, sizeof(unsigned) * c.nMS, s);
+    cudaMemsetAsync(c.partnerCnt, 0, sizeof(int) * c.nMS, s);
+    k_body_bound<<<nbl, kBlock, 0, s>>>(c.rec(), c.g, c.dCnt, c.dBodies, c.nMS, c.bodyR2);
+    dim3 grid(nblocks(c.nMS), c.nMS);
+    k_body_pairs<<<grid, kBlock, 0, s>>>(c.dBodies, c.nMS, c.g, c.bodyR2, reach, c.partnerCnt, c.partners,
+                                         c.maxPartners, c.dCnt);
+    k_marker_active<<<nbl, kBlock, 0, s>>>(c.rec(), c.g, c.dCnt, c.dBodies, c.nMS, c.bodyR2, c.partnerCnt,
+                                           c.partners, c.maxPartners, reach, c.iTmpA);
+    c.launches += 3;
+  } else {
+    cudaMemsetAsync(c.iTmpA, 0, sizeof(int) * c.capLocal, s);
+  }
+  scan_exclusive(c.iTmpA, c.iTmpB, c.capLocal, &c.dCnt->npLocal, &c.dCnt->nActive, c.scanScratch, s, &c.launches);
+  k_compact_active<<<nbl, kBlock, 0, s>>>(c.dCnt, c.iTmpA, c.iTmpB, c.activeList);
+  cudaMemsetAsync(c.pairCnt, 0, sizeof(int) * (c.capLocal + 1), s);
+  k_pair_scan<false><<<nbl, kBlock, 0, s>>>(c.rec(), c.g, c.dCnt, c.activeList, &c.dCnt->nActive, c.cellStart,
+                                            c.cellItems, c.pairCnt, nullptr, nullptr, c.capPairs, c.dCnt);
+  scan_exclusive(c.pairCnt, c.pairStart, c.capLocal + 1, nullptr, c.dTotal, c.scanScratch, s, &c.launches);
+  k_set_pair_total<<<1, 1, 0, s>>>(c.dCnt, c.dTotal, c.capPairs);
+  k_pair_scan<true><<<nbl, kBlock, 0, s>>>(c.rec(), c.g, c.dCnt, c.activeList, &c.dCnt->nActive, c.cellStart,
+                                           c.cellItems, c.pairCnt, c.pairStart, c.pairIdx, c.capPairs, c.dCnt);
+  c.launches += 4;
+}
+
+void launch_collision_force(Ctx& c) {
+  k_collision_force<<<nblocks(c.capLocal), kBlock, 0, c.stream>>>(c.rec(), c.g, c.dCnt, c.pairStart, c.pairIdx,
+                                                                  c.capPairs);
+  c.launches++;
+}
+
+}  // namespace ibmdem

@@ -1,0 +1,378 @@
+// ibm.cu — immersed-boundary interpolation, direct forcing and spreading.
+//
+// Reference: UpdateLocal/GhostCellWeightListDEM (ZJS_UPDATE_LIST_DEM.F90:323-416)
+// with GetWeight / DeltaFunction3D (ZJS_INTERPOLATE_DEM.F90:2-17,
+// interpolation.F90:2-33), UpdateFluidVelocityOnLagrangianPoints and
+// UpdateMomentumSourceTerm (ZJS_VOLUMEFRACTION_DEM.F90:2-67), VelocityPostGuess
+// (fluid.F90:135-153) and the periodic halo refill (boundary.F90:122-147).
+//
+// The reference evaluates the 3-point delta kernel on all 125 stencil cells.
+// Per axis at most three nodes have a non-zero weight: the unshifted kernel is
+// non-zero only on cells a-1..a+1 of the parcel's cell a, the half-cell-shifted
+// one on a-1..a+1 or a..a+2, and which of the two follows from |r| >= 1.5 at
+// the ends (weights there are exactly +0).  So each parcel carries 3 x 27
+// weights, each the same product (w1*w2)*w3 of the same 1-D values the
+// reference forms; skipping the exact zeros leaves every sum unchanged.
+//
+// Spreading is deterministic: every (node, contribution) pair is emitted in
+// part order, stably sorted by node, and each touched node sums its own run in
+// that order -- the order in which the reference's serial loop over part(1:np)
+// accumulates into fx.  Interpolation reads the halo layers directly, so the
+// spread kernel refreshes the periodic mirrors of every node it updates.
+#include "common.cuh"
+#include "kernels.cuh"
+#include "prims.cuh"
+
+namespace ibmdem {
+
+namespace {
+
+// one axis of DeltaFunction3D (interpolation.F90:7-30)
+template <int UNIT_H>
+__device__ inline double delta1(double xcp, double h) {
+  double r = fabs(UNIT_H ? xcp : xcp / h);
+  if (r <= 0.5) return (1.0 + sqrt(1.0 - 3.0 * r * r)) / 3.0;
+  if (r <= 1.5) return (5.0 - 3.0 * r - sqrt(1.0 - 3.0 * ((1.0 - r) * (1.0 - r)))) / 6.0;
+  return 0.0;
+}
+
+template <int UNIT_H>
+__global__ void __launch_bounds__(kBlock) k_weights(Recs R, Geom g, Counters* cnt, int locals, double* W,
+                                                    int4* win, int* cntInt) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  int e = locals ? t : cnt->npLocal + t;
+  if (locals ? (e >= cnt->npLocal) : (e >= cnt->np)) return;
+  int a[3];
+  cell_coords(g, R.I(I_CELL, e), a[0], a[1], a[2]);
+  double wu[3][3], ws[3][3];
+  int flags = 0;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const double xp = R.D(D_X + d, e), h = g.h[d];
+    double dl[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      // xc = (i-0.5d0)*dx (initialization.F90:251); deltax = xp - xc (GetWeight)
+      double xc = ((double)(a[d] - 1 + q) - 0.5);
+      if (!UNIT_H) xc = xc * h;
+      dl[q] = xp - xc;
+    }
+#pragma unroll
+    for (int q = 0; q < 3; ++q) wu[d][q] = delta1<UNIT_H>(dl[q], h);
+    // half-cell shifted component: deltax + 0.5d0*di
+    double s0 = dl[0] + g.halfh[d], s3 = dl[3] + g.halfh[d];
+    double r0 = fabs(UNIT_H ? s0 : s0 / h), r3 = fabs(UNIT_H ? s3 : s3 / h);
+    int st = r0 < 1.5 ? 0 : 1;
+    if (r0 < 1.5 && r3 < 1.5) set_err(cnt, E_WINDOW, e);
+    flags |= st << d;
+#pragma unroll
+    for (int q = 0; q < 3; ++q) ws[d][q] = delta1<UNIT_H>(dl[st + q] + g.halfh[d], h);
+  }
+  const int cap = R.cap;
+  int total = 0;
+#pragma unroll
+  for (int comp = 0; comp < 3; ++comp) {
+    int cntAx[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      int s = a[d] - 1 + (d == comp ? ((flags >> d) & 1) : 0);
+      int lo = max(s, 1), hi = min(s + 2, g.n[d]);
+      cntAx[d] = hi >= lo ? hi - lo + 1 : 0;
+    }
+    total += cntAx[0] * cntAx[1] * cntAx[2];
+#pragma unroll
+    for (int ky = 0; ky < 3; ++ky)
+#pragma unroll
+      for (int kx = 0; kx < 3; ++kx) {
+        double w1 = comp == 0 ? ws[0][kx] : wu[0][kx];
+        double w2 = comp == 1 ? ws[1][ky] : wu[1][ky];
+        double w12 = w1 * w2;
+#pragma unroll
+        for (int kz = 0; kz < 3; ++kz) {
+          double w3 = comp == 2 ? ws[2][kz] : wu[2][kz];
+          double wt = w12 * w3;
+          if (!UNIT_H) wt = wt / g.hprod;
+          W[(size_t)(comp * 27 + kz * 9 + ky * 3 + kx) * cap + e] = wt;
+        }
+      }
+  }
+  win[e] = make_int4(a[0], a[1], a[2], flags);
+  cntInt[e] = total;
+}
+
+__device__ inline void window_start(const int4& wn, int comp, int& sx, int& sy, int& sz) {
+  sx = wn.x - 1 + (comp == 0 ? (wn.w & 1) : 0);
+  sy = wn.y - 1 + (comp == 1 ? ((wn.w >> 1) & 1) : 0);
+  sz = wn.z - 1 + (comp == 2 ? ((wn.w >> 2) & 1) : 0);
+}
+
+__global__ void k_plan_emit(Geom g, const Counters* cnt, const int4* win, const int* off, uint32_t* keys,
+                            uint32_t* vals) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= cnt->np) return;
+  int4 wn = win[e];
+  int o = off[e];
+  for (int comp = 0; comp < 3; ++comp) {
+    int sx, sy, sz;
+    window_start(wn, comp, sx, sy, sz);
+    for (int kz = 0; kz < 3; ++kz)
+      for (int ky = 0; ky < 3; ++ky)
+        for (int kx = 0; kx < 3; ++kx) {
+          int i = sx + kx, j = sy + ky, k = sz + kz;
+          if (!interior(g, i, j, k)) continue;
+          long long node = ((long long)(k - 1) * g.n[1] + (j - 1)) * g.n[0] + (i - 1);
+          keys[o] = (uint32_t)(comp * g.nint + node);
+          vals[o] = (uint32_t)(e * kSlots + comp * 27 + kz * 9 + ky * 3 + kx);
+          ++o;
+        }
+  }
+}
+
+__global__ void k_set_contrib(Counters* cnt, const int* total) { cnt->nContrib = *total; }
+
+__global__ void k_run_heads(const uint32_t* keys, const Counters* cnt, int* flag) {
+  const long long n = cnt->nContrib;
+  GRID_STRIDE(i, n) flag[i] = (i == 0 || keys[i] != keys[i - 1]) ? 1 : 0;
+}
+
+__global__ void k_run_fill(const uint32_t* keys, const Counters* cnt, const int* flag, const int* idx,
+                           int* runStart, uint32_t* runKey) {
+  const long long n = cnt->nContrib;
+  GRID_STRIDE(i, n) {
+    if (!flag[i]) continue;
+    int r = idx[i];
+    runStart[r] = (int)i;
+    runKey[r] = keys[i];
+  }
+}
+
+__global__ void k_run_end(Counters* cnt, const int* total, int* runStart) {
+  cnt->nRuns = *total;
+  runStart[*total] = cnt->nContrib;
+}
+
+// write a value at an interior node and at all its periodic halo mirrors
+__device__ inline void put_mirrored(double* F, const Geom& g, int i, int j, int k, double val) {
+  int ox[2] = {0, 0}, oy[2] = {0, 0}, oz[2] = {0, 0};
+  int nxo = 1, nyo = 1, nzo = 1;
+  if (i <= kHalo) ox[nxo++] = g.n[0];
+  else if (i > g.n[0] - kHalo) ox[nxo++] = -g.n[0];
+  if (j <= kHalo) oy[nyo++] = g.n[1];
+  else if (j > g.n[1] - kHalo) oy[nyo++] = -g.n[1];
+  if (k <= kHalo) oz[nzo++] = g.n[2];
+  else if (k > g.n[2] - kHalo) oz[nzo++] = -g.n[2];
+  for (int c = 0; c < nzo; ++c)
+    for (int b = 0; b < nyo; ++b)
+      for (int a = 0; a < nxo; ++a) F[field_off(g, i + ox[a], j + oy[b], k + oz[c])] = val;
+}
+
+__device__ inline void node_of(const Geom& g, uint32_t key, int& comp, int& i, int& j, int& k) {
+  comp = (int)(key / (uint32_t)g.nint);
+  long long node = (long long)key - (long long)comp * g.nint;
+  i = (int)(node % g.n[0]) + 1;
+  node /= g.n[0];
+  j = (int)(node % g.n[1]) + 1;
+  k = (int)(node / g.n[1]) + 1;
+}
+
+struct Fields {
+  double *u, *v, *w, *u0, *v0, *w0, *fx, *fy, *fz;
+  __device__ double* U(int c) const { return c == 0 ? u : (c == 1 ? v : w); }
+  __device__ double* U0(int c) const { return c == 0 ? u0 : (c == 1 ? v0 : w0); }
+  __device__ double* F(int c) const { return c == 0 ? fx : (c == 1 ? fy : fz); }
+};
+
+// start of FirstOrderForwardEuler's particle side (fluid.F90:255-263): fdrag=0,
+// fx=fy=fz=0; with `frozen`, also restore the fluid where the last spread
+// changed it.
+__global__ void k_mdf_reset(Recs R, Geom g, Counters* cnt, Fields fl, const uint32_t* lastNodes, double* fCur,
+                            int frozen) {
+  const long long nLast = cnt->nLast, nRuns = cnt->nRuns, nl = cnt->npLocal;
+  const long long n = max(nLast, max(nRuns, nl));
+  GRID_STRIDE(t, n) {
+    if (t < nLast) {
+      int comp, i, j, k;
+      node_of(g, lastNodes[t], comp, i, j, k);
+      long long off = field_off(g, i, j, k);
+      fl.F(comp)[off] = 0.0;
+      if (frozen) put_mirrored(fl.U(comp), g, i, j, k, fl.U0(comp)[off]);
+    }
+    if (t < nRuns) fCur[t] = 0.0;
+    if (t < nl) {
+      R.D(D_FDRAG, (int)t) = 0.0;
+      R.D(D_FDRAG + 1, (int)t) = 0.0;
+      R.D(D_FDRAG + 2, (int)t) = 0.0;
+    }
+  }
+}
+
+// UpdateFluidVelocityOnLagrangianPoints (ZJS_VOLUMEFRACTION_DEM.F90:2-36);
+// blockIdx.y is the velocity component.
+template <int UNIT_H>
+__global__ void __launch_bounds__(kBlock) k_interp(Recs R, Geom g, const Counters* cnt, const double* __restrict__ W,
+                                                   const int4* __restrict__ win, Fields fl, double* fv) {
+  int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= cnt->npLocal) return;
+  const int comp = blockIdx.y;
+  const int cap = R.cap;
+  const double* __restrict__ F = fl.U(comp);
+  int sx, sy, sz;
+  window_start(win[m], comp, sx, sy, sz);
+  const double* Wc = W + (size_t)comp * 27 * cap + m;
+  double ulp = 0.0;
+#pragma unroll
+  for (int kz = 0; kz < 3; ++kz)
+#pragma unroll
+    for (int ky = 0; ky < 3; ++ky) {
+      const double* row = F + field_off(g, sx, sy + ky, sz + kz);
+#pragma unroll
+      for (int kx = 0; kx < 3; ++kx) {
+        double t = Wc[(size_t)(kz * 9 + ky * 3 + kx) * cap] * row[kx];
+        if (!UNIT_H) {
+          t = t * g.h[0];
+          t = t * g.h[1];
+          t = t * g.h[2];
+        }
+        ulp = ulp + t;
+      }
+    }
+  const double vp = R.D(D_V + comp, m);
+  R.D(D_VGAP + comp, m) = ulp - vp;
+  const double relaxfactor = 1.0;
+  double fd = R.D(D_FDRAG + comp, m) + relaxfactor * (ulp - vp) / g.dt;
+  R.D(D_FDRAG + comp, m) = fd;
+  fv[(size_t)comp * cap + m] = fd * R.D(D_VOL, m);
+}
+
+// UpdateMomentumSourceTerm (ZJS_VOLUMEFRACTION_DEM.F90:38-67) per touched node;
+// MODE 0: fused with VelocityPostGuess + halo refill, 1: spread only.
+template <int MODE>
+__global__ void __launch_bounds__(kBlock) k_spread(Geom g, const Counters* cnt, const int* __restrict__ runStart,
+                                                   const uint32_t* __restrict__ runKey,
+                                                   const uint32_t* __restrict__ vals, const double* __restrict__ W,
+                                                   const double* __restrict__ fv, const int* __restrict__ imgSrc,
+                                                   int cap, Fields fl, double* fCur, double* fPrev) {
+  const int npLocal = cnt->npLocal;
+  const long long nRuns = cnt->nRuns;
+  GRID_STRIDE(r, nRuns) {
+  int comp, i, j, k;
+  node_of(g, runKey[r], comp, i, j, k);
+  double f = 0.0;
+  const double* fvc = fv + (size_t)comp * cap;
+  for (int e = runStart[r], e1 = runStart[r + 1]; e < e1; ++e) {
+    uint32_t val = vals[e];
+    int p = (int)(val / kSlots);
+    int slot = (int)(val - (uint32_t)p * kSlots);
+    int root = p < npLocal ? p : imgSrc[p - npLocal];
+    f = f - fvc[root] * W[(size_t)slot * cap + p];
+  }
+  long long off = field_off(g, i, j, k);
+  fl.F(comp)[off] = f;
+  if (MODE == 0) {
+    double fo = fCur[r];
+    double* U = fl.U(comp);
+    put_mirrored(U, g, i, j, k, U[off] + g.dt * (f - fo));
+    fCur[r] = f;
+  } else {
+    fPrev[r] = fCur[r];
+    fCur[r] = f;
+  }
+  }
+}
+
+// VelocityPostGuess (fluid.F90:135-153) + halo refill, per touched node
+__global__ void k_post_guess(Geom g, const Counters* cnt, const uint32_t* runKey, Fields fl, const double* fCur,
+                             const double* fPrev) {
+  const long long nRuns = cnt->nRuns;
+  GRID_STRIDE(r, nRuns) {
+    int comp, i, j, k;
+    node_of(g, runKey[r], comp, i, j, k);
+    double* U = fl.U(comp);
+    long long off = field_off(g, i, j, k);
+    put_mirrored(U, g, i, j, k, U[off] + g.dt * (fCur[r] - fPrev[r]));
+  }
+}
+
+__global__ void k_record_written(Counters* cnt, const uint32_t* runKey, uint32_t* lastNodes) {
+  const long long n = cnt->nRuns;
+  GRID_STRIDE(t, n) lastNodes[t] = runKey[t];
+  if (blockIdx.x == 0 && threadIdx.x == 0) cnt->nLast = (int)n;
+}
+
+Fields fields_of(Ctx& c) { return Fields{c.u, c.v, c.w, c.u0, c.v0, c.w0, c.fx, c.fy, c.fz}; }
+
+}  // namespace
+
+void launch_weights(Ctx& c, bool locals) {
+  int n = locals ? c.capLocal : c.capImg;
+  if (n <= 0) return;
+  if (c.g.unit_h)
+    k_weights<1><<<nblocks(n), kBlock, 0, c.stream>>>(c.rec(), c.g, c.dCnt, locals, c.W, c.win, c.cntInt);
+  else
+    k_weights<0><<<nblocks(n), kBlock, 0, c.stream>>>(c.rec(), c.g, c.dCnt, locals, c.W, c.win, c.cntInt);
+  c.launches++;
+}
+
+void build_spread_plan(Ctx& c) {
+  cudaStream_t s = c.stream;
+  scan_exclusive(c.cntInt, c.iTmpA, c.cap, &c.dCnt->np, c.dTotal, c.scanScratch, s, &c.launches);
+  k_set_contrib<<<1, 1, 0, s>>>(c.dCnt, c.dTotal);
+  k_plan_emit<<<nblocks(c.cap), kBlock, 0, s>>>(c.g, c.dCnt, c.win, c.iTmpA, c.kA, c.vA);
+  c.launches += 2;
+  uint32_t *k0 = c.kA, *v0 = c.vA, *k1 = c.kB, *v1 = c.vB;
+  int bits = 1;
+  while ((1ll << bits) < 3 * c.g.nint) ++bits;
+  radix_sort_pairs(k0, v0, k1, v1, c.capContrib, &c.dCnt->nContrib, bits, c.sortHist, c.scanScratch, s,
+                   &c.launches);
+  c.planKeys = k0;
+  c.planVals = v0;
+  // run heads -> touched nodes; the flag/index scratch reuse the other sort pair
+  int* flag = reinterpret_cast<int*>(k1);
+  int* idx = reinterpret_cast<int*>(v1);
+  k_run_heads<<<gs_blocks(c.capContrib), kBlock, 0, s>>>(k0, c.dCnt, flag);
+  scan_exclusive(flag, idx, c.capContrib, &c.dCnt->nContrib, c.dTotal, c.scanScratch, s, &c.launches);
+  k_run_fill<<<gs_blocks(c.capContrib), kBlock, 0, s>>>(k0, c.dCnt, flag, idx, c.runStart, c.runKey);
+  k_run_end<<<1, 1, 0, s>>>(c.dCnt, c.dTotal, c.runStart);
+  c.launches += 3;
+  c.planReady = true;
+  c.spreadValid = false;
+}
+
+void launch_mdf_reset(Ctx& c, bool frozen) {
+  long long n = std::max<long long>(c.capRuns, c.capLocal);
+  k_mdf_reset<<<gs_blocks(n), kBlock, 0, c.stream>>>(c.rec(), c.g, c.dCnt, fields_of(c), c.lastNodes, c.fCur,
+                                                   frozen ? 1 : 0);
+  c.launches++;
+  c.spreadValid = true;
+}
+
+void launch_interp(Ctx& c) {
+  dim3 grid(nblocks(c.capLocal), 3);
+  if (c.g.unit_h)
+    k_interp<1><<<grid, kBlock, 0, c.stream>>>(c.rec(), c.g, c.dCnt, c.W, c.win, fields_of(c), c.fv);
+  else
+    k_interp<0><<<grid, kBlock, 0, c.stream>>>(c.rec(), c.g, c.dCnt, c.W, c.win, fields_of(c), c.fv);
+  c.launches++;
+}
+
+void launch_spread(Ctx& c, bool fused_post_guess) {
+  if (fused_post_guess)
+    k_spread<0><<<gs_blocks(c.capRuns), kBlock, 0, c.stream>>>(c.g, c.dCnt, c.runStart, c.runKey, c.planVals, c.W,
+                                                              c.fv, c.imgSrc, c.cap, fields_of(c), c.fCur, c.fPrev);
+  else
+    k_spread<1><<<gs_blocks(c.capRuns), kBlock, 0, c.stream>>>(c.g, c.dCnt, c.runStart, c.runKey, c.planVals, c.W,
+                                                              c.fv, c.imgSrc, c.cap, fields_of(c), c.fCur, c.fPrev);
+  c.launches++;
+}
+
+void launch_post_guess(Ctx& c) {
+  k_post_guess<<<gs_blocks(c.capRuns), kBlock, 0, c.stream>>>(c.g, c.dCnt, c.runKey, fields_of(c), c.fCur, c.fPrev);
+  c.launches++;
+}
+
+void record_written_nodes(Ctx& c) {
+  k_record_written<<<gs_blocks(c.capRuns), kBlock, 0, c.stream>>>(c.dCnt, c.runKey, c.lastNodes);
+  c.launches++;
+}
+
+}  // namespace ibmdem

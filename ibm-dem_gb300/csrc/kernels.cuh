@@ -1,0 +1,111 @@
+// kernels.cuh — the context that owns the device-resident case state, and the
+// launchers each translation unit provides.
+#pragma once
+#include <string>
+
+#include "common.cuh"
+
+namespace ibmdem {
+
+struct Ctx {
+  ibmdem_params p{};
+  Geom g{};
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err = "ok";
+  long long launches = 0;
+
+  // capacities (records, images, pairs, spread contributions)
+  int capLocal = 0, capImg = 0, cap = 0;
+  long long capPairs = 0, capContrib = 0;
+
+  // parcel records, double-buffered for CompressDEM
+  double* recD[2] = {nullptr, nullptr};
+  int* recI[2] = {nullptr, nullptr};
+  int cur = 0;
+  Recs rec() const { return Recs{recD[cur], recI[cur], cap}; }
+  Recs recAlt() const { return Recs{recD[cur ^ 1], recI[cur ^ 1], cap}; }
+  void swap_recs() { cur ^= 1; }
+
+  int* imgSrc = nullptr;    // [capImg] root local of each image
+  int* imgShift = nullptr;  // [capImg] 2-bit shift code per axis
+  int* cellStart = nullptr; // [ncell+1]
+  int* cellItems = nullptr; // [cap] part indices sorted by cell (stable)
+  int* bodyStart = nullptr; // [nMS+1]
+  int* bodyItems = nullptr; // [capLocal] locals grouped by body (stable)
+
+  // scratch
+  int* iTmpA = nullptr;  // [max(cap, 26*blocks)+]
+  int* iTmpB = nullptr;
+  int* scanScratch = nullptr;
+  int* sortHist = nullptr;
+  int* dTotal = nullptr;
+  uint32_t* kA = nullptr;  // sort buffers [capContrib]
+  uint32_t* vA = nullptr;
+  uint32_t* kB = nullptr;
+  uint32_t* vB = nullptr;
+
+  Counters* dCnt = nullptr;
+  Counters* hCnt = nullptr;  // pinned mirror
+
+  // bodies (MS == MSGlo on one rank)
+  ibmdem_multisphere* dBodies = nullptr;
+  int nMS = 0, capMS = 0;
+  unsigned* bodyR2 = nullptr;  // squared bounding radius (float bits)
+  int* partnerCnt = nullptr;
+  int* partners = nullptr;
+  int maxPartners = 64;
+
+  // contact lists
+  int* activeList = nullptr;  // [capLocal]
+  int* pairCnt = nullptr;     // [capLocal]
+  int* pairStart = nullptr;   // [capLocal+1]
+  int* pairIdx = nullptr;     // [capPairs] 0-based part indices
+
+  // delta weights and the spread plan
+  double* W = nullptr;     // [81*cap]
+  int4* win = nullptr;     // [cap] cell (a,b,c) + shifted-window flags
+  int* cntInt = nullptr;   // [cap] interior contributions per parcel
+  double* fv = nullptr;    // [3*cap] fdrag*vol of locals
+  uint32_t* planVals = nullptr;  // sorted contributions (points into vA/vB)
+  uint32_t* planKeys = nullptr;
+  int* runStart = nullptr;       // [capRuns+1]
+  uint32_t* runKey = nullptr;    // [capRuns]
+  double* fCur = nullptr;        // [capRuns]
+  double* fPrev = nullptr;       // [capRuns]
+  uint32_t* lastNodes = nullptr; // [capRuns] nodes written by the last spread
+  long long capRuns = 0;
+
+  // fluid
+  double *u = nullptr, *v = nullptr, *w = nullptr;
+  double *u0 = nullptr, *v0 = nullptr, *w0 = nullptr;
+  double *fx = nullptr, *fy = nullptr, *fz = nullptr;
+
+  // state flags
+  bool haveFluid = false, haveParcels = false, listsBuilt = false;
+  bool weightsLocal = false, weightsGhost = false, planReady = false;
+  bool spreadValid = false;  // fCur matches the current plan
+};
+
+// lists.cu
+void rebuild_cell_lists(Ctx& c);
+void launch_img_update(Ctx& c);
+// contact.cu
+void rebuild_collision_lists(Ctx& c);
+void launch_collision_force(Ctx& c);
+// ibm.cu
+void launch_weights(Ctx& c, bool locals);
+void build_spread_plan(Ctx& c);
+void launch_mdf_reset(Ctx& c, bool frozen);
+void launch_interp(Ctx& c);
+void launch_spread(Ctx& c, bool fused_post_guess);
+void launch_post_guess(Ctx& c);
+void record_written_nodes(Ctx& c);
+// bodies.cu
+void launch_body_sums(Ctx& c);
+void launch_evolution(Ctx& c);
+void launch_cloud_pre(Ctx& c);
+void launch_cloud_post(Ctx& c);
+void launch_marker_update(Ctx& c, bool reset, bool adjust);
+
+}  // namespace ibmdem

@@ -1,0 +1,208 @@
+"""Python mirror of the reference's particle-side subroutines over the C ABI.
+
+`Case` owns one device-resident case (an `ibmdem_ctx`).  Its methods carry the
+reference's subroutine names (InitializationDEM, RebuildAllListOrNot,
+UpdateFluidVelocityOnLagrangianPoints, ...) and call the CUDA library
+libibmdem.so; there is no CPU fallback: constructing a Case without the built
+library, or without a CUDA device, raises.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from .records import MULTISPHERE, PARAMS, PARCEL, field_shape
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libibmdem.so")
+
+# include/ibmdem.h exports (checked by the symbol test)
+EXPORTS = [
+    "ibmdem_create", "ibmdem_destroy", "ibmdem_last_error", "ibmdem_abi_version", "ibmdem_set_stream",
+    "ibmdem_synchronize", "ibmdem_set_fluid", "ibmdem_get_fluid", "ibmdem_set_parcels", "ibmdem_get_parcels",
+    "ibmdem_set_bodies", "ibmdem_get_bodies", "ibmdem_get_cell_lists", "ibmdem_get_collision_lists",
+    "ibmdem_RebuildAllListOrNot", "ibmdem_UpdateLocalCellWeightListDEM", "ibmdem_UpdateGhostCellWeightListDEM",
+    "ibmdem_UpdateParcelInfoInGhostRegion", "ibmdem_CalculateCollisionForce",
+    "ibmdem_UpdateFluidVelocityOnLagrangianPoints", "ibmdem_UpdateMomentumSourceTerm", "ibmdem_VelocityPostGuess",
+    "ibmdem_AssembleLocalForceMS", "ibmdem_EvolutionMS", "ibmdem_ResetVelocityAndPositionLagrangianPoints",
+    "ibmdem_AdjustParcelPosition", "ibmdem_InitializationDEM", "ibmdem_MultiDirectForcing",
+    "ibmdem_CloudEvolutionStepMS", "ibmdem_CloudEvolutionMS", "ibmdem_step", "ibmdem_launch_count",
+    "ibmdem_get_counters",
+]
+
+SUBROUTINES = [
+    "RebuildAllListOrNot", "UpdateLocalCellWeightListDEM", "UpdateGhostCellWeightListDEM",
+    "UpdateParcelInfoInGhostRegion", "CalculateCollisionForce", "UpdateFluidVelocityOnLagrangianPoints",
+    "UpdateMomentumSourceTerm", "VelocityPostGuess", "AssembleLocalForceMS", "EvolutionMS",
+    "ResetVelocityAndPositionLagrangianPoints", "AdjustParcelPosition", "InitializationDEM", "MultiDirectForcing",
+    "CloudEvolutionStepMS", "CloudEvolutionMS",
+]
+
+_lib = None
+
+
+def load(path=LIB_PATH):
+    """Load libibmdem.so and declare its prototypes; raises if it is missing."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"libibmdem.so not built ({path}); run __graft_entry__.build()")
+    lib = ctypes.CDLL(path)
+    vp, i32, i64 = ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64
+    P = ctypes.POINTER
+    lib.ibmdem_create.argtypes = [vp, i32, P(vp)]
+    lib.ibmdem_destroy.argtypes = [vp]
+    lib.ibmdem_last_error.restype = ctypes.c_char_p
+    lib.ibmdem_last_error.argtypes = [vp]
+    lib.ibmdem_set_stream.argtypes = [vp, vp]
+    lib.ibmdem_synchronize.argtypes = [vp]
+    lib.ibmdem_set_fluid.argtypes = [vp, vp, vp, vp]
+    lib.ibmdem_get_fluid.argtypes = [vp] + [vp] * 6
+    lib.ibmdem_set_parcels.argtypes = [vp, i32, vp]
+    lib.ibmdem_get_parcels.argtypes = [vp, vp, i32, P(i32), P(i32)]
+    lib.ibmdem_set_bodies.argtypes = [vp, i32, vp]
+    lib.ibmdem_get_bodies.argtypes = [vp, vp, i32, P(i32)]
+    lib.ibmdem_get_cell_lists.argtypes = [vp, vp, vp, P(i64), P(i32)]
+    lib.ibmdem_get_collision_lists.argtypes = [vp, vp, vp, P(i32), P(i32)]
+    lib.ibmdem_get_counters.argtypes = [vp, vp, i32]
+    lib.ibmdem_launch_count.restype = i64
+    lib.ibmdem_launch_count.argtypes = [vp]
+    lib.ibmdem_step.argtypes = [vp, i32]
+    for name in SUBROUTINES:
+        getattr(lib, "ibmdem_" + name).argtypes = [vp]
+    _lib = lib
+    return lib
+
+
+class IbmDemError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"[{code}] {msg}")
+        self.code = code
+
+
+class Case:
+    """One single-rank periodic case resident on a GB300."""
+
+    def __init__(self, params, parcels=None, bodies=None, field=None, device=0, stream=None):
+        self.lib = load()
+        self.params = np.array(params, dtype=PARAMS, copy=True)
+        h = ctypes.c_void_p()
+        rc = self.lib.ibmdem_create(self.params.ctypes.data, int(device), ctypes.byref(h))
+        if rc != 0:
+            raise IbmDemError(rc, "ibmdem_create failed (no CUDA device, or unsupported parameters)")
+        self.h = h
+        self.shape = field_shape(self.params)
+        if stream is not None:
+            self.set_stream(stream)
+        if field is not None:
+            self.set_fluid(*field)
+        if bodies is not None:
+            self.set_bodies(bodies)
+        if parcels is not None:
+            self.set_parcels(parcels)
+
+    # -- lifetime --------------------------------------------------------------
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.ibmdem_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _chk(self, rc, what):
+        if rc != 0:
+            raise IbmDemError(rc, f"{what}: {self.lib.ibmdem_last_error(self.h).decode()}")
+
+    def set_stream(self, stream):
+        handle = stream if isinstance(stream, int) else int(getattr(stream, "cuda_stream", stream))
+        self._chk(self.lib.ibmdem_set_stream(self.h, ctypes.c_void_p(handle)), "set_stream")
+
+    def synchronize(self):
+        self._chk(self.lib.ibmdem_synchronize(self.h), "synchronize")
+
+    @property
+    def launches(self):
+        return int(self.lib.ibmdem_launch_count(self.h))
+
+    # -- state -----------------------------------------------------------------
+    def set_fluid(self, u, v, w):
+        a = [np.ascontiguousarray(x, dtype=np.float64).reshape(self.shape) for x in (u, v, w)]
+        self._chk(self.lib.ibmdem_set_fluid(self.h, a[0].ctypes.data, a[1].ctypes.data, a[2].ctypes.data),
+                  "set_fluid")
+
+    def get_fluid(self):
+        out = [np.empty(self.shape) for _ in range(6)]
+        self._chk(self.lib.ibmdem_get_fluid(self.h, *[o.ctypes.data for o in out]), "get_fluid")
+        return out
+
+    def set_parcels(self, parcels):
+        a = np.ascontiguousarray(parcels, dtype=PARCEL)
+        self._chk(self.lib.ibmdem_set_parcels(self.h, len(a), a.ctypes.data), "set_parcels")
+
+    def get_parcels(self):
+        npo, nl = ctypes.c_int32(), ctypes.c_int32()
+        self._chk(self.lib.ibmdem_get_parcels(self.h, None, 0, ctypes.byref(npo), ctypes.byref(nl)), "get_parcels")
+        out = np.zeros(npo.value, PARCEL)
+        self._chk(self.lib.ibmdem_get_parcels(self.h, out.ctypes.data, len(out), ctypes.byref(npo),
+                                              ctypes.byref(nl)), "get_parcels")
+        return out, nl.value
+
+    def set_bodies(self, bodies):
+        a = np.ascontiguousarray(bodies, dtype=MULTISPHERE)
+        self._chk(self.lib.ibmdem_set_bodies(self.h, len(a), a.ctypes.data), "set_bodies")
+
+    def get_bodies(self):
+        n = ctypes.c_int32()
+        self._chk(self.lib.ibmdem_get_bodies(self.h, None, 0, ctypes.byref(n)), "get_bodies")
+        out = np.zeros(n.value, MULTISPHERE)
+        self._chk(self.lib.ibmdem_get_bodies(self.h, out.ctypes.data, n.value, ctypes.byref(n)), "get_bodies")
+        return out
+
+    def get_cell_lists(self):
+        nc, ni = ctypes.c_int64(), ctypes.c_int32()
+        self._chk(self.lib.ibmdem_get_cell_lists(self.h, None, None, ctypes.byref(nc), ctypes.byref(ni)), "cells")
+        start = np.empty(nc.value + 1, np.int32)
+        items = np.empty(ni.value, np.int32)
+        self._chk(self.lib.ibmdem_get_cell_lists(self.h, start.ctypes.data, items.ctypes.data, ctypes.byref(nc),
+                                                 ctypes.byref(ni)), "cells")
+        return start, items
+
+    def get_collision_lists(self):
+        nl, npairs = ctypes.c_int32(), ctypes.c_int32()
+        self._chk(self.lib.ibmdem_get_collision_lists(self.h, None, None, ctypes.byref(nl), ctypes.byref(npairs)),
+                  "pairs")
+        start = np.empty(nl.value + 1, np.int32)
+        idx = np.empty(npairs.value, np.int32)
+        self._chk(self.lib.ibmdem_get_collision_lists(self.h, start.ctypes.data, idx.ctypes.data, ctypes.byref(nl),
+                                                      ctypes.byref(npairs)), "pairs")
+        return start, idx
+
+    def counters(self):
+        out = np.zeros(7, np.int64)
+        self._chk(self.lib.ibmdem_get_counters(self.h, out.ctypes.data, 7), "counters")
+        keys = ["npLocal", "np", "pairs", "nodes_u", "nodes_v", "nodes_w", "contributions"]
+        return dict(zip(keys, (int(x) for x in out)))
+
+    # -- the reference subroutines ----------------------------------------------
+    def call(self, name):
+        self._chk(getattr(self.lib, "ibmdem_" + name)(self.h), name)
+
+    def step(self, n=1):
+        self._chk(self.lib.ibmdem_step(self.h, int(n)), "step")
+
+
+def _make_method(name):
+    def method(self):
+        self.call(name)
+    method.__name__ = name
+    method.__doc__ = f"ibmdem_{name} (the reference subroutine of the same name)."
+    return method
+
+
+for _name in SUBROUTINES:
+    setattr(Case, _name, _make_method(_name))

@@ -182,3 +182,21 @@ class OracleCase:
 
     def step(self, n=1):
         self._chk(self.lib.orc_step(self.h, int(n)), "step")
+
+
+_SUBROUTINES = ("RebuildAllListOrNot", "UpdateLocalCellWeightListDEM", "UpdateGhostCellWeightListDEM",
+                "UpdateParcelInfoInGhostRegion", "CalculateCollisionForce", "UpdateFluidVelocityOnLagrangianPoints",
+                "UpdateMomentumSourceTerm", "VelocityPostGuess", "AssembleLocalForceMS", "EvolutionMS",
+                "ResetVelocityAndPositionLagrangianPoints", "AdjustParcelPosition", "InitializationDEM",
+                "MultiDirectForcing", "CloudEvolutionStepMS", "CloudEvolutionMS")
+
+
+def _make(name):
+    def method(self):
+        self.call(name)
+    method.__name__ = name
+    return method
+
+
+for _n in _SUBROUTINES:
+    setattr(OracleCase, _n, _make(_n))
