@@ -1,0 +1,360 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 IBM-DEM particle hot path.
+
+One step = the particle side of one fluid step on a frozen synthetic fluid
+field: restore the field, 5 multi-direct-forcing iterations (interpolation,
+direct forcing, deterministic spreading, post-guess), the per-body force and
+torque reduction, then one DEM sub-step (contact forces, rigid-body update,
+marker motion, cell/contact/periodic-image list rebuild, delta weights and the
+spread plan).  Metric: particle-steps/s, a particle being one rigid sphere;
+marker-steps/s is reported beside it.
+
+Default workload: a triply periodic 256x256x512 grid (h = 1) with 2048 spheres
+of diameter 12h (452 Fibonacci markers each, 925,696 markers), seeded random
+sequential addition, body velocities N(0, 0.01), and a 64-mode divergence-free
+Fourier field of amplitude 0.05; dt = 1e-3.  The working set (fields, weights,
+spread plan) is several GB, far larger than L2, so no flush is needed between
+steps.
+
+  python bench.py [--gpus N --steps K --warmup W]       this library on the GPU
+  python bench.py --impl reference [...]                 the CPU restatement of the
+                                                         reference on the host cores
+Under torchrun each rank advances its own replica on its own GPU (no data-path
+exchange: the cases are independent), timing is the max over ranks, and rank 0
+prints one JSON line.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "ibm-dem_gb300"))
+
+WORKLOADS = {
+    # name: (nx, ny, nz, bodies, diameter, modes)
+    "resolved-2048-spheres-256x256x512": (256, 256, 512, 2048, 12.0, 64),
+    "resolved-64-spheres-128cube": (128, 128, 128, 64, 16.0, 32),
+}
+DEFAULT_WORKLOAD = "resolved-2048-spheres-256x256x512"
+METRIC = "particle-steps/s (contact+IBM) on 1 GB300, batched vs plain; p50/p99 serve latency"
+FP64_PEAK_GOPS = 504.0  # DFMA/DMUL/DADD issue rate measured on this GB300 pool (profiles/fp64_pipe_probe.md)
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=400)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--e2e-steps", type=int, default=20)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-steps", type=int, default=1)
+    return ap.parse_args()
+
+
+def make_case(workload, seed, field_device):
+    from ibmdem import scenario
+
+    nx, ny, nz, nb, d, modes = WORKLOADS[workload]
+    return scenario.resolved_case(nx, ny, nz, nb, d, seed=seed, n_modes=modes, amp=0.05, vel_std=0.01,
+                                  field_device=field_device)
+
+
+def config_of(workload, nparts):
+    nx, ny, nz, nb, d, modes = WORKLOADS[workload]
+    return {"workload": workload, "grid": [nx, ny, nz], "bodies": nb, "diameter_h": d, "markers": int(nparts),
+            "fourier_modes": modes, "mdf_iterations": 5, "dem_substeps": 1, "dt": 1e-3,
+            "boundary": "triply periodic", "l2": "working set several GB > 129 MB L2 (no flush needed)"}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), "--query-gpu=" + self.Q,
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        self.out = ""
+        if self.p:
+            self.p.terminate()
+            try:
+                self.out, _ = self.p.communicate(timeout=5)
+            except Exception:
+                self.p.kill()
+
+    def summary(self):
+        rows = []
+        for line in (self.out or "").splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) >= 9:
+                rows.append(f)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for n, v in zip(names, r[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": float(rows[0][2]),
+                "reasons": sorted(reasons), "samples": len(rows),
+                "power_w_max": max(float(r[3]) for r in rows if r[3].replace(".", "").isdigit())}
+
+
+def cpu_baseline(case_data, steps):
+    """The CPU restatement of the reference on this host's cores (all threads)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    O.build()
+    threads = os.cpu_count() or 1
+    O.set_threads(threads)
+    p, parts, bodies, field = case_data
+    r = O.OracleCase(p, parts, bodies, field)
+    r.InitializationDEM()
+    t0 = time.perf_counter()
+    r.step(steps)
+    dt = time.perf_counter() - t0
+    nb = len(bodies)
+    r.close()
+    return {"value": nb * steps / dt, "unit": "particle-steps/s", "cores": threads, "kind": "port",
+            "sample": f"{steps} full step(s) of the same {len(parts)}-marker case, OpenMP over the marker loops",
+            "seconds": dt, "marker_steps_per_s": len(parts) * steps / dt}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    O.build()
+    threads = os.cpu_count() or 1
+    O.set_threads(threads)
+    p, parts, bodies, field = make_case(args.workload, args.seed, "cpu")
+    r = O.OracleCase(p, parts, bodies, field)
+    r.InitializationDEM()
+    # bounded sample: one warm-up step, then as many of the requested steps as
+    # fit in about two minutes of host time
+    t0 = time.perf_counter()
+    r.step(min(args.warmup, 1))
+    per = max(time.perf_counter() - t0, 1e-3)
+    k = max(1, min(args.steps, int(120.0 / per)))
+    t0 = time.perf_counter()
+    r.step(k)
+    dt = time.perf_counter() - t0
+    nb = len(bodies)
+    val = nb * k / dt
+    line = {"impl": "reference", "metric": METRIC, "value": val, "unit": "particle-steps/s", "n_gpus": args.gpus,
+            "steps": k, "steps_requested": args.steps, "warmup": min(args.warmup, 1), "ms_per_step": dt / k * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": config_of(args.workload, len(parts)),
+            "cpu_baseline": {"value": val, "unit": "particle-steps/s", "cores": threads, "kind": "port",
+                             "sample": f"{k} full step(s) of the {len(parts)}-marker case (CPU restatement, "
+                                       f"OpenMP over marker loops)"},
+            "e2e": {"value": val, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "marker_steps_per_s": len(parts) * k / dt}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def algorithmic(counters, phases):
+    """Compulsory bytes and FP64 instructions per launch of the main kernels."""
+    M = counters["npLocal"]
+    C = counters["contributions"]
+    U = counters["nodes_u"] + counters["nodes_v"] + counters["nodes_w"]
+    out = {}
+    # interpolation (one launch = one MDF iteration, all 3 components):
+    # 81 weights, window, vol, and per component v, fdrag r/w, vgap w, fdrag*vol w; plus
+    # every touched node read once
+    out["interp"] = {"bytes": M * (81 * 8 + 16 + 8 + 3 * 5 * 8) + 8 * U,
+                     "fp64": M * 3 * (27 * 2 + 12)}
+    # spreading + post-guess: each contribution's index and weight, fdrag*vol of every
+    # parcel once, and per touched node its key, run start, u r/w, f r/w, fx w
+    out["spread"] = {"bytes": C * (4 + 8) + counters["np"] * 24 + U * (4 + 4 + 16 + 16 + 8),
+                     "fp64": C * 2 + U * 3}
+    # delta weights: position, cell, and 81 weights + window written per parcel
+    out["weights"] = {"bytes": counters["np"] * (24 + 4 + 81 * 8 + 16 + 4), "fp64": counters["np"] * 520}
+    return out
+
+
+def run_ours(args):
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    if not torch.cuda.is_available():
+        print(json.dumps({"error": "no CUDA device"}))
+        return 1
+    torch.cuda.set_device(local)
+    from ibmdem import api
+
+    api.load()
+    p, parts, bodies, field = make_case(args.workload, args.seed + rank, "cuda")
+    # CPU baseline on the same case (OpenMP threads in this process; no fork)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline((p, parts, bodies, field), args.cpu_steps)
+    stream = torch.cuda.Stream()
+    case = api.Case(p, parts, bodies, field, device=local, stream=stream)
+    nb, nm = len(bodies), len(parts)
+    case.InitializationDEM()
+    case.step(args.warmup)
+    case.synchronize()
+    counters = case.counters()
+    case.timing(True)
+    case.phase_times(reset=True)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    launches0 = case.launches
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            case.step(1)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    case.synchronize()
+    ms = e0.elapsed_time(e1)
+    launches = case.launches - launches0
+    phases = case.phase_times(reset=True)
+    case.timing(False)
+    t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    ms_max = float(t.item())
+    value = world * nb * args.steps / (ms_max / 1e3)
+
+    # end to end through the C ABI: host field in, fluid + forcing + bodies out
+    shape = case.shape
+    pin = lambda: torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()  # noqa: E731
+    hin = [pin() for _ in range(3)]
+    for a, b in zip(hin, field):
+        a[...] = b
+    hout = [pin() for _ in range(6)]
+    import numpy as np
+    from ibmdem.records import MULTISPHERE
+
+    hb = np.zeros(nb, MULTISPHERE)
+    import ctypes
+
+    def e2e_step():
+        case._chk(case.lib.ibmdem_set_fluid(case.h, *[a.ctypes.data for a in hin]), "set_fluid")
+        case.step(1)
+        case._chk(case.lib.ibmdem_get_fluid(case.h, *[a.ctypes.data for a in hout]), "get_fluid")
+        n = ctypes.c_int32()
+        case._chk(case.lib.ibmdem_get_bodies(case.h, hb.ctypes.data, nb, ctypes.byref(n)), "get_bodies")
+
+    e2e_step()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        e2e_step()
+    e2e_s = time.perf_counter() - t0
+    te = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
+    if world > 1:
+        torch.distributed.all_reduce(te, op=torch.distributed.ReduceOp.MAX)
+    e2e_val = world * nb * args.e2e_steps / float(te.item())
+    fbytes = int(np.prod(shape)) * 8
+
+    if rank == 0:
+        hbm_peak, peak_kind = measured_peaks()
+        alg = algorithmic(counters, phases)
+        per_phase = {}
+        for k, (tot, n) in phases.items():
+            if n:
+                per_phase[k] = {"ms_total": round(tot, 3), "launches": n, "ms_per_launch": tot / n}
+        # dominant kernel: the one with the largest share of the timed region
+        dom = max(("interp", "spread", "weights"), key=lambda k: phases.get(k, (0, 0))[0])
+        tot, n = phases[dom]
+        ms_launch = tot / max(n, 1)
+        achieved = alg[dom]["bytes"] / (ms_launch / 1e3) / 1e9
+        fp64_gops = alg[dom]["fp64"] / (ms_launch / 1e3) / 1e9
+        traffic = None
+        prof = os.path.join(ROOT, "profiles", "traffic.json")
+        if os.path.exists(prof):
+            try:
+                with open(prof) as f:
+                    tr = json.load(f).get(dom)
+                if tr:
+                    traffic = tr["bytes_per_marker"] * counters["npLocal"]
+            except Exception:
+                traffic = None
+        line = {
+            "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": config_of(args.workload, nm),
+            "marker_steps_per_s": world * nm * args.steps / (ms_max / 1e3),
+            "roofline": {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                         "frac": achieved / hbm_peak, "peak_kind": peak_kind, "traffic": traffic,
+                         "algorithmic_bytes_per_launch": alg[dom]["bytes"], "ms_per_launch": ms_launch,
+                         "fp64": {"achieved_gops": fp64_gops, "peak_gops": FP64_PEAK_GOPS,
+                                  "frac": fp64_gops / FP64_PEAK_GOPS,
+                                  "instr_per_launch": alg[dom]["fp64"]}},
+            "phases": per_phase,
+            "e2e": {"value": e2e_val, "unit": "particle-steps/s", "h2d_bytes_per_step": 3 * fbytes,
+                    "d2h_bytes_per_step": 6 * fbytes + nb * MULTISPHERE.itemsize, "steps": args.e2e_steps,
+                    "path": "ibmdem_set_fluid(host u,v,w) + ibmdem_step + ibmdem_get_fluid(u,v,w,fx,fy,fz) + "
+                            "ibmdem_get_bodies, pinned host buffers"},
+            "gpu_launches": launches,
+            "clocks": clk.summary(),
+            "counters": counters,
+        }
+        if cpu is not None:
+            line["cpu_baseline"] = cpu
+        print(json.dumps(line), flush=True)
+    case.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -185,7 +185,73 @@ int launch_status(ibmdem_ctx* h) {
 
 }  // namespace
 
+namespace ibmdem {
+static cudaEvent_t take_event(Ctx& c) {
+  if (!c.evFree.empty()) {
+    cudaEvent_t e = c.evFree.back();
+    c.evFree.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+PhaseScope::PhaseScope(Ctx& ctx, int ph) : c(ctx), phase(ph) {
+  if (!c.timing) return;
+  a = take_event(c);
+  b = take_event(c);
+  cudaEventRecord(a, c.stream);
+}
+PhaseScope::~PhaseScope() {
+  if (!c.timing || !a) return;
+  cudaEventRecord(b, c.stream);
+  c.spans.push_back({phase, a, b});
+}
+static void collect_timing(Ctx& c) {
+  cudaStreamSynchronize(c.stream);
+  for (auto& s : c.spans) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, s.a, s.b) == cudaSuccess) {
+      c.phaseMs[s.phase] += ms;
+      c.phaseCount[s.phase] += 1;
+    }
+    c.evFree.push_back(s.a);
+    c.evFree.push_back(s.b);
+  }
+  c.spans.clear();
+}
+}  // namespace ibmdem
+
+static const char* kPhaseNames[P_COUNT] = {"interp", "spread", "weights", "plan", "cells", "pairs",
+                                           "force", "bodysum", "bodymove", "markers", "images", "reset"};
+
 extern "C" {
+
+int ibmdem_timing_enable(ibmdem_ctx* h, int32_t on) {
+  if (!h) return IBMDEM_EINVAL;
+  h->c.timing = on != 0;
+  return IBMDEM_OK;
+}
+
+const char* ibmdem_phase_name(int32_t i) { return (i >= 0 && i < P_COUNT) ? kPhaseNames[i] : ""; }
+
+int ibmdem_get_timing(ibmdem_ctx* h, double* ms, int64_t* counts, int32_t n, int32_t reset) {
+  if (!h) return IBMDEM_EINVAL;
+  Ctx& c = h->c;
+  cudaSetDevice(c.device);
+  collect_timing(c);
+  for (int i = 0; i < n && i < P_COUNT; ++i) {
+    if (ms) ms[i] = c.phaseMs[i];
+    if (counts) counts[i] = c.phaseCount[i];
+  }
+  if (reset)
+    for (int i = 0; i < P_COUNT; ++i) {
+      c.phaseMs[i] = 0.0;
+      c.phaseCount[i] = 0;
+    }
+  return P_COUNT;
+}
+
 
 int ibmdem_abi_version(void) { return IBMDEM_ABI_VERSION; }
 
@@ -569,7 +635,10 @@ int ibmdem_UpdateFluidVelocityOnLagrangianPoints(ibmdem_ctx* h) {
 static int ensure_plan(ibmdem_ctx* h) {
   Ctx& c = h->c;
   REQUIRE(c.weightsLocal && c.weightsGhost, "weights are not computed");
-  if (!c.planReady) build_spread_plan(c);
+  if (!c.planReady) {
+    PhaseScope t(c, P_PLAN);
+    build_spread_plan(c);
+  }
   return IBMDEM_OK;
 }
 
@@ -634,13 +703,28 @@ static int mdf(ibmdem_ctx* h, bool frozen) {
   REQUIRE(c.haveFluid, "no fluid field");
   int rc = ensure_plan(h);
   if (rc) return rc;
-  launch_mdf_reset(c, frozen);
-  for (int it = 0; it < c.p.Ns; ++it) {
-    launch_interp(c);
-    launch_img_update(c);
-    launch_spread(c, true);
+  {
+    PhaseScope t(c, P_RESET);
+    launch_mdf_reset(c, frozen);
   }
-  record_written_nodes(c);
+  for (int it = 0; it < c.p.Ns; ++it) {
+    {
+      PhaseScope t(c, P_INTERP);
+      launch_interp(c);
+    }
+    {
+      PhaseScope t(c, P_IMAGES);
+      launch_img_update(c);
+    }
+    {
+      PhaseScope t(c, P_SPREAD);
+      launch_spread(c, true);
+    }
+  }
+  {
+    PhaseScope t(c, P_RESET);
+    record_written_nodes(c);
+  }
   return launch_status(h);
 }
 
@@ -653,17 +737,17 @@ int ibmdem_CloudEvolutionStepMS(ibmdem_ctx* h) {
   CHECK_CTX();
   Ctx& c = h->c;
   REQUIRE(c.listsBuilt && c.weightsLocal && c.weightsGhost, "lists and weights are not built");
-  launch_collision_force(c);
-  launch_body_sums(c);
-  launch_evolution(c);
-  launch_marker_update(c, true, true);
-  launch_img_update(c);
-  rebuild_cell_lists(c);
-  rebuild_collision_lists(c);
-  launch_weights(c, true);
-  launch_img_update(c);
-  launch_weights(c, false);
-  build_spread_plan(c);
+  { PhaseScope t(c, P_FORCE); launch_collision_force(c); }
+  { PhaseScope t(c, P_BODYSUM); launch_body_sums(c); }
+  { PhaseScope t(c, P_BODYMOVE); launch_evolution(c); }
+  { PhaseScope t(c, P_MARKERS); launch_marker_update(c, true, true); }
+  { PhaseScope t(c, P_IMAGES); launch_img_update(c); }
+  { PhaseScope t(c, P_CELLS); rebuild_cell_lists(c); }
+  { PhaseScope t(c, P_PAIRS); rebuild_collision_lists(c); }
+  { PhaseScope t(c, P_WEIGHTS); launch_weights(c, true); }
+  { PhaseScope t(c, P_IMAGES); launch_img_update(c); }
+  { PhaseScope t(c, P_WEIGHTS); launch_weights(c, false); }
+  { PhaseScope t(c, P_PLAN); build_spread_plan(c); }
   c.listsBuilt = c.weightsLocal = c.weightsGhost = true;
   return launch_status(h);
 }
@@ -672,9 +756,9 @@ int ibmdem_CloudEvolutionMS(ibmdem_ctx* h) {
   CHECK_CTX();
   Ctx& c = h->c;
   REQUIRE(c.listsBuilt, "lists are not built");
-  launch_cloud_pre(c);
-  launch_body_sums(c);
-  launch_cloud_post(c);
+  { PhaseScope t(c, P_BODYMOVE); launch_cloud_pre(c); }
+  { PhaseScope t(c, P_BODYSUM); launch_body_sums(c); }
+  { PhaseScope t(c, P_BODYMOVE); launch_cloud_post(c); }
   for (int s = 0; s < c.p.coupleInterval; ++s) {
     int rc = ibmdem_CloudEvolutionStepMS(h);
     if (rc) return rc;

@@ -2,6 +2,7 @@
 // launchers each translation unit provides.
 #pragma once
 #include <string>
+#include <vector>
 
 #include "common.cuh"
 
@@ -81,10 +82,35 @@ struct Ctx {
   double *u0 = nullptr, *v0 = nullptr, *w0 = nullptr;
   double *fx = nullptr, *fy = nullptr, *fz = nullptr;
 
+  // per-phase CUDA-event timing (ibmdem_timing_enable)
+  bool timing = false;
+  struct Span {
+    int phase;
+    cudaEvent_t a, b;
+  };
+  std::vector<Span> spans;
+  std::vector<cudaEvent_t> evFree;
+  double phaseMs[32] = {};
+  long long phaseCount[32] = {};
+
   // state flags
   bool haveFluid = false, haveParcels = false, listsBuilt = false;
   bool weightsLocal = false, weightsGhost = false, planReady = false;
   bool spreadValid = false;  // fCur matches the current plan
+};
+
+// timed phases (names in api.cu: ibmdem_phase_name)
+enum Phase : int {
+  P_INTERP = 0, P_SPREAD, P_WEIGHTS, P_PLAN, P_CELLS, P_PAIRS, P_FORCE, P_BODYSUM, P_BODYMOVE, P_MARKERS,
+  P_IMAGES, P_RESET, P_COUNT
+};
+// records CUDA events around one phase on the context's stream when timing is on
+struct PhaseScope {
+  Ctx& c;
+  int phase;
+  cudaEvent_t a = nullptr, b = nullptr;
+  PhaseScope(Ctx& ctx, int ph);
+  ~PhaseScope();
 };
 
 // lists.cu

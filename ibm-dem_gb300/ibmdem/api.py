@@ -27,7 +27,7 @@ EXPORTS = [
     "ibmdem_AssembleLocalForceMS", "ibmdem_EvolutionMS", "ibmdem_ResetVelocityAndPositionLagrangianPoints",
     "ibmdem_AdjustParcelPosition", "ibmdem_InitializationDEM", "ibmdem_MultiDirectForcing",
     "ibmdem_CloudEvolutionStepMS", "ibmdem_CloudEvolutionMS", "ibmdem_step", "ibmdem_launch_count",
-    "ibmdem_get_counters",
+    "ibmdem_get_counters", "ibmdem_timing_enable", "ibmdem_get_timing", "ibmdem_phase_name",
 ]
 
 SUBROUTINES = [
@@ -69,6 +69,10 @@ def load(path=LIB_PATH):
     lib.ibmdem_launch_count.restype = i64
     lib.ibmdem_launch_count.argtypes = [vp]
     lib.ibmdem_step.argtypes = [vp, i32]
+    lib.ibmdem_timing_enable.argtypes = [vp, i32]
+    lib.ibmdem_get_timing.argtypes = [vp, vp, vp, i32, i32]
+    lib.ibmdem_phase_name.restype = ctypes.c_char_p
+    lib.ibmdem_phase_name.argtypes = [i32]
     for name in SUBROUTINES:
         getattr(lib, "ibmdem_" + name).argtypes = [vp]
     _lib = lib
@@ -187,6 +191,16 @@ class Case:
         self._chk(self.lib.ibmdem_get_counters(self.h, out.ctypes.data, 7), "counters")
         keys = ["npLocal", "np", "pairs", "nodes_u", "nodes_v", "nodes_w", "contributions"]
         return dict(zip(keys, (int(x) for x in out)))
+
+    def timing(self, on=True):
+        self._chk(self.lib.ibmdem_timing_enable(self.h, 1 if on else 0), "timing_enable")
+
+    def phase_times(self, reset=True):
+        """{phase: (total ms, spans)} accumulated since the last reset."""
+        ms = np.zeros(32)
+        cnt = np.zeros(32, np.int64)
+        n = self.lib.ibmdem_get_timing(self.h, ms.ctypes.data, cnt.ctypes.data, 32, 1 if reset else 0)
+        return {self.lib.ibmdem_phase_name(i).decode(): (float(ms[i]), int(cnt[i])) for i in range(n)}
 
     # -- the reference subroutines ----------------------------------------------
     def call(self, name):

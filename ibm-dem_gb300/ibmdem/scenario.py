@@ -137,24 +137,25 @@ def fourier_field(p, n_modes, amp, seed, kmax=4, device="cpu"):
     w = rng.random(n_modes) + 0.5
     w *= amp / w.sum()
     shape = field_shape(p)
-    out = []
     dev = torch.device(device)
-    # face positions: component c is staggered by -h/2 along axis c
+    # plane waves at cell centres; component c sits half a cell lower along axis c,
+    # which is the phase factor exp(-i k_c h/2) on the same wave
+    cen = [(torch.arange(1, n + 1, dtype=torch.float64, device=dev) - 0.5) * h for n in (nx, ny, nz)]
+    accs = [torch.zeros((nz, ny, nx), dtype=torch.float64, device=dev) for _ in range(3)]
+    for m in range(n_modes):
+        k = ks[m]
+        ex = torch.exp(1j * (k[0] * cen[0]))
+        ey = torch.exp(1j * (k[1] * cen[1]))
+        ez = torch.exp(1j * (k[2] * cen[2] + phases[m]))
+        wave = (ez[:, None] * ey[None, :])[:, :, None] * ex[None, None, :]
+        for comp in range(3):
+            coef = complex(w[m] * amps[m][comp]) * complex(np.exp(-0.5j * k[comp] * h))
+            accs[comp] += (coef * wave).real
+        del wave
+    out = []
     for comp in range(3):
-        coords = []
-        for ax, n in enumerate((nx, ny, nz)):
-            idx = torch.arange(1, n + 1, dtype=torch.float64, device=dev)
-            coords.append((idx - 1.0) * h if ax == comp else (idx - 0.5) * h)
-        acc = torch.zeros((nz, ny, nx), dtype=torch.float64, device=dev)
-        for m in range(n_modes):
-            k = ks[m]
-            ex = torch.exp(1j * (k[0] * coords[0]))
-            ey = torch.exp(1j * (k[1] * coords[1]))
-            ez = torch.exp(1j * (k[2] * coords[2]) + 1j * phases[m])
-            plane = (ez[:, None] * ey[None, :])  # (nz, ny)
-            acc += (w[m] * amps[m][comp]) * (plane[:, :, None] * ex[None, None, :]).real
         full = torch.zeros(shape, dtype=torch.float64, device=dev)
-        full[2:-2, 2:-2, 2:-2] = acc
+        full[2:-2, 2:-2, 2:-2] = accs[comp]
         # periodic halo, as FillGhostRegionForFluid leaves it
         iz = (torch.arange(shape[0], device=dev) - 2) % nz + 2
         iy = (torch.arange(shape[1], device=dev) - 2) % ny + 2

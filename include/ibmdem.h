@@ -168,6 +168,14 @@ int ibmdem_CloudEvolutionMS(ibmdem_ctx* ctx);
 int ibmdem_step(ibmdem_ctx* ctx, int32_t nsteps);
 
 /* ---- instrumentation -------------------------------------------------- */
+/* Record CUDA events around every phase of the drivers (interpolation,
+ * spreading, weights, spread plan, cell lists, contact lists, contact force,
+ * body sums, body motion, marker motion, image refresh, resets). */
+int ibmdem_timing_enable(ibmdem_ctx* ctx, int32_t on);
+/* Accumulated milliseconds and span counts per phase (synchronises); returns
+ * the number of phases.  reset != 0 clears the accumulators. */
+int ibmdem_get_timing(ibmdem_ctx* ctx, double* ms, int64_t* counts, int32_t n, int32_t reset);
+const char* ibmdem_phase_name(int32_t i);
 /* Number of kernel launches this context has issued so far. */
 int64_t ibmdem_launch_count(const ibmdem_ctx* ctx);
 /* Counters of the current lists: [0]=npLocal [1]=np [2]=pairs
