@@ -62,7 +62,7 @@ void free_parcel_buffers(Ctx& c) {
   void* ps[] = {c.recD[0], c.recD[1], c.recI[0], c.recI[1], c.imgSrc, c.imgShift, c.cellItems, c.bodyItems,
                 c.iTmpA, c.iTmpB, c.scanScratch, c.sortHist, c.kA, c.vA, c.kB, c.vB, c.activeList, c.pairCnt,
                 c.pairStart, c.pairIdx, c.W, c.win, c.cntInt, c.fv, c.runStart, c.runKey, c.fCur, c.fPrev,
-                c.lastNodes};
+                c.lastNodes, c.touch, c.planRoot, c.planW, c.runCnt, c.planAlloc};
   for (void* p : ps) dfree(p);
   c.recD[0] = c.recD[1] = nullptr;
   c.recI[0] = c.recI[1] = nullptr;
@@ -77,6 +77,11 @@ void free_parcel_buffers(Ctx& c) {
   c.runKey = nullptr;
   c.fCur = c.fPrev = nullptr;
   c.lastNodes = nullptr;
+  c.touch = nullptr;
+  c.planRoot = nullptr;
+  c.planW = nullptr;
+  c.runCnt = nullptr;
+  c.planAlloc = nullptr;
   c.cap = c.capLocal = c.capImg = 0;
 }
 
@@ -102,12 +107,19 @@ int alloc_parcels(ibmdem_ctx* h, int np, long long nimg_est) {
   long long ci = nimg_est + nimg_est / 2 + 4096;
   c.capImg = (int)std::min<long long>(ci, 7ll * c.capLocal + 64);
   c.cap = c.capLocal + c.capImg;
+  // the spread plan packs a parcel index with its 7-bit slot into 32 bits
+  if (c.cap >= (1 << 25)) {
+    c.capImg = (1 << 25) - 1 - c.capLocal;
+    c.cap = c.capLocal + c.capImg;
+  }
   c.capPairs = 4ll * c.capLocal + 65536;
   c.capContrib = (long long)kSlots * c.cap;
-  c.capRuns = c.capContrib;
+  c.capRuns = std::min<long long>(c.capContrib, 3 * c.g.nint);
   long long tmpInts = std::max<long long>(c.cap + 1, 26ll * nblocks(c.capLocal) + 1);
-  long long scanInts = std::max({scan_scratch_ints(c.capContrib), scan_scratch_ints(sort_hist_ints(c.capContrib)),
-                                 scan_scratch_ints(c.g.ncell + 1), scan_scratch_ints(26ll * nblocks(c.capLocal))});
+  long long scanInts = std::max({scan_scratch_ints(c.capRuns + 1), scan_scratch_ints(sort_hist_ints(std::max<long long>(c.cap, c.capRuns))),
+                                 scan_scratch_ints(c.g.ncell + 1), scan_scratch_ints(26ll * nblocks(c.capLocal)),
+                                 scan_scratch_ints(nblocks((3 * c.g.nint + 15) / 16))});
+  tmpInts = std::max<long long>(tmpInts, nblocks((3 * c.g.nint + 15) / 16) + 1);
   CU(dalloc(c.recD[0], (size_t)ND * c.cap));
   CU(dalloc(c.recD[1], (size_t)ND * c.cap));
   CU(dalloc(c.recI[0], (size_t)NI * c.cap));
@@ -119,16 +131,21 @@ int alloc_parcels(ibmdem_ctx* h, int np, long long nimg_est) {
   CU(dalloc(c.iTmpA, tmpInts));
   CU(dalloc(c.iTmpB, tmpInts));
   CU(dalloc(c.scanScratch, scanInts));
-  CU(dalloc(c.sortHist, sort_hist_ints(c.capContrib)));
-  CU(dalloc(c.kA, c.capContrib));
-  CU(dalloc(c.vA, c.capContrib));
-  CU(dalloc(c.kB, c.capContrib));
-  CU(dalloc(c.vB, c.capContrib));
+  CU(dalloc(c.sortHist, sort_hist_ints(std::max<long long>(c.cap, c.capRuns))));
+  CU(dalloc(c.kA, c.cap));
+  CU(dalloc(c.vA, c.cap));
+  CU(dalloc(c.kB, c.cap));
+  CU(dalloc(c.vB, c.cap));
+  CU(dalloc(c.touch, ((3 * c.g.nint + 15) / 16) * 16));
+  CU(dalloc(c.planRoot, c.capContrib));
+  CU(dalloc(c.planW, c.capContrib));
+  CU(dalloc(c.runCnt, c.capRuns));
+  CU(dalloc(c.planAlloc, 1));
   CU(dalloc(c.activeList, c.capLocal));
   CU(dalloc(c.pairCnt, c.capLocal + 1));
   CU(dalloc(c.pairStart, c.capLocal + 1));
   CU(dalloc(c.pairIdx, c.capPairs));
-  CU(dalloc(c.W, (size_t)kSlots * c.cap));
+  CU(dalloc(c.W, (size_t)kWStride * c.cap));
   CU(dalloc(c.win, c.cap));
   CU(dalloc(c.cntInt, c.cap));
   CU(dalloc(c.fv, 3 * (size_t)c.cap));
@@ -160,6 +177,7 @@ int check_device(ibmdem_ctx* h) {
     return set_error(h, IBMDEM_ECAPACITY, "contact pairs exceed capacity %lld (%d)", c.capPairs, info);
   if (e & E_PARTNER) return set_error(h, IBMDEM_ECAPACITY, "body %d has more than %d near bodies", info, c.maxPartners);
   if (e & E_WINDOW) return set_error(h, IBMDEM_EUNSUPPORTED, "parcel %d needs a 4-node delta window", info);
+  if (e & E_HITS) return set_error(h, IBMDEM_ECAPACITY, "grid node %d receives more than 32 contributions", info);
   if (e & E_MSIDX) return set_error(h, IBMDEM_EINVAL, "parcel %d has a body index outside 1..nMS", info);
   return set_error(h, IBMDEM_ECUDA, "device error bits 0x%x", e);
 }
@@ -396,7 +414,7 @@ int ibmdem_get_fluid(ibmdem_ctx* h, double* u, double* v, double* w, double* fx,
 int ibmdem_set_parcels(ibmdem_ctx* h, int32_t np, const ibmdem_parcel* parts) {
   CHECK_CTX();
   if (np < 0 || (np > 0 && !parts)) return set_error(h, IBMDEM_EINVAL, "bad parcel array");
-  if ((long long)np * kSlots >= (1ll << 32)) return set_error(h, IBMDEM_EUNSUPPORTED, "too many parcels");
+  if (np >= (1 << 24)) return set_error(h, IBMDEM_EUNSUPPORTED, "too many parcels");
   Ctx& c = h->c;
   CU(cudaStreamSynchronize(c.stream));
   long long nimg = count_images(c.g, np, parts);

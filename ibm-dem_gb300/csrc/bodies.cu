@@ -3,8 +3,9 @@
 // AssembleLocalForceMS (ZJS_MS_DEM.F90:494-519) sums, per body and in part
 // order, fdrag*vol*rhof, fcol, (x-X) x (fdrag*vol) and (x-X) x fcol.  Every
 // body's locals are listed in part order (bodyItems, built with the cell
-// lists), and one thread per (body, component) folds them sequentially, so the
-// sums are bit-identical to the reference's serial loop.
+// lists); a warp per body forms the per-parcel terms in parallel and folds
+// each of the 12 sums sequentially in that order, so the sums are
+// bit-identical to the reference's serial loop.
 // CloudEvolutionMS / EvolutionMS / ResetVelocityAndPositionLagrangianPoints /
 // AdjustParcelPosition follow couplesolverCylinder.F90:2-74,189-217 and
 // ZJS_EVOLUTION_DEM.F90:121-150 statement by statement.
@@ -20,33 +21,59 @@ namespace ibmdem {
 
 namespace {
 
-__global__ void k_body_sums(Recs R, Geom g, ibmdem_multisphere* B, int nMS, const int* bodyStart,
-                            const int* bodyItems) {
-  int b = blockIdx.x * blockDim.x + threadIdx.x;
+// One warp per body.  The 32 lanes evaluate the per-parcel terms of a batch of
+// 32 parcels in parallel (each term is formed exactly as in the reference);
+// lanes 0..11 then fold one sum component each over the batch in part order.
+constexpr int kSumWarps = 8;
+__global__ void __launch_bounds__(kSumWarps * 32) k_body_sums(Recs R, Geom g, ibmdem_multisphere* B, int nMS,
+                                                              const int* __restrict__ bodyStart,
+                                                              const int* __restrict__ bodyItems) {
+  __shared__ double term[kSumWarps][32][13];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int b = blockIdx.x * kSumWarps + warp;
   if (b >= nMS) return;
-  const int k = blockIdx.y;  // component
-  const int k1 = (k + 1) % 3, k2 = (k + 2) % 3;
-  const double X1 = B[b].x[k1], X2 = B[b].x[k2];
+  const double X[3] = {B[b].x[0], B[b].x[1], B[b].x[2]};
   const double rhof = g.rhof;
-  double fd = 0.0, fc = 0.0, mom = 0.0, momc = 0.0;
-  for (int q = bodyStart[b], q1 = bodyStart[b + 1]; q < q1; ++q) {
-    int m = bodyItems[q];
-    const double vol = R.D(D_VOL, m);
-    fd = fd + R.D(D_FDRAG + k, m) * vol * rhof;
-    fc = fc + R.D(D_FCOL + k, m);
-    const double x1 = R.D(D_X + k1, m), x2 = R.D(D_X + k2, m);
-    const double r1 = x1 - body_ref(g, k1, x1, X1);
-    const double r2 = x2 - body_ref(g, k2, x2, X2);
-    const double fv1 = R.D(D_FDRAG + k1, m) * vol;
-    const double fv2 = R.D(D_FDRAG + k2, m) * vol;
-    // CrossMultiplication (ZJS_AUXILIARY_DEM.F90:20-30), component k
-    mom = mom + (r1 * fv2 - r2 * fv1);
-    momc = momc + (r1 * R.D(D_FCOL + k2, m) - r2 * R.D(D_FCOL + k1, m));
+  double acc = 0.0;  // lane L < 12 owns sum L: fdrag[0..2], fcol[0..2], fmom[0..2], fmomCol[0..2]
+  const int q0 = bodyStart[b], q1 = bodyStart[b + 1];
+  for (int base = q0; base < q1; base += 32) {
+    const int q = base + lane;
+    if (q < q1) {
+      const int m = bodyItems[q];
+      const double vol = R.D(D_VOL, m);
+      double fd[3], fc[3], rpc[3], fv[3];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        fd[k] = R.D(D_FDRAG + k, m);
+        fc[k] = R.D(D_FCOL + k, m);
+        const double x = R.D(D_X + k, m);
+        rpc[k] = x - body_ref(g, k, x, X[k]);
+        fv[k] = fd[k] * vol;
+      }
+      double* t = term[warp][lane];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        t[k] = fd[k] * vol * rhof;
+        t[3 + k] = fc[k];
+      }
+      // CrossMultiplication (ZJS_AUXILIARY_DEM.F90:20-30)
+      t[6] = rpc[1] * fv[2] - rpc[2] * fv[1];
+      t[7] = -rpc[0] * fv[2] + rpc[2] * fv[0];
+      t[8] = rpc[0] * fv[1] - rpc[1] * fv[0];
+      t[9] = rpc[1] * fc[2] - rpc[2] * fc[1];
+      t[10] = -rpc[0] * fc[2] + rpc[2] * fc[0];
+      t[11] = rpc[0] * fc[1] - rpc[1] * fc[0];
+    }
+    __syncwarp();
+    const int n = min(32, q1 - base);
+    if (lane < 12)
+      for (int j = 0; j < n; ++j) acc = acc + term[warp][j][lane];
+    __syncwarp();
   }
-  B[b].fdrag[k] = fd;
-  B[b].fcol[k] = fc;
-  B[b].fmom[k] = mom;
-  B[b].fmomCol[k] = momc;
+  if (lane < 3) B[b].fdrag[lane] = acc;
+  else if (lane < 6) B[b].fcol[lane - 3] = acc;
+  else if (lane < 9) B[b].fmom[lane - 6] = acc;
+  else if (lane < 12) B[b].fmomCol[lane - 9] = acc;
 }
 
 // CloudEvolutionMS before AssembleForceMS (couplesolverCylinder.F90:194-204)
@@ -178,8 +205,8 @@ __global__ void k_marker_update(Recs R, Geom g, const Counters* cnt, const ibmde
 
 void launch_body_sums(Ctx& c) {
   if (c.nMS <= 0) return;
-  dim3 grid(nblocks(c.nMS, 64), 3);
-  k_body_sums<<<grid, 64, 0, c.stream>>>(c.rec(), c.g, c.dBodies, c.nMS, c.bodyStart, c.bodyItems);
+  k_body_sums<<<nblocks(c.nMS, kSumWarps), kSumWarps * 32, 0, c.stream>>>(c.rec(), c.g, c.dBodies, c.nMS,
+                                                                           c.bodyStart, c.bodyItems);
   c.launches++;
 }
 

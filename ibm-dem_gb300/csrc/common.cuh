@@ -6,8 +6,8 @@
 //             part(i+1): locals first (0..npLocal), then periodic images.
 //   fields    u,v,w,fx,fy,fz in the reference's Fortran layout with the 2-cell
 //             halo: offset = ((k+1)*nj + (j+1))*ni + (i+1) for i in -1..nx+2.
-//   weights   W[slot*cap + i], slot = comp*27 + kz*9 + ky*3 + kx: the 27
-//             non-zero delta weights per component in stencil order.
+//   weights   W[i*84 + comp*28 + kz*9 + ky*3 + kx]: the 27 non-zero delta
+//             weights per component in stencil order, 28-double aligned rows.
 //   plan      the spread order: (node, contribution) pairs sorted by node with
 //             the reference's part order inside each node.
 // All FP64 arithmetic on the parity path is compiled with -fmad=false and keeps
@@ -23,6 +23,7 @@ namespace ibmdem {
 
 constexpr int kHalo = 2;
 constexpr int kSlots = 81;  // 3 components x 27 nodes
+constexpr int kWStride = 84;  // doubles of W per parcel: 3 x (27 weights + 1 pad), 32-byte aligned rows
 constexpr int kBlock = 256;
 
 // double fields of a parcel record
@@ -41,6 +42,7 @@ enum : int {
   E_WINDOW = 8,    // a delta stencil needed 4 nodes on one axis
   E_MSIDX = 16,    // parcel body index out of range
   E_PARTNER = 32,  // body partner list overflow
+  E_HITS = 64,     // more than 32 contributions to one grid node
 };
 
 struct Geom {

@@ -66,10 +66,10 @@ __global__ void __launch_bounds__(kBlock) k_weights(Recs R, Geom g, Counters* cn
     if (r0 < 1.5 && r3 < 1.5) set_err(cnt, E_WINDOW, e);
     flags |= st << d;
 #pragma unroll
-    for (int q = 0; q < 3; ++q) ws[d][q] = delta1<UNIT_H>(dl[st + q] + g.halfh[d], h);
+    for (int q = 0; q < 3; ++q) ws[d][q] = delta1<UNIT_H>((st ? dl[q + 1] : dl[q]) + g.halfh[d], h);
   }
-  const int cap = R.cap;
   int total = 0;
+  double4_32a* out = reinterpret_cast<double4_32a*>(W + (size_t)e * kWStride);
 #pragma unroll
   for (int comp = 0; comp < 3; ++comp) {
     int cntAx[3];
@@ -80,6 +80,7 @@ __global__ void __launch_bounds__(kBlock) k_weights(Recs R, Geom g, Counters* cn
       cntAx[d] = hi >= lo ? hi - lo + 1 : 0;
     }
     total += cntAx[0] * cntAx[1] * cntAx[2];
+    double wc[28];
 #pragma unroll
     for (int ky = 0; ky < 3; ++ky)
 #pragma unroll
@@ -92,9 +93,12 @@ __global__ void __launch_bounds__(kBlock) k_weights(Recs R, Geom g, Counters* cn
           double w3 = comp == 2 ? ws[2][kz] : wu[2][kz];
           double wt = w12 * w3;
           if (!UNIT_H) wt = wt / g.hprod;
-          W[(size_t)(comp * 27 + kz * 9 + ky * 3 + kx) * cap + e] = wt;
+          wc[kz * 9 + ky * 3 + kx] = wt;
         }
       }
+    wc[27] = 0.0;
+#pragma unroll
+    for (int q = 0; q < 7; ++q) out[comp * 7 + q] = make_double4_32a(wc[4 * q], wc[4 * q + 1], wc[4 * q + 2], wc[4 * q + 3]);
   }
   win[e] = make_int4(a[0], a[1], a[2], flags);
   cntInt[e] = total;
@@ -106,12 +110,22 @@ __device__ inline void window_start(const int4& wn, int comp, int& sx, int& sy, 
   sz = wn.z - 1 + (comp == 2 ? ((wn.w >> 2) & 1) : 0);
 }
 
-__global__ void k_plan_emit(Geom g, const Counters* cnt, const int4* win, const int* off, uint32_t* keys,
-                            uint32_t* vals) {
+// ---- spread plan -------------------------------------------------------------
+// A node (component c, interior (i,j,k)) receives from every parcel whose
+// c-window covers it.  Windows start at cell-1 on the unshifted axes and at
+// cell-1 or cell on the shifted axis, so the candidates live in a 4x3x3 block
+// of cells (4 along axis c).  The cell lists hold each cell's parcels in part
+// order; the hits are merged into part order by a branch-free insertion into a
+// register-resident sorted list.  Each plan
+// entry keeps the contributing root parcel (images share their source's
+// fdrag*vol) and its weight, so spreading streams the plan sequentially.
+constexpr int kMaxHits = 32;
+
+// mark the interior nodes touched by any parcel window
+__global__ void k_touch(Geom g, const Counters* cnt, const int4* win, uint8_t* flags) {
   int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= cnt->np) return;
   int4 wn = win[e];
-  int o = off[e];
   for (int comp = 0; comp < 3; ++comp) {
     int sx, sy, sz;
     window_start(wn, comp, sx, sy, sz);
@@ -121,34 +135,134 @@ __global__ void k_plan_emit(Geom g, const Counters* cnt, const int4* win, const 
           int i = sx + kx, j = sy + ky, k = sz + kz;
           if (!interior(g, i, j, k)) continue;
           long long node = ((long long)(k - 1) * g.n[1] + (j - 1)) * g.n[0] + (i - 1);
-          keys[o] = (uint32_t)(comp * g.nint + node);
-          vals[o] = (uint32_t)(e * kSlots + comp * 27 + kz * 9 + ky * 3 + kx);
-          ++o;
+          flags[comp * g.nint + node] = 1;
         }
   }
 }
 
-__global__ void k_set_contrib(Counters* cnt, const int* total) { cnt->nContrib = *total; }
-
-__global__ void k_run_heads(const uint32_t* keys, const Counters* cnt, int* flag) {
-  const long long n = cnt->nContrib;
-  GRID_STRIDE(i, n) flag[i] = (i == 0 || keys[i] != keys[i - 1]) ? 1 : 0;
+// compaction of the byte flags into the sorted node-key list (16 flags per thread)
+__device__ inline int nz_bytes(uint32_t w) {
+  return ((w & 0xffu) != 0) + ((w & 0xff00u) != 0) + ((w & 0xff0000u) != 0) + ((w & 0xff000000u) != 0);
 }
-
-__global__ void k_run_fill(const uint32_t* keys, const Counters* cnt, const int* flag, const int* idx,
-                           int* runStart, uint32_t* runKey) {
-  const long long n = cnt->nContrib;
-  GRID_STRIDE(i, n) {
-    if (!flag[i]) continue;
-    int r = idx[i];
-    runStart[r] = (int)i;
-    runKey[r] = keys[i];
+__global__ void k_flag_count(const uint4* flags, long long nvec, int* blockCnt) {
+  __shared__ int sh[kBlock / 32];
+  long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  int c = 0;
+  if (v < nvec) {
+    uint4 q = flags[v];
+    c = nz_bytes(q.x) + nz_bytes(q.y) + nz_bytes(q.z) + nz_bytes(q.w);
+  }
+  for (int o = 16; o; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = c;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int t = 0;
+    for (int w = 0; w < kBlock / 32; ++w) t += sh[w];
+    blockCnt[blockIdx.x] = t;
+  }
+}
+__global__ void k_flag_emit(const uint4* flags, long long nvec, long long nflags, const int* blockOff,
+                            uint32_t* keys) {
+  __shared__ int sh[kBlock / 32];
+  long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  uint32_t w4[4] = {0, 0, 0, 0};
+  if (v < nvec) {
+    uint4 q = flags[v];
+    w4[0] = q.x; w4[1] = q.y; w4[2] = q.z; w4[3] = q.w;
+  }
+  int c = nz_bytes(w4[0]) + nz_bytes(w4[1]) + nz_bytes(w4[2]) + nz_bytes(w4[3]);
+  // exclusive prefix of c over the block
+  int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int x = c;
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) sh[warp] = x;
+  __syncthreads();
+  int base = blockOff[blockIdx.x];
+  for (int w = 0; w < warp; ++w) base += sh[w];
+  int pos = base + x - c;
+  long long f0 = v * 16;
+  for (int q = 0; q < 16; ++q) {
+    uint32_t byte = (w4[q >> 2] >> (8 * (q & 3))) & 0xffu;
+    if (byte && f0 + q < nflags) keys[pos++] = (uint32_t)(f0 + q);
   }
 }
 
-__global__ void k_run_end(Counters* cnt, const int* total, int* runStart) {
-  cnt->nRuns = *total;
-  runStart[*total] = cnt->nContrib;
+__global__ void k_set_runs(Counters* cnt, const int* total) { cnt->nRuns = *total; }
+__global__ void k_set_contrib(Counters* cnt, const int* total, int* runStart) {
+  cnt->nContrib = *total;
+  runStart[cnt->nRuns] = *total;
+}
+
+template <bool FILL>
+__global__ void __launch_bounds__(kBlock) k_pull(Geom g, Counters* cnt, const uint32_t* __restrict__ runKey,
+                                                 const int* __restrict__ cellStart,
+                                                 const int* __restrict__ cellItems, const int4* __restrict__ win,
+                                                 const double* __restrict__ W, const int* __restrict__ imgSrc,
+                                                 int cap, int* runCnt, const int* __restrict__ runStart,
+                                                 uint32_t* planRoot, double* planW) {
+  const long long nRuns = cnt->nRuns;
+  const int npLocal = cnt->npLocal;
+  GRID_STRIDE(r, nRuns) {
+    int comp, i, j, k;
+    {
+      uint32_t key = runKey[r];
+      comp = (int)(key / (uint32_t)g.nint);
+      long long node = (long long)key - (long long)comp * g.nint;
+      i = (int)(node % g.n[0]) + 1;
+      node /= g.n[0];
+      j = (int)(node % g.n[1]) + 1;
+      k = (int)(node / g.n[1]) + 1;
+    }
+    const int alo = i - (comp == 0 ? 2 : 1), ahi = i + 1;
+    const int blo = j - (comp == 1 ? 2 : 1), bhi = j + 1;
+    const int clo = k - (comp == 2 ? 2 : 1), chi = k + 1;
+    // hits (p << 7 | slot) kept sorted ascending in registers; unused = ~0u
+    uint32_t hit[kMaxHits];
+    if (FILL) {
+#pragma unroll
+      for (int t = 0; t < kMaxHits; ++t) hit[t] = 0xffffffffu;
+    }
+    int nh = 0;
+    for (int cz = clo; cz <= chi; ++cz)
+      for (int cy = blo; cy <= bhi; ++cy) {
+        int c0 = cell_id(g, alo, cy, cz);
+        int q0 = cellStart[c0 - 1], q1 = cellStart[c0 + (ahi - alo)];
+        for (int q = q0; q < q1; ++q) {
+          int p = cellItems[q];
+          int sx, sy, sz;
+          window_start(win[p], comp, sx, sy, sz);
+          int dx = i - sx, dy = j - sy, dz = k - sz;
+          if ((unsigned)dx > 2u || (unsigned)dy > 2u || (unsigned)dz > 2u) continue;
+          if (FILL) {
+            uint32_t x = ((uint32_t)p << 7) | (uint32_t)(comp * 27 + dz * 9 + dy * 3 + dx);
+#pragma unroll
+            for (int t = kMaxHits - 1; t >= 1; --t) hit[t] = min(hit[t], max(hit[t - 1], x));
+            hit[0] = min(hit[0], x);
+          }
+          ++nh;
+        }
+      }
+    if (!FILL) {
+      runCnt[r] = nh;
+      if (nh > kMaxHits) set_err(cnt, E_HITS, (int)r);
+    } else {
+      const long long o = runStart[r];
+#pragma unroll
+      for (int t = 0; t < kMaxHits; ++t) {
+        if (t < nh) {
+          const int p = (int)(hit[t] >> 7);
+          const int slot = (int)(hit[t] & 127u);
+          const uint32_t root = (uint32_t)(p < npLocal ? p : imgSrc[p - npLocal]);
+          planRoot[o + t] = root | ((uint32_t)comp << 30);
+          const int sc = slot / 27;
+          planW[o + t] = W[(size_t)p * kWStride + sc * 28 + (slot - sc * 27)];
+        }
+      }
+    }
+  }
 }
 
 // write a value at an interior node and at all its periodic halo mirrors
@@ -218,7 +332,16 @@ __global__ void __launch_bounds__(kBlock) k_interp(Recs R, Geom g, const Counter
   const double* __restrict__ F = fl.U(comp);
   int sx, sy, sz;
   window_start(win[m], comp, sx, sy, sz);
-  const double* Wc = W + (size_t)comp * 27 * cap + m;
+  const double4_32a* Wc = reinterpret_cast<const double4_32a*>(W + (size_t)m * kWStride + comp * 28);
+  double wv[28];
+#pragma unroll
+  for (int q = 0; q < 7; ++q) {
+    double4_32a t4 = Wc[q];
+    wv[4 * q] = t4.x;
+    wv[4 * q + 1] = t4.y;
+    wv[4 * q + 2] = t4.z;
+    wv[4 * q + 3] = t4.w;
+  }
   double ulp = 0.0;
 #pragma unroll
   for (int kz = 0; kz < 3; ++kz)
@@ -227,7 +350,7 @@ __global__ void __launch_bounds__(kBlock) k_interp(Recs R, Geom g, const Counter
       const double* row = F + field_off(g, sx, sy + ky, sz + kz);
 #pragma unroll
       for (int kx = 0; kx < 3; ++kx) {
-        double t = Wc[(size_t)(kz * 9 + ky * 3 + kx) * cap] * row[kx];
+        double t = wv[kz * 9 + ky * 3 + kx] * row[kx];
         if (!UNIT_H) {
           t = t * g.h[0];
           t = t * g.h[1];
@@ -246,39 +369,67 @@ __global__ void __launch_bounds__(kBlock) k_interp(Recs R, Geom g, const Counter
 
 // UpdateMomentumSourceTerm (ZJS_VOLUMEFRACTION_DEM.F90:38-67) per touched node;
 // MODE 0: fused with VelocityPostGuess + halo refill, 1: spread only.
+// A warp takes 32 consecutive touched nodes, whose plan entries are contiguous:
+// the lanes form the products (fdrag*vol)*weight of the whole range in
+// parallel from coalesced reads, then each lane folds its own node's products
+// in part order -- the reference's fx = fx - fdrag*vol*weight, term by term.
+constexpr int kSpreadWarps = kBlock / 32;
+constexpr int kSpreadBuf = 512;  // products per warp held in shared memory
+// Touched nodes stay in grid order: neighbouring lanes update neighbouring
+// nodes, which keeps the field and plan accesses local.
 template <int MODE>
 __global__ void __launch_bounds__(kBlock) k_spread(Geom g, const Counters* cnt, const int* __restrict__ runStart,
                                                    const uint32_t* __restrict__ runKey,
-                                                   const uint32_t* __restrict__ vals, const double* __restrict__ W,
-                                                   const double* __restrict__ fv, const int* __restrict__ imgSrc,
+                                                   const uint32_t* __restrict__ planRoot,
+                                                   const double* __restrict__ planW, const double* __restrict__ fv,
                                                    int cap, Fields fl, double* fCur, double* fPrev) {
-  const int npLocal = cnt->npLocal;
+  extern __shared__ double spread_smem[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  double* pw = spread_smem + warp * kSpreadBuf;
   const long long nRuns = cnt->nRuns;
-  GRID_STRIDE(r, nRuns) {
-  int comp, i, j, k;
-  node_of(g, runKey[r], comp, i, j, k);
-  double f = 0.0;
-  const double* fvc = fv + (size_t)comp * cap;
-  for (int e = runStart[r], e1 = runStart[r + 1]; e < e1; ++e) {
-    uint32_t val = vals[e];
-    int p = (int)(val / kSlots);
-    int slot = (int)(val - (uint32_t)p * kSlots);
-    int root = p < npLocal ? p : imgSrc[p - npLocal];
-    f = f - fvc[root] * W[(size_t)slot * cap + p];
-  }
-  long long off = field_off(g, i, j, k);
-  fl.F(comp)[off] = f;
-  if (MODE == 0) {
-    double fo = fCur[r];
-    double* U = fl.U(comp);
-    put_mirrored(U, g, i, j, k, U[off] + g.dt * (f - fo));
-    fCur[r] = f;
-  } else {
-    fPrev[r] = fCur[r];
-    fCur[r] = f;
-  }
+  for (long long r0 = ((long long)blockIdx.x * kSpreadWarps + warp) * 32; r0 < nRuns;
+       r0 += (long long)gridDim.x * kSpreadWarps * 32) {
+    const long long r = r0 + lane;
+    const bool has = r < nRuns;
+    const long long rEnd = min(r0 + 32, nRuns);
+    const int base = runStart[r0], end = runStart[rEnd];
+    const int s = has ? runStart[r] : 0, e = has ? runStart[r + 1] : 0;
+    const bool staged = end - base <= kSpreadBuf;
+    if (staged) {
+      for (int q = lane; q < end - base; q += 32) {
+        uint32_t rc = planRoot[base + q];
+        pw[q] = fv[(size_t)(rc >> 30) * cap + (rc & 0x3fffffffu)] * planW[base + q];
+      }
+    }
+    __syncwarp();
+    if (has) {
+      int comp, i, j, k;
+      node_of(g, runKey[r], comp, i, j, k);
+      double f = 0.0;
+      if (staged) {
+        for (int q = s; q < e; ++q) f = f - pw[q - base];
+      } else {
+        for (int q = s; q < e; ++q) {
+          uint32_t rc = planRoot[q];
+          f = f - fv[(size_t)(rc >> 30) * cap + (rc & 0x3fffffffu)] * planW[q];
+        }
+      }
+      long long off = field_off(g, i, j, k);
+      fl.F(comp)[off] = f;
+      if (MODE == 0) {
+        double fo = fCur[r];
+        double* U = fl.U(comp);
+        put_mirrored(U, g, i, j, k, U[off] + g.dt * (f - fo));
+        fCur[r] = f;
+      } else {
+        fPrev[r] = fCur[r];
+        fCur[r] = f;
+      }
+    }
+    __syncwarp();
   }
 }
+constexpr size_t kSpreadSmem = sizeof(double) * kSpreadBuf * kSpreadWarps;
 
 // VelocityPostGuess (fluid.F90:135-153) + halo refill, per touched node
 __global__ void k_post_guess(Geom g, const Counters* cnt, const uint32_t* runKey, Fields fl, const double* fCur,
@@ -315,25 +466,24 @@ void launch_weights(Ctx& c, bool locals) {
 
 void build_spread_plan(Ctx& c) {
   cudaStream_t s = c.stream;
-  scan_exclusive(c.cntInt, c.iTmpA, c.cap, &c.dCnt->np, c.dTotal, c.scanScratch, s, &c.launches);
-  k_set_contrib<<<1, 1, 0, s>>>(c.dCnt, c.dTotal);
-  k_plan_emit<<<nblocks(c.cap), kBlock, 0, s>>>(c.g, c.dCnt, c.win, c.iTmpA, c.kA, c.vA);
-  c.launches += 2;
-  uint32_t *k0 = c.kA, *v0 = c.vA, *k1 = c.kB, *v1 = c.vB;
-  int bits = 1;
-  while ((1ll << bits) < 3 * c.g.nint) ++bits;
-  radix_sort_pairs(k0, v0, k1, v1, c.capContrib, &c.dCnt->nContrib, bits, c.sortHist, c.scanScratch, s,
-                   &c.launches);
-  c.planKeys = k0;
-  c.planVals = v0;
-  // run heads -> touched nodes; the flag/index scratch reuse the other sort pair
-  int* flag = reinterpret_cast<int*>(k1);
-  int* idx = reinterpret_cast<int*>(v1);
-  k_run_heads<<<gs_blocks(c.capContrib), kBlock, 0, s>>>(k0, c.dCnt, flag);
-  scan_exclusive(flag, idx, c.capContrib, &c.dCnt->nContrib, c.dTotal, c.scanScratch, s, &c.launches);
-  k_run_fill<<<gs_blocks(c.capContrib), kBlock, 0, s>>>(k0, c.dCnt, flag, idx, c.runStart, c.runKey);
-  k_run_end<<<1, 1, 0, s>>>(c.dCnt, c.dTotal, c.runStart);
-  c.launches += 3;
+  const long long nflags = 3 * c.g.nint;
+  const long long nvec = (nflags + 15) / 16;
+  cudaMemsetAsync(c.touch, 0, nvec * 16, s);
+  k_touch<<<nblocks(c.cap), kBlock, 0, s>>>(c.g, c.dCnt, c.win, c.touch);
+  const uint4* fv4 = reinterpret_cast<const uint4*>(c.touch);
+  const long long nb = nblocks(nvec);
+  k_flag_count<<<(unsigned)nb, kBlock, 0, s>>>(fv4, nvec, c.iTmpA);
+  scan_exclusive(c.iTmpA, c.iTmpA, nb, nullptr, c.dTotal, c.scanScratch, s, &c.launches);
+  k_set_runs<<<1, 1, 0, s>>>(c.dCnt, c.dTotal);
+  k_flag_emit<<<(unsigned)nb, kBlock, 0, s>>>(fv4, nvec, nflags, c.iTmpA, c.runKey);
+  k_pull<false><<<gs_blocks(c.capRuns), kBlock, 0, s>>>(c.g, c.dCnt, c.runKey, c.cellStart, c.cellItems, c.win, c.W,
+                                                        c.imgSrc, c.cap, c.runCnt, c.runStart, c.planRoot,
+                                                        c.planW);
+  scan_exclusive(c.runCnt, c.runStart, c.capRuns, &c.dCnt->nRuns, c.dTotal, c.scanScratch, s, &c.launches);
+  k_set_contrib<<<1, 1, 0, s>>>(c.dCnt, c.dTotal, c.runStart);
+  k_pull<true><<<gs_blocks(c.capRuns), kBlock, 0, s>>>(c.g, c.dCnt, c.runKey, c.cellStart, c.cellItems, c.win, c.W,
+                                                       c.imgSrc, c.cap, c.runCnt, c.runStart, c.planRoot, c.planW);
+  c.launches += 7;
   c.planReady = true;
   c.spreadValid = false;
 }
@@ -356,12 +506,14 @@ void launch_interp(Ctx& c) {
 }
 
 void launch_spread(Ctx& c, bool fused_post_guess) {
+  cudaFuncSetAttribute(k_spread<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSpreadSmem);
+  cudaFuncSetAttribute(k_spread<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSpreadSmem);
   if (fused_post_guess)
-    k_spread<0><<<gs_blocks(c.capRuns), kBlock, 0, c.stream>>>(c.g, c.dCnt, c.runStart, c.runKey, c.planVals, c.W,
-                                                              c.fv, c.imgSrc, c.cap, fields_of(c), c.fCur, c.fPrev);
+    k_spread<0><<<gs_blocks(c.capRuns), kBlock, kSpreadSmem, c.stream>>>(c.g, c.dCnt, c.runStart, c.runKey, c.planRoot,
+                                                              c.planW, c.fv, c.cap, fields_of(c), c.fCur, c.fPrev);
   else
-    k_spread<1><<<gs_blocks(c.capRuns), kBlock, 0, c.stream>>>(c.g, c.dCnt, c.runStart, c.runKey, c.planVals, c.W,
-                                                              c.fv, c.imgSrc, c.cap, fields_of(c), c.fCur, c.fPrev);
+    k_spread<1><<<gs_blocks(c.capRuns), kBlock, kSpreadSmem, c.stream>>>(c.g, c.dCnt, c.runStart, c.runKey, c.planRoot,
+                                                              c.planW, c.fv, c.cap, fields_of(c), c.fCur, c.fPrev);
   c.launches++;
 }
 

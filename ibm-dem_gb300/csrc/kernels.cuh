@@ -41,7 +41,7 @@ struct Ctx {
   int* scanScratch = nullptr;
   int* sortHist = nullptr;
   int* dTotal = nullptr;
-  uint32_t* kA = nullptr;  // sort buffers [capContrib]
+  uint32_t* kA = nullptr;  // sort buffers [cap]
   uint32_t* vA = nullptr;
   uint32_t* kB = nullptr;
   uint32_t* vB = nullptr;
@@ -64,12 +64,15 @@ struct Ctx {
   int* pairIdx = nullptr;     // [capPairs] 0-based part indices
 
   // delta weights and the spread plan
-  double* W = nullptr;     // [81*cap]
+  double* W = nullptr;     // [84*cap] marker-major delta weights
   int4* win = nullptr;     // [cap] cell (a,b,c) + shifted-window flags
   int* cntInt = nullptr;   // [cap] interior contributions per parcel
   double* fv = nullptr;    // [3*cap] fdrag*vol of locals
-  uint32_t* planVals = nullptr;  // sorted contributions (points into vA/vB)
-  uint32_t* planKeys = nullptr;
+  uint8_t* touch = nullptr;      // [3*nint rounded to 16] touched-node flags
+  uint32_t* planRoot = nullptr;  // [capContrib] contributing root parcel, node-major, part order
+  double* planW = nullptr;       // [capContrib] its delta weight
+  int* runCnt = nullptr;         // [capRuns] contributions per touched node
+  unsigned long long* planAlloc = nullptr;  // (contributions << 32 | runs) reservation counter
   int* runStart = nullptr;       // [capRuns+1]
   uint32_t* runKey = nullptr;    // [capRuns]
   double* fCur = nullptr;        // [capRuns]
