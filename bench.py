@@ -45,6 +45,19 @@ METRIC = "particle-steps/s (contact+IBM) on 1 GB300, batched vs plain; p50/p99 s
 FP64_PEAK_GOPS = 504.0  # DFMA/DMUL/DADD issue rate measured on this GB300 pool (profiles/fp64_pipe_probe.md)
 
 
+def max_over_ranks(x):
+    """Max of a float over all ranks (the slowest replica sets the job time)."""
+    import torch
+    import torch.distributed as dist
+
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(x)
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def measured_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -257,10 +270,7 @@ def run_ours(args):
     launches = case.launches - launches0
     phases = case.phase_times(reset=True)
     case.timing(False)
-    t = torch.tensor([ms], dtype=torch.float64, device="cuda")
-    if world > 1:
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-    ms_max = float(t.item())
+    ms_max = max_over_ranks(ms)
     value = world * nb * args.steps / (ms_max / 1e3)
 
     # end to end through the C ABI: host field in, fluid + forcing + bodies out
@@ -293,10 +303,7 @@ def run_ours(args):
         for _ in range(args.e2e_steps):
             e2e_step()
         e2e_s = time.perf_counter() - t0
-        te = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
-        if world > 1:
-            torch.distributed.all_reduce(te, op=torch.distributed.ReduceOp.MAX)
-        e2e_val = world * nb * args.e2e_steps / float(te.item())
+        e2e_val = world * nb * args.e2e_steps / max_over_ranks(e2e_s)
     fbytes = int(np.prod(shape)) * 8
 
     if rank == 0:

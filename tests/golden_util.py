@@ -1,0 +1,45 @@
+"""Load the golden fixtures and compare a case (oracle or GPU) against them."""
+import os
+
+import numpy as np
+
+HERE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+NAMES = ("sphere_contact", "cylinders")
+
+
+def load(name):
+    d = np.load(os.path.join(HERE, name + ".npz"))
+    field = [d["in_" + c].astype(np.float64) for c in "uvw"]
+    return d, (d["params"], d["in_parcels"], d["in_bodies"], field)
+
+
+def check(case, d, rtol_bodies):
+    """Run init + 2 steps on `case` and compare with fixture `d`."""
+    case.InitializationDEM()
+    s, i = case.get_cell_lists()
+    assert np.array_equal(s, d["cell_start"]) and np.array_equal(i, d["cell_items"]), "cell lists"
+    s, i = case.get_collision_lists()
+    assert np.array_equal(s, d["pair_start"]) and np.array_equal(i, d["pair_idx"]), "contact lists"
+    pi, nli = case.get_parcels()
+    assert nli == int(d["init_nlocal"])
+    assert np.array_equal(pi["x"], d["init_parcels"]["x"])
+    assert np.array_equal(pi["cellIdx"], d["init_parcels"]["cellIdx"])
+    case.step(2)
+    pp, nl = case.get_parcels()
+    g = d["parcels"]
+    assert nl == int(d["nlocal"]) and len(pp) == len(g)
+    assert np.array_equal(pp["globalIdx"], g["globalIdx"]) and np.array_equal(pp["MSIdx"], g["MSIdx"])
+    for f in ("x", "v", "fcol", "fdrag", "vgap"):
+        a, b = pp[f][:nl], g[f][:nl]
+        scale = max(np.abs(b).max(), 1e-300)
+        assert np.abs(a - b).max() <= rtol_bodies * scale, f
+    gb, b = case.get_bodies(), d["bodies"]
+    for f in ("x", "v", "omega", "AngMom", "fdrag", "fcol", "fmom", "fmomCol", "rotMatGlo"):
+        scale = max(np.abs(b[f]).max(), 1e-300)
+        assert np.abs(gb[f] - b[f]).max() <= rtol_bodies * scale, f
+    fl = case.get_fluid()
+    for name, a in zip(("u", "v", "w", "fx", "fy", "fz"), fl):
+        idx, val = d[name + "_idx"], d[name + "_val"]
+        got = a.ravel()[idx]
+        scale = max(np.abs(val).max(), 1e-300)
+        assert np.abs(got - val).max() <= rtol_bodies * scale, name
