@@ -42,7 +42,12 @@ WORKLOADS = {
 }
 DEFAULT_WORKLOAD = "resolved-2048-spheres-256x256x512"
 METRIC = "particle-steps/s (contact+IBM) on 1 GB300, batched vs plain; p50/p99 serve latency"
-FP64_PEAK_GOPS = 504.0  # DFMA/DMUL/DADD issue rate measured on this GB300 pool (profiles/fp64_pipe_probe.md)
+
+
+# DRAM bytes (read + write) per local marker and launch of the main kernels, from
+# one ncu capture of the 512-sphere 256^3 case (profiles/ncu_ibm_kernels_resolved-512-spheres-256cube.md);
+# the bench workload has the same per-marker structure, so traffic scales with markers.
+DRAM_BYTES_PER_MARKER = {"interp": 1188.0, "spread": 1734.0, "weights": 480.0}
 
 
 def max_over_ranks(x):
@@ -240,6 +245,7 @@ def run_ours(args):
     from ibmdem import api
 
     api.load()
+    fp64_peak = api.fp64_rate(local)
     p, parts, bodies, field = make_case(args.workload, args.seed + rank, "cuda")
     # CPU baseline on the same case (OpenMP threads in this process; no fork)
     cpu = None
@@ -319,16 +325,8 @@ def run_ours(args):
         ms_launch = tot / max(n, 1)
         achieved = alg[dom]["bytes"] / (ms_launch / 1e3) / 1e9
         fp64_gops = alg[dom]["fp64"] / (ms_launch / 1e3) / 1e9
-        traffic = None
-        prof = os.path.join(ROOT, "profiles", "traffic.json")
-        if os.path.exists(prof):
-            try:
-                with open(prof) as f:
-                    tr = json.load(f).get(dom)
-                if tr:
-                    traffic = tr["bytes_per_marker"] * counters["npLocal"]
-            except Exception:
-                traffic = None
+        per_marker = DRAM_BYTES_PER_MARKER.get(dom)
+        traffic = per_marker * counters["npLocal"] if per_marker else None
         line = {
             "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -338,8 +336,9 @@ def run_ours(args):
             "roofline": {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                          "frac": achieved / hbm_peak, "peak_kind": peak_kind, "traffic": traffic,
                          "algorithmic_bytes_per_launch": alg[dom]["bytes"], "ms_per_launch": ms_launch,
-                         "fp64": {"achieved_gops": fp64_gops, "peak_gops": FP64_PEAK_GOPS,
-                                  "frac": fp64_gops / FP64_PEAK_GOPS,
+                         "fp64": {"achieved_gops": fp64_gops, "peak_gops": fp64_peak,
+                                  "peak_kind": "measured live (ibmdem_measure_fp64_rate)",
+                                  "frac": fp64_gops / fp64_peak,
                                   "instr_per_launch": alg[dom]["fp64"]}},
             "phases": per_phase,
             "e2e": {"value": e2e_val, "unit": "particle-steps/s", "h2d_bytes_per_step": 3 * fbytes,

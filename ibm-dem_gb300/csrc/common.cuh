@@ -42,7 +42,6 @@ enum : int {
   E_WINDOW = 8,    // a delta stencil needed 4 nodes on one axis
   E_MSIDX = 16,    // parcel body index out of range
   E_PARTNER = 32,  // body partner list overflow
-  E_HITS = 64,     // more than 32 contributions to one grid node
 };
 
 struct Geom {

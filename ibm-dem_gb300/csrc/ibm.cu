@@ -219,7 +219,11 @@ __global__ void __launch_bounds__(kBlock) k_pull(Geom g, Counters* cnt, const ui
     const int alo = i - (comp == 0 ? 2 : 1), ahi = i + 1;
     const int blo = j - (comp == 1 ? 2 : 1), bhi = j + 1;
     const int clo = k - (comp == 2 ? 2 : 1), chi = k + 1;
-    // hits (p << 7 | slot) kept sorted ascending in registers; unused = ~0u
+    // hits (p << 7 | slot) kept sorted ascending in registers; unused = ~0u.
+    // Nodes with more than kMaxHits contributions (dense or overlapping bodies)
+    // write their hits unsorted into their own plan range and sort it in place.
+    const long long o = FILL ? runStart[r] : 0;
+    const bool wide = FILL && (runStart[r + 1] - runStart[r]) > kMaxHits;
     uint32_t hit[kMaxHits];
     if (FILL) {
 #pragma unroll
@@ -238,18 +242,40 @@ __global__ void __launch_bounds__(kBlock) k_pull(Geom g, Counters* cnt, const ui
           if ((unsigned)dx > 2u || (unsigned)dy > 2u || (unsigned)dz > 2u) continue;
           if (FILL) {
             uint32_t x = ((uint32_t)p << 7) | (uint32_t)(comp * 27 + dz * 9 + dy * 3 + dx);
+            if (wide) {
+              planRoot[o + nh] = x;
+            } else {
 #pragma unroll
-            for (int t = kMaxHits - 1; t >= 1; --t) hit[t] = min(hit[t], max(hit[t - 1], x));
-            hit[0] = min(hit[0], x);
+              for (int t = kMaxHits - 1; t >= 1; --t) hit[t] = min(hit[t], max(hit[t - 1], x));
+              hit[0] = min(hit[0], x);
+            }
           }
           ++nh;
         }
       }
     if (!FILL) {
       runCnt[r] = nh;
-      if (nh > kMaxHits) set_err(cnt, E_HITS, (int)r);
+    } else if (wide) {
+      // in-place insertion sort of the packed hits, then expand to (root, weight)
+      for (int t = 1; t < nh; ++t) {
+        uint32_t x = planRoot[o + t];
+        int at = t;
+        while (at > 0 && planRoot[o + at - 1] > x) {
+          planRoot[o + at] = planRoot[o + at - 1];
+          --at;
+        }
+        planRoot[o + at] = x;
+      }
+      for (int t = 0; t < nh; ++t) {
+        const uint32_t x = planRoot[o + t];
+        const int p = (int)(x >> 7);
+        const int slot = (int)(x & 127u);
+        const uint32_t root = (uint32_t)(p < npLocal ? p : imgSrc[p - npLocal]);
+        planRoot[o + t] = root | ((uint32_t)comp << 30);
+        const int sc = slot / 27;
+        planW[o + t] = W[(size_t)p * kWStride + sc * 28 + (slot - sc * 27)];
+      }
     } else {
-      const long long o = runStart[r];
 #pragma unroll
       for (int t = 0; t < kMaxHits; ++t) {
         if (t < nh) {

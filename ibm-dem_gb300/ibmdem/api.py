@@ -28,6 +28,7 @@ EXPORTS = [
     "ibmdem_AdjustParcelPosition", "ibmdem_InitializationDEM", "ibmdem_MultiDirectForcing",
     "ibmdem_CloudEvolutionStepMS", "ibmdem_CloudEvolutionMS", "ibmdem_step", "ibmdem_launch_count",
     "ibmdem_get_counters", "ibmdem_timing_enable", "ibmdem_get_timing", "ibmdem_phase_name",
+    "ibmdem_measure_fp64_rate",
 ]
 
 SUBROUTINES = [
@@ -73,10 +74,21 @@ def load(path=LIB_PATH):
     lib.ibmdem_get_timing.argtypes = [vp, vp, vp, i32, i32]
     lib.ibmdem_phase_name.restype = ctypes.c_char_p
     lib.ibmdem_phase_name.argtypes = [i32]
+    lib.ibmdem_measure_fp64_rate.argtypes = [i32, P(ctypes.c_double)]
     for name in SUBROUTINES:
         getattr(lib, "ibmdem_" + name).argtypes = [vp]
     _lib = lib
     return lib
+
+
+def fp64_rate(device=0):
+    """Measured FP64 multiply-add rate of the device in G operations/s."""
+    lib = load()
+    g = ctypes.c_double()
+    rc = lib.ibmdem_measure_fp64_rate(int(device), ctypes.byref(g))
+    if rc != 0:
+        raise RuntimeError(f"ibmdem_measure_fp64_rate failed ({rc})")
+    return g.value
 
 
 class IbmDemError(RuntimeError):

