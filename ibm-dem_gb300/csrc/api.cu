@@ -177,6 +177,7 @@ int check_device(ibmdem_ctx* h) {
     return set_error(h, IBMDEM_ECAPACITY, "contact pairs exceed capacity %lld (%d)", c.capPairs, info);
   if (e & E_PARTNER) return set_error(h, IBMDEM_ECAPACITY, "body %d has more than %d near bodies", info, c.maxPartners);
   if (e & E_WINDOW) return set_error(h, IBMDEM_EUNSUPPORTED, "parcel %d needs a 4-node delta window", info);
+  if (e & E_PLANCAP) return set_error(h, IBMDEM_ECAPACITY, "spread plan exceeds capacity %lld", c.capContrib);
   if (e & E_MSIDX) return set_error(h, IBMDEM_EINVAL, "parcel %d has a body index outside 1..nMS", info);
   return set_error(h, IBMDEM_ECUDA, "device error bits 0x%x", e);
 }

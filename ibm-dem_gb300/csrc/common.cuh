@@ -42,6 +42,7 @@ enum : int {
   E_WINDOW = 8,    // a delta stencil needed 4 nodes on one axis
   E_MSIDX = 16,    // parcel body index out of range
   E_PARTNER = 32,  // body partner list overflow
+  E_PLANCAP = 64,  // spread-plan capacity exceeded
 };
 
 struct Geom {

@@ -17,11 +17,8 @@ namespace ibmdem {
 
 namespace {
 
-__device__ inline float min_image_f(float d, float L) {
-  if (d > 0.5f * L) return d - L;
-  if (d < -0.5f * L) return d + L;
-  return d;
-}
+// minimum-image difference (body centres are not wrapped and may drift)
+__device__ inline float min_image_f(float d, float L) { return d - L * rintf(d / L); }
 
 __global__ void k_body_bound(Recs R, Geom g, const Counters* cnt, const ibmdem_multisphere* B, int nMS,
                              unsigned* r2bits) {
@@ -92,45 +89,72 @@ __global__ void k_compact_active(const Counters* cnt, const int* flag, const int
 }
 
 // Collision (ZJS_COLLISION_DEM.F90:2-19) inside the 125-cell scan of
-// RebuildParcelCollisionListDEM; FILL = false counts, true writes.
+// RebuildParcelCollisionListDEM, one warp per candidate parcel: in each round
+// the 32 lanes take 32 consecutive stencil cells (kk, jj, ii order), count
+// their hits, and a warp prefix places them, so the list keeps the reference's
+// order (stencil cell, then the cell's part order).  FILL = false counts.
 template <bool FILL>
 __global__ void k_pair_scan(Recs R, Geom g, const Counters* cnt, const int* activeList, const int* nActive,
                             const int* cellStart, const int* cellItems, int* pairCnt, const int* pairStart,
                             int* pairIdx, long long capPairs, Counters* cntw) {
-  int q = blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= *nActive) return;
-  int ii = activeList[q];
-  int ci, cj, ck;
-  cell_coords(g, R.I(I_CELL, ii), ci, cj, ck);
-  const int msi = R.I(I_MSIDX, ii);
-  const double xi0 = R.D(D_X, ii), xi1 = R.D(D_X + 1, ii), xi2 = R.D(D_X + 2, ii);
-  int count = 0;
-  long long base = FILL ? pairStart[ii] : 0;
-  for (int kk = -2; kk <= 2; ++kk)
-    for (int jj = -2; jj <= 2; ++jj)
-      for (int i2 = -2; i2 <= 2; ++i2) {
-        int a = ci + i2, b = cj + jj, c = ck + kk;
-        if (a < -1 || a > g.n[0] + 2 || b < -1 || b > g.n[1] + 2 || c < -1 || c > g.n[2] + 2) continue;
-        int cell = cell_id(g, a, b, c);
-        int s = cellStart[cell - 1], e = cellStart[cell];
+  const int lane = threadIdx.x & 31;
+  const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+  const int na = *nActive;
+  for (long long q = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < na; q += nw) {
+    const int ii = activeList[q];
+    int ci, cj, ck;
+    cell_coords(g, R.I(I_CELL, ii), ci, cj, ck);
+    const int msi = R.I(I_MSIDX, ii);
+    const double xi0 = R.D(D_X, ii), xi1 = R.D(D_X + 1, ii), xi2 = R.D(D_X + 2, ii);
+    const long long base = FILL ? pairStart[ii] : 0;
+    int total = 0;
+    for (int round = 0; round < 4; ++round) {
+      const int jst = round * 32 + lane;
+      int s = 0, e = 0;
+      if (jst < 125) {
+        const int a = ci + jst % 5 - 2, b = cj + (jst / 5) % 5 - 2, c = ck + jst / 25 - 2;
+        if (a >= -1 && a <= g.n[0] + 2 && b >= -1 && b <= g.n[1] + 2 && c >= -1 && c <= g.n[2] + 2) {
+          const int cell = cell_id(g, a, b, c);
+          s = cellStart[cell - 1];
+          e = cellStart[cell];
+        }
+      }
+      int mine = 0;
+      for (int k = s; k < e; ++k) {
+        const int jjx = cellItems[k];
+        if (R.I(I_MSIDX, jjx) == msi) continue;
+        const double xij1 = xi0 - R.D(D_X, jjx);
+        const double xij2 = xi1 - R.D(D_X + 1, jjx);
+        const double xij3 = xi2 - R.D(D_X + 2, jjx);
+        const double distSqr = xij1 * xij1 + xij2 * xij2 + xij3 * xij3;
+        if (distSqr < g.cut2 && jjx != ii) ++mine;
+      }
+      int x = mine;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+      }
+      if (FILL && mine) {
+        long long at = base + total + x - mine;
         for (int k = s; k < e; ++k) {
-          int jjx = cellItems[k];
+          const int jjx = cellItems[k];
           if (R.I(I_MSIDX, jjx) == msi) continue;
-          double xij1 = xi0 - R.D(D_X, jjx);
-          double xij2 = xi1 - R.D(D_X + 1, jjx);
-          double xij3 = xi2 - R.D(D_X + 2, jjx);
-          double distSqr = xij1 * xij1 + xij2 * xij2 + xij3 * xij3;
+          const double xij1 = xi0 - R.D(D_X, jjx);
+          const double xij2 = xi1 - R.D(D_X + 1, jjx);
+          const double xij3 = xi2 - R.D(D_X + 2, jjx);
+          const double distSqr = xij1 * xij1 + xij2 * xij2 + xij3 * xij3;
           if (distSqr < g.cut2 && jjx != ii) {
-            if (FILL) {
-              long long at = base + count;
-              if (at < capPairs) pairIdx[at] = jjx;
-              else set_err(cntw, E_PAIRCAP, (int)at);
-            }
-            ++count;
+            if (at < capPairs) pairIdx[at] = jjx;
+            else set_err(cntw, E_PAIRCAP, (int)at);
+            ++at;
           }
         }
       }
-  if (!FILL) pairCnt[ii] = count;
+      total += __shfl_sync(0xffffffffu, x, 31);
+    }
+    if (!FILL && lane == 0) pairCnt[ii] = total;
+  }
 }
 
 __global__ void k_set_pair_total(Counters* cnt, const int* total, long long capPairs) {
@@ -208,11 +232,12 @@ void rebuild_collision_lists(Ctx& c) {
   scan_exclusive(c.iTmpA, c.iTmpB, c.capLocal, &c.dCnt->npLocal, &c.dCnt->nActive, c.scanScratch, s, &c.launches);
   k_compact_active<<<nbl, kBlock, 0, s>>>(c.dCnt, c.iTmpA, c.iTmpB, c.activeList);
   cudaMemsetAsync(c.pairCnt, 0, sizeof(int) * (c.capLocal + 1), s);
-  k_pair_scan<false><<<nbl, kBlock, 0, s>>>(c.rec(), c.g, c.dCnt, c.activeList, &c.dCnt->nActive, c.cellStart,
+  const int nbw = gs_blocks(32ll * c.capLocal);
+  k_pair_scan<false><<<nbw, kBlock, 0, s>>>(c.rec(), c.g, c.dCnt, c.activeList, &c.dCnt->nActive, c.cellStart,
                                             c.cellItems, c.pairCnt, nullptr, nullptr, c.capPairs, c.dCnt);
   scan_exclusive(c.pairCnt, c.pairStart, c.capLocal + 1, nullptr, c.dTotal, c.scanScratch, s, &c.launches);
   k_set_pair_total<<<1, 1, 0, s>>>(c.dCnt, c.dTotal, c.capPairs);
-  k_pair_scan<true><<<nbl, kBlock, 0, s>>>(c.rec(), c.g, c.dCnt, c.activeList, &c.dCnt->nActive, c.cellStart,
+  k_pair_scan<true><<<nbw, kBlock, 0, s>>>(c.rec(), c.g, c.dCnt, c.activeList, &c.dCnt->nActive, c.cellStart,
                                            c.cellItems, c.pairCnt, c.pairStart, c.pairIdx, c.capPairs, c.dCnt);
   c.launches += 4;
 }

@@ -27,12 +27,26 @@ namespace ibmdem {
 
 namespace {
 
+// Correctly rounded x/3 with three FP64 operations (Markstein's correction
+// step, P. Markstein, IBM J. Res. Dev. 34(1), 1990): q0 = x*RN(1/3) is within an
+// ulp of x/3, r = x - 3*q0 is exact, and q0 + r*RN(1/3) is within 2^-50 ulp of
+// x/3.  Since x/(3*ulp) always has fractional part 0, 1/3 or 2/3, x/3 is never
+// nearer than ulp/6 to a rounding midpoint, so the final rounding is the
+// correctly rounded quotient for every finite x (tests/test_gpu_division.py
+// compares it with IEEE division).  x/6 = RN(x/3)*0.5 exactly (normal range).
+__device__ inline double div3(double x) {
+  const double c = 0x1.5555555555555p-2;  // RN(1/3)
+  const double q0 = __dmul_rn(x, c);
+  const double r = __fma_rn(-q0, 3.0, x);
+  return __fma_rn(r, c, q0);
+}
+
 // one axis of DeltaFunction3D (interpolation.F90:7-30)
 template <int UNIT_H>
 __device__ inline double delta1(double xcp, double h) {
   double r = fabs(UNIT_H ? xcp : xcp / h);
-  if (r <= 0.5) return (1.0 + sqrt(1.0 - 3.0 * r * r)) / 3.0;
-  if (r <= 1.5) return (5.0 - 3.0 * r - sqrt(1.0 - 3.0 * ((1.0 - r) * (1.0 - r)))) / 6.0;
+  if (r <= 0.5) return div3(1.0 + sqrt(1.0 - 3.0 * r * r));
+  if (r <= 1.5) return div3(5.0 - 3.0 * r - sqrt(1.0 - 3.0 * ((1.0 - r) * (1.0 - r)))) * 0.5;
   return 0.0;
 }
 
@@ -191,104 +205,139 @@ __global__ void k_flag_emit(const uint4* flags, long long nvec, long long nflags
 }
 
 __global__ void k_set_runs(Counters* cnt, const int* total) { cnt->nRuns = *total; }
-__global__ void k_set_contrib(Counters* cnt, const int* total, int* runStart) {
-  cnt->nContrib = *total;
-  runStart[cnt->nRuns] = *total;
+
+// One pass per touched node: scan the candidate cells, keep the hits sorted in
+// registers, then reserve the block's contribution range with one atomic (the
+// 256 nodes of a block own one contiguous range, which the spread relies on)
+// and write (root | comp << 30, weight).  Nodes with more than kMaxHits hits
+// rescan into their own range and sort it in place.
+__device__ inline void node_coords(const Geom& g, uint32_t key, int& comp, int& i, int& j, int& k) {
+  comp = (int)(key / (uint32_t)g.nint);
+  long long node = (long long)key - (long long)comp * g.nint;
+  i = (int)(node % g.n[0]) + 1;
+  node /= g.n[0];
+  j = (int)(node % g.n[1]) + 1;
+  k = (int)(node / g.n[1]) + 1;
 }
 
-template <bool FILL>
-__global__ void __launch_bounds__(kBlock) k_pull(Geom g, Counters* cnt, const uint32_t* __restrict__ runKey,
-                                                 const int* __restrict__ cellStart,
-                                                 const int* __restrict__ cellItems, const int4* __restrict__ win,
-                                                 const double* __restrict__ W, const int* __restrict__ imgSrc,
-                                                 int cap, int* runCnt, const int* __restrict__ runStart,
-                                                 uint32_t* planRoot, double* planW) {
+__global__ void __launch_bounds__(kBlock) k_plan_fill(Geom g, Counters* cnt, const uint32_t* __restrict__ runKey,
+                                                      const int* __restrict__ cellStart,
+                                                      const int* __restrict__ cellItems,
+                                                      const int4* __restrict__ win, const double* __restrict__ W,
+                                                      const int* __restrict__ imgSrc, int* runStart, int* runCnt,
+                                                      uint32_t* planRoot, double* planW,
+                                                      unsigned long long* cursor, long long capContrib) {
+  __shared__ int warpSum[kBlock / 32];
+  __shared__ long long blockBase;
   const long long nRuns = cnt->nRuns;
   const int npLocal = cnt->npLocal;
-  GRID_STRIDE(r, nRuns) {
-    int comp, i, j, k;
-    {
-      uint32_t key = runKey[r];
-      comp = (int)(key / (uint32_t)g.nint);
-      long long node = (long long)key - (long long)comp * g.nint;
-      i = (int)(node % g.n[0]) + 1;
-      node /= g.n[0];
-      j = (int)(node % g.n[1]) + 1;
-      k = (int)(node / g.n[1]) + 1;
-    }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (long long r0 = (long long)blockIdx.x * kBlock; r0 < nRuns; r0 += (long long)gridDim.x * kBlock) {
+    const long long r = r0 + threadIdx.x;
+    const bool has = r < nRuns;
+    int comp = 0, i = 1, j = 1, k = 1;
+    if (has) node_coords(g, runKey[r], comp, i, j, k);
     const int alo = i - (comp == 0 ? 2 : 1), ahi = i + 1;
     const int blo = j - (comp == 1 ? 2 : 1), bhi = j + 1;
     const int clo = k - (comp == 2 ? 2 : 1), chi = k + 1;
-    // hits (p << 7 | slot) kept sorted ascending in registers; unused = ~0u.
-    // Nodes with more than kMaxHits contributions (dense or overlapping bodies)
-    // write their hits unsorted into their own plan range and sort it in place.
-    const long long o = FILL ? runStart[r] : 0;
-    const bool wide = FILL && (runStart[r + 1] - runStart[r]) > kMaxHits;
     uint32_t hit[kMaxHits];
-    if (FILL) {
 #pragma unroll
-      for (int t = 0; t < kMaxHits; ++t) hit[t] = 0xffffffffu;
-    }
+    for (int t = 0; t < kMaxHits; ++t) hit[t] = 0xffffffffu;
     int nh = 0;
-    for (int cz = clo; cz <= chi; ++cz)
-      for (int cy = blo; cy <= bhi; ++cy) {
-        int c0 = cell_id(g, alo, cy, cz);
-        int q0 = cellStart[c0 - 1], q1 = cellStart[c0 + (ahi - alo)];
-        for (int q = q0; q < q1; ++q) {
-          int p = cellItems[q];
-          int sx, sy, sz;
-          window_start(win[p], comp, sx, sy, sz);
-          int dx = i - sx, dy = j - sy, dz = k - sz;
-          if ((unsigned)dx > 2u || (unsigned)dy > 2u || (unsigned)dz > 2u) continue;
-          if (FILL) {
-            uint32_t x = ((uint32_t)p << 7) | (uint32_t)(comp * 27 + dz * 9 + dy * 3 + dx);
-            if (wide) {
-              planRoot[o + nh] = x;
-            } else {
+    if (has)
+      for (int cz = clo; cz <= chi; ++cz)
+        for (int cy = blo; cy <= bhi; ++cy) {
+          const int c0 = cell_id(g, alo, cy, cz);
+          const int q0 = cellStart[c0 - 1], q1 = cellStart[c0 + (ahi - alo)];
+          for (int q = q0; q < q1; ++q) {
+            const int p = cellItems[q];
+            int sx, sy, sz;
+            window_start(win[p], comp, sx, sy, sz);
+            const int dx = i - sx, dy = j - sy, dz = k - sz;
+            if ((unsigned)dx > 2u || (unsigned)dy > 2u || (unsigned)dz > 2u) continue;
+            const uint32_t x = ((uint32_t)p << 7) | (uint32_t)(comp * 27 + dz * 9 + dy * 3 + dx);
 #pragma unroll
-              for (int t = kMaxHits - 1; t >= 1; --t) hit[t] = min(hit[t], max(hit[t - 1], x));
-              hit[0] = min(hit[0], x);
+            for (int t = kMaxHits - 1; t >= 1; --t) hit[t] = min(hit[t], max(hit[t - 1], x));
+            hit[0] = min(hit[0], x);
+            ++nh;
+          }
+        }
+    // block-exclusive prefix of nh and one reservation for the block
+    int x = nh;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) warpSum[warp] = x;
+    __syncthreads();
+    int pre = 0, tot = 0;
+#pragma unroll
+    for (int w = 0; w < kBlock / 32; ++w) {
+      pre += w < warp ? warpSum[w] : 0;
+      tot += warpSum[w];
+    }
+    if (threadIdx.x == 0) blockBase = (long long)atomicAdd(cursor, (unsigned long long)tot);
+    __syncthreads();
+    const long long o = blockBase + pre + x - nh;
+    if (has) {
+      runStart[r] = (int)o;
+      runCnt[r] = nh;
+      if (o + nh > capContrib) {
+        set_err(cnt, E_PLANCAP, (int)r);
+      } else if (nh <= kMaxHits) {
+#pragma unroll
+        for (int t = 0; t < kMaxHits; ++t) {
+          if (t < nh) {
+            const int p = (int)(hit[t] >> 7);
+            const int slot = (int)(hit[t] & 127u);
+            const uint32_t root = (uint32_t)(p < npLocal ? p : imgSrc[p - npLocal]);
+            planRoot[o + t] = root | ((uint32_t)comp << 30);
+            const int sc = slot / 27;
+            planW[o + t] = W[(size_t)p * kWStride + sc * 28 + (slot - sc * 27)];
+          }
+        }
+      } else {
+        int t = 0;
+        for (int cz = clo; cz <= chi; ++cz)
+          for (int cy = blo; cy <= bhi; ++cy) {
+            const int c0 = cell_id(g, alo, cy, cz);
+            const int q0 = cellStart[c0 - 1], q1 = cellStart[c0 + (ahi - alo)];
+            for (int q = q0; q < q1; ++q) {
+              const int p = cellItems[q];
+              int sx, sy, sz;
+              window_start(win[p], comp, sx, sy, sz);
+              const int dx = i - sx, dy = j - sy, dz = k - sz;
+              if ((unsigned)dx > 2u || (unsigned)dy > 2u || (unsigned)dz > 2u) continue;
+              planRoot[o + t++] = ((uint32_t)p << 7) | (uint32_t)(comp * 27 + dz * 9 + dy * 3 + dx);
             }
           }
-          ++nh;
+        for (int a = 1; a < nh; ++a) {
+          const uint32_t v = planRoot[o + a];
+          int at = a;
+          while (at > 0 && planRoot[o + at - 1] > v) {
+            planRoot[o + at] = planRoot[o + at - 1];
+            --at;
+          }
+          planRoot[o + at] = v;
         }
-      }
-    if (!FILL) {
-      runCnt[r] = nh;
-    } else if (wide) {
-      // in-place insertion sort of the packed hits, then expand to (root, weight)
-      for (int t = 1; t < nh; ++t) {
-        uint32_t x = planRoot[o + t];
-        int at = t;
-        while (at > 0 && planRoot[o + at - 1] > x) {
-          planRoot[o + at] = planRoot[o + at - 1];
-          --at;
-        }
-        planRoot[o + at] = x;
-      }
-      for (int t = 0; t < nh; ++t) {
-        const uint32_t x = planRoot[o + t];
-        const int p = (int)(x >> 7);
-        const int slot = (int)(x & 127u);
-        const uint32_t root = (uint32_t)(p < npLocal ? p : imgSrc[p - npLocal]);
-        planRoot[o + t] = root | ((uint32_t)comp << 30);
-        const int sc = slot / 27;
-        planW[o + t] = W[(size_t)p * kWStride + sc * 28 + (slot - sc * 27)];
-      }
-    } else {
-#pragma unroll
-      for (int t = 0; t < kMaxHits; ++t) {
-        if (t < nh) {
-          const int p = (int)(hit[t] >> 7);
-          const int slot = (int)(hit[t] & 127u);
+        for (int a = 0; a < nh; ++a) {
+          const uint32_t v = planRoot[o + a];
+          const int p = (int)(v >> 7);
+          const int slot = (int)(v & 127u);
           const uint32_t root = (uint32_t)(p < npLocal ? p : imgSrc[p - npLocal]);
-          planRoot[o + t] = root | ((uint32_t)comp << 30);
+          planRoot[o + a] = root | ((uint32_t)comp << 30);
           const int sc = slot / 27;
-          planW[o + t] = W[(size_t)p * kWStride + sc * 28 + (slot - sc * 27)];
+          planW[o + a] = W[(size_t)p * kWStride + sc * 28 + (slot - sc * 27)];
         }
       }
     }
+    __syncthreads();
   }
+}
+
+__global__ void k_plan_total(Counters* cnt, const unsigned long long* cursor) {
+  cnt->nContrib = (int)*cursor;
 }
 
 // write a value at an interior node and at all its periodic halo mirrors
@@ -399,63 +448,121 @@ __global__ void __launch_bounds__(kBlock) k_interp(Recs R, Geom g, const Counter
 // the lanes form the products (fdrag*vol)*weight of the whole range in
 // parallel from coalesced reads, then each lane folds its own node's products
 // in part order -- the reference's fx = fx - fdrag*vol*weight, term by term.
-constexpr int kSpreadWarps = kBlock / 32;
-constexpr int kSpreadBuf = 512;  // products per warp held in shared memory
-// Touched nodes stay in grid order: neighbouring lanes update neighbouring
-// nodes, which keeps the field and plan accesses local.
+constexpr int kSpreadBuf = 3072;  // products per block held in shared memory
+constexpr int kLenBins = 64;
+// A block takes 256 consecutive touched nodes (one contiguous plan range).
+// Their products (fdrag*vol)*weight are formed in parallel from coalesced
+// reads; a counting sort by run length then hands nodes of similar length to
+// the same warp, so the FP64 lanes fold in step.  Each thread folds its node in
+// part order -- the reference's fx = fx - fdrag*vol*weight, term by term --
+// then applies the post-guess update with the periodic mirrors (MODE 0) or
+// keeps fx and fxOld for a separate VelocityPostGuess (MODE 1).
 template <int MODE>
 __global__ void __launch_bounds__(kBlock) k_spread(Geom g, const Counters* cnt, const int* __restrict__ runStart,
+                                                   const int* __restrict__ runCnt,
                                                    const uint32_t* __restrict__ runKey,
                                                    const uint32_t* __restrict__ planRoot,
                                                    const double* __restrict__ planW, const double* __restrict__ fv,
                                                    int cap, Fields fl, double* fCur, double* fPrev) {
-  extern __shared__ double spread_smem[];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  double* pw = spread_smem + warp * kSpreadBuf;
+  extern __shared__ double prod[];
+  __shared__ int bins[kLenBins];
+  __shared__ int order[kBlock];
+  __shared__ int sStart[kBlock], sLen[kBlock];
+  __shared__ double fres[kBlock];
   const long long nRuns = cnt->nRuns;
-  for (long long r0 = ((long long)blockIdx.x * kSpreadWarps + warp) * 32; r0 < nRuns;
-       r0 += (long long)gridDim.x * kSpreadWarps * 32) {
-    const long long r = r0 + lane;
-    const bool has = r < nRuns;
-    const long long rEnd = min(r0 + 32, nRuns);
-    const int base = runStart[r0], end = runStart[rEnd];
-    const int s = has ? runStart[r] : 0, e = has ? runStart[r + 1] : 0;
-    const bool staged = end - base <= kSpreadBuf;
-    if (staged) {
-      for (int q = lane; q < end - base; q += 32) {
-        uint32_t rc = planRoot[base + q];
-        pw[q] = fv[(size_t)(rc >> 30) * cap + (rc & 0x3fffffffu)] * planW[base + q];
-      }
-    }
-    __syncwarp();
+  for (long long r0 = (long long)blockIdx.x * kBlock; r0 < nRuns; r0 += (long long)gridDim.x * kBlock) {
+    const long long rLast = min(r0 + kBlock, nRuns) - 1;
+    const int nHere = (int)(rLast - r0 + 1);
+    // this thread's own node: everything its epilogue needs, loaded up front
+    const long long myR = r0 + threadIdx.x;
+    const bool has = (int)threadIdx.x < nHere;
+    int comp = 0, i = 1, j = 1, k = 1, myLen = 0;
+    long long off = 0;
+    double uOld = 0.0, fo = 0.0;
     if (has) {
-      int comp, i, j, k;
-      node_of(g, runKey[r], comp, i, j, k);
+      node_of(g, runKey[myR], comp, i, j, k);
+      off = field_off(g, i, j, k);
+      myLen = runCnt[myR];
+      sStart[threadIdx.x] = runStart[myR];
+      sLen[threadIdx.x] = myLen;
+      fo = fCur[myR];
+      if (MODE == 0) uOld = fl.U(comp)[off];
+    }
+    if (threadIdx.x < kLenBins) bins[threadIdx.x] = 0;
+    __syncthreads();
+    const int base = sStart[0];
+    const int total = sStart[nHere - 1] + sLen[nHere - 1] - base;
+    const bool staged = total <= kSpreadBuf;
+    if (staged)
+      for (int q0 = threadIdx.x; q0 < total; q0 += 4 * kBlock) {
+        // four independent plan loads and gathers in flight per thread
+        uint32_t rc[4];
+        double w[4], a[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int q = q0 + u * kBlock;
+          rc[u] = q < total ? planRoot[base + q] : 0u;
+          w[u] = q < total ? planW[base + q] : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+          a[u] = q0 + u * kBlock < total ? fv[(size_t)(rc[u] >> 30) * cap + (rc[u] & 0x3fffffffu)] : 0.0;
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+          if (q0 + u * kBlock < total) prod[q0 + u * kBlock] = a[u] * w[u];
+      }
+    const int bin = min(myLen, kLenBins - 1);
+    if (has) atomicAdd(&bins[bin], 1);
+    __syncthreads();
+    if (threadIdx.x < 32) {  // exclusive prefix of the 64 bins by one warp
+      int a0 = bins[threadIdx.x], a1 = bins[threadIdx.x + 32];
+      int x0 = a0, x1 = a1;
+      for (int o = 1; o < 32; o <<= 1) {
+        int y0 = __shfl_up_sync(0xffffffffu, x0, o), y1 = __shfl_up_sync(0xffffffffu, x1, o);
+        if (threadIdx.x >= o) {
+          x0 += y0;
+          x1 += y1;
+        }
+      }
+      int t0 = __shfl_sync(0xffffffffu, x0, 31);
+      bins[threadIdx.x] = x0 - a0;
+      bins[threadIdx.x + 32] = t0 + x1 - a1;
+    }
+    __syncthreads();
+    if (has) order[atomicAdd(&bins[bin], 1)] = threadIdx.x;
+    __syncthreads();
+    // fold a node of similar length to the warp's other nodes, in part order
+    if ((int)threadIdx.x < nHere) {
+      const int loc = order[threadIdx.x];
+      const int s0 = sStart[loc] - base, n = sLen[loc];
       double f = 0.0;
       if (staged) {
-        for (int q = s; q < e; ++q) f = f - pw[q - base];
+        for (int q = s0; q < s0 + n; ++q) f = f - prod[q];
       } else {
-        for (int q = s; q < e; ++q) {
-          uint32_t rc = planRoot[q];
+        for (int q = base + s0; q < base + s0 + n; ++q) {
+          const uint32_t rc = planRoot[q];
           f = f - fv[(size_t)(rc >> 30) * cap + (rc & 0x3fffffffu)] * planW[q];
         }
       }
-      long long off = field_off(g, i, j, k);
+      fres[loc] = f;
+    }
+    __syncthreads();
+    if (has) {
+      const double f = fres[threadIdx.x];
       fl.F(comp)[off] = f;
       if (MODE == 0) {
-        double fo = fCur[r];
-        double* U = fl.U(comp);
-        put_mirrored(U, g, i, j, k, U[off] + g.dt * (f - fo));
-        fCur[r] = f;
+        put_mirrored(fl.U(comp), g, i, j, k, uOld + g.dt * (f - fo));
+        fCur[myR] = f;
       } else {
-        fPrev[r] = fCur[r];
-        fCur[r] = f;
+        fPrev[myR] = fo;
+        fCur[myR] = f;
       }
     }
-    __syncwarp();
+    __syncthreads();
   }
 }
-constexpr size_t kSpreadSmem = sizeof(double) * kSpreadBuf * kSpreadWarps;
+constexpr size_t kSpreadSmem = sizeof(double) * kSpreadBuf;
+
 
 // VelocityPostGuess (fluid.F90:135-153) + halo refill, per touched node
 __global__ void k_post_guess(Geom g, const Counters* cnt, const uint32_t* runKey, Fields fl, const double* fCur,
@@ -502,14 +609,12 @@ void build_spread_plan(Ctx& c) {
   scan_exclusive(c.iTmpA, c.iTmpA, nb, nullptr, c.dTotal, c.scanScratch, s, &c.launches);
   k_set_runs<<<1, 1, 0, s>>>(c.dCnt, c.dTotal);
   k_flag_emit<<<(unsigned)nb, kBlock, 0, s>>>(fv4, nvec, nflags, c.iTmpA, c.runKey);
-  k_pull<false><<<gs_blocks(c.capRuns), kBlock, 0, s>>>(c.g, c.dCnt, c.runKey, c.cellStart, c.cellItems, c.win, c.W,
-                                                        c.imgSrc, c.cap, c.runCnt, c.runStart, c.planRoot,
-                                                        c.planW);
-  scan_exclusive(c.runCnt, c.runStart, c.capRuns, &c.dCnt->nRuns, c.dTotal, c.scanScratch, s, &c.launches);
-  k_set_contrib<<<1, 1, 0, s>>>(c.dCnt, c.dTotal, c.runStart);
-  k_pull<true><<<gs_blocks(c.capRuns), kBlock, 0, s>>>(c.g, c.dCnt, c.runKey, c.cellStart, c.cellItems, c.win, c.W,
-                                                       c.imgSrc, c.cap, c.runCnt, c.runStart, c.planRoot, c.planW);
-  c.launches += 7;
+  cudaMemsetAsync(c.planAlloc, 0, sizeof(unsigned long long), s);
+  k_plan_fill<<<gs_blocks(c.capRuns), kBlock, 0, s>>>(c.g, c.dCnt, c.runKey, c.cellStart, c.cellItems, c.win, c.W,
+                                                      c.imgSrc, c.runStart, c.runCnt, c.planRoot, c.planW,
+                                                      c.planAlloc, c.capContrib);
+  k_plan_total<<<1, 1, 0, s>>>(c.dCnt, c.planAlloc);
+  c.launches += 6;
   c.planReady = true;
   c.spreadValid = false;
 }
@@ -535,11 +640,13 @@ void launch_spread(Ctx& c, bool fused_post_guess) {
   cudaFuncSetAttribute(k_spread<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSpreadSmem);
   cudaFuncSetAttribute(k_spread<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSpreadSmem);
   if (fused_post_guess)
-    k_spread<0><<<gs_blocks(c.capRuns), kBlock, kSpreadSmem, c.stream>>>(c.g, c.dCnt, c.runStart, c.runKey, c.planRoot,
-                                                              c.planW, c.fv, c.cap, fields_of(c), c.fCur, c.fPrev);
+    k_spread<0><<<gs_blocks(c.capRuns), kBlock, kSpreadSmem, c.stream>>>(c.g, c.dCnt, c.runStart, c.runCnt, c.runKey,
+                                                              c.planRoot, c.planW, c.fv, c.cap, fields_of(c), c.fCur,
+                                                              c.fPrev);
   else
-    k_spread<1><<<gs_blocks(c.capRuns), kBlock, kSpreadSmem, c.stream>>>(c.g, c.dCnt, c.runStart, c.runKey, c.planRoot,
-                                                              c.planW, c.fv, c.cap, fields_of(c), c.fCur, c.fPrev);
+    k_spread<1><<<gs_blocks(c.capRuns), kBlock, kSpreadSmem, c.stream>>>(c.g, c.dCnt, c.runStart, c.runCnt, c.runKey,
+                                                              c.planRoot, c.planW, c.fv, c.cap, fields_of(c), c.fCur,
+                                                              c.fPrev);
   c.launches++;
 }
 
