@@ -795,4 +795,26 @@ int ibmdem_step(ibmdem_ctx* h, int32_t nsteps) {
   return IBMDEM_OK;
 }
 
+// For callers that must not allocate inside their time loop (device memory
+// committed to the fluid solver's own arrays, or other streams kept busy that a
+// cudaMalloc/cudaFree would synchronise): the weights go to a fixed static
+// device array, so nothing is allocated here, and n is capped by its size.
+int ibmdem_interpolate_velocity_noalloc(ibmdem_ctx* h, int32_t n, const double* x, double* ulp) {
+  CHECK_CTX();
+  Ctx& c = h->c;
+  if (n < 0) return set_error(h, IBMDEM_EINVAL, "negative point count %d", n);
+  if (n > IBMDEM_PROBE_MAX_POINTS)
+    return set_error(h, IBMDEM_ERANGE,
+                     "%d points exceed the %d that ibmdem_interpolate_velocity_noalloc holds in its static array", n,
+                     IBMDEM_PROBE_MAX_POINTS);
+  if (n > 0 && (!x || !ulp)) return set_error(h, IBMDEM_EINVAL, "null point or result array");
+  REQUIRE(c.haveFluid, "no fluid field");
+  int bad = -1;
+  const cudaError_t e = interpolate_points_noalloc(c, n, x, ulp, &bad);
+  if (e != cudaSuccess)
+    return set_error(h, IBMDEM_ECUDA, "ibmdem_interpolate_velocity_noalloc: %s", cudaGetErrorString(e));
+  if (bad >= 0) return set_error(h, IBMDEM_ERANGE, "point %d lies outside the periodic box", bad);
+  return IBMDEM_OK;
+}
+
 }  // extern "C"

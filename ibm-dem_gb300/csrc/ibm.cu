@@ -19,6 +19,8 @@
 // that order -- the order in which the reference's serial loop over part(1:np)
 // accumulates into fx.  Interpolation reads the halo layers directly, so the
 // spread kernel refreshes the periodic mirrors of every node it updates.
+#include <mutex>
+
 #include "common.cuh"
 #include "kernels.cuh"
 #include "prims.cuh"
@@ -658,6 +660,185 @@ void launch_post_guess(Ctx& c) {
 void record_written_nodes(Ctx& c) {
   k_record_written<<<gs_blocks(c.capRuns), kBlock, 0, c.stream>>>(c.dCnt, c.runKey, c.lastNodes);
   c.launches++;
+}
+
+
+// ---- interpolation at caller-given points, without allocation ---------------
+// Some callers sample the fluid at probe points from inside their own time
+// loop, where they must not allocate device memory: a fluid solver that has
+// committed the device memory to its own arrays (an allocation there can fail
+// in the middle of a run), or one that keeps other streams busy while the
+// particles advance (cudaMalloc and cudaFree synchronise the whole device).
+// This variant of the weight and interpolation kernels keeps the per-point
+// weights and windows in one fixed static device array instead of context
+// buffers, so a call allocates nothing.  The array is shared by every call on
+// a device: calls that overlap in time race on it.
+
+constexpr size_t kProbeWBytes = (size_t)IBMDEM_PROBE_MAX_POINTS * kWStride * sizeof(double);
+constexpr size_t kProbeWinBytes = (size_t)IBMDEM_PROBE_MAX_POINTS * sizeof(int4);
+constexpr size_t kProbeScratchBytes = kProbeWBytes + kProbeWinBytes + 256;
+static_assert(kProbeWBytes % 256 == 0 && kProbeWinBytes % 256 == 0, "sections start on 256-byte boundaries");
+constexpr int kProbeMaxDevices = 64;
+
+// weights (kWStride doubles per point) | windows (int4 per point) | status
+// word; about 11.3 MB for 16384 points.
+static __device__ __align__(256) unsigned char g_probeScratch[kProbeScratchBytes];
+
+namespace {
+
+std::mutex g_probeMutex;
+void* g_probeBase[kProbeMaxDevices] = {};
+
+// k_weights for n caller-given points.  A point's cell is floor((x-xStart)/dx)+1
+// per axis, as the cell lists compute it.  A point outside the box (or NaN)
+// gets no window and raises *status to n - index, so that the lowest offending
+// index is n - *status (*status stays 0 when every point is inside).
+template <int UNIT_H>
+__global__ void __launch_bounds__(kBlock) k_probe_weights(Geom g, int n, const double* __restrict__ x, double* W,
+                                                          int4* win, int* status) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  double xp[3];
+  int a[3];
+  bool in = true;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    xp[d] = x[(size_t)3 * e + d];
+    const double t = floor((xp[d] - g.start[d]) / g.h[d]);
+    in = in && t >= 0.0 && t < (double)g.n[d];
+    a[d] = in ? (int)t + 1 : 1;
+  }
+  if (!in) {
+    atomicMax(status, n - e);
+    win[e] = make_int4(0, 0, 0, -1);
+    return;
+  }
+  double wu[3][3], ws[3][3];
+  int flags = 0;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const double h = g.h[d];
+    double dl[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      double xc = ((double)(a[d] - 1 + q) - 0.5);
+      if (!UNIT_H) xc = xc * h;
+      dl[q] = xp[d] - xc;
+    }
+#pragma unroll
+    for (int q = 0; q < 3; ++q) wu[d][q] = delta1<UNIT_H>(dl[q], h);
+    const double s0 = dl[0] + g.halfh[d];
+    const int st = fabs(UNIT_H ? s0 : s0 / h) < 1.5 ? 0 : 1;
+    flags |= st << d;
+#pragma unroll
+    for (int q = 0; q < 3; ++q) ws[d][q] = delta1<UNIT_H>((st ? dl[q + 1] : dl[q]) + g.halfh[d], h);
+  }
+  double4_32a* out = reinterpret_cast<double4_32a*>(W + (size_t)e * kWStride);
+#pragma unroll
+  for (int comp = 0; comp < 3; ++comp) {
+    double wc[28];
+#pragma unroll
+    for (int ky = 0; ky < 3; ++ky)
+#pragma unroll
+      for (int kx = 0; kx < 3; ++kx) {
+        const double w12 = (comp == 0 ? ws[0][kx] : wu[0][kx]) * (comp == 1 ? ws[1][ky] : wu[1][ky]);
+#pragma unroll
+        for (int kz = 0; kz < 3; ++kz) {
+          double wt = w12 * (comp == 2 ? ws[2][kz] : wu[2][kz]);
+          if (!UNIT_H) wt = wt / g.hprod;
+          wc[kz * 9 + ky * 3 + kx] = wt;
+        }
+      }
+    wc[27] = 0.0;
+#pragma unroll
+    for (int q = 0; q < 7; ++q) out[comp * 7 + q] = make_double4_32a(wc[4 * q], wc[4 * q + 1], wc[4 * q + 2], wc[4 * q + 3]);
+  }
+  win[e] = make_int4(a[0], a[1], a[2], flags);
+}
+
+// k_interp's sum for the points (blockIdx.y = component); ulp is (u,v,w) per
+// point, NaN for a point outside the box.
+template <int UNIT_H>
+__global__ void __launch_bounds__(kBlock) k_probe_interp(Geom g, int n, const double* __restrict__ W,
+                                                         const int4* __restrict__ win, Fields fl, double* ulpOut) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= n) return;
+  const int comp = blockIdx.y;
+  const int4 wn = win[m];
+  if (wn.w < 0) {
+    ulpOut[(size_t)3 * m + comp] = __longlong_as_double(0x7ff8000000000000ll);
+    return;
+  }
+  const double* __restrict__ F = fl.U(comp);
+  int sx, sy, sz;
+  window_start(wn, comp, sx, sy, sz);
+  const double* Wc = W + (size_t)m * kWStride + comp * 28;
+  double ulp = 0.0;
+#pragma unroll
+  for (int kz = 0; kz < 3; ++kz)
+#pragma unroll
+    for (int ky = 0; ky < 3; ++ky) {
+      const double* row = F + field_off(g, sx, sy + ky, sz + kz);
+#pragma unroll
+      for (int kx = 0; kx < 3; ++kx) {
+        double t = Wc[kz * 9 + ky * 3 + kx] * row[kx];
+        if (!UNIT_H) {
+          t = t * g.h[0];
+          t = t * g.h[1];
+          t = t * g.h[2];
+        }
+        ulp = ulp + t;
+      }
+    }
+  ulpOut[(size_t)3 * m + comp] = ulp;
+}
+
+}  // namespace
+
+cudaError_t interpolate_points_noalloc(Ctx& c, int n, const double* x, double* ulp, int* bad) {
+  *bad = -1;
+  if (n < 0 || n > IBMDEM_PROBE_MAX_POINTS) return cudaErrorInvalidValue;
+  if (c.device < 0 || c.device >= kProbeMaxDevices) return cudaErrorInvalidDevice;
+  void* base = nullptr;
+  {
+    // Setup, once per device, with that device current (the caller set it):
+    // the address of the static array on this device.  The first call may load
+    // the module, so it belongs before any stream capture.
+    std::lock_guard<std::mutex> lock(g_probeMutex);
+    base = g_probeBase[c.device];
+    if (!base) {
+      const cudaError_t e = cudaGetSymbolAddress(&base, g_probeScratch);
+      if (e != cudaSuccess) return e;
+      g_probeBase[c.device] = base;
+    }
+  }
+  unsigned char* s = static_cast<unsigned char*>(base);
+  double* W = reinterpret_cast<double*>(s);
+  int4* win = reinterpret_cast<int4*>(s + kProbeWBytes);
+  int* status = reinterpret_cast<int*>(s + kProbeWBytes + kProbeWinBytes);
+  // The status word is the one part of the array that must start at zero;
+  // every weight and window a call reads is written by that call first.
+  cudaError_t e = cudaMemsetAsync(status, 0, sizeof(int), c.stream);
+  if (e != cudaSuccess) return e;
+  if (n > 0) {
+    const dim3 grid(nblocks(n), 3);
+    if (c.g.unit_h) {
+      k_probe_weights<1><<<nblocks(n), kBlock, 0, c.stream>>>(c.g, n, x, W, win, status);
+      k_probe_interp<1><<<grid, kBlock, 0, c.stream>>>(c.g, n, W, win, fields_of(c), ulp);
+    } else {
+      k_probe_weights<0><<<nblocks(n), kBlock, 0, c.stream>>>(c.g, n, x, W, win, status);
+      k_probe_interp<0><<<grid, kBlock, 0, c.stream>>>(c.g, n, W, win, fields_of(c), ulp);
+    }
+    c.launches += 2;
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  int h = 0;
+  e = cudaMemcpyAsync(&h, status, sizeof h, cudaMemcpyDeviceToHost, c.stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
+  if (e != cudaSuccess) return e;
+  if (h > 0) *bad = n - h;
+  return cudaSuccess;
 }
 
 }  // namespace ibmdem

@@ -130,6 +130,10 @@ void launch_interp(Ctx& c);
 void launch_spread(Ctx& c, bool fused_post_guess);
 void launch_post_guess(Ctx& c);
 void record_written_nodes(Ctx& c);
+// Interpolation at n <= IBMDEM_PROBE_MAX_POINTS device points with the
+// weights in a static device array (no allocation); synchronises c.stream.
+// *bad = the lowest index of a point outside the box, or -1.
+cudaError_t interpolate_points_noalloc(Ctx& c, int n, const double* x, double* ulp, int* bad);
 // bodies.cu
 void launch_body_sums(Ctx& c);
 void launch_evolution(Ctx& c);

@@ -28,7 +28,7 @@ EXPORTS = [
     "ibmdem_AdjustParcelPosition", "ibmdem_InitializationDEM", "ibmdem_MultiDirectForcing",
     "ibmdem_CloudEvolutionStepMS", "ibmdem_CloudEvolutionMS", "ibmdem_step", "ibmdem_launch_count",
     "ibmdem_get_counters", "ibmdem_timing_enable", "ibmdem_get_timing", "ibmdem_phase_name",
-    "ibmdem_measure_fp64_rate",
+    "ibmdem_measure_fp64_rate", "ibmdem_interpolate_velocity_noalloc",
 ]
 
 SUBROUTINES = [
@@ -70,6 +70,7 @@ def load(path=LIB_PATH):
     lib.ibmdem_launch_count.restype = i64
     lib.ibmdem_launch_count.argtypes = [vp]
     lib.ibmdem_step.argtypes = [vp, i32]
+    lib.ibmdem_interpolate_velocity_noalloc.argtypes = [vp, i32, vp, vp]
     lib.ibmdem_timing_enable.argtypes = [vp, i32]
     lib.ibmdem_get_timing.argtypes = [vp, vp, vp, i32, i32]
     lib.ibmdem_phase_name.restype = ctypes.c_char_p

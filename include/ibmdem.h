@@ -167,6 +167,21 @@ int ibmdem_CloudEvolutionMS(ibmdem_ctx* ctx);
  * then ibmdem_MultiDirectForcing + ibmdem_CloudEvolutionMS. */
 int ibmdem_step(ibmdem_ctx* ctx, int32_t nsteps);
 
+/* Fluid velocity interpolated at n caller-given points from the context's
+ * resident u, v, w: for each point the ulp that
+ * ibmdem_UpdateFluidVelocityOnLagrangianPoints forms for a parcel there, same
+ * arithmetic.  x: device array of n points (x, y, z), each inside the box
+ * [0, nx*dx) x [0, ny*dy) x [0, nz*dz); ulp: device array of n (u, v, w).
+ * Allocates nothing: the per-point weights live in a fixed static device array
+ * of IBMDEM_PROBE_MAX_POINTS points, and a larger n returns IBMDEM_ERANGE.
+ * The call synchronises the context's stream and returns IBMDEM_ERANGE when a
+ * point lies outside the box.  Calls that overlap in time on one device (from
+ * several threads or contexts) share that array and race.  The first call on a
+ * device looks the array up (which may load the module): make it before any
+ * stream capture.  No counterpart in the reference. */
+#define IBMDEM_PROBE_MAX_POINTS 16384
+int ibmdem_interpolate_velocity_noalloc(ibmdem_ctx* ctx, int32_t n, const double* x, double* ulp);
+
 /* ---- instrumentation -------------------------------------------------- */
 /* Record CUDA events around every phase of the drivers (interpolation,
  * spreading, weights, spread plan, cell lists, contact lists, contact force,
