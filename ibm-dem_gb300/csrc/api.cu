@@ -9,6 +9,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <vector>
 
@@ -17,10 +18,6 @@
 #include "prims.cuh"
 
 using namespace ibmdem;
-
-struct ibmdem_ctx {
-  Ctx c;
-};
 
 namespace {
 
@@ -41,14 +38,59 @@ int set_error(ibmdem_ctx* h, int code, const char* fmt, ...) {
       return set_error(h, IBMDEM_ECUDA, "%s failed: %s", #call, cudaGetErrorString(e_));       \
   } while (0)
 
+// Device memory is stream-ordered (the device's default pool, on the context's
+// stream): unlike cudaMalloc/cudaFree, setting up or tearing down one case
+// does not serialise the work other cases have in flight on other streams.
 template <typename T>
-cudaError_t dalloc(T*& p, size_t n) {
+cudaError_t dalloc(Ctx& c, T*& p, size_t n) {
   p = nullptr;
-  return cudaMalloc(reinterpret_cast<void**>(&p), std::max<size_t>(n, 1) * sizeof(T));
+  const size_t bytes = std::max<size_t>(n, 1) * sizeof(T);
+  const cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(&p), bytes, c.stream);
+  if (e == cudaSuccess) c.bytes += bytes;
+  return e;
 }
 
-void dfree(void* p) {
-  if (p) cudaFree(p);
+void dfree(Ctx& c, void* p) {
+  if (p) cudaFreeAsync(p, c.stream);
+}
+
+// Keep freed blocks in the device's default pool (a process-local attribute) so
+// that cases created after others finished reuse them without new mappings.
+void retain_pool_memory(int device) {
+  static std::mutex mu;
+  static bool done[64] = {};
+  std::lock_guard<std::mutex> lock(mu);
+  if (device < 0 || device >= 64 || done[device]) return;
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+    uint64_t keep = UINT64_MAX;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  }
+  done[device] = true;
+}
+
+// Pinned mirrors of the device counters come from shared slabs: a pinned host
+// allocation per case would serialise the device like cudaMalloc does.
+std::mutex g_pinMutex;
+std::vector<Counters*> g_pinFree;
+
+Counters* pinned_counters() {
+  std::lock_guard<std::mutex> lock(g_pinMutex);
+  if (g_pinFree.empty()) {
+    constexpr int kSlab = 256;
+    Counters* slab = nullptr;
+    if (cudaMallocHost(reinterpret_cast<void**>(&slab), sizeof(Counters) * kSlab) != cudaSuccess) return nullptr;
+    for (int i = kSlab - 1; i >= 0; --i) g_pinFree.push_back(slab + i);
+  }
+  Counters* q = g_pinFree.back();
+  g_pinFree.pop_back();
+  return q;
+}
+
+void release_counters(Counters* q) {
+  if (!q) return;
+  std::lock_guard<std::mutex> lock(g_pinMutex);
+  g_pinFree.push_back(q);
 }
 
 double eta_of(double e) {
@@ -63,7 +105,11 @@ void free_parcel_buffers(Ctx& c) {
                 c.iTmpA, c.iTmpB, c.scanScratch, c.sortHist, c.kA, c.vA, c.kB, c.vB, c.activeList, c.pairCnt,
                 c.pairStart, c.pairIdx, c.W, c.win, c.cntInt, c.fv, c.runStart, c.runKey, c.fCur, c.fPrev,
                 c.lastNodes, c.touch, c.planRoot, c.planW, c.runCnt, c.planAlloc};
-  for (void* p : ps) dfree(p);
+  for (void* p : ps) dfree(c, p);
+  c.bytes -= c.bytesParcels + c.bytesRuns;
+  c.bytesParcels = c.bytesRuns = 0;
+  c.capRuns = 0;
+  c.runsSized = false;
   c.recD[0] = c.recD[1] = nullptr;
   c.recI[0] = c.recI[1] = nullptr;
   c.imgSrc = c.imgShift = c.cellItems = c.bodyItems = c.iTmpA = c.iTmpB = c.scanScratch = c.sortHist = nullptr;
@@ -85,6 +131,49 @@ void free_parcel_buffers(Ctx& c) {
   c.cap = c.capLocal = c.capImg = 0;
 }
 
+int check_params(const ibmdem_params* p) {
+  if (p->nx < 4 || p->ny < 4 || p->nz < 4 || p->coupleInterval < 1 || p->Ns < 0 || !(p->dx > 0) || !(p->dy > 0) ||
+      !(p->dz > 0) || !(p->dt > 0))
+    return IBMDEM_EINVAL;
+  for (int f = 0; f < 6; ++f)
+    if (p->bType[f] != 0) return IBMDEM_EUNSUPPORTED;  // periodic faces only
+  long long ncell = (long long)(p->nx + 4) * (p->ny + 4) * (p->nz + 4);
+  long long nint = (long long)p->nx * p->ny * p->nz;
+  if (ncell >= (1ll << 31) || 3 * nint >= (1ll << 32)) return IBMDEM_EUNSUPPORTED;
+  return IBMDEM_OK;
+}
+
+void init_geom(Geom& g, const ibmdem_params* p) {
+  g.n[0] = p->nx;
+  g.n[1] = p->ny;
+  g.n[2] = p->nz;
+  g.ni = p->nx + 4;
+  g.nj = p->ny + 4;
+  g.nk = p->nz + 4;
+  g.ncell = (long long)g.ni * g.nj * g.nk;
+  g.nint = (long long)p->nx * p->ny * p->nz;
+  double hh[3] = {p->dx, p->dy, p->dz};
+  for (int d = 0; d < 3; ++d) {
+    g.h[d] = hh[d];
+    g.start[d] = (1 - 1) * hh[d];
+    g.end[d] = (g.n[d] - 1 + 1) * hh[d];
+    g.len[d] = hh[d] * g.n[d];
+    g.halfh[d] = 0.5 * hh[d];
+    g.err[d] = hh[d] * 1e-20;
+  }
+  g.hprod = p->dx * p->dy * p->dz;
+  g.unit_h = (p->dx == 1.0 && p->dy == 1.0 && p->dz == 1.0) ? 1 : 0;
+  g.dt = p->dt;
+  g.dtDEM = p->dt / p->coupleInterval;
+  g.rhof = p->rhof;
+  g.eta = eta_of(p->ResistCoeff);
+  double cd = p->collisionDist * (1.0 + p->collisionBuffer);
+  g.cut2 = cd * cd;
+  g.knCoeff = p->knCoeff;
+  g.di = p->dx;
+  for (int k = 0; k < 3; ++k) g.g[k] = p->gravity[k];
+}
+
 // images the configuration needs right now (host estimate for the capacity)
 long long count_images(const Geom& g, int np, const ibmdem_parcel* parts) {
   long long n = 0;
@@ -100,9 +189,7 @@ long long count_images(const Geom& g, int np, const ibmdem_parcel* parts) {
   return n;
 }
 
-int alloc_parcels(ibmdem_ctx* h, int np, long long nimg_est) {
-  Ctx& c = h->c;
-  free_parcel_buffers(c);
+void set_parcel_caps(Ctx& c, int np, long long nimg_est) {
   c.capLocal = std::max(np, 1);
   long long ci = nimg_est + nimg_est / 2 + 4096;
   c.capImg = (int)std::min<long long>(ci, 7ll * c.capLocal + 64);
@@ -114,46 +201,78 @@ int alloc_parcels(ibmdem_ctx* h, int np, long long nimg_est) {
   }
   c.capPairs = 4ll * c.capLocal + 65536;
   c.capContrib = (long long)kSlots * c.cap;
-  c.capRuns = std::min<long long>(c.capContrib, 3 * c.g.nint);
+  c.capRuns = 0;  // sized from the touched nodes at the first spread plan
+}
+
+// every parcel-side device buffer with its element count, for the current caps
+template <class F>
+void for_each_parcel_buffer(Ctx& c, F&& f) {
   long long tmpInts = std::max<long long>(c.cap + 1, 26ll * nblocks(c.capLocal) + 1);
   long long scanInts = std::max({scan_scratch_ints(c.capRuns + 1), scan_scratch_ints(sort_hist_ints(std::max<long long>(c.cap, c.capRuns))),
                                  scan_scratch_ints(c.g.ncell + 1), scan_scratch_ints(26ll * nblocks(c.capLocal)),
                                  scan_scratch_ints(nblocks((3 * c.g.nint + 15) / 16))});
   tmpInts = std::max<long long>(tmpInts, nblocks((3 * c.g.nint + 15) / 16) + 1);
-  CU(dalloc(c.recD[0], (size_t)ND * c.cap));
-  CU(dalloc(c.recD[1], (size_t)ND * c.cap));
-  CU(dalloc(c.recI[0], (size_t)NI * c.cap));
-  CU(dalloc(c.recI[1], (size_t)NI * c.cap));
-  CU(dalloc(c.imgSrc, c.capImg));
-  CU(dalloc(c.imgShift, c.capImg));
-  CU(dalloc(c.cellItems, c.cap));
-  CU(dalloc(c.bodyItems, c.capLocal));
-  CU(dalloc(c.iTmpA, tmpInts));
-  CU(dalloc(c.iTmpB, tmpInts));
-  CU(dalloc(c.scanScratch, scanInts));
-  CU(dalloc(c.sortHist, sort_hist_ints(std::max<long long>(c.cap, c.capRuns))));
-  CU(dalloc(c.kA, c.cap));
-  CU(dalloc(c.vA, c.cap));
-  CU(dalloc(c.kB, c.cap));
-  CU(dalloc(c.vB, c.cap));
-  CU(dalloc(c.touch, ((3 * c.g.nint + 15) / 16) * 16));
-  CU(dalloc(c.planRoot, c.capContrib));
-  CU(dalloc(c.planW, c.capContrib));
-  CU(dalloc(c.runCnt, c.capRuns));
-  CU(dalloc(c.planAlloc, 1));
-  CU(dalloc(c.activeList, c.capLocal));
-  CU(dalloc(c.pairCnt, c.capLocal + 1));
-  CU(dalloc(c.pairStart, c.capLocal + 1));
-  CU(dalloc(c.pairIdx, c.capPairs));
-  CU(dalloc(c.W, (size_t)kWStride * c.cap));
-  CU(dalloc(c.win, c.cap));
-  CU(dalloc(c.cntInt, c.cap));
-  CU(dalloc(c.fv, 3 * (size_t)c.cap));
-  CU(dalloc(c.runStart, c.capRuns + 1));
-  CU(dalloc(c.runKey, c.capRuns));
-  CU(dalloc(c.fCur, c.capRuns));
-  CU(dalloc(c.fPrev, c.capRuns));
-  CU(dalloc(c.lastNodes, c.capRuns));
+  f(c.recD[0], (size_t)ND * c.cap);
+  f(c.recD[1], (size_t)ND * c.cap);
+  f(c.recI[0], (size_t)NI * c.cap);
+  f(c.recI[1], (size_t)NI * c.cap);
+  f(c.imgSrc, (size_t)c.capImg);
+  f(c.imgShift, (size_t)c.capImg);
+  f(c.cellItems, (size_t)c.cap);
+  f(c.bodyItems, (size_t)c.capLocal);
+  f(c.iTmpA, (size_t)tmpInts);
+  f(c.iTmpB, (size_t)tmpInts);
+  f(c.scanScratch, (size_t)scanInts);
+  f(c.sortHist, (size_t)sort_hist_ints(std::max<long long>(c.cap, c.capRuns)));
+  f(c.kA, (size_t)c.cap);
+  f(c.vA, (size_t)c.cap);
+  f(c.kB, (size_t)c.cap);
+  f(c.vB, (size_t)c.cap);
+  f(c.touch, (size_t)(((3 * c.g.nint + 15) / 16) * 16));
+  f(c.planRoot, (size_t)c.capContrib);
+  f(c.planW, (size_t)c.capContrib);
+  f(c.planAlloc, (size_t)1);
+  f(c.activeList, (size_t)c.capLocal);
+  f(c.pairCnt, (size_t)c.capLocal + 1);
+  f(c.pairStart, (size_t)c.capLocal + 1);
+  f(c.pairIdx, (size_t)c.capPairs);
+  f(c.W, (size_t)kWStride * c.cap);
+  f(c.win, (size_t)c.cap);
+  f(c.cntInt, (size_t)c.cap);
+  f(c.fv, 3 * (size_t)c.cap);
+}
+
+// the per-touched-node arrays of the spread plan, for the current capRuns
+template <class F>
+void for_each_run_buffer(Ctx& c, F&& f) {
+  f(c.runCnt, (size_t)c.capRuns);
+  f(c.runStart, (size_t)c.capRuns + 1);
+  f(c.runKey, (size_t)c.capRuns);
+  f(c.fCur, (size_t)c.capRuns);
+  f(c.fPrev, (size_t)c.capRuns);
+  f(c.lastNodes, (size_t)c.capRuns);
+}
+
+// run capacity for `touched` nodes: room to double, never above every node
+long long run_capacity(const Ctx& c, long long touched) {
+  return std::min<long long>(3 * c.g.nint, std::max(2 * touched, touched + 65536));
+}
+
+int alloc_parcels(ibmdem_ctx* h, int np, long long nimg_est) {
+  Ctx& c = h->c;
+  free_parcel_buffers(c);
+  set_parcel_caps(c, np, nimg_est);
+  const size_t b0 = c.bytes;
+  cudaError_t e = cudaSuccess;
+  for_each_parcel_buffer(c, [&](auto& q, size_t n) {
+    if (e == cudaSuccess) e = dalloc(c, q, n);
+  });
+  c.bytesParcels = c.bytes - b0;
+  c.allocGen++;
+  if (e != cudaSuccess) {
+    free_parcel_buffers(c);
+    return set_error(h, IBMDEM_ENOMEM, "parcel buffers: %s", cudaGetErrorString(e));
+  }
   CU(cudaMemsetAsync(c.cntInt, 0, sizeof(int) * c.cap, c.stream));
   CU(cudaMemsetAsync(c.pairStart, 0, sizeof(int) * (c.capLocal + 1), c.stream));
   CU(cudaMemsetAsync(c.recD[0], 0, sizeof(double) * ND * (size_t)c.cap, c.stream));
@@ -278,91 +397,93 @@ const char* ibmdem_last_error(const ibmdem_ctx* h) { return h ? h->c.err.c_str()
 int64_t ibmdem_launch_count(const ibmdem_ctx* h) { return h ? h->c.launches : 0; }
 
 int ibmdem_create(const ibmdem_params* p, int32_t device, ibmdem_ctx** out) {
+  return create_on_stream(p, device, nullptr, out);
+}
+
+}  // extern "C"
+
+int create_on_stream(const ibmdem_params* p, int device, cudaStream_t stream, ibmdem_ctx** out) {
   if (!p || !out) return IBMDEM_EINVAL;
   *out = nullptr;
-  if (p->nx < 4 || p->ny < 4 || p->nz < 4 || p->coupleInterval < 1 || p->Ns < 0 || !(p->dx > 0) || !(p->dy > 0) ||
-      !(p->dz > 0) || !(p->dt > 0))
-    return IBMDEM_EINVAL;
-  for (int f = 0; f < 6; ++f)
-    if (p->bType[f] != 0) return IBMDEM_EUNSUPPORTED;  // periodic faces only
-  long long ncell = (long long)(p->nx + 4) * (p->ny + 4) * (p->nz + 4);
-  long long nint = (long long)p->nx * p->ny * p->nz;
-  if (ncell >= (1ll << 31) || 3 * nint >= (1ll << 32)) return IBMDEM_EUNSUPPORTED;
+  const int pc = check_params(p);
+  if (pc) return pc;
   ibmdem_ctx* h = new (std::nothrow) ibmdem_ctx();
   if (!h) return IBMDEM_ENOMEM;
   Ctx& c = h->c;
   c.p = *p;
   c.device = device;
+  c.stream = stream;
   if (cudaSetDevice(device) != cudaSuccess) {
     delete h;
     return IBMDEM_ECUDA;
   }
-  Geom& g = c.g;
-  g.n[0] = p->nx;
-  g.n[1] = p->ny;
-  g.n[2] = p->nz;
-  g.ni = p->nx + 4;
-  g.nj = p->ny + 4;
-  g.nk = p->nz + 4;
-  g.ncell = ncell;
-  g.nint = nint;
-  double hh[3] = {p->dx, p->dy, p->dz};
-  for (int d = 0; d < 3; ++d) {
-    g.h[d] = hh[d];
-    g.start[d] = (1 - 1) * hh[d];
-    g.end[d] = (g.n[d] - 1 + 1) * hh[d];
-    g.len[d] = hh[d] * g.n[d];
-    g.halfh[d] = 0.5 * hh[d];
-    g.err[d] = hh[d] * 1e-20;
-  }
-  g.hprod = p->dx * p->dy * p->dz;
-  g.unit_h = (p->dx == 1.0 && p->dy == 1.0 && p->dz == 1.0) ? 1 : 0;
-  g.dt = p->dt;
-  g.dtDEM = p->dt / p->coupleInterval;
-  g.rhof = p->rhof;
-  g.eta = eta_of(p->ResistCoeff);
-  double cd = p->collisionDist * (1.0 + p->collisionBuffer);
-  g.cut2 = cd * cd;
-  g.knCoeff = p->knCoeff;
-  g.di = p->dx;
-  for (int k = 0; k < 3; ++k) g.g[k] = p->gravity[k];
+  retain_pool_memory(device);
+  init_geom(c.g, p);
 
   int rc = IBMDEM_OK;
-  size_t nf = (size_t)ncell;
+  size_t nf = (size_t)c.g.ncell;
   double** f[] = {&c.u, &c.v, &c.w, &c.u0, &c.v0, &c.w0, &c.fx, &c.fy, &c.fz};
   for (double** q : f)
-    if (dalloc(*q, nf) != cudaSuccess) rc = IBMDEM_ENOMEM;
-  if (rc == IBMDEM_OK && dalloc(c.cellStart, (size_t)ncell + 1) != cudaSuccess) rc = IBMDEM_ENOMEM;
-  if (rc == IBMDEM_OK && dalloc(c.dCnt, 1) != cudaSuccess) rc = IBMDEM_ENOMEM;
-  if (rc == IBMDEM_OK && dalloc(c.dTotal, 4) != cudaSuccess) rc = IBMDEM_ENOMEM;
-  if (rc == IBMDEM_OK && cudaMallocHost(reinterpret_cast<void**>(&c.hCnt), sizeof(Counters)) != cudaSuccess)
-    rc = IBMDEM_ENOMEM;
+    if (rc == IBMDEM_OK && dalloc(c, *q, nf) != cudaSuccess) rc = IBMDEM_ENOMEM;
+  if (rc == IBMDEM_OK && dalloc(c, c.cellStart, nf + 1) != cudaSuccess) rc = IBMDEM_ENOMEM;
+  if (rc == IBMDEM_OK && dalloc(c, c.dCnt, 1) != cudaSuccess) rc = IBMDEM_ENOMEM;
+  if (rc == IBMDEM_OK && dalloc(c, c.dTotal, 4) != cudaSuccess) rc = IBMDEM_ENOMEM;
+  if (rc == IBMDEM_OK && !(c.hCnt = pinned_counters())) rc = IBMDEM_ENOMEM;
+  if (rc == IBMDEM_OK) {
+    for (double** q : f) cudaMemsetAsync(*q, 0, nf * sizeof(double), c.stream);
+    cudaMemsetAsync(c.dCnt, 0, sizeof(Counters), c.stream);
+    cudaMemsetAsync(c.cellStart, 0, sizeof(int) * (nf + 1), c.stream);
+    if (cudaStreamSynchronize(c.stream) != cudaSuccess) rc = IBMDEM_ECUDA;
+  }
   if (rc != IBMDEM_OK) {
     ibmdem_destroy(h);
     return rc;
-  }
-  for (double** q : f) cudaMemset(*q, 0, nf * sizeof(double));
-  cudaMemset(c.dCnt, 0, sizeof(Counters));
-  cudaMemset(c.cellStart, 0, sizeof(int) * (nf + 1));
-  if (cudaDeviceSynchronize() != cudaSuccess) {
-    ibmdem_destroy(h);
-    return IBMDEM_ECUDA;
   }
   *out = h;
   return IBMDEM_OK;
 }
 
+extern "C" {
+
 int ibmdem_destroy(ibmdem_ctx* h) {
   if (!h) return IBMDEM_EINVAL;
   Ctx& c = h->c;
   cudaSetDevice(c.device);
-  if (c.stream) cudaStreamSynchronize(c.stream);
+  cudaStreamSynchronize(c.stream);
   free_parcel_buffers(c);
   void* ps[] = {c.u, c.v, c.w, c.u0, c.v0, c.w0, c.fx, c.fy, c.fz, c.cellStart, c.dCnt, c.dTotal, c.dBodies,
                 c.bodyStart, c.bodyR2, c.partnerCnt, c.partners};
-  for (void* p : ps) dfree(p);
-  if (c.hCnt) cudaFreeHost(c.hCnt);
+  for (void* p : ps) dfree(c, p);
+  // the frees are ordered on the context's stream; let them complete before
+  // the stream may be destroyed by its owner
+  cudaStreamSynchronize(c.stream);
+  release_counters(c.hCnt);
+  for (auto& sp : c.spans) {
+    cudaEventDestroy(sp.a);
+    cudaEventDestroy(sp.b);
+  }
+  for (cudaEvent_t e : c.evFree) cudaEventDestroy(e);
   delete h;
+  return IBMDEM_OK;
+}
+
+int ibmdem_case_bytes(const ibmdem_params* p, int32_t np, const ibmdem_parcel* parts, int32_t nMS, int64_t* bytes) {
+  if (!p || !bytes || np < 0 || nMS < 0 || (np > 0 && !parts)) return IBMDEM_EINVAL;
+  const int pc = check_params(p);
+  if (pc) return pc;
+  Ctx c;
+  init_geom(c.g, p);
+  const long long nf = c.g.ncell;
+  long long b = 9 * nf * (long long)sizeof(double) + (nf + 1) * (long long)sizeof(int) + (long long)sizeof(Counters) +
+                4 * (long long)sizeof(int);
+  set_parcel_caps(c, np, count_images(c.g, np, parts));
+  for_each_parcel_buffer(c, [&](auto& q, size_t n) { b += (long long)(std::max<size_t>(n, 1) * sizeof(*q)); });
+  // touched nodes: about 8 per marker on a closed surface with marker spacing h
+  c.capRuns = run_capacity(c, 8ll * c.cap);
+  for_each_run_buffer(c, [&](auto& q, size_t n) { b += (long long)(std::max<size_t>(n, 1) * sizeof(*q)); });
+  const long long nb = std::max(nMS, 1);
+  b += nb * (long long)sizeof(ibmdem_multisphere) + (nb + 1) * 4 + nb * 4 + nb * 4 + nb * (long long)c.maxPartners * 4;
+  *bytes = b;
   return IBMDEM_OK;
 }
 
@@ -449,11 +570,12 @@ int ibmdem_set_parcels(ibmdem_ctx* h, int32_t np, const ibmdem_parcel* parts) {
     if (!in) return set_error(h, IBMDEM_ERANGE, "parcel %d at (%g,%g,%g) exceeds the region", i + 1, p.x[0], p.x[1], p.x[2]);
     hi[(size_t)I_CELL * c.cap + i] = cell_id(c.g, a[0], a[1], a[2]);
   }
-  CU(cudaMemcpy(c.recD[c.cur], hd.data(), sizeof(double) * hd.size(), cudaMemcpyHostToDevice));
-  CU(cudaMemcpy(c.recI[c.cur], hi.data(), sizeof(int) * hi.size(), cudaMemcpyHostToDevice));
+  CU(cudaMemcpyAsync(c.recD[c.cur], hd.data(), sizeof(double) * hd.size(), cudaMemcpyHostToDevice, c.stream));
+  CU(cudaMemcpyAsync(c.recI[c.cur], hi.data(), sizeof(int) * hi.size(), cudaMemcpyHostToDevice, c.stream));
   Counters hc{};
   hc.npLocal = hc.np = np;
-  CU(cudaMemcpy(c.dCnt, &hc, sizeof hc, cudaMemcpyHostToDevice));
+  CU(cudaMemcpyAsync(c.dCnt, &hc, sizeof hc, cudaMemcpyHostToDevice, c.stream));
+  CU(cudaStreamSynchronize(c.stream));
   c.haveParcels = true;
   c.listsBuilt = c.weightsLocal = c.weightsGhost = c.planReady = c.spreadValid = false;
   return IBMDEM_OK;
@@ -471,8 +593,10 @@ int ibmdem_get_parcels(ibmdem_ctx* h, ibmdem_parcel* parts, int32_t cap, int32_t
   int n = std::min(np, cap);
   std::vector<double> hd((size_t)ND * c.cap);
   std::vector<int> hi((size_t)NI * c.cap);
-  CU(cudaMemcpy(hd.data(), c.recD[c.cur], sizeof(double) * hd.size(), cudaMemcpyDeviceToHost));
-  CU(cudaMemcpy(hi.data(), c.recI[c.cur], sizeof(int) * hi.size(), cudaMemcpyDeviceToHost));
+  CU(cudaMemcpyAsync(hd.data(), c.recD[c.cur], sizeof(double) * hd.size(), cudaMemcpyDeviceToHost, c.stream));
+  CU(cudaStreamSynchronize(c.stream));
+  CU(cudaMemcpyAsync(hi.data(), c.recI[c.cur], sizeof(int) * hi.size(), cudaMemcpyDeviceToHost, c.stream));
+  CU(cudaStreamSynchronize(c.stream));
   for (int i = 0; i < n; ++i) {
     ibmdem_parcel& p = parts[i];
     std::memset(&p, 0, sizeof p);
@@ -506,23 +630,27 @@ int ibmdem_set_bodies(ibmdem_ctx* h, int32_t nMS, const ibmdem_multisphere* ms) 
   Ctx& c = h->c;
   CU(cudaStreamSynchronize(c.stream));
   if (nMS > c.capMS) {
-    dfree(c.dBodies);
-    dfree(c.bodyStart);
-    dfree(c.bodyR2);
-    dfree(c.partnerCnt);
-    dfree(c.partners);
+    dfree(c, c.dBodies);
+    dfree(c, c.bodyStart);
+    dfree(c, c.bodyR2);
+    dfree(c, c.partnerCnt);
+    dfree(c, c.partners);
     c.dBodies = nullptr;
     c.bodyStart = nullptr;
     c.bodyR2 = nullptr;
     c.partnerCnt = c.partners = nullptr;
-    CU(dalloc(c.dBodies, nMS));
-    CU(dalloc(c.bodyStart, nMS + 1));
-    CU(dalloc(c.bodyR2, nMS));
-    CU(dalloc(c.partnerCnt, nMS));
-    CU(dalloc(c.partners, (size_t)nMS * c.maxPartners));
+    CU(dalloc(c, c.dBodies, nMS));
+    CU(dalloc(c, c.bodyStart, nMS + 1));
+    CU(dalloc(c, c.bodyR2, nMS));
+    CU(dalloc(c, c.partnerCnt, nMS));
+    CU(dalloc(c, c.partners, (size_t)nMS * c.maxPartners));
     c.capMS = nMS;
+    c.allocGen++;
   }
-  if (nMS > 0) CU(cudaMemcpy(c.dBodies, ms, sizeof(ibmdem_multisphere) * nMS, cudaMemcpyHostToDevice));
+  if (nMS > 0) {
+    CU(cudaMemcpyAsync(c.dBodies, ms, sizeof(ibmdem_multisphere) * nMS, cudaMemcpyHostToDevice, c.stream));
+    CU(cudaStreamSynchronize(c.stream));
+  }
   c.nMS = nMS;
   c.listsBuilt = false;  // body lists are built with the cell lists
   return IBMDEM_OK;
@@ -535,7 +663,8 @@ int ibmdem_get_bodies(ibmdem_ctx* h, ibmdem_multisphere* ms, int32_t cap, int32_
   if (rc) return rc;
   if (nMS_out) *nMS_out = c.nMS;
   if (ms && c.nMS > 0)
-    CU(cudaMemcpy(ms, c.dBodies, sizeof(ibmdem_multisphere) * std::min(c.nMS, cap), cudaMemcpyDeviceToHost));
+    CU(cudaMemcpyAsync(ms, c.dBodies, sizeof(ibmdem_multisphere) * std::min(c.nMS, cap), cudaMemcpyDeviceToHost, c.stream));
+  CU(cudaStreamSynchronize(c.stream));
   return IBMDEM_OK;
 }
 
@@ -548,10 +677,12 @@ int ibmdem_get_cell_lists(ibmdem_ctx* h, int32_t* cell_start, int32_t* items, in
   if (ncell_out) *ncell_out = c.g.ncell;
   if (nitems_out) *nitems_out = c.hCnt->np;
   REQUIRE(c.listsBuilt, "cell lists are not built");
-  if (cell_start) CU(cudaMemcpy(cell_start, c.cellStart, sizeof(int) * (c.g.ncell + 1), cudaMemcpyDeviceToHost));
+  if (cell_start) CU(cudaMemcpyAsync(cell_start, c.cellStart, sizeof(int) * (c.g.ncell + 1), cudaMemcpyDeviceToHost, c.stream));
+  CU(cudaStreamSynchronize(c.stream));
   if (items) {
     int n = c.hCnt->np;
-    CU(cudaMemcpy(items, c.cellItems, sizeof(int) * n, cudaMemcpyDeviceToHost));
+    CU(cudaMemcpyAsync(items, c.cellItems, sizeof(int) * n, cudaMemcpyDeviceToHost, c.stream));
+    CU(cudaStreamSynchronize(c.stream));
     for (int i = 0; i < n; ++i) items[i] += 1;
   }
   return IBMDEM_OK;
@@ -567,9 +698,11 @@ int ibmdem_get_collision_lists(ibmdem_ctx* h, int32_t* start, int32_t* idx, int3
   int nl = c.hCnt->npLocal, npairs = c.hCnt->nPairs;
   if (nlocal_out) *nlocal_out = nl;
   if (npairs_out) *npairs_out = npairs;
-  if (start) CU(cudaMemcpy(start, c.pairStart, sizeof(int) * (nl + 1), cudaMemcpyDeviceToHost));
+  if (start) CU(cudaMemcpyAsync(start, c.pairStart, sizeof(int) * (nl + 1), cudaMemcpyDeviceToHost, c.stream));
+  CU(cudaStreamSynchronize(c.stream));
   if (idx) {
-    CU(cudaMemcpy(idx, c.pairIdx, sizeof(int) * npairs, cudaMemcpyDeviceToHost));
+    CU(cudaMemcpyAsync(idx, c.pairIdx, sizeof(int) * npairs, cudaMemcpyDeviceToHost, c.stream));
+    CU(cudaStreamSynchronize(c.stream));
     for (int i = 0; i < npairs; ++i) idx[i] += 1;
   }
   return IBMDEM_OK;
@@ -584,7 +717,8 @@ int ibmdem_get_counters(ibmdem_ctx* h, int64_t* out, int32_t n) {
   // touched nodes per component from the run keys
   if (c.planReady && c.hCnt->nRuns > 0) {
     std::vector<uint32_t> keys(c.hCnt->nRuns);
-    CU(cudaMemcpy(keys.data(), c.runKey, sizeof(uint32_t) * keys.size(), cudaMemcpyDeviceToHost));
+    CU(cudaMemcpyAsync(keys.data(), c.runKey, sizeof(uint32_t) * keys.size(), cudaMemcpyDeviceToHost, c.stream));
+    CU(cudaStreamSynchronize(c.stream));
     for (uint32_t k : keys) v[3 + (int)(k / (uint32_t)c.g.nint)]++;
   }
   for (int q = 0; q < n && q < 7; ++q) out[q] = v[q];
@@ -592,6 +726,8 @@ int ibmdem_get_counters(ibmdem_ctx* h, int64_t* out, int32_t n) {
 }
 
 // ---- reference subroutines ------------------------------------------------
+
+static int plan(ibmdem_ctx* h);
 
 int ibmdem_RebuildAllListOrNot(ibmdem_ctx* h) {
   CHECK_CTX();
@@ -621,7 +757,10 @@ int ibmdem_UpdateGhostCellWeightListDEM(ibmdem_ctx* h) {
   launch_weights(c, false);
   c.weightsGhost = true;
   c.planReady = false;
-  if (c.weightsLocal) build_spread_plan(c);
+  if (c.weightsLocal) {
+    int rc = plan(h);
+    if (rc) return rc;
+  }
   return launch_status(h);
 }
 
@@ -650,12 +789,47 @@ int ibmdem_UpdateFluidVelocityOnLagrangianPoints(ibmdem_ctx* h) {
   return launch_status(h);
 }
 
+// Allocate the run arrays for the nodes the current weights touch (counted on
+// the device; synchronises), with room to double.  Done once per parcel set,
+// before the first spread plan, outside any stream capture.
+static int size_runs(ibmdem_ctx* h) {
+  Ctx& c = h->c;
+  const long long touched = count_touched_nodes(c);
+  if (touched < 0) return set_error(h, IBMDEM_ECUDA, "counting touched nodes failed");
+  for_each_run_buffer(c, [&](auto& q, size_t) {
+    dfree(c, q);
+    q = nullptr;
+  });
+  c.bytes -= c.bytesRuns;
+  c.capRuns = run_capacity(c, touched);
+  const size_t b0 = c.bytes;
+  cudaError_t e = cudaSuccess;
+  for_each_run_buffer(c, [&](auto& q, size_t n) {
+    if (e == cudaSuccess) e = dalloc(c, q, n);
+  });
+  c.bytesRuns = c.bytes - b0;
+  c.allocGen++;
+  if (e != cudaSuccess) return set_error(h, IBMDEM_ENOMEM, "spread-plan runs: %s", cudaGetErrorString(e));
+  c.runsSized = true;
+  return IBMDEM_OK;
+}
+
+static int plan(ibmdem_ctx* h) {
+  Ctx& c = h->c;
+  if (!c.runsSized) {
+    int rc = size_runs(h);
+    if (rc) return rc;
+  }
+  build_spread_plan(c);
+  return IBMDEM_OK;
+}
+
 static int ensure_plan(ibmdem_ctx* h) {
   Ctx& c = h->c;
   REQUIRE(c.weightsLocal && c.weightsGhost, "weights are not computed");
   if (!c.planReady) {
     PhaseScope t(c, P_PLAN);
-    build_spread_plan(c);
+    return plan(h);
   }
   return IBMDEM_OK;
 }
@@ -765,7 +939,11 @@ int ibmdem_CloudEvolutionStepMS(ibmdem_ctx* h) {
   { PhaseScope t(c, P_WEIGHTS); launch_weights(c, true); }
   { PhaseScope t(c, P_IMAGES); launch_img_update(c); }
   { PhaseScope t(c, P_WEIGHTS); launch_weights(c, false); }
-  { PhaseScope t(c, P_PLAN); build_spread_plan(c); }
+  {
+    PhaseScope t(c, P_PLAN);
+    int rc = plan(h);
+    if (rc) return rc;
+  }
   c.listsBuilt = c.weightsLocal = c.weightsGhost = true;
   return launch_status(h);
 }

@@ -178,7 +178,7 @@ __global__ void k_flag_count(const uint4* flags, long long nvec, int* blockCnt) 
   }
 }
 __global__ void k_flag_emit(const uint4* flags, long long nvec, long long nflags, const int* blockOff,
-                            uint32_t* keys) {
+                            uint32_t* keys, long long capRuns) {
   __shared__ int sh[kBlock / 32];
   long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   uint32_t w4[4] = {0, 0, 0, 0};
@@ -202,11 +202,19 @@ __global__ void k_flag_emit(const uint4* flags, long long nvec, long long nflags
   long long f0 = v * 16;
   for (int q = 0; q < 16; ++q) {
     uint32_t byte = (w4[q >> 2] >> (8 * (q & 3))) & 0xffu;
-    if (byte && f0 + q < nflags) keys[pos++] = (uint32_t)(f0 + q);
+    if (byte && f0 + q < nflags) {
+      if (pos < capRuns) keys[pos] = (uint32_t)(f0 + q);
+      ++pos;
+    }
   }
 }
 
-__global__ void k_set_runs(Counters* cnt, const int* total) { cnt->nRuns = *total; }
+// touched nodes beyond the run capacity are dropped and reported
+__global__ void k_set_runs(Counters* cnt, const int* total, long long capRuns) {
+  const int t = *total;
+  if (t > capRuns) set_err(cnt, E_PLANCAP, t);
+  cnt->nRuns = (int)min((long long)t, capRuns);
+}
 
 // One pass per touched node: scan the candidate cells, keep the hits sorted in
 // registers, then reserve the block's contribution range with one atomic (the
@@ -599,24 +607,42 @@ void launch_weights(Ctx& c, bool locals) {
   c.launches++;
 }
 
+// touched-node flags, their per-block counts (iTmpA, scanned) and the total (dTotal)
+static void flag_touched_nodes(Ctx& c) {
+  cudaStream_t s = c.stream;
+  const long long nvec = (3 * c.g.nint + 15) / 16;
+  cudaMemsetAsync(c.touch, 0, nvec * 16, s);
+  k_touch<<<nblocks(c.cap), kBlock, 0, s>>>(c.g, c.dCnt, c.win, c.touch);
+  const long long nb = nblocks(nvec);
+  k_flag_count<<<(unsigned)nb, kBlock, 0, s>>>(reinterpret_cast<const uint4*>(c.touch), nvec, c.iTmpA);
+  scan_exclusive(c.iTmpA, c.iTmpA, nb, nullptr, c.dTotal, c.scanScratch, s, &c.launches);
+  c.launches += 2;
+}
+
+long long count_touched_nodes(Ctx& c) {
+  flag_touched_nodes(c);
+  int total = 0;
+  if (cudaMemcpyAsync(&total, c.dTotal, sizeof total, cudaMemcpyDeviceToHost, c.stream) != cudaSuccess ||
+      cudaStreamSynchronize(c.stream) != cudaSuccess)
+    return -1;
+  return total;
+}
+
 void build_spread_plan(Ctx& c) {
   cudaStream_t s = c.stream;
   const long long nflags = 3 * c.g.nint;
   const long long nvec = (nflags + 15) / 16;
-  cudaMemsetAsync(c.touch, 0, nvec * 16, s);
-  k_touch<<<nblocks(c.cap), kBlock, 0, s>>>(c.g, c.dCnt, c.win, c.touch);
+  flag_touched_nodes(c);
   const uint4* fv4 = reinterpret_cast<const uint4*>(c.touch);
   const long long nb = nblocks(nvec);
-  k_flag_count<<<(unsigned)nb, kBlock, 0, s>>>(fv4, nvec, c.iTmpA);
-  scan_exclusive(c.iTmpA, c.iTmpA, nb, nullptr, c.dTotal, c.scanScratch, s, &c.launches);
-  k_set_runs<<<1, 1, 0, s>>>(c.dCnt, c.dTotal);
-  k_flag_emit<<<(unsigned)nb, kBlock, 0, s>>>(fv4, nvec, nflags, c.iTmpA, c.runKey);
+  k_set_runs<<<1, 1, 0, s>>>(c.dCnt, c.dTotal, c.capRuns);
+  k_flag_emit<<<(unsigned)nb, kBlock, 0, s>>>(fv4, nvec, nflags, c.iTmpA, c.runKey, c.capRuns);
   cudaMemsetAsync(c.planAlloc, 0, sizeof(unsigned long long), s);
   k_plan_fill<<<gs_blocks(c.capRuns), kBlock, 0, s>>>(c.g, c.dCnt, c.runKey, c.cellStart, c.cellItems, c.win, c.W,
                                                       c.imgSrc, c.runStart, c.runCnt, c.planRoot, c.planW,
                                                       c.planAlloc, c.capContrib);
   k_plan_total<<<1, 1, 0, s>>>(c.dCnt, c.planAlloc);
-  c.launches += 6;
+  c.launches += 4;
   c.planReady = true;
   c.spreadValid = false;
 }

@@ -15,6 +15,9 @@ struct Ctx {
   cudaStream_t stream = nullptr;
   std::string err = "ok";
   long long launches = 0;
+  size_t bytes = 0;         // device bytes this context holds
+  size_t bytesParcels = 0;  // of which parcel-side buffers
+  long long allocGen = 0;   // bumped whenever device buffers are replaced
 
   // capacities (records, images, pairs, spread contributions)
   int capLocal = 0, capImg = 0, cap = 0;
@@ -79,6 +82,8 @@ struct Ctx {
   double* fPrev = nullptr;       // [capRuns]
   uint32_t* lastNodes = nullptr; // [capRuns] nodes written by the last spread
   long long capRuns = 0;
+  bool runsSized = false;  // run arrays allocated for the counted touched nodes
+  size_t bytesRuns = 0;
 
   // fluid
   double *u = nullptr, *v = nullptr, *w = nullptr;
@@ -125,6 +130,9 @@ void launch_collision_force(Ctx& c);
 // ibm.cu
 void launch_weights(Ctx& c, bool locals);
 void build_spread_plan(Ctx& c);
+// number of touched (component, node) pairs for the current weights; synchronises
+// c.stream (-1 on a CUDA error)
+long long count_touched_nodes(Ctx& c);
 void launch_mdf_reset(Ctx& c, bool frozen);
 void launch_interp(Ctx& c);
 void launch_spread(Ctx& c, bool fused_post_guess);
@@ -142,3 +150,11 @@ void launch_cloud_post(Ctx& c);
 void launch_marker_update(Ctx& c, bool reset, bool adjust);
 
 }  // namespace ibmdem
+
+// the opaque handle of the C ABI
+struct ibmdem_ctx {
+  ibmdem::Ctx c;
+};
+
+// ibmdem_create with the context's allocations and work ordered on `stream`
+int create_on_stream(const ibmdem_params* p, int device, cudaStream_t stream, ibmdem_ctx** out);

@@ -28,7 +28,12 @@ EXPORTS = [
     "ibmdem_AdjustParcelPosition", "ibmdem_InitializationDEM", "ibmdem_MultiDirectForcing",
     "ibmdem_CloudEvolutionStepMS", "ibmdem_CloudEvolutionMS", "ibmdem_step", "ibmdem_launch_count",
     "ibmdem_get_counters", "ibmdem_timing_enable", "ibmdem_get_timing", "ibmdem_phase_name",
-    "ibmdem_measure_fp64_rate", "ibmdem_interpolate_velocity_noalloc",
+    "ibmdem_measure_fp64_rate", "ibmdem_interpolate_velocity_noalloc", "ibmdem_case_bytes",
+    "ibmdem_batch_create", "ibmdem_batch_destroy", "ibmdem_batch_last_error", "ibmdem_batch_add",
+    "ibmdem_batch_set_lanes", "ibmdem_batch_step", "ibmdem_batch_synchronize", "ibmdem_batch_autotune",
+    "ibmdem_server_create", "ibmdem_server_destroy", "ibmdem_server_last_error", "ibmdem_server_submit",
+    "ibmdem_server_poll", "ibmdem_server_status", "ibmdem_server_result", "ibmdem_server_release",
+    "ibmdem_server_memory",
 ]
 
 SUBROUTINES = [
@@ -78,6 +83,27 @@ def load(path=LIB_PATH):
     lib.ibmdem_measure_fp64_rate.argtypes = [i32, P(ctypes.c_double)]
     for name in SUBROUTINES:
         getattr(lib, "ibmdem_" + name).argtypes = [vp]
+    dp = P(ctypes.c_double)
+    lib.ibmdem_case_bytes.argtypes = [vp, i32, vp, i32, P(i64)]
+    lib.ibmdem_batch_create.argtypes = [i32, P(vp)]
+    lib.ibmdem_batch_destroy.argtypes = [vp]
+    lib.ibmdem_batch_last_error.restype = ctypes.c_char_p
+    lib.ibmdem_batch_last_error.argtypes = [vp]
+    lib.ibmdem_batch_add.argtypes = [vp, vp]
+    lib.ibmdem_batch_set_lanes.argtypes = [vp, i32]
+    lib.ibmdem_batch_step.argtypes = [vp, i32]
+    lib.ibmdem_batch_synchronize.argtypes = [vp, P(i32)]
+    lib.ibmdem_batch_autotune.argtypes = [vp, i32, P(i32)]
+    lib.ibmdem_server_create.argtypes = [i32, i64, i32, P(vp)]
+    lib.ibmdem_server_destroy.argtypes = [vp]
+    lib.ibmdem_server_last_error.restype = ctypes.c_char_p
+    lib.ibmdem_server_last_error.argtypes = [vp]
+    lib.ibmdem_server_submit.argtypes = [vp, vp, i32, vp, i32, vp, vp, vp, vp, i32, i32, P(i64)]
+    lib.ibmdem_server_poll.argtypes = [vp, P(i32)]
+    lib.ibmdem_server_status.argtypes = [vp, i64, P(i32), dp, dp]
+    lib.ibmdem_server_result.argtypes = [vp, i64, vp, i32, P(i32), P(i32), vp, i32, P(i32)]
+    lib.ibmdem_server_release.argtypes = [vp, i64]
+    lib.ibmdem_server_memory.argtypes = [vp, P(i64), P(i64)]
     _lib = lib
     return lib
 
@@ -233,3 +259,147 @@ def _make_method(name):
 
 for _name in SUBROUTINES:
     setattr(Case, _name, _make_method(_name))
+
+
+def case_bytes(params, parcels, n_bodies):
+    """Device bytes a case takes once created and initialised (ibmdem_case_bytes)."""
+    lib = load()
+    p = np.array(params, dtype=PARAMS, copy=True)
+    a = np.ascontiguousarray(parcels, dtype=PARCEL)
+    out = ctypes.c_int64()
+    rc = lib.ibmdem_case_bytes(p.ctypes.data, len(a), a.ctypes.data if len(a) else None, int(n_bodies),
+                               ctypes.byref(out))
+    if rc != 0:
+        raise IbmDemError(rc, "ibmdem_case_bytes")
+    return out.value
+
+
+class Batch:
+    """Many cases advanced together, one CUDA graph launch per step (ibmdem_batch_*).
+
+    The member `Case` objects stay owned by the caller and must outlive the batch."""
+
+    def __init__(self, cases=(), device=0, lanes=0):
+        self.lib = load()
+        h = ctypes.c_void_p()
+        rc = self.lib.ibmdem_batch_create(int(device), ctypes.byref(h))
+        if rc != 0:
+            raise IbmDemError(rc, "ibmdem_batch_create failed")
+        self.h = h
+        self.cases = []
+        for c in cases:
+            self.add(c)
+        if lanes:
+            self.set_lanes(lanes)
+
+    def _chk(self, rc, what):
+        if rc != 0:
+            raise IbmDemError(rc, f"{what}: {self.lib.ibmdem_batch_last_error(self.h).decode()}")
+
+    def add(self, case):
+        self._chk(self.lib.ibmdem_batch_add(self.h, case.h), "batch_add")
+        self.cases.append(case)
+
+    def set_lanes(self, lanes):
+        self._chk(self.lib.ibmdem_batch_set_lanes(self.h, int(lanes)), "batch_set_lanes")
+
+    def step(self, n=1):
+        self._chk(self.lib.ibmdem_batch_step(self.h, int(n)), "batch_step")
+
+    def synchronize(self):
+        failed = ctypes.c_int32(-1)
+        self._chk(self.lib.ibmdem_batch_synchronize(self.h, ctypes.byref(failed)), "batch_synchronize")
+
+    def autotune(self, trial_steps=3):
+        lanes = ctypes.c_int32()
+        self._chk(self.lib.ibmdem_batch_autotune(self.h, int(trial_steps), ctypes.byref(lanes)), "batch_autotune")
+        return lanes.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.ibmdem_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """A request server on one device (ibmdem_server_*): admission by device
+    memory budget, each admitted case on its own stream, results read back on
+    completion.  Input arrays are kept referenced until the request is admitted."""
+
+    QUEUED, RUNNING, DONE = 0, 1, 2
+
+    def __init__(self, hbm_budget, max_active=64, device=0):
+        self.lib = load()
+        h = ctypes.c_void_p()
+        rc = self.lib.ibmdem_server_create(int(device), int(hbm_budget), int(max_active), ctypes.byref(h))
+        if rc != 0:
+            raise IbmDemError(rc, "ibmdem_server_create failed")
+        self.h = h
+        self._inputs = {}
+
+    def _chk(self, rc, what):
+        if rc != 0:
+            raise IbmDemError(rc, f"{what}: {self.lib.ibmdem_server_last_error(self.h).decode()}")
+
+    def submit(self, params, parcels, bodies, field=None, nsteps=100, keep_parcels=False):
+        p = np.array(params, dtype=PARAMS, copy=True)
+        a = np.ascontiguousarray(parcels, dtype=PARCEL)
+        b = np.ascontiguousarray(bodies, dtype=MULTISPHERE)
+        shape = field_shape(p)
+        f = None if field is None else [np.ascontiguousarray(x, dtype=np.float64).reshape(shape) for x in field]
+        fp = [None, None, None] if f is None else [x.ctypes.data for x in f]
+        rid = ctypes.c_int64()
+        self._chk(self.lib.ibmdem_server_submit(self.h, p.ctypes.data, len(a), a.ctypes.data, len(b), b.ctypes.data,
+                                                fp[0], fp[1], fp[2], int(nsteps), int(bool(keep_parcels)),
+                                                ctypes.byref(rid)), "server_submit")
+        self._inputs[rid.value] = (p, a, b, f)
+        return rid.value
+
+    def poll(self):
+        pending = ctypes.c_int32()
+        self._chk(self.lib.ibmdem_server_poll(self.h, ctypes.byref(pending)), "server_poll")
+        for rid in [r for r in self._inputs if self.state(r)[0] != self.QUEUED]:
+            del self._inputs[rid]
+        return pending.value
+
+    def state(self, rid):
+        st, lat, q = ctypes.c_int32(), ctypes.c_double(), ctypes.c_double()
+        self._chk(self.lib.ibmdem_server_status(self.h, int(rid), ctypes.byref(st), ctypes.byref(lat),
+                                                ctypes.byref(q)), "server_status")
+        return st.value, lat.value, q.value
+
+    def result(self, rid):
+        npo, nl, nb = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+        self._chk(self.lib.ibmdem_server_result(self.h, int(rid), None, 0, ctypes.byref(npo), ctypes.byref(nl), None, 0,
+                                                ctypes.byref(nb)), "server_result")
+        parts = np.zeros(npo.value, PARCEL)
+        bodies = np.zeros(nb.value, MULTISPHERE)
+        self._chk(self.lib.ibmdem_server_result(self.h, int(rid), parts.ctypes.data, len(parts), ctypes.byref(npo),
+                                                ctypes.byref(nl), bodies.ctypes.data, len(bodies),
+                                                ctypes.byref(nb)), "server_result")
+        return parts, nl.value, bodies
+
+    def release(self, rid):
+        self._chk(self.lib.ibmdem_server_release(self.h, int(rid)), "server_release")
+
+    def memory(self):
+        used, budget = ctypes.c_int64(), ctypes.c_int64()
+        self._chk(self.lib.ibmdem_server_memory(self.h, ctypes.byref(used), ctypes.byref(budget)), "server_memory")
+        return used.value, budget.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.ibmdem_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -180,3 +180,60 @@ def resolved_case(nx, ny, nz, nbodies, d, seed=0, h=1.0, vel_std=0.01, n_modes=3
     field = fourier_field(p, n_modes, amp, seed, device=field_device) if n_modes > 0 else \
         [np.zeros(field_shape(p)) for _ in range(3)]
     return p, parts, bodies, field
+
+
+def kolmogorov_field(p, amp=0.05):
+    """Periodic shear u_x = amp*sin(2*pi*z/Lz) on the u faces (z = (k-1/2)h), v = w = 0,
+    Fortran layout with the periodic 2-cell halo."""
+    nz = int(p["nz"])
+    h = float(p["dz"])
+    shape = field_shape(p)
+    k = (np.arange(shape[0]) - 2) % nz + 1  # interior index of every z layer, halo wrapped
+    prof = amp * np.sin(2 * math.pi * ((k - 0.5) * h) / (nz * h))
+    u = np.broadcast_to(prof[:, None, None], shape).copy()
+    return [u, np.zeros(shape), np.zeros(shape)]
+
+
+def _capped_bodies(n_cells, d, nb, max_fraction):
+    cap = int(max_fraction * n_cells / (math.pi / 6.0 * d ** 3))
+    return max(1, min(nb, cap))
+
+
+def batched_mix(n_cases=256, seed=0, max_fraction=0.25, n_modes=32, field_device="cpu"):
+    """Independent resolved cases of uneven size: case i draws (seed + i) a cubic
+    grid from {32, 64, 96, 128}^3, a diameter from {8, 12, 16}h and a body count
+    log-uniform in 8..512, capped so that the spheres fill at most max_fraction
+    of the box; positions, velocities and the Fourier field as resolved_case."""
+    out = []
+    for i in range(n_cases):
+        r = np.random.default_rng(seed + i)
+        n = int(r.choice([32, 64, 96, 128]))
+        d = float(r.choice([8.0, 12.0, 16.0]))
+        nb = int(round(math.exp(r.uniform(math.log(8), math.log(512)))))
+        nb = _capped_bodies(n ** 3, d, nb, max_fraction)
+        out.append(resolved_case(n, n, n, nb, d, seed=seed + i, n_modes=n_modes, field_device=field_device))
+    return out
+
+
+def serve_requests(n_requests=32, seed=0, rate=200.0, d=12.0, max_fraction=0.2, grids=(64, 96, 128, 192, 256)):
+    """A Poisson request stream (mean `rate` per second): request i has an
+    arrival time, a body count log-uniform in 16..2048 on the smallest cubic grid
+    of `grids` that keeps the solid fraction at most max_fraction (the largest
+    grid caps the count), and is a settling case (fluid at rest, gravity) or a
+    shear case (Kolmogorov field of amplitude 0.05), alternating at random.
+    Returns a list of dicts with arrival, kind and the case (params, parcels,
+    bodies, field or None)."""
+    rng = np.random.default_rng(seed)
+    t = 0.0
+    out = []
+    for i in range(n_requests):
+        t += rng.exponential(1.0 / rate)
+        nb = int(round(math.exp(rng.uniform(math.log(16), math.log(2048)))))
+        vol = math.pi / 6.0 * d ** 3
+        n = next((g for g in grids if nb * vol <= max_fraction * g ** 3), grids[-1])
+        nb = _capped_bodies(n ** 3, d, nb, max_fraction)
+        kind = "shear" if rng.random() < 0.5 else "settling"
+        p, parts, bodies, _ = resolved_case(n, n, n, nb, d, seed=seed * 100003 + i, n_modes=0)
+        field = kolmogorov_field(p) if kind == "shear" else None
+        out.append({"arrival": t, "kind": kind, "case": (p, parts, bodies, field)})
+    return out

@@ -182,6 +182,65 @@ int ibmdem_step(ibmdem_ctx* ctx, int32_t nsteps);
 #define IBMDEM_PROBE_MAX_POINTS 16384
 int ibmdem_interpolate_velocity_noalloc(ibmdem_ctx* ctx, int32_t n, const double* x, double* ulp);
 
+/* ---- many cases on one device ---------------------------------------- */
+/* Device bytes a case of these parameters, np parcels at the given positions
+ * and nMS bodies takes once created and initialised (fields, lists, weights
+ * and spread-plan capacities).  No counterpart in the reference. */
+int ibmdem_case_bytes(const ibmdem_params* p, int32_t np, const ibmdem_parcel* parts, int32_t nMS, int64_t* bytes);
+
+/* A batch advances many independent cases together: one frozen-fluid step of
+ * every member (ibmdem_step) is captured into one CUDA graph whose `lanes`
+ * concurrent chains each run a share of the cases, and each batch step is one
+ * graph launch.  A case's results are the same in a batch as alone.  Member
+ * contexts stay owned by the caller and must be initialised
+ * (ibmdem_InitializationDEM) before the first batch step; a member changed
+ * outside the batch (new parcels, bodies or lists) is re-captured at the next
+ * batch step.  Work on a member's own stream is ordered before and after each
+ * ibmdem_batch_step call.  No counterpart in the reference (one case per MPI
+ * job there). */
+typedef struct ibmdem_batch ibmdem_batch;
+int ibmdem_batch_create(int32_t device, ibmdem_batch** out);
+int ibmdem_batch_destroy(ibmdem_batch* b);
+const char* ibmdem_batch_last_error(const ibmdem_batch* b);
+int ibmdem_batch_add(ibmdem_batch* b, ibmdem_ctx* ctx);
+/* Number of concurrent chains; 0 = one per case. */
+int ibmdem_batch_set_lanes(ibmdem_batch* b, int32_t lanes);
+int ibmdem_batch_step(ibmdem_batch* b, int32_t nsteps);
+/* Waits for the batch and checks every member for device errors; the first
+ * failing member's index goes to *failed_case (-1 if none). */
+int ibmdem_batch_synchronize(ibmdem_batch* b, int32_t* failed_case);
+/* Times trial_steps batch steps for several lane counts (all, 128, 64, ..., 1)
+ * and keeps the fastest in *lanes_out.  The trials advance every member. */
+int ibmdem_batch_autotune(ibmdem_batch* b, int32_t trial_steps, int32_t* lanes_out);
+
+/* A request server on one device.  Requests wait first-in first-out and are
+ * admitted while the running cases' summed ibmdem_case_bytes stays within
+ * hbm_budget and fewer than max_active run.  An admitted case is created on
+ * its own stream, initialised, its step captured as a graph and all of its
+ * nsteps frozen-fluid steps queued at once, so requests admitted at different
+ * times overlap on the device.  ibmdem_server_poll (non-blocking) retires
+ * finished cases -- bodies (and parcels when keep_parcels) are read back and
+ * the device memory returned -- and admits waiting ones.  The parcel, body and
+ * field arrays of a request are borrowed until it leaves the queue; u = v = w =
+ * NULL means a fluid at rest.  Latency = completion - submission (host clock).
+ * No counterpart in the reference. */
+typedef struct ibmdem_server ibmdem_server;
+int ibmdem_server_create(int32_t device, int64_t hbm_budget, int32_t max_active, ibmdem_server** out);
+int ibmdem_server_destroy(ibmdem_server* s);
+const char* ibmdem_server_last_error(const ibmdem_server* s);
+int ibmdem_server_submit(ibmdem_server* s, const ibmdem_params* p, int32_t np, const ibmdem_parcel* parts,
+                         int32_t nMS, const ibmdem_multisphere* bodies, const double* u, const double* v,
+                         const double* w, int32_t nsteps, int32_t keep_parcels, int64_t* id);
+/* *pending = requests queued or running. */
+int ibmdem_server_poll(ibmdem_server* s, int32_t* pending);
+/* *state: 0 queued, 1 running, 2 done, < 0 failed with that status code. */
+int ibmdem_server_status(ibmdem_server* s, int64_t id, int32_t* state, double* latency_s, double* queue_s);
+int ibmdem_server_result(ibmdem_server* s, int64_t id, ibmdem_parcel* parts, int32_t cap_parts, int32_t* np,
+                         int32_t* nlocal, ibmdem_multisphere* bodies, int32_t cap_bodies, int32_t* nMS);
+/* Drops a finished request's record and results. */
+int ibmdem_server_release(ibmdem_server* s, int64_t id);
+int ibmdem_server_memory(const ibmdem_server* s, int64_t* in_use, int64_t* budget);
+
 /* ---- instrumentation -------------------------------------------------- */
 /* Record CUDA events around every phase of the drivers (interpolation,
  * spreading, weights, spread plan, cell lists, contact lists, contact force,

@@ -1,0 +1,139 @@
+"""Many cases on one device: batch (one graph launch per step) and request server.
+
+Each case must give the same parcels, bodies and fields in a batch, or through
+the server while other requests overlap it, as when it runs alone.  The
+kernels of a case are the same in all three paths and none of them sums across
+cases, so the comparison is exact.
+"""
+import numpy as np
+import pytest
+
+import cases
+from ibmdem import api, scenario
+
+pytestmark = pytest.mark.gpu
+
+PARCEL_FIELDS = ("x", "v", "fcol", "fdrag", "vgap", "globalIdx", "MSIdx", "cellIdx")
+BODY_FIELDS = ("x", "v", "omega", "AngMom", "rotMatGlo", "fcol", "fdrag", "fmom", "fmomCol")
+
+
+def mixed_cases():
+    out = [cases.contact_case(seed=3)]
+    out.append(scenario.resolved_case(32, 32, 32, 6, 8.0, seed=5, n_modes=8))
+    out.append(scenario.resolved_case(40, 32, 24, 3, 10.0, seed=6, n_modes=8))
+    p, parts, bodies, _ = scenario.resolved_case(28, 28, 28, 4, 8.0, seed=7, n_modes=0)
+    out.append((p, parts, bodies, None))  # a fluid at rest
+    return out
+
+
+def make_case(c):
+    p, parts, bodies, field = c
+    if field is None:
+        shape = api.field_shape(np.array(p, dtype=api.PARAMS))
+        field = [np.zeros(shape) for _ in range(3)]
+    case = api.Case(p, parts, bodies, field, device=0)
+    case.InitializationDEM()
+    return case
+
+
+def snapshot(case):
+    parts, nl = case.get_parcels()
+    bodies = case.get_bodies()
+    u, v, w, fx, fy, fz = case.get_fluid()
+    return parts, nl, bodies, (u, v, w, fx, fy, fz)
+
+
+def assert_same(a, b, fields=True):
+    pa, nla, ba, fa = a
+    pb, nlb, bb, fb = b
+    assert nla == nlb and len(pa) == len(pb)
+    for f in PARCEL_FIELDS:
+        assert np.array_equal(pa[f], pb[f]), f
+    for f in BODY_FIELDS:
+        assert np.array_equal(ba[f], bb[f]), f
+    if fields:
+        for x, y in zip(fa, fb):
+            assert np.array_equal(x, y)
+
+
+def alone(c, steps):
+    case = make_case(c)
+    case.step(steps)
+    out = snapshot(case)
+    case.close()
+    return out
+
+
+@pytest.mark.parametrize("lanes", [0, 1, 2])
+def test_batch_matches_each_case_alone(gpu_lib, lanes):
+    cs = mixed_cases()
+    steps = 3
+    ref = [alone(c, steps) for c in cs]
+    members = [make_case(c) for c in cs]
+    b = api.Batch(members, lanes=lanes)
+    b.step(1)
+    b.step(steps - 1)
+    b.synchronize()
+    for case, r in zip(members, ref):
+        assert_same(snapshot(case), r)
+    b.close()
+    for case in members:
+        case.close()
+
+
+def test_batch_autotune_and_recapture(gpu_lib):
+    cs = mixed_cases()[:3]
+    members = [make_case(c) for c in cs]
+    b = api.Batch(members)
+    lanes = b.autotune(trial_steps=1)
+    assert 1 <= lanes <= len(cs)
+    n_auto = 2 * len({len(cs), 2, 1})  # each candidate: one warm-up + one trial step
+    b.step(2)
+    b.synchronize()
+    # a member changed outside the batch is re-captured: reload case 0 and rebuild it
+    p, parts, bodies, field = cs[0]
+    members[0].set_parcels(parts)
+    members[0].set_bodies(bodies)
+    members[0].set_fluid(*field)
+    members[0].InitializationDEM()
+    b.step(2)
+    b.synchronize()
+    assert_same(snapshot(members[0]), alone(cs[0], 2))
+    for i in (1, 2):
+        assert_same(snapshot(members[i]), alone(cs[i], n_auto + 4))
+    b.close()
+    for case in members:
+        case.close()
+
+
+def test_server_results_match_alone_under_overlap(gpu_lib):
+    cs = mixed_cases()
+    steps = 4
+    ref = [alone(c, steps) for c in cs]
+    sizes = [api.case_bytes(c[0], c[1], len(c[2])) for c in cs]
+    # room for the largest case and one more: the rest wait in the queue
+    budget = max(sizes) + min(sizes)
+    srv = api.Server(budget, max_active=8)
+    ids = [srv.submit(c[0], c[1], c[2], c[3], nsteps=steps, keep_parcels=True) for c in cs]
+    peak = 0
+    for _ in range(200000):
+        pending = srv.poll()
+        used, _ = srv.memory()
+        peak = max(peak, used)
+        if pending == 0:
+            break
+    assert pending == 0
+    assert 0 < peak <= budget
+    lat = []
+    for rid, r in zip(ids, ref):
+        st, latency, queued = srv.state(rid)
+        assert st == api.Server.DONE, st
+        assert latency >= queued >= 0
+        lat.append(latency)
+        parts, nl, bodies = srv.result(rid)
+        assert_same((parts, nl, bodies, None), r, fields=False)
+        srv.release(rid)
+    with pytest.raises(api.IbmDemError):
+        big = scenario.resolved_case(64, 64, 64, 8, 12.0, seed=1, n_modes=0)
+        srv.submit(big[0], big[1], big[2], None, nsteps=1)
+    srv.close()

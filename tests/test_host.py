@@ -79,3 +79,24 @@ def test_max_over_ranks_gloo_two_ranks():
         pr.join(timeout=60)
         assert pr.exitcode == 0
     assert out == {0: 2.5, 1: 2.5}
+
+
+def test_case_bytes_estimate():
+    """ibmdem_case_bytes is host arithmetic over the same buffer list the
+    context allocates: it grows with the grid and the parcels, counts the
+    periodic images, and rejects what ibmdem_create rejects."""
+    from ibmdem import api
+    p, parts, bodies, _ = scenario.resolved_case(32, 32, 32, 4, 8.0, seed=2, n_modes=0)
+    b0 = api.case_bytes(p, parts[:0], 0)
+    b1 = api.case_bytes(p, parts, len(bodies))
+    assert b1 > b0 > 9 * 36 ** 3 * 8
+    p2 = make_params(48, 48, 48)
+    assert api.case_bytes(p2, parts, len(bodies)) - b1 >= 9 * 8 * (52 ** 3 - 36 ** 3)
+    # the same parcels moved next to a face need image capacity
+    edge = parts.copy()
+    edge["x"][:, 0] = 0.25
+    assert api.case_bytes(p, edge, len(bodies)) > b1
+    bad = p.copy()
+    bad["bType"][0] = 1
+    with pytest.raises(api.IbmDemError):
+        api.case_bytes(bad, parts, len(bodies))
