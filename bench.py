@@ -90,6 +90,11 @@ def parse():
     ap.add_argument("--batch-steps", type=int, default=10)
     ap.add_argument("--serve-requests", type=int, default=32, help="requests of the served stream (0 = skip)")
     ap.add_argument("--serve-steps", type=int, default=100)
+    ap.add_argument("--unresolved-particles", type=int, default=1_048_576,
+                    help="particles of the unresolved CFD-DEM case (0 = skip)")
+    ap.add_argument("--unresolved-steps", type=int, default=100)
+    ap.add_argument("--serve-work-limit", type=int, default=2_000_000,
+                    help="markers the running requests may hold together (0 = no limit)")
     return ap.parse_args()
 
 
@@ -325,7 +330,7 @@ def run_served(args, device, stream):
         plain_lat.append(done - r["arrival"])
     plain_span = done - reqs[0]["arrival"]
     # served
-    srv = api.Server(budget, max_active=64, device=device)
+    srv = api.Server(budget, max_active=64, device=device, work_limit=args.serve_work_limit)
     ids = []
     t0 = time.perf_counter()
     i = 0
@@ -360,10 +365,64 @@ def run_served(args, device, stream):
             "steps_per_request": steps, "rate_per_s": 200.0,
             "bodies": sum(len(r["case"][2]) for r in reqs), "markers": sum(len(r["case"][1]) for r in reqs),
             "hbm_budget_bytes": budget, "peak_bytes_admitted": peak, "max_active": 64,
+            "work_limit_markers": args.serve_work_limit,
             "workload": "Poisson arrivals (200/s, seed %d) of settling (fluid at rest, gravity) and shear "
                         "(Kolmogorov u_x = 0.05 sin(2 pi z/L)) cases, 16..2048 bodies d = 12h on the smallest of "
                         "64..256^3 holding them at <= 20%% solid fraction" % args.seed,
             "latency": "completion - arrival, host clock"}
+
+
+def run_unresolved(args, device, stream, cpu=True):
+    """Unresolved CFD-DEM: 1,048,576 polydisperse point particles on a 128^3 periodic
+    fluid grid (packed bed plus gas region, upward flow 0.5 with a 5% Fourier
+    perturbation), Gaussian volume fraction, drag of CalculateDragForce, contacts
+    with Coulomb friction and tangential history.  Device-timed steps; the CPU
+    restatement times one step of the same case on all host threads."""
+    import torch
+    from ibmdem import api, scenario
+
+    n = args.unresolved_particles
+    p, parts, field = scenario.unresolved_case(128, n, seed=args.seed, n_modes=32, field_device="cuda",
+                                               bed_spacing=0.9)
+    g = api.Unresolved(p, parts, field, device=device, stream=stream)
+    g.step(3)
+    g.synchronize()
+    k = args.unresolved_steps
+    l0 = g.launches
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    g.step(k)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    g.synchronize()
+    ms = e0.elapsed_time(e1)
+    launches = g.launches - l0
+    st, partner, _ = g.get_contacts()
+    g.close()
+    out = {"value": n * k / (ms / 1e3), "unit": "particle-steps/s", "steps": k, "ms_per_step": ms / k,
+           "particles": n, "contacts_last_step": int(len(partner)), "gpu_launches": launches,
+           "workload": "128^3 periodic fluid cells (h = 1 mm), d ~ U[0.8,1.2] x 0.25 h, 75%% in a packed bed "
+                       "(jittered lattice of 0.9 x the largest diameter from z = 0, so neighbours start in contact), "
+                       "25%% in the gas region, upward flow 0.5 m/s + 5%% 32-mode "
+                       "Fourier perturbation, Gaussian volume fraction (sigma = 3 d, 5^3 cells), Di Felice drag "
+                       "(CalculateDragForce), spring-dashpot with Coulomb friction (mu = 0.3, kt = 2/7 kn), "
+                       "dt = 1e-5 s, seed %d" % args.seed,
+           "timing": "CUDA events on the launching stream"}
+    if cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+
+        O.build()
+        threads = os.cpu_count() or 1
+        O.set_threads(threads)
+        r = O.OracleUnresolved(p, parts, field)
+        t0 = time.perf_counter()
+        r.step(1)
+        dt = time.perf_counter() - t0
+        r.close()
+        out["cpu_baseline"] = {"value": n / dt, "unit": "particle-steps/s", "cores": threads, "kind": "port",
+                               "sample": "1 step of the same case (CPU restatement, OpenMP)", "seconds": dt}
+    return out
 
 
 def run_ours(args):
@@ -495,6 +554,8 @@ def run_ours(args):
             line["batched"] = run_batched(args, local, stream)
         if args.serve_requests > 0:
             line["served"] = run_served(args, local, stream)
+        if args.unresolved_particles > 0:
+            line["unresolved"] = run_unresolved(args, local, stream, cpu=not args.no_cpu_baseline)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -240,7 +240,7 @@ struct Request {
   const double *u = nullptr, *v = nullptr, *w = nullptr;
   bool keepParcels = false;
   long long bytes = 0;
-  bool reserved = false;  // bytes counted in the server's in-use total
+  bool reserved = false;  // bytes and parcels counted in the server's in-use totals
   double tSubmit = 0, tAdmit = 0, tDone = 0;
   int state = 0;  // 0 queued, 1 running, 2 done, < 0 failed (status code)
   ibmdem_ctx* ctx = nullptr;
@@ -261,6 +261,8 @@ struct ibmdem_server {
   long long budget = 0;
   int maxActive = 0;
   long long inUse = 0;
+  long long workLimit = 0;  // parcels in flight (0: no limit)
+  long long workInUse = 0;
   long long nextId = 1;
   std::deque<Request*> queue;
   std::vector<Request*> running;
@@ -281,7 +283,10 @@ void release_device(ibmdem_server* s, Request* r) {
   r->done = nullptr;
   if (r->stream) cudaStreamDestroy(r->stream);
   r->stream = nullptr;
-  if (r->reserved) s->inUse -= r->bytes;
+  if (r->reserved) {
+    s->inUse -= r->bytes;
+    s->workInUse -= r->np;
+  }
   r->reserved = false;
 }
 
@@ -298,6 +303,7 @@ int fail(ibmdem_server* s, Request* r, int code) {
 int admit(ibmdem_server* s, Request* r) {
   r->tAdmit = now_s();
   s->inUse += r->bytes;
+  s->workInUse += r->np;
   r->reserved = true;
   r->state = 1;
   auto cu = [&](cudaError_t e, const char* what) {
@@ -578,9 +584,11 @@ int ibmdem_server_poll(ibmdem_server* s, int32_t* pending) {
     s->running[i] = s->running.back();
     s->running.pop_back();
   }
-  // admit in arrival order while the budget and the slots allow
+  // admit in arrival order while the budget, the slots and the work limit
+  // allow (the work limit always lets one case run)
   while (!s->queue.empty() && (int)s->running.size() < s->maxActive &&
-         s->inUse + s->queue.front()->bytes <= s->budget) {
+         s->inUse + s->queue.front()->bytes <= s->budget &&
+         (s->workLimit <= 0 || s->running.empty() || s->workInUse + s->queue.front()->np <= s->workLimit)) {
     Request* r = s->queue.front();
     s->queue.pop_front();
     admit(s, r);
@@ -637,6 +645,12 @@ int ibmdem_server_release(ibmdem_server* s, int64_t id) {
   }
   s->all.erase(it);
   delete r;
+  return IBMDEM_OK;
+}
+
+int ibmdem_server_set_work_limit(ibmdem_server* s, int64_t parcels) {
+  if (!s || parcels < 0) return IBMDEM_EINVAL;
+  s->workLimit = parcels;
   return IBMDEM_OK;
 }
 

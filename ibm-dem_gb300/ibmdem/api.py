@@ -11,7 +11,7 @@ import os
 
 import numpy as np
 
-from .records import MULTISPHERE, PARAMS, PARCEL, field_shape
+from .records import MULTISPHERE, PARAMS, PARCEL, PARTICLE, UPARAMS, field_shape, ufield_shape
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_lib", "libibmdem.so")
@@ -33,7 +33,12 @@ EXPORTS = [
     "ibmdem_batch_set_lanes", "ibmdem_batch_step", "ibmdem_batch_synchronize", "ibmdem_batch_autotune",
     "ibmdem_server_create", "ibmdem_server_destroy", "ibmdem_server_last_error", "ibmdem_server_submit",
     "ibmdem_server_poll", "ibmdem_server_status", "ibmdem_server_result", "ibmdem_server_release",
-    "ibmdem_server_memory",
+    "ibmdem_server_memory", "ibmdem_server_set_work_limit",
+    "ibmdem_unresolved_create", "ibmdem_unresolved_destroy", "ibmdem_unresolved_last_error",
+    "ibmdem_unresolved_set_stream", "ibmdem_unresolved_set_fluid", "ibmdem_unresolved_set_particles",
+    "ibmdem_unresolved_get_particles", "ibmdem_unresolved_get_volume_fraction", "ibmdem_unresolved_get_contacts",
+    "ibmdem_unresolved_step", "ibmdem_unresolved_synchronize", "ibmdem_unresolved_launch_count",
+    "ibmdem_CalculateDragForce",
 ]
 
 SUBROUTINES = [
@@ -104,6 +109,22 @@ def load(path=LIB_PATH):
     lib.ibmdem_server_result.argtypes = [vp, i64, vp, i32, P(i32), P(i32), vp, i32, P(i32)]
     lib.ibmdem_server_release.argtypes = [vp, i64]
     lib.ibmdem_server_memory.argtypes = [vp, P(i64), P(i64)]
+    lib.ibmdem_server_set_work_limit.argtypes = [vp, i64]
+    lib.ibmdem_unresolved_create.argtypes = [vp, i32, P(vp)]
+    lib.ibmdem_unresolved_destroy.argtypes = [vp]
+    lib.ibmdem_unresolved_last_error.restype = ctypes.c_char_p
+    lib.ibmdem_unresolved_last_error.argtypes = [vp]
+    lib.ibmdem_unresolved_set_stream.argtypes = [vp, vp]
+    lib.ibmdem_unresolved_set_fluid.argtypes = [vp, vp, vp, vp]
+    lib.ibmdem_unresolved_set_particles.argtypes = [vp, i32, vp]
+    lib.ibmdem_unresolved_get_particles.argtypes = [vp, vp, i32, P(i32)]
+    lib.ibmdem_unresolved_get_volume_fraction.argtypes = [vp, vp]
+    lib.ibmdem_unresolved_get_contacts.argtypes = [vp, vp, vp, vp, P(i32)]
+    lib.ibmdem_unresolved_step.argtypes = [vp, i32]
+    lib.ibmdem_unresolved_synchronize.argtypes = [vp]
+    lib.ibmdem_unresolved_launch_count.restype = i64
+    lib.ibmdem_unresolved_launch_count.argtypes = [vp]
+    lib.ibmdem_CalculateDragForce.argtypes = [i32, vp, vp, vp, ctypes.c_double, vp, vp, vp, vp]
     _lib = lib
     return lib
 
@@ -334,7 +355,7 @@ class Server:
 
     QUEUED, RUNNING, DONE = 0, 1, 2
 
-    def __init__(self, hbm_budget, max_active=64, device=0):
+    def __init__(self, hbm_budget, max_active=64, device=0, work_limit=0):
         self.lib = load()
         h = ctypes.c_void_p()
         rc = self.lib.ibmdem_server_create(int(device), int(hbm_budget), int(max_active), ctypes.byref(h))
@@ -342,6 +363,8 @@ class Server:
             raise IbmDemError(rc, "ibmdem_server_create failed")
         self.h = h
         self._inputs = {}
+        if work_limit:
+            self._chk(self.lib.ibmdem_server_set_work_limit(self.h, int(work_limit)), "server_set_work_limit")
 
     def _chk(self, rc, what):
         if rc != 0:
@@ -403,3 +426,83 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+class Unresolved:
+    """One unresolved CFD-DEM case (point particles) resident on a GB300 (ibmdem_unresolved_*)."""
+
+    def __init__(self, params, particles=None, field=None, device=0, stream=None):
+        self.lib = load()
+        self.params = np.array(params, dtype=UPARAMS, copy=True)
+        h = ctypes.c_void_p()
+        rc = self.lib.ibmdem_unresolved_create(self.params.ctypes.data, int(device), ctypes.byref(h))
+        if rc != 0:
+            raise IbmDemError(rc, "ibmdem_unresolved_create failed (no CUDA device, or unsupported parameters)")
+        self.h = h
+        self.shape = ufield_shape(self.params)
+        self.nint = int(self.params["nx"]) * int(self.params["ny"]) * int(self.params["nz"])
+        if stream is not None:
+            handle = stream if isinstance(stream, int) else int(getattr(stream, "cuda_stream", stream))
+            self._chk(self.lib.ibmdem_unresolved_set_stream(self.h, ctypes.c_void_p(handle)), "set_stream")
+        if field is not None:
+            self.set_fluid(*field)
+        if particles is not None:
+            self.set_particles(particles)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.ibmdem_unresolved_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _chk(self, rc, what):
+        if rc != 0:
+            raise IbmDemError(rc, f"{what}: {self.lib.ibmdem_unresolved_last_error(self.h).decode()}")
+
+    @property
+    def launches(self):
+        return int(self.lib.ibmdem_unresolved_launch_count(self.h))
+
+    def set_fluid(self, u, v, w):
+        a = [np.ascontiguousarray(x, dtype=np.float64).reshape(self.shape) for x in (u, v, w)]
+        self._chk(self.lib.ibmdem_unresolved_set_fluid(self.h, *[x.ctypes.data for x in a]), "set_fluid")
+
+    def set_particles(self, parts):
+        a = np.ascontiguousarray(parts, dtype=PARTICLE)
+        self._chk(self.lib.ibmdem_unresolved_set_particles(self.h, len(a), a.ctypes.data), "set_particles")
+
+    def get_particles(self):
+        n = ctypes.c_int32()
+        self._chk(self.lib.ibmdem_unresolved_get_particles(self.h, None, 0, ctypes.byref(n)), "get_particles")
+        out = np.zeros(n.value, PARTICLE)
+        self._chk(self.lib.ibmdem_unresolved_get_particles(self.h, out.ctypes.data, len(out), ctypes.byref(n)),
+                  "get_particles")
+        return out
+
+    def get_volume_fraction(self):
+        out = np.zeros(self.nint)
+        self._chk(self.lib.ibmdem_unresolved_get_volume_fraction(self.h, out.ctypes.data), "get_volume_fraction")
+        return out
+
+    def get_contacts(self):
+        n = ctypes.c_int32()
+        self._chk(self.lib.ibmdem_unresolved_get_contacts(self.h, None, None, None, ctypes.byref(n)), "get_contacts")
+        nparts = ctypes.c_int32()
+        self._chk(self.lib.ibmdem_unresolved_get_particles(self.h, None, 0, ctypes.byref(nparts)), "get_particles")
+        start = np.zeros(nparts.value + 1, np.int32)
+        partner = np.zeros(max(n.value, 1), np.int32)
+        xi = np.zeros((max(n.value, 1), 3))
+        self._chk(self.lib.ibmdem_unresolved_get_contacts(self.h, start.ctypes.data, partner.ctypes.data,
+                                                          xi.ctypes.data, ctypes.byref(n)), "get_contacts")
+        return start, partner[:n.value], xi[:n.value]
+
+    def step(self, n=1):
+        self._chk(self.lib.ibmdem_unresolved_step(self.h, int(n)), "step")
+
+    def synchronize(self):
+        self._chk(self.lib.ibmdem_unresolved_synchronize(self.h), "synchronize")

@@ -55,3 +55,38 @@ def make_params(nx, ny, nz, h=1.0, dt=1e-3, coupleInterval=1, Ns=5, rhof=1e3, kn
 def field_shape(p):
     """(nk, nj, ni) C-order view of a Fortran (lg1:ug1, lg2:ug2, lg3:ug3) array."""
     return (int(p["nz"]) + 4, int(p["ny"]) + 4, int(p["nx"]) + 4)
+
+
+# unresolved CFD-DEM path (point particles); no counterpart record in the reference
+PARTICLE = np.dtype([
+    ("globalIdx", "<i4"), ("pad_", "<i4"),
+    ("rad", "<f8"), ("rho", "<f8"), ("vol", "<f8"), ("m", "<f8"), ("I", "<f8"),
+    ("x", "<f8", 3), ("v", "<f8", 3), ("omega", "<f8", 3),
+    ("fcol", "<f8", 3), ("tcol", "<f8", 3), ("fdrag", "<f8", 3), ("alphaf", "<f8"),
+])
+assert PARTICLE.itemsize == 200
+
+UPARAMS = np.dtype([
+    ("nx", "<i4"), ("ny", "<i4"), ("nz", "<i4"), ("maxContacts", "<i4"),
+    ("dx", "<f8"), ("dcell", "<f8"), ("dt", "<f8"), ("rhof", "<f8"), ("viscf", "<f8"),
+    ("knCoeff", "<f8"), ("ResistCoeff", "<f8"), ("ktRatio", "<f8"), ("mu", "<f8"),
+    ("bandwidth", "<f8"), ("alphaMin", "<f8"), ("gravity", "<f8", 3),
+])
+assert UPARAMS.itemsize == 128
+
+
+def make_uparams(nx, ny, nz, dx, dcell, dt=1e-5, rhof=1.2, viscf=1e-5, knCoeff=1e4, ResistCoeff=0.9,
+                 ktRatio=2.0 / 7.0, mu=0.3, bandwidth=3.0, alphaMin=0.2, maxContacts=16,
+                 gravity=(0.0, 0.0, -9.81)):
+    """Unresolved-path parameters (viscf defaults to the reference's 1e-5, ZJS_VARS.F90:77)."""
+    p = np.zeros((), UPARAMS)
+    p["nx"], p["ny"], p["nz"], p["maxContacts"] = nx, ny, nz, maxContacts
+    p["dx"], p["dcell"], p["dt"], p["rhof"], p["viscf"] = dx, dcell, dt, rhof, viscf
+    p["knCoeff"], p["ResistCoeff"], p["ktRatio"], p["mu"] = knCoeff, ResistCoeff, ktRatio, mu
+    p["bandwidth"], p["alphaMin"], p["gravity"] = bandwidth, alphaMin, gravity
+    return p
+
+
+def ufield_shape(p):
+    """Fluid array shape of an unresolved case (same layout as field_shape)."""
+    return (int(p["nz"]) + 4, int(p["ny"]) + 4, int(p["nx"]) + 4)

@@ -237,3 +237,62 @@ def serve_requests(n_requests=32, seed=0, rate=200.0, d=12.0, max_fraction=0.2, 
         field = kolmogorov_field(p) if kind == "shear" else None
         out.append({"arrival": t, "kind": kind, "case": (p, parts, bodies, field)})
     return out
+
+
+def unresolved_case(n=128, n_particles=1_048_576, seed=0, h=1e-3, d_mean=0.25, bed_share=0.75, u_up=0.5,
+                    perturb=0.05, n_modes=32, rho_p=2500.0, field_device="cpu", bed_spacing=1.05, **param_kw):
+    """Unresolved CFD-DEM case: n^3 periodic fluid cells of size h, polydisperse
+    spheres with d uniform in [0.8, 1.2] * d_mean * h.  A packed bed: the first
+    bed_share of the particles on a jittered lattice of spacing 1.05 * max d
+    filling layers from z = 0 (bed_spacing < 1 packs them into contact); the
+    rest on a coarser jittered lattice spread over the gas region above.  Fluid: uniform upward flow u_up
+    plus a divergence-free Fourier perturbation of amplitude perturb * u_up.
+    Bed particles start at rest, gas particles with N(0, 0.01 u_up) velocities.
+    DEM cells of 1.1 * max d.  Returns (params, particles, (u, v, w))."""
+    from .records import PARTICLE, make_params, make_uparams
+
+    rng = np.random.default_rng(seed)
+    L = n * h
+    dmax = 1.2 * d_mean * h
+    d = rng.uniform(0.8, 1.2, n_particles) * d_mean * h
+    nbed = int(round(bed_share * n_particles))
+    a = bed_spacing * dmax
+    m = int(L // a)
+    per_layer = m * m
+    k = np.arange(nbed)
+    lay, rem = k // per_layer, k % per_layer
+    jit = abs(a - dmax) / 2
+    bed = np.stack([(rem % m + 0.5) * a, (rem // m + 0.5) * a, (lay + 0.5) * a], axis=1)
+    bed += rng.uniform(-jit, jit, bed.shape)
+    top = (lay.max() + 1) * a if nbed else 0.0
+    ngas = n_particles - nbed
+    gas = np.zeros((0, 3))
+    if ngas:
+        hgt = L - top - a
+        ag = (L * L * hgt / ngas) ** (1.0 / 3.0)
+        mx, mz = max(int(L // ag), 1), max(int(hgt // ag), 1)
+        while mx * mx * mz < ngas:
+            ag *= 0.98
+            mx, mz = max(int(L // ag), 1), max(int(hgt // ag), 1)
+        pick = rng.permutation(mx * mx * mz)[:ngas]
+        gx, gy, gz = pick % mx, (pick // mx) % mx, pick // (mx * mx)
+        sx, sz = L / mx, hgt / mz
+        gas = np.stack([(gx + 0.5) * sx, (gy + 0.5) * sx, top + a / 2 + (gz + 0.5) * sz], axis=1)
+        gj = (min(sx, sz) - dmax) / 2
+        gas += rng.uniform(-gj, gj, gas.shape)
+    x = np.concatenate([bed, gas]) % L
+    parts = np.zeros(n_particles, PARTICLE)
+    parts["globalIdx"] = np.arange(1, n_particles + 1)
+    parts["x"] = x
+    parts["rad"] = d / 2
+    parts["rho"] = rho_p
+    parts["vol"] = np.pi / 6.0 * d ** 3
+    parts["m"] = rho_p * parts["vol"]
+    parts["I"] = 0.1 * parts["m"] * d ** 2
+    parts["v"][nbed:] = rng.standard_normal((ngas, 3)) * 0.01 * u_up
+    p = make_uparams(n, n, n, h, 1.1 * dmax, **param_kw)
+    pf = make_params(n, n, n, h=h)
+    field = fourier_field(pf, n_modes, perturb * u_up, seed, device=field_device) if n_modes else \
+        [np.zeros(field_shape(pf)) for _ in range(3)]
+    field[2] = field[2] + u_up
+    return p, parts, field

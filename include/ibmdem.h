@@ -182,6 +182,82 @@ int ibmdem_step(ibmdem_ctx* ctx, int32_t nsteps);
 #define IBMDEM_PROBE_MAX_POINTS 16384
 int ibmdem_interpolate_velocity_noalloc(ibmdem_ctx* ctx, int32_t n, const double* x, double* ulp);
 
+/* ---- unresolved CFD-DEM path ------------------------------------------ */
+/* Point particles smaller than a fluid cell (every particle its own body).
+ * The reference only holds the drag law of this path (CalculateDragForce,
+ * ZJS_DRAGFORCE_DEM.F90:2-35, never called there), a point-particle
+ * integrator skeleton (Integration, ZJS_EVOLUTION_DEM.F90:43-75) and an empty
+ * LogVolumeFraction (ZJS_EVOLUTION_DEM.F90:27-32); the rest of this path is
+ * defined here.  One step:
+ *   1. DEM cell lists on a periodic grid of cells >= dcell (stable part order);
+ *   2. contacts: for each particle the 27 neighbour cells (k,j,i order,
+ *      periodic) in part order; a pair touches when the minimum-image distance
+ *      is below rad_i + rad_j.  Normal force as CalculateCollisionForce
+ *      (ZJS_COLLISION_DEM.F90:30-57: meff = 2 m_i m_j/(m_i+m_j),
+ *      kn = knCoeff/(0.1 dx) meff, etan = eta sqrt(meff kn)); tangential
+ *      spring kt = ktRatio kn, etat = eta sqrt(meff kt), Coulomb limit
+ *      mu |Fn| with the spring reset to the sliding value; the tangential
+ *      displacement of each touching pair is kept per particle across steps
+ *      (at most maxContacts partners) and projected on the new tangent plane;
+ *   3. solid volume fraction on the fluid cells: each particle spreads its
+ *      volume with a Gaussian of sigma = bandwidth * diameter over the 5x5x5
+ *      cells around its cell, normalised per particle; a cell sums, for the
+ *      source cells at offsets (dz,dy,dx) in -2..2 (z outermost) and their
+ *      particles in part order, ((s*gz)*gy)*gx; alphaf = max(1 - alphap, alphaMin);
+ *   4. fluid velocity (trilinear on the MAC faces) and alphaf (trilinear on
+ *      the cell centres) at the particle; drag acceleration beta*(u - v) per
+ *      component with beta from CalculateDragForce;
+ *   5. v += dt*((fdrag + fcol)/m + (1 - rhof/rho) g), omega += dt*tcol/I,
+ *      x += dt*v, periodic wrap.
+ * The fluid is frozen (the caller owns its solve). */
+typedef struct ibmdem_particle {
+  int32_t globalIdx, pad_;
+  double rad, rho, vol, m, I;    /* radius, density, volume, mass, moment of inertia */
+  double x[3], v[3], omega[3];
+  double fcol[3], tcol[3];       /* contact force and torque of the last step */
+  double fdrag[3];               /* drag force m*beta*(u - v) of the last step */
+  double alphaf;                 /* fluid fraction at the particle, last step */
+} ibmdem_particle;
+
+typedef struct ibmdem_uparams {
+  int32_t nx, ny, nz;            /* fluid cells (cubic, size dx), periodic       */
+  int32_t maxContacts;           /* tangential-history partners per particle     */
+  double dx;                     /* fluid cell size                              */
+  double dcell;                  /* minimum DEM cell size (>= largest diameter)  */
+  double dt, rhof, viscf;        /* viscf as ZJS_VARS.F90:77 (1e-5)              */
+  double knCoeff, ResistCoeff;   /* normal law as the resolved contacts          */
+  double ktRatio, mu;            /* kt = ktRatio*kn (2/7), Coulomb coefficient   */
+  double bandwidth;              /* Gaussian sigma = bandwidth * diameter (3)    */
+  double alphaMin;               /* lower bound of the fluid fraction            */
+  double gravity[3];
+} ibmdem_uparams;
+
+typedef struct ibmdem_ucase ibmdem_ucase;
+int ibmdem_unresolved_create(const ibmdem_uparams* p, int32_t device, ibmdem_ucase** out);
+int ibmdem_unresolved_destroy(ibmdem_ucase* u);
+const char* ibmdem_unresolved_last_error(const ibmdem_ucase* u);
+int ibmdem_unresolved_set_stream(ibmdem_ucase* u, void* stream);
+/* u, v, w as ibmdem_set_fluid: (nx+4)*(ny+4)*(nz+4) doubles, 2-cell periodic halo. */
+int ibmdem_unresolved_set_fluid(ibmdem_ucase* u, const double* uf, const double* vf, const double* wf);
+int ibmdem_unresolved_set_particles(ibmdem_ucase* u, int32_t n, const ibmdem_particle* parts);
+int ibmdem_unresolved_get_particles(ibmdem_ucase* u, ibmdem_particle* parts, int32_t cap, int32_t* n);
+/* alphaf of the last step on the nx*ny*nz cells, i fastest. */
+int ibmdem_unresolved_get_volume_fraction(ibmdem_ucase* u, double* alphaf);
+/* Touching pairs of the last step per particle (CSR over particles, 0-based
+ * partner indices) and their tangential displacement (3 doubles each).  Any
+ * pointer may be NULL; *ncontacts gets the total. */
+int ibmdem_unresolved_get_contacts(ibmdem_ucase* u, int32_t* start, int32_t* partner, double* xi,
+                                   int32_t* ncontacts);
+int ibmdem_unresolved_step(ibmdem_ucase* u, int32_t nsteps);
+int ibmdem_unresolved_synchronize(ibmdem_ucase* u);
+int64_t ibmdem_unresolved_launch_count(const ibmdem_ucase* u);
+/* CalculateDragForce (ZJS_DRAGFORCE_DEM.F90:2-35) for n particles on device
+ * arrays: beta[3i+j] from rho[i], rad[i], v[3i+j], denf, alphaf[i] and the
+ * fluid velocity velf[3i+j]; viscf is the reference's 1e-5.  Stream-ordered
+ * on `stream`. */
+int ibmdem_CalculateDragForce(int32_t n, const double* rho, const double* rad, const double* v, double denf,
+                              const double* alphaf, const double* velf, double* beta, void* stream);
+
 /* ---- many cases on one device ---------------------------------------- */
 /* Device bytes a case of these parameters, np parcels at the given positions
  * and nMS bodies takes once created and initialised (fields, lists, weights
@@ -240,6 +316,10 @@ int ibmdem_server_result(ibmdem_server* s, int64_t id, ibmdem_parcel* parts, int
 /* Drops a finished request's record and results. */
 int ibmdem_server_release(ibmdem_server* s, int64_t id);
 int ibmdem_server_memory(const ibmdem_server* s, int64_t* in_use, int64_t* budget);
+/* Admit a case only while the running cases hold at most `parcels` markers in
+ * total (one case always runs; 0 = no limit): bounds the work that shares the
+ * device, so that early requests finish early under load. */
+int ibmdem_server_set_work_limit(ibmdem_server* s, int64_t parcels);
 
 /* ---- instrumentation -------------------------------------------------- */
 /* Record CUDA events around every phase of the drivers (interpolation,

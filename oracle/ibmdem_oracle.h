@@ -69,6 +69,19 @@ void orc_CalculateDragForce(double rho_p, double rad_p, const double* v_p, doubl
 /* eta of ZJS_COLLISION_DEM.F90:30 (single-precision pi literal reproduced). */
 double orc_eta(double ResistCoeff);
 
+/* Unresolved CFD-DEM path (unresolved_oracle.c): the definition in
+ * include/ibmdem.h, same loop and evaluation order as the CUDA path. */
+typedef struct orc_ucase orc_ucase;
+orc_ucase* orc_u_create(const ibmdem_uparams* p);
+void orc_u_destroy(orc_ucase* u);
+const char* orc_u_last_error(const orc_ucase* u);
+int orc_u_set_fluid(orc_ucase* u, const double* uf, const double* vf, const double* wf);
+int orc_u_set_particles(orc_ucase* u, int32_t np, const ibmdem_particle* parts);
+int orc_u_get_particles(orc_ucase* u, ibmdem_particle* parts, int32_t cap, int32_t* n);
+int orc_u_get_volume_fraction(orc_ucase* u, double* alphaf);
+int orc_u_get_contacts(orc_ucase* u, int32_t* start, int32_t* partner, double* xi, int32_t* ncontacts);
+int orc_u_step(orc_ucase* u, int32_t nsteps);
+
 #ifdef __cplusplus
 }
 #endif

@@ -63,6 +63,17 @@ def _load():
     lib.orc_eta.argtypes = [ctypes.c_double]
     lib.orc_CalculateDragForce.argtypes = [ctypes.c_double, ctypes.c_double, vp, ctypes.c_double,
                                            ctypes.c_double, vp, vp]
+    lib.orc_u_create.restype = vp
+    lib.orc_u_create.argtypes = [vp]
+    lib.orc_u_destroy.argtypes = [vp]
+    lib.orc_u_last_error.restype = ctypes.c_char_p
+    lib.orc_u_last_error.argtypes = [vp]
+    lib.orc_u_set_fluid.argtypes = [vp, vp, vp, vp]
+    lib.orc_u_set_particles.argtypes = [vp, i32, vp]
+    lib.orc_u_get_particles.argtypes = [vp, vp, i32, P(i32)]
+    lib.orc_u_get_volume_fraction.argtypes = [vp, vp]
+    lib.orc_u_get_contacts.argtypes = [vp, vp, vp, vp, P(i32)]
+    lib.orc_u_step.argtypes = [vp, i32]
     _lib = lib
     return lib
 
@@ -200,3 +211,75 @@ def _make(name):
 
 for _n in _SUBROUTINES:
     setattr(OracleCase, _n, _make(_n))
+
+
+class OracleUnresolved:
+    """One unresolved CFD-DEM case held by the CPU restatement (unresolved_oracle.c)."""
+
+    def __init__(self, params, particles=None, field=None):
+        import sys
+        sys.path.insert(0, os.path.join(os.path.dirname(_HERE), "ibm-dem_gb300"))
+        from ibmdem.records import PARTICLE, UPARAMS, ufield_shape
+
+        self._PARTICLE = PARTICLE
+        self.lib = _load()
+        self.params = np.array(params, dtype=UPARAMS, copy=True)
+        self.h = self.lib.orc_u_create(self.params.ctypes.data)
+        if not self.h:
+            raise RuntimeError("orc_u_create rejected the parameters")
+        self.shape = ufield_shape(self.params)
+        n = self.params
+        self.nint = int(n["nx"]) * int(n["ny"]) * int(n["nz"])
+        if field is not None:
+            self.set_fluid(*field)
+        if particles is not None:
+            self.set_particles(particles)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.orc_u_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _chk(self, rc, what):
+        if rc != 0:
+            raise RuntimeError(f"{what} [{rc}]: {self.lib.orc_u_last_error(self.h).decode()}")
+
+    def set_fluid(self, u, v, w):
+        a = [np.ascontiguousarray(x, dtype=np.float64).reshape(self.shape) for x in (u, v, w)]
+        self._chk(self.lib.orc_u_set_fluid(self.h, *[x.ctypes.data for x in a]), "set_fluid")
+
+    def set_particles(self, parts):
+        a = np.ascontiguousarray(parts, dtype=self._PARTICLE)
+        self._chk(self.lib.orc_u_set_particles(self.h, len(a), a.ctypes.data), "set_particles")
+
+    def get_particles(self):
+        n = ctypes.c_int32()
+        self._chk(self.lib.orc_u_get_particles(self.h, None, 0, ctypes.byref(n)), "get_particles")
+        out = np.zeros(n.value, self._PARTICLE)
+        self._chk(self.lib.orc_u_get_particles(self.h, out.ctypes.data, len(out), ctypes.byref(n)), "get_particles")
+        return out
+
+    def get_volume_fraction(self):
+        out = np.zeros(self.nint)
+        self._chk(self.lib.orc_u_get_volume_fraction(self.h, out.ctypes.data), "get_volume_fraction")
+        return out
+
+    def get_contacts(self):
+        n = ctypes.c_int32()
+        self._chk(self.lib.orc_u_get_contacts(self.h, None, None, None, ctypes.byref(n)), "get_contacts")
+        np_ = len(self.get_particles())
+        start = np.zeros(np_ + 1, np.int32)
+        partner = np.zeros(max(n.value, 1), np.int32)
+        xi = np.zeros((max(n.value, 1), 3))
+        self._chk(self.lib.orc_u_get_contacts(self.h, start.ctypes.data, partner.ctypes.data, xi.ctypes.data,
+                                              ctypes.byref(n)), "get_contacts")
+        return start, partner[:n.value], xi[:n.value]
+
+    def step(self, n=1):
+        self._chk(self.lib.orc_u_step(self.h, int(n)), "step")
