@@ -50,7 +50,7 @@ METRIC = "particle-steps/s (contact+IBM) on 1 GB300, batched vs plain; p50/p99 s
 # DRAM bytes (read + write) per local marker and launch of the main kernels, from
 # one ncu capture of the 512-sphere 256^3 case (profiles/ncu_ibm_kernels_resolved-512-spheres-256cube.md);
 # the bench workload has the same per-marker structure, so traffic scales with markers.
-DRAM_BYTES_PER_MARKER = {"interp": 1188.0, "spread": 1734.0, "weights": 480.0}
+DRAM_BYTES_PER_MARKER = {"interp": 1189.0, "spread": 1781.0, "weights": 477.0}
 
 
 def max_over_ranks(x):
