@@ -43,6 +43,8 @@ WORKLOADS = {
     "resolved-64-spheres-128cube": (128, 128, 128, 64, 16.0, 32),
     "resolved-512-spheres-256cube": (256, 256, 256, 512, 12.0, 64),
 }
+# unresolved CFD-DEM: name -> (fluid cells per axis, particles)
+UNRESOLVED_WORKLOADS = {"unresolved-1048576-particles-128cube": (128, 1_048_576)}
 DEFAULT_WORKLOAD = "resolved-2048-spheres-256x256x512"
 METRIC = "particle-steps/s (contact+IBM) on 1 GB300, batched vs plain; p50/p99 serve latency"
 
@@ -81,7 +83,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=400)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS) + sorted(UNRESOLVED_WORKLOADS))
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -193,6 +195,8 @@ def run_reference(args):
     O.build()
     threads = os.cpu_count() or 1
     O.set_threads(threads)
+    if args.workload in UNRESOLVED_WORKLOADS:
+        return run_reference_unresolved(args, O, threads)
     p, parts, bodies, field = make_case(args.workload, args.seed, "cpu")
     r = O.OracleCase(p, parts, bodies, field)
     r.InitializationDEM()
@@ -216,6 +220,32 @@ def run_reference(args):
                                        f"OpenMP over marker loops)"},
             "e2e": {"value": val, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "marker_steps_per_s": len(parts) * k / dt}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_reference_unresolved(args, O, threads):
+    from ibmdem import scenario
+
+    ncell, n = UNRESOLVED_WORKLOADS[args.workload]
+    p, parts, field = scenario.unresolved_case(ncell, n, seed=args.seed, n_modes=32, bed_spacing=0.9)
+    r = O.OracleUnresolved(p, parts, field)
+    t0 = time.perf_counter()
+    r.step(min(args.warmup, 1))
+    per = max(time.perf_counter() - t0, 1e-3)
+    k = max(1, min(args.steps, int(120.0 / per)))
+    t0 = time.perf_counter()
+    r.step(k)
+    dt = time.perf_counter() - t0
+    r.close()
+    val = n * k / dt
+    line = {"impl": "reference", "metric": METRIC, "value": val, "unit": "particle-steps/s", "n_gpus": args.gpus,
+            "steps": k, "steps_requested": args.steps, "warmup": min(args.warmup, 1), "ms_per_step": dt / k * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": args.workload, "fluid_cells": [ncell] * 3, "particles": n},
+            "cpu_baseline": {"value": val, "unit": "particle-steps/s", "cores": threads, "kind": "port",
+                             "sample": f"{k} step(s) of the {n}-particle case (CPU restatement, OpenMP)"},
+            "e2e": {"value": val, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -425,6 +455,125 @@ def run_unresolved(args, device, stream, cpu=True):
     return out
 
 
+def unresolved_algorithmic(n, nint, contacts):
+    """Compulsory bytes and FP64 instructions per launch of the unresolved kernels."""
+    return {
+        # each stamp (25 partial products + 5 gx) read once, cell starts, alphaf written
+        "alpha": {"bytes": n * 30 * 8 + nint * (4 + 8), "fp64": n * 125 * 2},
+        # particle state read and written, 3 x 8 face values + 8 fractions gathered, fdrag/alphaf written
+        "drag": {"bytes": n * (2 * 16 * 8 + 32 * 8 + 4 * 8), "fp64": n * 330},
+        # per pair: both particles' x, v, omega, m, r, the old and new displacement, the two terms
+        "contacts": {"bytes": contacts * (2 * 11 * 8 + 2 * 24 + 48) + n * 6 * 8, "fp64": contacts * 150},
+        "stamps": {"bytes": n * (5 * 8 + 32 * 8), "fp64": n * 220},
+    }
+
+
+def run_unresolved_main(args, world, rank, local):
+    """bench.py --workload unresolved-...: the unresolved step as the headline line."""
+    import numpy as np
+    import torch
+    from ibmdem import api, scenario
+
+    ncell, n = UNRESOLVED_WORKLOADS[args.workload]
+    fp64_peak = api.fp64_rate(local)
+    p, parts, field = scenario.unresolved_case(ncell, n, seed=args.seed + rank, n_modes=32, field_device="cuda",
+                                               bed_spacing=0.9)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+
+        O.build()
+        threads = os.cpu_count() or 1
+        O.set_threads(threads)
+        r = O.OracleUnresolved(p, parts, field)
+        t0 = time.perf_counter()
+        r.step(1)
+        dt = time.perf_counter() - t0
+        r.close()
+        cpu = {"value": n / dt, "unit": "particle-steps/s", "cores": threads, "kind": "port",
+               "sample": "1 step of the same case (CPU restatement, OpenMP)", "seconds": dt}
+    stream = torch.cuda.Stream()
+    g = api.Unresolved(p, parts, field, device=local, stream=stream)
+    g.step(args.warmup)
+    g.synchronize()
+    g.timing(True)
+    g.phase_times(reset=True)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    l0 = g.launches
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        g.step(args.steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    g.synchronize()
+    ms = e0.elapsed_time(e1)
+    launches = g.launches - l0
+    phases = g.phase_times(reset=True)
+    g.timing(False)
+    ms_max = max_over_ranks(ms)
+    value = world * n * args.steps / (ms_max / 1e3)
+    _, partner, _ = g.get_contacts()
+    # end to end: host fluid in, step, fluid fraction out (what a coupled fluid solver exchanges)
+    shape = g.shape
+    hin = [torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy() for _ in range(3)]
+    for a, b in zip(hin, field):
+        a[...] = b
+    hout = torch.empty(g.nint, dtype=torch.float64, pin_memory=True).numpy()
+    import ctypes
+
+    def e2e_step():
+        g._chk(g.lib.ibmdem_unresolved_set_fluid(g.h, *[a.ctypes.data for a in hin]), "set_fluid")
+        g.step(1)
+        g._chk(g.lib.ibmdem_unresolved_get_volume_fraction(g.h, hout.ctypes.data), "get_volume_fraction")
+
+    e2e_val = None
+    if args.e2e_steps > 0:
+        e2e_step()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            e2e_step()
+        e2e_val = world * n * args.e2e_steps / max_over_ranks(time.perf_counter() - t0)
+    g.close()
+    if rank == 0:
+        hbm_peak, peak_kind = measured_peaks()
+        alg = unresolved_algorithmic(n, g.nint, len(partner))
+        dom = max(alg, key=lambda k: phases.get(k, (0, 0))[0])
+        tot, cnt = phases[dom]
+        ms_launch = tot / max(cnt, 1)
+        achieved = alg[dom]["bytes"] / (ms_launch / 1e3) / 1e9
+        fp64_gops = alg[dom]["fp64"] / (ms_launch / 1e3) / 1e9
+        line = {
+            "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": args.workload, "fluid_cells": [ncell] * 3, "particles": n,
+                       "contacts_last_step": int(len(partner)), "dt": float(p["dt"]),
+                       "l2": "working set several GB > 129 MB L2 (no flush needed)"},
+            "roofline": {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                         "frac": achieved / hbm_peak, "peak_kind": peak_kind, "traffic": None,
+                         "algorithmic_bytes_per_launch": alg[dom]["bytes"], "ms_per_launch": ms_launch,
+                         "fp64": {"achieved_gops": fp64_gops, "peak_gops": fp64_peak,
+                                  "peak_kind": "measured live (ibmdem_measure_fp64_rate)",
+                                  "frac": fp64_gops / fp64_peak, "instr_per_launch": alg[dom]["fp64"]}},
+            "phases": {k: {"ms_total": round(t, 3), "launches": c, "ms_per_launch": t / c}
+                       for k, (t, c) in phases.items() if c},
+            "e2e": {"value": e2e_val, "unit": "particle-steps/s", "h2d_bytes_per_step": 3 * int(np.prod(shape)) * 8,
+                    "d2h_bytes_per_step": g.nint * 8, "steps": args.e2e_steps,
+                    "path": "ibmdem_unresolved_set_fluid(host u,v,w) + ibmdem_unresolved_step + "
+                            "ibmdem_unresolved_get_volume_fraction, pinned host buffers"},
+            "gpu_launches": launches, "clocks": clk.summary(),
+        }
+        if cpu is not None:
+            line["cpu_baseline"] = cpu
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_ours(args):
     import torch
 
@@ -442,6 +591,11 @@ def run_ours(args):
     from ibmdem import api
 
     api.load()
+    if args.workload in UNRESOLVED_WORKLOADS:
+        rc = run_unresolved_main(args, world, rank, local)
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return rc
     fp64_peak = api.fp64_rate(local)
     p, parts, bodies, field = make_case(args.workload, args.seed + rank, "cuda")
     # CPU baseline on the same case (OpenMP threads in this process; no fork)

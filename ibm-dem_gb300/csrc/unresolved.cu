@@ -12,8 +12,9 @@
 // Every sum has a fixed order, so results do not depend on scheduling:
 //   fcol, tcol  over the 27 neighbour DEM cells (z outermost, periodic) and,
 //               within a cell, part order;
-//   alphap      over the 125 source fluid cells at offsets (dz,dy,dx) in -2..2
-//               (z outermost) and, within a cell, part order.
+//   alphap      per source fluid cell over its particles in part order (the
+//               cell stamp), then over the 125 source cells at offsets
+//               (dz,dy,dx) in -2..2 (z outermost).
 #include <algorithm>
 #include <cmath>
 #include <cstdarg>
@@ -49,7 +50,7 @@ struct UGeom {
   double cs[3];        // DEM cell size per axis
   long long ncd;       // DEM cells
   int K;               // history slots per particle
-  double dt, rhof, viscf, knCoeff, eta, ktRatio, mu, bandwidth, alphaMin, grav[3];
+  double dt, rhof, viscf, knCoeff, knScale, eta, ktRatio, mu, bandwidth, alphaMin, grav[3];
 };
 
 struct UPtr {
@@ -109,9 +110,20 @@ __global__ void k_u_pos32(UPtr P, int np, const int* __restrict__ items, float4*
 
 // Touching partners of particle i in scan order: 27 neighbour DEM cells (z
 // outermost, periodic), part order within a cell.  An FP32 test with a 1e-3
-// relative margin discards pairs that are far apart (the FP32 distance differs
-// from the FP64 one by far less than the margin); the FP64 test
-// d2 < (r_i + r_j)^2 decides every remaining pair.
+// relative margin keeps the candidates (the FP32 distance differs from the FP64
+// one by far less than the margin); after the scan the FP64 test
+// d2 < (r_i + r_j)^2 decides each candidate in scan order, so FP64 instructions
+// are not issued inside the divergent cell loop.  A particle with more than
+// kCand candidates rescans with the FP64 test inline.
+constexpr int kCand = 16;
+__device__ inline bool touches(const UGeom& g, const UPtr& P, int i, int j) {
+  const double r1 = min_image(P.D(U_X, i) - P.D(U_X, j), g.L[0], g.halfL[0]);
+  const double r2 = min_image(P.D(U_X + 1, i) - P.D(U_X + 1, j), g.L[1], g.halfL[1]);
+  const double r3 = min_image(P.D(U_X + 2, i) - P.D(U_X + 2, j), g.L[2], g.halfL[2]);
+  const double rij = P.D(U_RAD, i) + P.D(U_RAD, j);
+  return r1 * r1 + r2 * r2 + r3 * r3 < rij * rij;
+}
+
 __global__ void __launch_bounds__(kBlock) k_u_find(UGeom g, UPtr P, int np, const int* __restrict__ cellStart,
                                                    const int* __restrict__ items, const float4* __restrict__ pos,
                                                    int* nc, int* partner, int* err, int* info) {
@@ -121,131 +133,175 @@ __global__ void __launch_bounds__(kBlock) k_u_find(UGeom g, UPtr P, int np, cons
   const float4 pi = pos[t];
   const float Lx = (float)g.L[0], Ly = (float)g.L[1], Lz = (float)g.L[2];
   const float Hx = (float)g.halfL[0], Hy = (float)g.halfL[1], Hz = (float)g.halfL[2];
-  const double xi0 = P.D(U_X, i), xi1 = P.D(U_X + 1, i), xi2 = P.D(U_X + 2, i), ri = P.D(U_RAD, i);
-  const int c0 = dem_cell_axis(g, 0, xi0), c1 = dem_cell_axis(g, 1, xi1), c2 = dem_cell_axis(g, 2, xi2);
-  int m = 0;
-  for (int dz = -1; dz <= 1; ++dz) {
-    const int cz = (c2 + dz + g.nc[2]) % g.nc[2];
-    for (int dy = -1; dy <= 1; ++dy) {
-      const int cy = (c1 + dy + g.nc[1]) % g.nc[1];
-      for (int dx = -1; dx <= 1; ++dx) {
-        const int cx = (c0 + dx + g.nc[0]) % g.nc[0];
-        const long long cell = ((long long)cz * g.nc[1] + cy) * g.nc[0] + cx;
-        const int q1 = cellStart[cell + 1];
-        for (int q = cellStart[cell]; q < q1; ++q) {
-          if (q == t) continue;
-          const float4 pj = pos[q];
-          float ex = pi.x - pj.x, ey = pi.y - pj.y, ez = pi.z - pj.z;
-          ex = ex > Hx ? ex - Lx : (ex < -Hx ? ex + Lx : ex);
-          ey = ey > Hy ? ey - Ly : (ey < -Hy ? ey + Ly : ey);
-          ez = ez > Hz ? ez - Lz : (ez < -Hz ? ez + Lz : ez);
-          const float rf = (pi.w + pj.w) * 1.001f;
-          if (ex * ex + ey * ey + ez * ez > rf * rf) continue;
-          const int j = items[q];
-          const double r1 = min_image(xi0 - P.D(U_X, j), g.L[0], g.halfL[0]);
-          const double r2 = min_image(xi1 - P.D(U_X + 1, j), g.L[1], g.halfL[1]);
-          const double r3 = min_image(xi2 - P.D(U_X + 2, j), g.L[2], g.halfL[2]);
-          const double rij = ri + P.D(U_RAD, j);
-          if (!(r1 * r1 + r2 * r2 + r3 * r3 < rij * rij)) continue;
-          if (m < g.K)
-            partner[(size_t)i * g.K + m] = j;
-          else
-            uset_err(err, UE_CONTACTS, info, i);
-          ++m;
+  // the particle's DEM cell from its FP64 position (as the cell keys)
+  const int c0 = dem_cell_axis(g, 0, P.D(U_X, i)), c1 = dem_cell_axis(g, 1, P.D(U_X + 1, i)),
+            c2 = dem_cell_axis(g, 2, P.D(U_X + 2, i));
+  int cand[kCand];
+  int ncand = 0;
+  for (int pass = 0; pass < 2; ++pass) {
+    int m = 0;
+    for (int dz = -1; dz <= 1; ++dz) {
+      const int cz = (c2 + dz + g.nc[2]) % g.nc[2];
+      for (int dy = -1; dy <= 1; ++dy) {
+        const int cy = (c1 + dy + g.nc[1]) % g.nc[1];
+        for (int dx = -1; dx <= 1; ++dx) {
+          const int cx = (c0 + dx + g.nc[0]) % g.nc[0];
+          const long long cell = ((long long)cz * g.nc[1] + cy) * g.nc[0] + cx;
+          const int q1 = cellStart[cell + 1];
+          for (int q = cellStart[cell]; q < q1; ++q) {
+            if (q == t) continue;
+            const float4 pj = pos[q];
+            float ex = pi.x - pj.x, ey = pi.y - pj.y, ez = pi.z - pj.z;
+            ex = ex > Hx ? ex - Lx : (ex < -Hx ? ex + Lx : ex);
+            ey = ey > Hy ? ey - Ly : (ey < -Hy ? ey + Ly : ey);
+            ez = ez > Hz ? ez - Lz : (ez < -Hz ? ez + Lz : ez);
+            const float rf = (pi.w + pj.w) * 1.001f;
+            if (ex * ex + ey * ey + ez * ez > rf * rf) continue;
+            if (pass == 0) {
+              if (ncand < kCand) cand[ncand] = q;
+              ++ncand;
+            } else {
+              const int j = items[q];
+              if (!touches(g, P, i, j)) continue;
+              if (m < g.K)
+                partner[(size_t)i * g.K + m] = j;
+              else
+                uset_err(err, UE_CONTACTS, info, i);
+              ++m;
+            }
+          }
         }
       }
     }
+    if (pass == 1) {
+      nc[i] = min(m, g.K);
+      return;
+    }
+    if (ncand <= kCand) break;
+  }
+  int m = 0;
+  for (int c = 0; c < ncand; ++c) {
+    const int j = items[cand[c]];
+    if (!touches(g, P, i, j)) continue;
+    if (m < g.K)
+      partner[(size_t)i * g.K + m] = j;
+    else
+      uset_err(err, UE_CONTACTS, info, i);
+    ++m;
   }
   nc[i] = min(m, g.K);
 }
 
-// Contact force and torque of particle i over its partners in list order.
-// The tangential displacement of a pair continues from i's previous slot for
-// the same partner, else starts at zero.
-__global__ void __launch_bounds__(kBlock) k_u_force(UGeom g, UPtr P, int np, const int* __restrict__ items,
-                                                    const int* __restrict__ ncOld, const int* __restrict__ pOld,
-                                                    const double* __restrict__ xOld, const int* __restrict__ ncNew,
-                                                    const int* __restrict__ pNew, double* xNew) {
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= np) return;
-  const int i = items[t];
-  const int n = ncNew[i];
-  double f0 = 0, f1 = 0, f2 = 0, t0 = 0, t1 = 0, t2 = 0;
-  if (n > 0) {
-    const double xi0 = P.D(U_X, i), xi1 = P.D(U_X + 1, i), xi2 = P.D(U_X + 2, i);
-    const double vi0 = P.D(U_V, i), vi1 = P.D(U_V + 1, i), vi2 = P.D(U_V + 2, i);
-    const double wi0 = P.D(U_W, i), wi1 = P.D(U_W + 1, i), wi2 = P.D(U_W + 2, i);
-    const double mi = P.D(U_M, i), ri = P.D(U_RAD, i);
+// Flat contact list: slot ids (i*K + m) of all touching pairs, particle-major.
+__global__ void k_u_owner(int np, int K, const int* __restrict__ nc, const int* __restrict__ cstart, int* owner) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= np) return;
+  const int n = nc[i], e0 = cstart[i];
+  for (int m = 0; m < n; ++m) owner[e0 + m] = i * K + m;
+}
+
+// One thread per touching pair (all lanes busy whatever the contact counts):
+// the pair's force term fn*n + ft and torque term ri*(n x ft) for particle i,
+// and its new tangential displacement.  The tangential displacement continues
+// from i's previous slot for the same partner, else starts at zero.
+__global__ void __launch_bounds__(kBlock) k_u_pair(UGeom g, UPtr P, const int* __restrict__ total,
+                                                   const int* __restrict__ owner, const int* __restrict__ ncOld,
+                                                   const int* __restrict__ pOld, const double* __restrict__ xOld,
+                                                   const int* __restrict__ pNew, double* xNew, double* fterm,
+                                                   double* tterm) {
+  const long long nPairs = *total;
+  GRID_STRIDE(e, nPairs) {
+    const int slot = owner[e];
+    const int i = slot / g.K;
+    const int j = pNew[slot];
+    const double ri = P.D(U_RAD, i), rj = P.D(U_RAD, j);
+    const double r1 = min_image(P.D(U_X, i) - P.D(U_X, j), g.L[0], g.halfL[0]);
+    const double r2 = min_image(P.D(U_X + 1, i) - P.D(U_X + 1, j), g.L[1], g.halfL[1]);
+    const double r3 = min_image(P.D(U_X + 2, i) - P.D(U_X + 2, j), g.L[2], g.halfL[2]);
+    const double rij = ri + rj;
+    const double d2 = r1 * r1 + r2 * r2 + r3 * r3;
+    const double dist = sqrt(d2);
+    const double n1 = r1 / dist, n2 = r2 / dist, n3 = r3 / dist;
+    const double mi = P.D(U_M, i), mj = P.D(U_M, j);
+    const double meff = 2 * mi * mj / (mi + mj);
+    const double deltan = rij - dist;
+    const double kn = g.knScale * meff;  // knCoeff/(0.1*dx)*meff
+    const double etan = g.eta * sqrt(meff * kn);
+    const double u1 = P.D(U_V, i) - P.D(U_V, j), u2 = P.D(U_V + 1, i) - P.D(U_V + 1, j),
+                 u3 = P.D(U_V + 2, i) - P.D(U_V + 2, j);
+    const double vn = n1 * u1 + n2 * u2 + n3 * u3;
+    const double fn = kn * deltan - etan * vn;
+    // relative velocity of the contact point: u - (ri wi + rj wj) x n
+    const double s1 = ri * P.D(U_W, i) + rj * P.D(U_W, j);
+    const double s2 = ri * P.D(U_W + 1, i) + rj * P.D(U_W + 1, j);
+    const double s3 = ri * P.D(U_W + 2, i) + rj * P.D(U_W + 2, j);
+    const double vr1 = u1 - (s2 * n3 - s3 * n2);
+    const double vr2 = u2 - (s3 * n1 - s1 * n3);
+    const double vr3 = u3 - (s1 * n2 - s2 * n1);
+    const double vrn = n1 * vr1 + n2 * vr2 + n3 * vr3;
+    const double vt1 = vr1 - vrn * n1, vt2 = vr2 - vrn * n2, vt3 = vr3 - vrn * n3;
+    double h1 = 0, h2 = 0, h3 = 0;
     const int nOld = ncOld[i];
-    for (int m = 0; m < n; ++m) {
-      const int j = pNew[(size_t)i * g.K + m];
-      const double r1 = min_image(xi0 - P.D(U_X, j), g.L[0], g.halfL[0]);
-      const double r2 = min_image(xi1 - P.D(U_X + 1, j), g.L[1], g.halfL[1]);
-      const double r3 = min_image(xi2 - P.D(U_X + 2, j), g.L[2], g.halfL[2]);
-      const double rj = P.D(U_RAD, j);
-      const double rij = ri + rj;
-      const double d2 = r1 * r1 + r2 * r2 + r3 * r3;
-      const double dist = sqrt(d2);
-      const double n1 = r1 / dist, n2 = r2 / dist, n3 = r3 / dist;
-      const double mj = P.D(U_M, j);
-      const double meff = 2 * mi * mj / (mi + mj);
-      const double deltan = rij - dist;
-      const double kn = g.knCoeff / (0.1 * g.h) * meff;
-      const double etan = g.eta * sqrt(meff * kn);
-      const double u1 = vi0 - P.D(U_V, j), u2 = vi1 - P.D(U_V + 1, j), u3 = vi2 - P.D(U_V + 2, j);
-      const double vn = n1 * u1 + n2 * u2 + n3 * u3;
-      const double fn = kn * deltan - etan * vn;
-      // relative velocity of the contact point: u - (ri wi + rj wj) x n
-      const double s1 = ri * wi0 + rj * P.D(U_W, j);
-      const double s2 = ri * wi1 + rj * P.D(U_W + 1, j);
-      const double s3 = ri * wi2 + rj * P.D(U_W + 2, j);
-      const double vr1 = u1 - (s2 * n3 - s3 * n2);
-      const double vr2 = u2 - (s3 * n1 - s1 * n3);
-      const double vr3 = u3 - (s1 * n2 - s2 * n1);
-      const double vrn = n1 * vr1 + n2 * vr2 + n3 * vr3;
-      const double vt1 = vr1 - vrn * n1, vt2 = vr2 - vrn * n2, vt3 = vr3 - vrn * n3;
-      double h1 = 0, h2 = 0, h3 = 0;
-      for (int s = 0; s < nOld; ++s)
-        if (pOld[(size_t)i * g.K + s] == j) {
-          const double* o = xOld + ((size_t)i * g.K + s) * 3;
-          h1 = o[0];
-          h2 = o[1];
-          h3 = o[2];
-          break;
-        }
-      const double hn = n1 * h1 + n2 * h2 + n3 * h3;
-      h1 = h1 - hn * n1;
-      h2 = h2 - hn * n2;
-      h3 = h3 - hn * n3;
-      h1 = h1 + g.dt * vt1;
-      h2 = h2 + g.dt * vt2;
-      h3 = h3 + g.dt * vt3;
-      const double kt = g.ktRatio * kn;
-      const double etat = g.eta * sqrt(meff * kt);
-      double ft1 = -kt * h1 - etat * vt1, ft2 = -kt * h2 - etat * vt2, ft3 = -kt * h3 - etat * vt3;
-      const double ftm = sqrt(ft1 * ft1 + ft2 * ft2 + ft3 * ft3);
-      const double lim = g.mu * fabs(fn);
-      if (ftm > lim) {
-        const double sc = lim / ftm;
-        ft1 = ft1 * sc;
-        ft2 = ft2 * sc;
-        ft3 = ft3 * sc;
-        h1 = -(ft1 + etat * vt1) / kt;
-        h2 = -(ft2 + etat * vt2) / kt;
-        h3 = -(ft3 + etat * vt3) / kt;
+    for (int s = 0; s < nOld; ++s)
+      if (pOld[(size_t)i * g.K + s] == j) {
+        const double* o = xOld + ((size_t)i * g.K + s) * 3;
+        h1 = o[0];
+        h2 = o[1];
+        h3 = o[2];
+        break;
       }
-      f0 = f0 + (fn * n1 + ft1);
-      f1 = f1 + (fn * n2 + ft2);
-      f2 = f2 + (fn * n3 + ft3);
-      // torque (-ri n) x ft
-      t0 = t0 - ri * (n2 * ft3 - n3 * ft2);
-      t1 = t1 - ri * (n3 * ft1 - n1 * ft3);
-      t2 = t2 - ri * (n1 * ft2 - n2 * ft1);
-      double* o = xNew + ((size_t)i * g.K + m) * 3;
-      o[0] = h1;
-      o[1] = h2;
-      o[2] = h3;
+    const double hn = n1 * h1 + n2 * h2 + n3 * h3;
+    h1 = h1 - hn * n1;
+    h2 = h2 - hn * n2;
+    h3 = h3 - hn * n3;
+    h1 = h1 + g.dt * vt1;
+    h2 = h2 + g.dt * vt2;
+    h3 = h3 + g.dt * vt3;
+    const double kt = g.ktRatio * kn;
+    const double etat = g.eta * sqrt(meff * kt);
+    double ft1 = -kt * h1 - etat * vt1, ft2 = -kt * h2 - etat * vt2, ft3 = -kt * h3 - etat * vt3;
+    const double ftm = sqrt(ft1 * ft1 + ft2 * ft2 + ft3 * ft3);
+    const double lim = g.mu * fabs(fn);
+    if (ftm > lim) {
+      const double sc = lim / ftm;
+      ft1 = ft1 * sc;
+      ft2 = ft2 * sc;
+      ft3 = ft3 * sc;
+      h1 = -(ft1 + etat * vt1) / kt;
+      h2 = -(ft2 + etat * vt2) / kt;
+      h3 = -(ft3 + etat * vt3) / kt;
     }
+    double* xo = xNew + (size_t)slot * 3;
+    xo[0] = h1;
+    xo[1] = h2;
+    xo[2] = h3;
+    double* fo = fterm + (size_t)slot * 3;
+    fo[0] = fn * n1 + ft1;
+    fo[1] = fn * n2 + ft2;
+    fo[2] = fn * n3 + ft3;
+    double* to = tterm + (size_t)slot * 3;
+    to[0] = ri * (n2 * ft3 - n3 * ft2);
+    to[1] = ri * (n3 * ft1 - n1 * ft3);
+    to[2] = ri * (n1 * ft2 - n2 * ft1);
+  }
+}
+
+// fcol and tcol of particle i: its pair terms folded in list order
+__global__ void k_u_sum(UPtr P, int np, int K, const int* __restrict__ nc, const double* __restrict__ fterm,
+                        const double* __restrict__ tterm) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= np) return;
+  double f0 = 0, f1 = 0, f2 = 0, t0 = 0, t1 = 0, t2 = 0;
+  const int n = nc[i];
+  for (int m = 0; m < n; ++m) {
+    const double* fo = fterm + ((size_t)i * K + m) * 3;
+    const double* to = tterm + ((size_t)i * K + m) * 3;
+    f0 = f0 + fo[0];
+    f1 = f1 + fo[1];
+    f2 = f2 + fo[2];
+    t0 = t0 - to[0];
+    t1 = t1 - to[1];
+    t2 = t2 - to[2];
   }
   P.D(U_FCOL, i) = f0;
   P.D(U_FCOL + 1, i) = f1;
@@ -259,22 +315,32 @@ __global__ void __launch_bounds__(kBlock) k_u_force(UGeom g, UPtr P, int np, con
 // Gaussian weights gx, gy, gz on the 5 fluid cells around its cell per axis,
 // the scale s = vol / (sum of the 125 weights * cell volume), and the partial
 // products (s*gz[qz])*gy[qy] that every term ((s*gz)*gy)*gx shares.
+// With u_q = (x - xc_q)/sigma and d = h/sigma, u_{q+1} = u_q - d, so
+// exp(-u_{q+1}^2/2) = exp(-u_q^2/2) * exp(d u_q) * exp(-d^2/2) and
+// exp(d u_{q+1}) = exp(d u_q) * exp(-d^2): three exponentials per axis and one
+// per particle give the 15 weights (relative difference from 15 direct
+// exponentials of order 1e-15).
 constexpr int kStamp = 32;  // 25 partial products, 5 gx, 2 spare
 __global__ void k_u_gauss(UGeom g, UPtr P, int np, const int* __restrict__ items, double* st) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= np) return;
   const int i = items[t];
   const double sigma = g.bandwidth * (2.0 * P.D(U_RAD, i));
+  const double dd = g.h / sigma;
+  const double c2 = exp(-(dd * dd));      // ratio of successive growth factors
   double w[3][5], sum[3];
   for (int d = 0; d < 3; ++d) {
     const double x = P.D(U_X + d, i);
     const int a = min(max((int)floor(x / g.h), 0), g.n[d] - 1);
+    const double u0 = (x - ((double)(a - 2) + 0.5) * g.h) / sigma;
+    double wq = exp(-0.5 * (u0 * u0));
+    double r = exp(dd * u0 - 0.5 * (dd * dd));  // w_{q+1} / w_q at q = 0
     double s = 0.0;
     for (int q = 0; q < 5; ++q) {
-      const double xc = ((double)(a - 2 + q) + 0.5) * g.h;
-      const double u = (x - xc) / sigma;
-      w[d][q] = exp(-0.5 * (u * u));
-      s = s + w[d][q];
+      w[d][q] = wq;
+      s = s + wq;
+      wq = wq * r;
+      r = r * c2;
     }
     sum[d] = s;
   }
@@ -285,11 +351,57 @@ __global__ void k_u_gauss(UGeom g, UPtr P, int np, const int* __restrict__ items
   for (int qx = 0; qx < 5; ++qx) o[25 + qx] = w[0][qx];
 }
 
-// alphaf of every fluid cell, gathered from the 125 source cells around it:
-// for the source cells at offsets (dz,dy,dx) in -2..2, z outermost, and their
-// particles in part order, alphap += ((s*gz)*gy)*gx.
+// Occupied fluid cells: flag, then (after an exclusive scan into rank) the list.
+__global__ void k_u_occ_flag(long long nint, const int* __restrict__ flStart, int* flag) {
+  long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < nint) flag[c] = flStart[c + 1] > flStart[c] ? 1 : 0;
+}
+__global__ void k_u_occ_list(long long nint, const int* __restrict__ flStart, const int* __restrict__ rank,
+                             int* occ) {
+  long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < nint && flStart[c + 1] > flStart[c]) occ[rank[c]] = (int)c;
+}
+
+// Cell stamps: for every occupied fluid cell (one warp each) and every offset
+// (qz,qy,qx) of the 5x5x5 cells it reaches, the sum over its particles in part
+// order of ((s*gz[qz])*gy[qy])*gx[qx].  Lane l holds offsets l, l+32, l+64, l+96.
+constexpr int kCellStamp = 128;  // 125 offsets, padded
+__global__ void __launch_bounds__(kBlock) k_u_cellsum(const int* __restrict__ nOcc, const int* __restrict__ occ,
+                                                      const int* __restrict__ flStart,
+                                                      const double* __restrict__ st, double* T) {
+  const int lane = threadIdx.x & 31;
+  const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+  const int n = *nOcc;
+  int pq[4], qx[4];
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const int o = min(lane + 32 * r, 124);
+    pq[r] = o / 5;       // qz*5 + qy
+    qx[r] = o % 5;
+  }
+  for (long long w = warp; w < n; w += nwarps) {
+    const int c = occ[w];
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    const int q1 = flStart[c + 1];
+    for (int q = flStart[c]; q < q1; ++q) {
+      const double* x = st + (size_t)q * kStamp;
+#pragma unroll
+      for (int r = 0; r < 4; ++r) acc[r] = acc[r] + x[pq[r]] * x[25 + qx[r]];
+    }
+    double* out = T + (size_t)w * kCellStamp;
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+      if (lane + 32 * r < 125) out[lane + 32 * r] = acc[r];
+  }
+}
+
+// alphaf of every fluid cell: alphap = sum over the source cells at offsets
+// (dz,dy,dx) in -2..2, z outermost, of their cell stamp at the offset that
+// reaches this cell; alphaf = max(1 - alphap, alphaMin).
 __global__ void __launch_bounds__(kBlock) k_u_alpha(UGeom g, const int* __restrict__ flStart,
-                                                    const double* __restrict__ st, double* alphaf) {
+                                                    const int* __restrict__ rank, const double* __restrict__ T,
+                                                    double* alphaf) {
   long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= g.nint) return;
   const int i = (int)(c % g.n[0]);
@@ -300,15 +412,11 @@ __global__ void __launch_bounds__(kBlock) k_u_alpha(UGeom g, const int* __restri
     const int sz = (k + oz + g.n[2]) % g.n[2];
     for (int oy = -2; oy <= 2; ++oy) {
       const int sy = (j + oy + g.n[1]) % g.n[1];
-      const int pq = (2 - oz) * 5 + (2 - oy);
       const long long row = ((long long)sz * g.n[1] + sy) * g.n[0];
+      const int pq5 = ((2 - oz) * 5 + (2 - oy)) * 5;
       for (int ox = -2; ox <= 2; ++ox) {
-        const int sx = (i + ox + g.n[0]) % g.n[0];
-        const int q1 = flStart[row + sx + 1];
-        for (int q = flStart[row + sx]; q < q1; ++q) {
-          const double* w = st + (size_t)q * kStamp;
-          ap = ap + w[pq] * w[25 + 2 - ox];
-        }
+        const long long src = row + (i + ox + g.n[0]) % g.n[0];
+        if (flStart[src + 1] > flStart[src]) ap = ap + T[(size_t)rank[src] * kCellStamp + pq5 + (2 - ox)];
       }
     }
   }
@@ -317,27 +425,33 @@ __global__ void __launch_bounds__(kBlock) k_u_alpha(UGeom g, const int* __restri
 
 // CalculateDragForce (ZJS_DRAGFORCE_DEM.F90:2-35): the literals 3.7, 0.65,
 // 0.687, 0.0183, 8.33, 0.0972 and 0.8 are default-real (single precision) there.
+// log10(Rep) and Rep**0.687 share log(Rep); alphaf**(-zeta) is
+// exp(-zeta*log(alphaf)) with log(alphaf) shared by the three components
+// (relative difference from pow/log10 of order 1e-15).
 __device__ inline void drag_beta(double rho, double rad, const double* v, double denf, double alphaf, const double* velf,
                                  double viscf, double* beta) {
   const double c37 = (double)3.7f, c065 = (double)0.65f, c0687 = (double)0.687f, c00183 = (double)0.0183f;
   const double c833 = (double)8.33f, c00972 = (double)0.0972f, c08 = (double)0.8f;
+  const double inv_ln10 = 0.43429448190325182765;  // 1/ln(10)
   const double spg = rho / denf;
   const double diameter = 2.0 * rad;
+  const double la = alphaf < c08 ? 0.0 : log(alphaf);
   for (int j = 0; j < 3; ++j) {
     const double Ur = fabs(velf[j] - v[j]);
     double Rep = Ur * diameter / viscf;
     Rep = Rep > 1.0 ? Rep : 1.0;
-    const double t = 1.5 - log10(Rep);
+    const double lr = log(Rep);
+    const double t = 1.5 - lr * inv_ln10;
     const double zeta = c37 - c065 * exp(-0.5 * (t * t));
     double fbase, f;
     if (Rep < 1000)
-      fbase = 1 + 1.0 / 6.0 * pow(Rep, c0687);
+      fbase = 1 + 1.0 / 6.0 * exp(c0687 * lr);
     else
       fbase = c00183 * Rep;
     if (alphaf < c08)
       f = c833 * (1 - alphaf) / alphaf + c00972 * Rep;
     else
-      f = fbase * pow(alphaf, -zeta);
+      f = fbase * exp(-zeta * la);
     const double Cd = 24.0 / Rep * f;
     beta[j] = 0.75 * (Cd * Ur) / (diameter * spg);
   }
@@ -468,10 +582,25 @@ struct ibmdem_ucase {
   double* xi[2] = {nullptr, nullptr};
   int hcur = 0;
   double* st = nullptr;     // [kStamp * cap] Gaussian stamps in fluid-cell order
+  int* occFlag = nullptr;   // [nint + 1] occupied-cell flags, then their exclusive scan
+  int* occ = nullptr;       // [min(nint, cap)] occupied fluid cells
+  int* nOcc = nullptr;      // their number
+  double* T = nullptr;      // [kCellStamp * min(nint, cap)] cell stamps
   float4* pos = nullptr;    // [cap] FP32 positions and radii in DEM-cell order
+  int* cstart = nullptr;    // [cap + 1] first flat contact of each particle
+  int* owner = nullptr;     // [K * cap] slot of each flat contact
+  double* fterm = nullptr;  // [3 * K * cap] per-slot force term
+  double* tterm = nullptr;  // [3 * K * cap] per-slot torque term
+  int* dTotal = nullptr;    // contacts of the step
   double* alphaf = nullptr;
   double *uf = nullptr, *vf = nullptr, *wf = nullptr;
   int* dErr = nullptr;  // [0] bits, [1] first particle
+  // per-phase CUDA-event timing (ibmdem_unresolved_timing_enable)
+  bool timing = false;
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> spans;
+  std::vector<cudaEvent_t> evFree;
+  double phaseMs[8] = {};
+  long long phaseCount[8] = {};
   int* scan = nullptr;
   int* hist = nullptr;
   bool haveFluid = false, stepped = false;
@@ -503,7 +632,8 @@ cudaError_t ualloc(ibmdem_ucase* u, T*& p, size_t n) {
 
 void ufree_particles(ibmdem_ucase* u) {
   void* ps[] = {u->pd, u->gidx, u->kA, u->vA, u->kB, u->vB, u->kC, u->vC, u->kD, u->vD, u->demItems, u->flItems,
-                u->nc[0], u->nc[1], u->partner[0], u->partner[1], u->xi[0], u->xi[1], u->st, u->pos, u->scan, u->hist};
+                u->nc[0], u->nc[1], u->partner[0], u->partner[1], u->xi[0], u->xi[1], u->st, u->pos, u->scan, u->hist, u->cstart, u->owner,
+                u->fterm, u->tterm, u->occFlag, u->occ, u->nOcc, u->T};
   for (void* q : ps)
     if (q) cudaFreeAsync(q, u->stream);
   u->pd = nullptr;
@@ -513,6 +643,10 @@ void ufree_particles(ibmdem_ucase* u) {
   u->xi[0] = u->xi[1] = nullptr;
   u->st = nullptr;
   u->pos = nullptr;
+  u->cstart = u->owner = nullptr;
+  u->fterm = u->tterm = nullptr;
+  u->occFlag = u->occ = u->nOcc = nullptr;
+  u->T = nullptr;
   u->scan = u->hist = nullptr;
   u->cap = u->np = 0;
 }
@@ -529,6 +663,52 @@ int check_errors(ibmdem_ucase* u) {
 
 UPtr uptr(ibmdem_ucase* u) { return UPtr{u->pd, u->gidx, u->cap}; }
 
+enum UPhase : int { UP_LISTS = 0, UP_SEARCH, UP_CONTACTS, UP_STAMPS, UP_ALPHA, UP_DRAG, UP_COUNT };
+const char* kUPhaseNames[UP_COUNT] = {"lists", "search", "contacts", "stamps", "alpha", "drag"};
+
+cudaEvent_t take_event(ibmdem_ucase* u) {
+  if (!u->evFree.empty()) {
+    cudaEvent_t e = u->evFree.back();
+    u->evFree.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+
+// CUDA events around one phase on the case's stream when timing is on
+struct UScope {
+  ibmdem_ucase* u;
+  int ph;
+  cudaEvent_t a = nullptr;
+  UScope(ibmdem_ucase* uu, int p) : u(uu), ph(p) {
+    if (!u->timing) return;
+    a = take_event(u);
+    cudaEventRecord(a, u->stream);
+  }
+  ~UScope() {
+    if (!a) return;
+    cudaEvent_t b = take_event(u);
+    cudaEventRecord(b, u->stream);
+    u->spans.push_back({ph, {a, b}});
+  }
+};
+
+void collect_timing(ibmdem_ucase* u) {
+  cudaStreamSynchronize(u->stream);
+  for (auto& sp : u->spans) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, sp.second.first, sp.second.second) == cudaSuccess) {
+      u->phaseMs[sp.first] += ms;
+      u->phaseCount[sp.first] += 1;
+    }
+    u->evFree.push_back(sp.second.first);
+    u->evFree.push_back(sp.second.second);
+  }
+  u->spans.clear();
+}
+
 int one_step(ibmdem_ucase* u) {
   UGeom& g = u->g;
   cudaStream_t s = u->stream;
@@ -536,6 +716,8 @@ int one_step(ibmdem_ucase* u) {
   if (np == 0) return IBMDEM_OK;
   const int nb = nblocks(np);
   UPtr P = uptr(u);
+  {
+  UScope ts(u, UP_LISTS);
   cudaMemsetAsync(u->demStart, 0, sizeof(int) * (g.ncd + 1), s);
   cudaMemsetAsync(u->flStart, 0, sizeof(int) * (g.nint + 1), s);
   k_u_keys<<<nb, kBlock, 0, s>>>(g, P, np, u->kA, u->vA, u->demStart, u->kC, u->vC, u->flStart, u->dErr,
@@ -549,16 +731,41 @@ int one_step(ibmdem_ucase* u) {
   radix_sort_pairs(k0, v0, k1, v1, np, nullptr, bits_of(g.nint), u->hist, u->scan, s, &u->launches);
   k_copy_items<<<nb, kBlock, 0, s>>>(np, v0, u->flItems);
   scan_exclusive(u->flStart, u->flStart, g.nint, nullptr, u->flStart + g.nint, u->scan, s, &u->launches);
+  }
   const int o = u->hcur, n = u->hcur ^ 1;
+  {
+  UScope ts(u, UP_SEARCH);
   k_u_pos32<<<nb, kBlock, 0, s>>>(P, np, u->demItems, u->pos);
   k_u_find<<<nb, kBlock, 0, s>>>(g, P, np, u->demStart, u->demItems, u->pos, u->nc[n], u->partner[n], u->dErr,
                                  u->dErr + 1);
-  k_u_force<<<nb, kBlock, 0, s>>>(g, P, np, u->demItems, u->nc[o], u->partner[o], u->xi[o], u->nc[n],
-                                  u->partner[n], u->xi[n]);
+  scan_exclusive(u->nc[n], u->cstart, np, nullptr, u->dTotal, u->scan, s, &u->launches);
+  k_u_owner<<<nb, kBlock, 0, s>>>(np, g.K, u->nc[n], u->cstart, u->owner);
+  }
+  {
+  UScope ts(u, UP_CONTACTS);
+  k_u_pair<<<gs_blocks((long long)np * g.K), kBlock, 0, s>>>(g, P, u->dTotal, u->owner, u->nc[o], u->partner[o],
+                                                            u->xi[o], u->partner[n], u->xi[n], u->fterm, u->tterm);
+  k_u_sum<<<nb, kBlock, 0, s>>>(P, np, g.K, u->nc[n], u->fterm, u->tterm);
+  }
+  {
+  UScope ts(u, UP_STAMPS);
   k_u_gauss<<<nb, kBlock, 0, s>>>(g, P, np, u->flItems, u->st);
-  k_u_alpha<<<nblocks(g.nint), kBlock, 0, s>>>(g, u->flStart, u->st, u->alphaf);
+  }
+  {
+  UScope ts(u, UP_ALPHA);
+  const int nbc = nblocks(g.nint);
+  k_u_occ_flag<<<nbc, kBlock, 0, s>>>(g.nint, u->flStart, u->occFlag);
+  scan_exclusive(u->occFlag, u->occFlag, g.nint, nullptr, u->nOcc, u->scan, s, &u->launches);
+  k_u_occ_list<<<nbc, kBlock, 0, s>>>(g.nint, u->flStart, u->occFlag, u->occ);
+  k_u_cellsum<<<gs_blocks(32ll * std::min<long long>(g.nint, np)), kBlock, 0, s>>>(u->nOcc, u->occ, u->flStart,
+                                                                                   u->st, u->T);
+  k_u_alpha<<<nbc, kBlock, 0, s>>>(g, u->flStart, u->occFlag, u->T, u->alphaf);
+  }
+  {
+  UScope ts(u, UP_DRAG);
   k_u_drag_move<<<nb, kBlock, 0, s>>>(g, P, np, u->uf, u->vf, u->wf, u->alphaf);
-  u->launches += 8;
+  }
+  u->launches += 12;
   u->hcur = n;
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return uerr(u, IBMDEM_ECUDA, "kernel launch: %s", cudaGetErrorString(e));
@@ -603,6 +810,7 @@ int ibmdem_unresolved_create(const ibmdem_uparams* p, int32_t device, ibmdem_uca
   g.rhof = p->rhof;
   g.viscf = p->viscf;
   g.knCoeff = p->knCoeff;
+  g.knScale = p->knCoeff / (0.1 * p->dx);  // the kn prefactor of every pair
   g.eta = eta_of(p->ResistCoeff);
   g.ktRatio = p->ktRatio;
   g.mu = p->mu;
@@ -624,6 +832,7 @@ int ibmdem_unresolved_create(const ibmdem_uparams* p, int32_t device, ibmdem_uca
   A(u->demStart, (size_t)g.ncd + 1);
   A(u->flStart, (size_t)g.nint + 1);
   A(u->dErr, 2);
+  A(u->dTotal, 1);
   if (e == cudaSuccess) {
     cudaMemsetAsync(u->uf, 0, nf * sizeof(double), u->stream);
     cudaMemsetAsync(u->vf, 0, nf * sizeof(double), u->stream);
@@ -644,10 +853,15 @@ int ibmdem_unresolved_destroy(ibmdem_ucase* u) {
   cudaSetDevice(u->device);
   cudaStreamSynchronize(u->stream);
   ufree_particles(u);
-  void* ps[] = {u->uf, u->vf, u->wf, u->alphaf, u->demStart, u->flStart, u->dErr};
+  void* ps[] = {u->uf, u->vf, u->wf, u->alphaf, u->demStart, u->flStart, u->dErr, u->dTotal};
   for (void* q : ps)
     if (q) cudaFreeAsync(q, u->stream);
   cudaStreamSynchronize(u->stream);
+  for (auto& sp : u->spans) {
+    cudaEventDestroy(sp.second.first);
+    cudaEventDestroy(sp.second.second);
+  }
+  for (cudaEvent_t e : u->evFree) cudaEventDestroy(e);
   delete u;
   return IBMDEM_OK;
 }
@@ -702,6 +916,15 @@ int ibmdem_unresolved_set_particles(ibmdem_ucase* u, int32_t np, const ibmdem_pa
   }
   A(u->st, (size_t)kStamp * cap);
   A(u->pos, (size_t)cap);
+  A(u->cstart, (size_t)cap + 1);
+  const size_t maxOcc = (size_t)std::min<long long>(g.nint, cap);
+  A(u->occFlag, (size_t)g.nint + 1);
+  A(u->occ, maxOcc);
+  A(u->nOcc, 1);
+  A(u->T, (size_t)kCellStamp * maxOcc);
+  A(u->owner, K * cap);
+  A(u->fterm, 3 * K * cap);
+  A(u->tterm, 3 * K * cap);
   const long long scanN = std::max<long long>(std::max(g.ncd, g.nint) + 1, sort_hist_ints(cap));
   A(u->scan, (size_t)std::max(scan_scratch_ints(scanN), scan_scratch_ints(sort_hist_ints(cap))));
   A(u->hist, (size_t)sort_hist_ints(cap));
@@ -834,6 +1057,29 @@ int ibmdem_unresolved_step(ibmdem_ucase* u, int32_t nsteps) {
   }
   return IBMDEM_OK;
 }
+
+int ibmdem_unresolved_timing_enable(ibmdem_ucase* u, int32_t on) {
+  if (!u) return IBMDEM_EINVAL;
+  u->timing = on != 0;
+  return IBMDEM_OK;
+}
+
+int ibmdem_unresolved_get_timing(ibmdem_ucase* u, double* ms, int64_t* counts, int32_t n, int32_t reset) {
+  if (!u) return IBMDEM_EINVAL;
+  collect_timing(u);
+  for (int i = 0; i < n && i < UP_COUNT; ++i) {
+    if (ms) ms[i] = u->phaseMs[i];
+    if (counts) counts[i] = u->phaseCount[i];
+  }
+  if (reset)
+    for (int i = 0; i < UP_COUNT; ++i) {
+      u->phaseMs[i] = 0.0;
+      u->phaseCount[i] = 0;
+    }
+  return UP_COUNT;
+}
+
+const char* ibmdem_unresolved_phase_name(int32_t i) { return (i >= 0 && i < UP_COUNT) ? kUPhaseNames[i] : ""; }
 
 int ibmdem_unresolved_synchronize(ibmdem_ucase* u) {
   if (!u) return IBMDEM_EINVAL;

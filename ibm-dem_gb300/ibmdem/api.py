@@ -38,7 +38,8 @@ EXPORTS = [
     "ibmdem_unresolved_set_stream", "ibmdem_unresolved_set_fluid", "ibmdem_unresolved_set_particles",
     "ibmdem_unresolved_get_particles", "ibmdem_unresolved_get_volume_fraction", "ibmdem_unresolved_get_contacts",
     "ibmdem_unresolved_step", "ibmdem_unresolved_synchronize", "ibmdem_unresolved_launch_count",
-    "ibmdem_CalculateDragForce",
+    "ibmdem_CalculateDragForce", "ibmdem_unresolved_timing_enable", "ibmdem_unresolved_get_timing",
+    "ibmdem_unresolved_phase_name",
 ]
 
 SUBROUTINES = [
@@ -125,6 +126,10 @@ def load(path=LIB_PATH):
     lib.ibmdem_unresolved_launch_count.restype = i64
     lib.ibmdem_unresolved_launch_count.argtypes = [vp]
     lib.ibmdem_CalculateDragForce.argtypes = [i32, vp, vp, vp, ctypes.c_double, vp, vp, vp, vp]
+    lib.ibmdem_unresolved_timing_enable.argtypes = [vp, i32]
+    lib.ibmdem_unresolved_get_timing.argtypes = [vp, vp, vp, i32, i32]
+    lib.ibmdem_unresolved_phase_name.restype = ctypes.c_char_p
+    lib.ibmdem_unresolved_phase_name.argtypes = [i32]
     _lib = lib
     return lib
 
@@ -506,3 +511,13 @@ class Unresolved:
 
     def synchronize(self):
         self._chk(self.lib.ibmdem_unresolved_synchronize(self.h), "synchronize")
+
+    def timing(self, on=True):
+        self._chk(self.lib.ibmdem_unresolved_timing_enable(self.h, int(bool(on))), "timing_enable")
+
+    def phase_times(self, reset=False):
+        """{phase: (total ms, spans)} accumulated since the last reset (synchronises)."""
+        ms = np.zeros(8)
+        cnt = np.zeros(8, np.int64)
+        n = self.lib.ibmdem_unresolved_get_timing(self.h, ms.ctypes.data, cnt.ctypes.data, 8, int(bool(reset)))
+        return {self.lib.ibmdem_unresolved_phase_name(i).decode(): (float(ms[i]), int(cnt[i])) for i in range(n)}

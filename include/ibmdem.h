@@ -201,9 +201,11 @@ int ibmdem_interpolate_velocity_noalloc(ibmdem_ctx* ctx, int32_t n, const double
  *      (at most maxContacts partners) and projected on the new tangent plane;
  *   3. solid volume fraction on the fluid cells: each particle spreads its
  *      volume with a Gaussian of sigma = bandwidth * diameter over the 5x5x5
- *      cells around its cell, normalised per particle; a cell sums, for the
- *      source cells at offsets (dz,dy,dx) in -2..2 (z outermost) and their
- *      particles in part order, ((s*gz)*gy)*gx; alphaf = max(1 - alphap, alphaMin);
+ *      cells around its cell, normalised per particle (weight ((s*gz)*gy)*gx,
+ *      s = vol / (sum of the 125 weights * cell volume)); a source cell sums
+ *      its particles' weights for one target in part order, and a target sums
+ *      those partial sums over the source cells at offsets (dz,dy,dx) in -2..2
+ *      (z outermost); alphaf = max(1 - alphap, alphaMin);
  *   4. fluid velocity (trilinear on the MAC faces) and alphaf (trilinear on
  *      the cell centres) at the particle; drag acceleration beta*(u - v) per
  *      component with beta from CalculateDragForce;
@@ -251,6 +253,11 @@ int ibmdem_unresolved_get_contacts(ibmdem_ucase* u, int32_t* start, int32_t* par
 int ibmdem_unresolved_step(ibmdem_ucase* u, int32_t nsteps);
 int ibmdem_unresolved_synchronize(ibmdem_ucase* u);
 int64_t ibmdem_unresolved_launch_count(const ibmdem_ucase* u);
+/* Per-phase CUDA-event timing of the unresolved step (lists, search, contacts,
+ * stamps, alpha, drag); get_timing synchronises and returns the phase count. */
+int ibmdem_unresolved_timing_enable(ibmdem_ucase* u, int32_t on);
+int ibmdem_unresolved_get_timing(ibmdem_ucase* u, double* ms, int64_t* counts, int32_t n, int32_t reset);
+const char* ibmdem_unresolved_phase_name(int32_t i);
 /* CalculateDragForce (ZJS_DRAGFORCE_DEM.F90:2-35) for n particles on device
  * arrays: beta[3i+j] from rho[i], rad[i], v[3i+j], denf, alphaf[i] and the
  * fluid velocity velf[3i+j]; viscf is the reference's 1e-5.  Stream-ordered

@@ -433,7 +433,8 @@ static int one_step(orc_ucase* u) {
     o[15] = D(F_VOL, i) / (((sum[0] * sum[1]) * sum[2]) * u->vcell);
   }
 
-  /* solid volume fraction, gathered per fluid cell */
+  /* solid volume fraction, gathered per fluid cell from the partial sums of the
+     125 source cells around it (z outermost) */
 #pragma omp parallel for schedule(static) num_threads(orc_get_threads())
   for (long long c = 0; c < u->nint; ++c) {
     int i = (int)(c % u->n[0]);
@@ -447,10 +448,13 @@ static int one_step(orc_ucase* u) {
         for (int ox = -2; ox <= 2; ++ox) {
           int sx = (i + ox + u->n[0]) % u->n[0];
           long long src = ((long long)sz * u->n[1] + sy) * u->n[0] + sx;
+          /* the source cell's partial sum over its particles in part order */
+          double t = 0.0;
           for (int q = u->flStart[src]; q < u->flStart[src + 1]; ++q) {
             const double* w = u->gw + (size_t)u->flItems[q] * 16;
-            ap = ap + ((w[15] * w[10 + 2 - oz]) * w[5 + 2 - oy]) * w[2 - ox];
+            t = t + ((w[15] * w[10 + 2 - oz]) * w[5 + 2 - oy]) * w[2 - ox];
           }
+          ap = ap + t;
         }
       }
     }
