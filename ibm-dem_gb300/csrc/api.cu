@@ -463,6 +463,7 @@ int ibmdem_destroy(ibmdem_ctx* h) {
     cudaEventDestroy(sp.b);
   }
   for (cudaEvent_t e : c.evFree) cudaEventDestroy(e);
+  if (c.fieldsRead) cudaEventDestroy(c.fieldsRead);
   delete h;
   return IBMDEM_OK;
 }
@@ -504,6 +505,7 @@ int ibmdem_set_fluid(ibmdem_ctx* h, const double* u, const double* v, const doub
   CHECK_CTX();
   if (!u || !v || !w) return set_error(h, IBMDEM_EINVAL, "null field");
   Ctx& c = h->c;
+  wait_fields_read(c);
   size_t nb = sizeof(double) * (size_t)c.g.ncell;
   CU(cudaMemcpyAsync(c.u, u, nb, cudaMemcpyHostToDevice, c.stream));
   CU(cudaMemcpyAsync(c.v, v, nb, cudaMemcpyHostToDevice, c.stream));
@@ -521,9 +523,31 @@ int ibmdem_set_fluid(ibmdem_ctx* h, const double* u, const double* v, const doub
   return IBMDEM_OK;
 }
 
+int ibmdem_get_fluid_async(ibmdem_ctx* h, double* u, double* v, double* w, double* fx, double* fy, double* fz,
+                           void* copy_stream) {
+  CHECK_CTX();
+  Ctx& c = h->c;
+  cudaStream_t cs = reinterpret_cast<cudaStream_t>(copy_stream);
+  if (cs == c.stream) return set_error(h, IBMDEM_EINVAL, "copy_stream must differ from the context's stream");
+  if (!c.fieldsRead) CU(cudaEventCreateWithFlags(&c.fieldsRead, cudaEventDisableTiming));
+  const size_t nb = sizeof(double) * (size_t)c.g.ncell;
+  // the copies start after the work issued so far on the context's stream ...
+  CU(cudaEventRecord(c.fieldsRead, c.stream));
+  CU(cudaStreamWaitEvent(cs, c.fieldsRead, 0));
+  double* dst[6] = {u, v, w, fx, fy, fz};
+  double* src[6] = {c.u, c.v, c.w, c.fx, c.fy, c.fz};
+  for (int q = 0; q < 6; ++q)
+    if (dst[q]) CU(cudaMemcpyAsync(dst[q], src[q], nb, cudaMemcpyDeviceToHost, cs));
+  // ... and the next context work that writes the fields waits for them
+  CU(cudaEventRecord(c.fieldsRead, cs));
+  c.fieldsReadPending = true;
+  return launch_status(h);
+}
+
 int ibmdem_get_fluid(ibmdem_ctx* h, double* u, double* v, double* w, double* fx, double* fy, double* fz) {
   CHECK_CTX();
   Ctx& c = h->c;
+  wait_fields_read(c);
   size_t nb = sizeof(double) * (size_t)c.g.ncell;
   double* dst[6] = {u, v, w, fx, fy, fz};
   double* src[6] = {c.u, c.v, c.w, c.fx, c.fy, c.fz};
@@ -837,6 +861,7 @@ static int ensure_plan(ibmdem_ctx* h) {
 int ibmdem_UpdateMomentumSourceTerm(ibmdem_ctx* h) {
   CHECK_CTX();
   Ctx& c = h->c;
+  wait_fields_read(c);
   int rc = ensure_plan(h);
   if (rc) return rc;
   REQUIRE(c.spreadValid, "spreading needs MultiDirectForcing's reset after the weights change");
@@ -847,6 +872,7 @@ int ibmdem_UpdateMomentumSourceTerm(ibmdem_ctx* h) {
 int ibmdem_VelocityPostGuess(ibmdem_ctx* h) {
   CHECK_CTX();
   Ctx& c = h->c;
+  wait_fields_read(c);
   REQUIRE(c.planReady && c.spreadValid, "no spread to apply");
   launch_post_guess(c);
   return launch_status(h);
@@ -893,6 +919,7 @@ int ibmdem_InitializationDEM(ibmdem_ctx* h) {
 static int mdf(ibmdem_ctx* h, bool frozen) {
   Ctx& c = h->c;
   REQUIRE(c.haveFluid, "no fluid field");
+  wait_fields_read(c);
   int rc = ensure_plan(h);
   if (rc) return rc;
   {

@@ -152,6 +152,9 @@ int capture_batch(ibmdem_batch* b) {
     load[best] += case_work(b->cases[i]->c);
   }
   b->launchesPerStep.assign(n, 0);
+  // a pending asynchronous field read-out is waited for on the member's own
+  // stream (the graph is ordered after it), not inside the capture
+  for (ibmdem_ctx* m : b->cases) wait_fields_read(m->c);
   e = cudaStreamBeginCapture(b->origin, cudaStreamCaptureModeRelaxed);
   if (e != cudaSuccess) return batch_error(b, IBMDEM_ECUDA, "begin capture: %s", cudaGetErrorString(e));
   cudaEventRecord(b->fork, b->origin);
@@ -209,6 +212,7 @@ int launch_batch(ibmdem_batch* b, int nsteps) {
   if (b->cases.empty() || nsteps <= 0) return IBMDEM_OK;
   // order the batch after what each case's own stream already holds
   for (size_t i = 0; i < b->cases.size(); ++i) {
+    wait_fields_read(b->cases[i]->c);
     cudaEventRecord(b->inputs[i], b->cases[i]->c.stream);
     cudaStreamWaitEvent(b->origin, b->inputs[i], 0);
   }

@@ -135,7 +135,7 @@ __device__ inline void window_start(const int4& wn, int comp, int& sx, int& sy, 
 // register-resident sorted list.  Each plan
 // entry keeps the contributing root parcel (images share their source's
 // fdrag*vol) and its weight, so spreading streams the plan sequentially.
-constexpr int kMaxHits = 32;
+constexpr int kMaxHits = 16;
 
 // mark the interior nodes touched by any parcel window
 __global__ void k_touch(Geom g, const Counters* cnt, const int4* win, uint8_t* flags) {

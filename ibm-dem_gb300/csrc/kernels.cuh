@@ -101,6 +101,11 @@ struct Ctx {
   double phaseMs[32] = {};
   long long phaseCount[32] = {};
 
+  // asynchronous read-out of the fields (ibmdem_get_fluid_async): later work
+  // that writes them waits for the copies
+  cudaEvent_t fieldsRead = nullptr;
+  bool fieldsReadPending = false;
+
   // state flags
   bool haveFluid = false, haveParcels = false, listsBuilt = false;
   bool weightsLocal = false, weightsGhost = false, planReady = false;
@@ -155,6 +160,14 @@ void launch_marker_update(Ctx& c, bool reset, bool adjust);
 struct ibmdem_ctx {
   ibmdem::Ctx c;
 };
+
+// order the context's stream after an ibmdem_get_fluid_async still reading the fields
+inline void wait_fields_read(ibmdem::Ctx& c) {
+  if (c.fieldsReadPending) {
+    cudaStreamWaitEvent(c.stream, c.fieldsRead, 0);
+    c.fieldsReadPending = false;
+  }
+}
 
 // ibmdem_create with the context's allocations and work ordered on `stream`
 int create_on_stream(const ibmdem_params* p, int device, cudaStream_t stream, ibmdem_ctx** out);

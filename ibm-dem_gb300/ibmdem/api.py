@@ -39,7 +39,7 @@ EXPORTS = [
     "ibmdem_unresolved_get_particles", "ibmdem_unresolved_get_volume_fraction", "ibmdem_unresolved_get_contacts",
     "ibmdem_unresolved_step", "ibmdem_unresolved_synchronize", "ibmdem_unresolved_launch_count",
     "ibmdem_CalculateDragForce", "ibmdem_unresolved_timing_enable", "ibmdem_unresolved_get_timing",
-    "ibmdem_unresolved_phase_name",
+    "ibmdem_unresolved_phase_name", "ibmdem_get_fluid_async",
 ]
 
 SUBROUTINES = [
@@ -71,6 +71,7 @@ def load(path=LIB_PATH):
     lib.ibmdem_synchronize.argtypes = [vp]
     lib.ibmdem_set_fluid.argtypes = [vp, vp, vp, vp]
     lib.ibmdem_get_fluid.argtypes = [vp] + [vp] * 6
+    lib.ibmdem_get_fluid_async.argtypes = [vp] + [vp] * 6 + [vp]
     lib.ibmdem_set_parcels.argtypes = [vp, i32, vp]
     lib.ibmdem_get_parcels.argtypes = [vp, vp, i32, P(i32), P(i32)]
     lib.ibmdem_set_bodies.argtypes = [vp, i32, vp]

@@ -105,6 +105,14 @@ int ibmdem_set_fluid(ibmdem_ctx* ctx, const double* u, const double* v, const do
  * Any pointer may be NULL. */
 int ibmdem_get_fluid(ibmdem_ctx* ctx, double* u, double* v, double* w,
                      double* fx, double* fy, double* fz);
+/* ibmdem_get_fluid without waiting: the copies run on `copy_stream` (a
+ * cudaStream_t other than the context's), after the work issued so far on the
+ * context, and the call returns at once.  Context work that does not write the
+ * fields (ibmdem_CloudEvolutionMS) overlaps them; context work that writes the
+ * fields waits for them.  Synchronise copy_stream before reading the buffers;
+ * they should be pinned for the copies to overlap anything. */
+int ibmdem_get_fluid_async(ibmdem_ctx* ctx, double* u, double* v, double* w,
+                           double* fx, double* fy, double* fz, void* copy_stream);
 /* Local parcels part(1:npLocal) (ZJS_VARS.F90:20); pType is set to -1. */
 int ibmdem_set_parcels(ibmdem_ctx* ctx, int32_t np, const ibmdem_parcel* parts);
 /* Copy out part(1:np): locals first, then periodic images (np_out gets np,

@@ -105,3 +105,32 @@ def test_trajectory(gpu_lib, oracle_mod, couple):
     rp, _ = r.get_parcels()
     assert len(gp) == len(rp)
     assert cases.rel_close(gp["x"][:nl], rp["x"][:nl], 1e-12)
+
+
+def test_async_fluid_readout_matches_sync(gpu_lib):
+    """ibmdem_get_fluid_async overlapping CloudEvolutionMS returns the fields that
+    ibmdem_get_fluid returns right after MultiDirectForcing, and the next step,
+    which writes the fields, waits for the copies."""
+    import ctypes
+
+    import torch
+
+    p, parts, bodies, field = cases.contact_case(seed=6)
+    case = gpu_lib.Case(p, parts, bodies, field, device=0)
+    case.InitializationDEM()
+    case.MultiDirectForcing()
+    ref = case.get_fluid()
+    case.close()
+    case = gpu_lib.Case(p, parts, bodies, field, device=0)
+    case.InitializationDEM()
+    case.MultiDirectForcing()
+    out = [torch.empty(f.shape, dtype=torch.float64, pin_memory=True).numpy() for f in ref]
+    s = torch.cuda.Stream()
+    rc = case.lib.ibmdem_get_fluid_async(case.h, *[o.ctypes.data for o in out], ctypes.c_void_p(s.cuda_stream))
+    assert rc == 0
+    case.CloudEvolutionMS()
+    case.step(1)  # writes the fields: ordered after the copies
+    s.synchronize()
+    for a, b in zip(out, ref):
+        assert np.array_equal(a, b)
+    case.close()
