@@ -172,6 +172,11 @@ void init_geom(Geom& g, const ibmdem_params* p) {
   g.knCoeff = p->knCoeff;
   g.di = p->dx;
   for (int k = 0; k < 3; ++k) g.g[k] = p->gravity[k];
+  g.fdNint = FastDiv((uint32_t)g.nint);
+  g.fdN0 = FastDiv((uint32_t)g.n[0]);
+  g.fdN1 = FastDiv((uint32_t)g.n[1]);
+  g.fdNi = FastDiv((uint32_t)g.ni);
+  g.fdNj = FastDiv((uint32_t)g.nj);
 }
 
 // images the configuration needs right now (host estimate for the capacity)

@@ -45,6 +45,30 @@ enum : int {
   E_PLANCAP = 64,  // spread-plan capacity exceeded
 };
 
+// Division of a 32-bit unsigned numerator by a fixed divisor d >= 2 with one
+// high multiply (Granlund and Montgomery's round-up method, "Division by
+// invariant integers using multiplication", PLDI 1994): with l = ceil(log2 d)
+// and m = floor(2^32 (2^l - d) / d) + 1, n / d = (t + ((n - t) >> 1)) >> (l - 1)
+// where t = high 32 bits of m * n, for every n < 2^32.
+struct FastDiv {
+  uint32_t d = 2, m = 0, s = 0;
+  __host__ FastDiv() = default;
+  __host__ explicit FastDiv(uint32_t div) : d(div) {
+    uint32_t l = 0;
+    while ((1ull << l) < div) ++l;
+    m = (uint32_t)((((1ull << 32) * ((1ull << l) - div)) / div) + 1);
+    s = l - 1;
+  }
+  __host__ __device__ uint32_t div(uint32_t n) const {
+#ifdef __CUDA_ARCH__
+    const uint32_t t = __umulhi(n, m);
+#else
+    const uint32_t t = (uint32_t)(((unsigned long long)n * m) >> 32);
+#endif
+    return (t + ((n - t) >> 1)) >> s;
+  }
+};
+
 struct Geom {
   int n[3];
   int ni, nj, nk;
@@ -58,6 +82,8 @@ struct Geom {
   int unit_h;       // dx == dy == dz == 1: /h, *dx*dy*dz are exact identities
   double dt, dtDEM, rhof, eta, cut2, knCoeff, di;
   double g[3];
+  FastDiv fdNint, fdN0, fdN1;  // interior nodes per component, nx, ny
+  FastDiv fdNi, fdNj;          // nx + 4, ny + 4 (cells with the halo)
 };
 
 struct Counters {
@@ -83,11 +109,12 @@ __host__ __device__ inline int cell_id(const Geom& g, int i, int j, int k) {
   return (int)(field_off(g, i, j, k) + 1);
 }
 __host__ __device__ inline void cell_coords(const Geom& g, int id, int& i, int& j, int& k) {
-  int t = id - 1;
-  i = t % g.ni - 1;
-  t /= g.ni;
-  j = t % g.nj - 1;
-  k = t / g.nj - 1;
+  const uint32_t t = (uint32_t)(id - 1);
+  const uint32_t a = g.fdNi.div(t);
+  const uint32_t b = g.fdNj.div(a);
+  i = (int)(t - a * (uint32_t)g.ni) - 1;
+  j = (int)(a - b * (uint32_t)g.nj) - 1;
+  k = (int)b - 1;
 }
 // floor((x-xStart)/di)+SG (ZJS_UPDATE_LIST_DEM.F90:41-43)
 __device__ inline int cell_of(const Geom& g, int d, double x) {

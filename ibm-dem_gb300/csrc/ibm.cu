@@ -222,12 +222,14 @@ __global__ void k_set_runs(Counters* cnt, const int* total, long long capRuns) {
 // and write (root | comp << 30, weight).  Nodes with more than kMaxHits hits
 // rescan into their own range and sort it in place.
 __device__ inline void node_coords(const Geom& g, uint32_t key, int& comp, int& i, int& j, int& k) {
-  comp = (int)(key / (uint32_t)g.nint);
-  long long node = (long long)key - (long long)comp * g.nint;
-  i = (int)(node % g.n[0]) + 1;
-  node /= g.n[0];
-  j = (int)(node % g.n[1]) + 1;
-  k = (int)(node / g.n[1]) + 1;
+  const uint32_t c = g.fdNint.div(key);
+  const uint32_t node = key - c * (uint32_t)g.nint;
+  const uint32_t row = g.fdN0.div(node);
+  const uint32_t kk = g.fdN1.div(row);
+  comp = (int)c;
+  i = (int)(node - row * (uint32_t)g.n[0]) + 1;
+  j = (int)(row - kk * (uint32_t)g.n[1]) + 1;
+  k = (int)kk + 1;
 }
 
 __global__ void __launch_bounds__(kBlock) k_plan_fill(Geom g, Counters* cnt, const uint32_t* __restrict__ runKey,
@@ -254,24 +256,36 @@ __global__ void __launch_bounds__(kBlock) k_plan_fill(Geom g, Counters* cnt, con
 #pragma unroll
     for (int t = 0; t < kMaxHits; ++t) hit[t] = 0xffffffffu;
     int nh = 0;
+    // The candidates of the node's 9 or 12 cell rows, walked as one flat list:
+    // the lanes of a warp then diverge only on their totals, not row by row.
+    int lo[12], hi[12];
+    int nrow = 0, total = 0;
     if (has)
       for (int cz = clo; cz <= chi; ++cz)
         for (int cy = blo; cy <= bhi; ++cy) {
           const int c0 = cell_id(g, alo, cy, cz);
-          const int q0 = cellStart[c0 - 1], q1 = cellStart[c0 + (ahi - alo)];
-          for (int q = q0; q < q1; ++q) {
-            const int p = cellItems[q];
-            int sx, sy, sz;
-            window_start(win[p], comp, sx, sy, sz);
-            const int dx = i - sx, dy = j - sy, dz = k - sz;
-            if ((unsigned)dx > 2u || (unsigned)dy > 2u || (unsigned)dz > 2u) continue;
-            const uint32_t x = ((uint32_t)p << 7) | (uint32_t)(comp * 27 + dz * 9 + dy * 3 + dx);
-#pragma unroll
-            for (int t = kMaxHits - 1; t >= 1; --t) hit[t] = min(hit[t], max(hit[t - 1], x));
-            hit[0] = min(hit[0], x);
-            ++nh;
-          }
+          lo[nrow] = cellStart[c0 - 1];
+          hi[nrow] = cellStart[c0 + (ahi - alo)];
+          total += hi[nrow] - lo[nrow];
+          ++nrow;
         }
+    int row = 0, q = nrow ? lo[0] : 0;
+    for (int t = 0; t < total; ++t, ++q) {
+      while (q >= hi[row]) {
+        ++row;
+        q = lo[row];
+      }
+      const int p = cellItems[q];
+      int sx, sy, sz;
+      window_start(win[p], comp, sx, sy, sz);
+      const int dx = i - sx, dy = j - sy, dz = k - sz;
+      if ((unsigned)dx > 2u || (unsigned)dy > 2u || (unsigned)dz > 2u) continue;
+      const uint32_t x = ((uint32_t)p << 7) | (uint32_t)(comp * 27 + dz * 9 + dy * 3 + dx);
+#pragma unroll
+      for (int u = kMaxHits - 1; u >= 1; --u) hit[u] = min(hit[u], max(hit[u - 1], x));
+      hit[0] = min(hit[0], x);
+      ++nh;
+    }
     // block-exclusive prefix of nh and one reservation for the block
     int x = nh;
 #pragma unroll
@@ -459,6 +473,7 @@ __global__ void __launch_bounds__(kBlock) k_interp(Recs R, Geom g, const Counter
 // parallel from coalesced reads, then each lane folds its own node's products
 // in part order -- the reference's fx = fx - fdrag*vol*weight, term by term.
 constexpr int kSpreadBuf = 3072;  // products per block held in shared memory
+constexpr int kStageDepth = 4;    // plan loads in flight per thread while staging
 constexpr int kLenBins = 64;
 // A block takes 256 consecutive touched nodes (one contiguous plan range).
 // Their products (fdrag*vol)*weight are formed in parallel from coalesced
@@ -504,21 +519,21 @@ __global__ void __launch_bounds__(kBlock) k_spread(Geom g, const Counters* cnt, 
     const int total = sStart[nHere - 1] + sLen[nHere - 1] - base;
     const bool staged = total <= kSpreadBuf;
     if (staged)
-      for (int q0 = threadIdx.x; q0 < total; q0 += 4 * kBlock) {
-        // four independent plan loads and gathers in flight per thread
-        uint32_t rc[4];
-        double w[4], a[4];
+      for (int q0 = threadIdx.x; q0 < total; q0 += kStageDepth * kBlock) {
+        // kStageDepth independent plan loads and gathers in flight per thread
+        uint32_t rc[kStageDepth];
+        double w[kStageDepth], a[kStageDepth];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
+        for (int u = 0; u < kStageDepth; ++u) {
           const int q = q0 + u * kBlock;
           rc[u] = q < total ? planRoot[base + q] : 0u;
           w[u] = q < total ? planW[base + q] : 0.0;
         }
 #pragma unroll
-        for (int u = 0; u < 4; ++u)
+        for (int u = 0; u < kStageDepth; ++u)
           a[u] = q0 + u * kBlock < total ? fv[(size_t)(rc[u] >> 30) * cap + (rc[u] & 0x3fffffffu)] : 0.0;
 #pragma unroll
-        for (int u = 0; u < 4; ++u)
+        for (int u = 0; u < kStageDepth; ++u)
           if (q0 + u * kBlock < total) prod[q0 + u * kBlock] = a[u] * w[u];
       }
     const int bin = min(myLen, kLenBins - 1);
