@@ -13,6 +13,8 @@
 #include <new>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "common.cuh"
 #include "kernels.cuh"
 #include "prims.cuh"
@@ -338,13 +340,19 @@ static cudaEvent_t take_event(Ctx& c) {
   cudaEventCreate(&e);
   return e;
 }
+static const char* const kPhaseLabels[P_COUNT] = {"interp", "spread", "weights", "plan", "cells", "pairs",
+                                                  "force", "bodysum", "bodymove", "markers", "images", "reset"};
+// Every phase is an NVTX range (visible to any attached profiler, a few ns
+// otherwise); with timing on it is also bracketed by CUDA events.
 PhaseScope::PhaseScope(Ctx& ctx, int ph) : c(ctx), phase(ph) {
+  nvtxRangePushA(kPhaseLabels[ph]);
   if (!c.timing) return;
   a = take_event(c);
   b = take_event(c);
   cudaEventRecord(a, c.stream);
 }
 PhaseScope::~PhaseScope() {
+  nvtxRangePop();
   if (!c.timing || !a) return;
   cudaEventRecord(b, c.stream);
   c.spans.push_back({phase, a, b});
@@ -364,8 +372,6 @@ static void collect_timing(Ctx& c) {
 }
 }  // namespace ibmdem
 
-static const char* kPhaseNames[P_COUNT] = {"interp", "spread", "weights", "plan", "cells", "pairs",
-                                           "force", "bodysum", "bodymove", "markers", "images", "reset"};
 
 extern "C" {
 
@@ -375,7 +381,7 @@ int ibmdem_timing_enable(ibmdem_ctx* h, int32_t on) {
   return IBMDEM_OK;
 }
 
-const char* ibmdem_phase_name(int32_t i) { return (i >= 0 && i < P_COUNT) ? kPhaseNames[i] : ""; }
+const char* ibmdem_phase_name(int32_t i) { return (i >= 0 && i < P_COUNT) ? kPhaseLabels[i] : ""; }
 
 int ibmdem_get_timing(ibmdem_ctx* h, double* ms, int64_t* counts, int32_t n, int32_t reset) {
   if (!h) return IBMDEM_EINVAL;
@@ -593,8 +599,8 @@ int ibmdem_set_parcels(ibmdem_ctx* h, int32_t np, const ibmdem_parcel* parts) {
     hi[(size_t)I_GIDX * c.cap + i] = p.globalIdx;
     hi[(size_t)I_MSIDX * c.cap + i] = p.MSIdx;
     int a[3];
-    for (int d = 0; d < 3; ++d) a[d] = (int)std::floor((p.x[d] - c.g.start[d]) / c.g.h[d]) + 1;
-    bool in = true;
+    bool in = std::isfinite(p.x[0]) && std::isfinite(p.x[1]) && std::isfinite(p.x[2]);
+    for (int d = 0; d < 3; ++d) a[d] = in ? (int)std::floor((p.x[d] - c.g.start[d]) / c.g.h[d]) + 1 : 0;
     for (int d = 0; d < 3; ++d) in = in && a[d] >= -1 && a[d] <= c.g.n[d] + 2;
     if (!in) return set_error(h, IBMDEM_ERANGE, "parcel %d at (%g,%g,%g) exceeds the region", i + 1, p.x[0], p.x[1], p.x[2]);
     hi[(size_t)I_CELL * c.cap + i] = cell_id(c.g, a[0], a[1], a[2]);

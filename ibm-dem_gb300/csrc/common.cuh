@@ -52,7 +52,7 @@ enum : int {
 // where t = high 32 bits of m * n, for every n < 2^32.
 struct FastDiv {
   uint32_t d = 2, m = 0, s = 0;
-  __host__ FastDiv() = default;
+  FastDiv() = default;
   __host__ explicit FastDiv(uint32_t div) : d(div) {
     uint32_t l = 0;
     while ((1ull << l) < div) ++l;

@@ -89,3 +89,17 @@ def test_create_rejects_unsupported_parameters(oracle_mod):
     p = make_params(2, 16, 16)
     with pytest.raises(ValueError):
         oracle_mod.OracleCase(p)
+
+
+def test_null_handles_are_rejected(gpu_lib):
+    """No CUDA call is made for a null handle, so this runs without a GPU."""
+    import ctypes
+    lib = ctypes.CDLL(gpu_lib.LIB_PATH)
+    for name in ("ibmdem_synchronize", "ibmdem_step", "ibmdem_MultiDirectForcing", "ibmdem_batch_step",
+                 "ibmdem_server_poll", "ibmdem_unresolved_step", "ibmdem_destroy", "ibmdem_batch_destroy",
+                 "ibmdem_server_destroy", "ibmdem_unresolved_destroy"):
+        f = getattr(lib, name)
+        rc = f(None, 1) if name.endswith("_step") else f(None, None) if name == "ibmdem_server_poll" else f(None)
+        assert rc == -1, name
+    lib.ibmdem_last_error.restype = ctypes.c_char_p
+    assert lib.ibmdem_last_error(None) == b"null context"

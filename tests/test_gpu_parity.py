@@ -90,7 +90,7 @@ def test_one_step(gpu_lib, oracle_mod):
     _cmp_state(g, r)
 
 
-@pytest.mark.parametrize("couple", [1, 3])
+@pytest.mark.parametrize("couple", [1, 3, 10])
 def test_trajectory(gpu_lib, oracle_mod, couple):
     g, r = _pair(gpu_lib, oracle_mod, cases.contact_case(seed=11, coupleInterval=couple))
     for c in (g, r):
