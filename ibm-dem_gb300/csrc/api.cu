@@ -106,7 +106,7 @@ void free_parcel_buffers(Ctx& c) {
   void* ps[] = {c.recD[0], c.recD[1], c.recI[0], c.recI[1], c.imgSrc, c.imgShift, c.cellItems, c.bodyItems,
                 c.iTmpA, c.iTmpB, c.scanScratch, c.sortHist, c.kA, c.vA, c.kB, c.vB, c.activeList, c.pairCnt,
                 c.pairStart, c.pairIdx, c.W, c.win, c.cntInt, c.fv, c.runStart, c.runKey, c.fCur, c.fPrev,
-                c.lastNodes, c.touch, c.planRoot, c.planW, c.runCnt, c.planAlloc};
+                c.lastNodes, c.touch, c.planRoot, c.planW, c.runCnt, c.planAlloc, c.winC};
   for (void* p : ps) dfree(c, p);
   c.bytes -= c.bytesParcels + c.bytesRuns;
   c.bytesParcels = c.bytesRuns = 0;
@@ -119,6 +119,7 @@ void free_parcel_buffers(Ctx& c) {
   c.activeList = c.pairCnt = c.pairStart = c.pairIdx = nullptr;
   c.W = nullptr;
   c.win = nullptr;
+  c.winC = nullptr;
   c.cntInt = nullptr;
   c.fv = nullptr;
   c.runStart = nullptr;
@@ -245,6 +246,7 @@ void for_each_parcel_buffer(Ctx& c, F&& f) {
   f(c.pairIdx, (size_t)c.capPairs);
   f(c.W, (size_t)kWStride * c.cap);
   f(c.win, (size_t)c.cap);
+  f(c.winC, (size_t)c.cap);
   f(c.cntInt, (size_t)c.cap);
   f(c.fv, 3 * (size_t)c.cap);
 }

@@ -216,8 +216,9 @@ __global__ void k_set_runs(Counters* cnt, const int* total, long long capRuns) {
   cnt->nRuns = (int)min((long long)t, capRuns);
 }
 
-// One pass per touched node: scan the candidate cells, keep the hits sorted in
-// registers, then reserve the block's contribution range with one atomic (the
+// One pass per touched node: scan the candidate cells, append the hits to the
+// thread's shared-memory column and insertion-sort them (a node has 7 hits on
+// average), then reserve the block's contribution range with one atomic (the
 // 256 nodes of a block own one contiguous range, which the spread relies on)
 // and write (root | comp << 30, weight).  Nodes with more than kMaxHits hits
 // rescan into their own range and sort it in place.
@@ -235,12 +236,16 @@ __device__ inline void node_coords(const Geom& g, uint32_t key, int& comp, int& 
 __global__ void __launch_bounds__(kBlock) k_plan_fill(Geom g, Counters* cnt, const uint32_t* __restrict__ runKey,
                                                       const int* __restrict__ cellStart,
                                                       const int* __restrict__ cellItems,
-                                                      const int4* __restrict__ win, const double* __restrict__ W,
+                                                      const int4* __restrict__ win, const int4* __restrict__ winC,
+                                                      const double* __restrict__ W,
                                                       const int* __restrict__ imgSrc, int* runStart, int* runCnt,
                                                       uint32_t* planRoot, double* planW,
                                                       unsigned long long* cursor, long long capContrib) {
   __shared__ int warpSum[kBlock / 32];
   __shared__ long long blockBase;
+  // each thread's hits, column-major (hits[h * kBlock + thread]: conflict-free)
+  __shared__ uint32_t hits[kMaxHits * kBlock];
+  uint32_t* hit = hits + threadIdx.x;
   const long long nRuns = cnt->nRuns;
   const int npLocal = cnt->npLocal;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -252,40 +257,34 @@ __global__ void __launch_bounds__(kBlock) k_plan_fill(Geom g, Counters* cnt, con
     const int alo = i - (comp == 0 ? 2 : 1), ahi = i + 1;
     const int blo = j - (comp == 1 ? 2 : 1), bhi = j + 1;
     const int clo = k - (comp == 2 ? 2 : 1), chi = k + 1;
-    uint32_t hit[kMaxHits];
-#pragma unroll
-    for (int t = 0; t < kMaxHits; ++t) hit[t] = 0xffffffffu;
     int nh = 0;
-    // The candidates of the node's 9 or 12 cell rows, walked as one flat list:
-    // the lanes of a warp then diverge only on their totals, not row by row.
-    int lo[12], hi[12];
-    int nrow = 0, total = 0;
     if (has)
       for (int cz = clo; cz <= chi; ++cz)
         for (int cy = blo; cy <= bhi; ++cy) {
           const int c0 = cell_id(g, alo, cy, cz);
-          lo[nrow] = cellStart[c0 - 1];
-          hi[nrow] = cellStart[c0 + (ahi - alo)];
-          total += hi[nrow] - lo[nrow];
-          ++nrow;
+          const int q0 = cellStart[c0 - 1], q1 = cellStart[c0 + (ahi - alo)];
+          for (int q = q0; q < q1; ++q) {
+            // windows in cell order: no dependent gather per candidate
+            int sx, sy, sz;
+            window_start(winC[q], comp, sx, sy, sz);
+            const int dx = i - sx, dy = j - sy, dz = k - sz;
+            if ((unsigned)dx > 2u || (unsigned)dy > 2u || (unsigned)dz > 2u) continue;
+            if (nh < kMaxHits)
+              hit[nh * kBlock] = ((uint32_t)cellItems[q] << 7) | (uint32_t)(comp * 27 + dz * 9 + dy * 3 + dx);
+            ++nh;
+          }
         }
-    int row = 0, q = nrow ? lo[0] : 0;
-    for (int t = 0; t < total; ++t, ++q) {
-      while (q >= hi[row]) {
-        ++row;
-        q = lo[row];
+    // part order: insertion sort of the (few) hits in place
+    if (nh <= kMaxHits)
+      for (int a = 1; a < nh; ++a) {
+        const uint32_t v = hit[a * kBlock];
+        int at = a;
+        while (at > 0 && hit[(at - 1) * kBlock] > v) {
+          hit[at * kBlock] = hit[(at - 1) * kBlock];
+          --at;
+        }
+        hit[at * kBlock] = v;
       }
-      const int p = cellItems[q];
-      int sx, sy, sz;
-      window_start(win[p], comp, sx, sy, sz);
-      const int dx = i - sx, dy = j - sy, dz = k - sz;
-      if ((unsigned)dx > 2u || (unsigned)dy > 2u || (unsigned)dz > 2u) continue;
-      const uint32_t x = ((uint32_t)p << 7) | (uint32_t)(comp * 27 + dz * 9 + dy * 3 + dx);
-#pragma unroll
-      for (int u = kMaxHits - 1; u >= 1; --u) hit[u] = min(hit[u], max(hit[u - 1], x));
-      hit[0] = min(hit[0], x);
-      ++nh;
-    }
     // block-exclusive prefix of nh and one reservation for the block
     int x = nh;
 #pragma unroll
@@ -310,16 +309,14 @@ __global__ void __launch_bounds__(kBlock) k_plan_fill(Geom g, Counters* cnt, con
       if (o + nh > capContrib) {
         set_err(cnt, E_PLANCAP, (int)r);
       } else if (nh <= kMaxHits) {
-#pragma unroll
-        for (int t = 0; t < kMaxHits; ++t) {
-          if (t < nh) {
-            const int p = (int)(hit[t] >> 7);
-            const int slot = (int)(hit[t] & 127u);
-            const uint32_t root = (uint32_t)(p < npLocal ? p : imgSrc[p - npLocal]);
-            planRoot[o + t] = root | ((uint32_t)comp << 30);
-            const int sc = slot / 27;
-            planW[o + t] = W[(size_t)p * kWStride + sc * 28 + (slot - sc * 27)];
-          }
+        for (int t = 0; t < nh; ++t) {
+          const uint32_t v = hit[t * kBlock];
+          const int p = (int)(v >> 7);
+          const int slot = (int)(v & 127u);
+          const uint32_t root = (uint32_t)(p < npLocal ? p : imgSrc[p - npLocal]);
+          planRoot[o + t] = root | ((uint32_t)comp << 30);
+          const int sc = slot / 27;
+          planW[o + t] = W[(size_t)p * kWStride + sc * 28 + (slot - sc * 27)];
         }
       } else {
         int t = 0;
@@ -358,6 +355,13 @@ __global__ void __launch_bounds__(kBlock) k_plan_fill(Geom g, Counters* cnt, con
     }
     __syncthreads();
   }
+}
+
+// windows of the cell items, in cell order
+__global__ void k_win_by_cell(const Counters* cnt, const int* __restrict__ cellItems, const int4* __restrict__ win,
+                              int4* winC) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < cnt->np) winC[q] = win[cellItems[q]];
 }
 
 __global__ void k_plan_total(Counters* cnt, const unsigned long long* cursor) {
@@ -653,11 +657,12 @@ void build_spread_plan(Ctx& c) {
   k_set_runs<<<1, 1, 0, s>>>(c.dCnt, c.dTotal, c.capRuns);
   k_flag_emit<<<(unsigned)nb, kBlock, 0, s>>>(fv4, nvec, nflags, c.iTmpA, c.runKey, c.capRuns);
   cudaMemsetAsync(c.planAlloc, 0, sizeof(unsigned long long), s);
-  k_plan_fill<<<gs_blocks(c.capRuns), kBlock, 0, s>>>(c.g, c.dCnt, c.runKey, c.cellStart, c.cellItems, c.win, c.W,
-                                                      c.imgSrc, c.runStart, c.runCnt, c.planRoot, c.planW,
+  k_win_by_cell<<<nblocks(c.cap), kBlock, 0, s>>>(c.dCnt, c.cellItems, c.win, c.winC);
+  k_plan_fill<<<gs_blocks(c.capRuns), kBlock, 0, s>>>(c.g, c.dCnt, c.runKey, c.cellStart, c.cellItems, c.win, c.winC,
+                                                      c.W, c.imgSrc, c.runStart, c.runCnt, c.planRoot, c.planW,
                                                       c.planAlloc, c.capContrib);
   k_plan_total<<<1, 1, 0, s>>>(c.dCnt, c.planAlloc);
-  c.launches += 4;
+  c.launches += 5;
   c.planReady = true;
   c.spreadValid = false;
 }

@@ -69,6 +69,7 @@ struct Ctx {
   // delta weights and the spread plan
   double* W = nullptr;     // [84*cap] marker-major delta weights
   int4* win = nullptr;     // [cap] cell (a,b,c) + shifted-window flags
+  int4* winC = nullptr;    // [cap] the same, in cell-list order (spread plan)
   int* cntInt = nullptr;   // [cap] interior contributions per parcel
   double* fv = nullptr;    // [3*cap] fdrag*vol of locals
   uint8_t* touch = nullptr;      // [3*nint rounded to 16] touched-node flags
