@@ -745,9 +745,17 @@ int ibmdem_get_collision_lists(ibmdem_ctx* h, int32_t* start, int32_t* idx, int3
   return IBMDEM_OK;
 }
 
+static int ensure_plan(ibmdem_ctx* h);
+
 int ibmdem_get_counters(ibmdem_ctx* h, int64_t* out, int32_t n) {
   CHECK_CTX();
   Ctx& c = h->c;
+  // the touched nodes and contributions are those of the plan the next spread
+  // uses: build it if the weights changed since the last one
+  if (c.weightsLocal && c.weightsGhost && !c.planReady) {
+    int rp = ensure_plan(h);
+    if (rp) return rp;
+  }
   int rc = check_device(h);
   if (rc) return rc;
   int64_t v[7] = {c.hCnt->npLocal, c.hCnt->np, c.hCnt->nPairs, 0, 0, 0, c.hCnt->nContrib};
@@ -765,6 +773,7 @@ int ibmdem_get_counters(ibmdem_ctx* h, int64_t* out, int32_t n) {
 // ---- reference subroutines ------------------------------------------------
 
 static int plan(ibmdem_ctx* h);
+static int size_runs(ibmdem_ctx* h);
 
 int ibmdem_RebuildAllListOrNot(ibmdem_ctx* h) {
   CHECK_CTX();
@@ -794,8 +803,11 @@ int ibmdem_UpdateGhostCellWeightListDEM(ibmdem_ctx* h) {
   launch_weights(c, false);
   c.weightsGhost = true;
   c.planReady = false;
-  if (c.weightsLocal) {
-    int rc = plan(h);
+  // size the spread plan's run arrays here, outside any stream capture (this
+  // synchronises); the plan itself is built by the next spread, as after a
+  // sub-step, so that a step leaves the host state it found
+  if (c.weightsLocal && !c.runsSized) {
+    int rc = size_runs(h);
     if (rc) return rc;
   }
   return launch_status(h);
@@ -979,12 +991,10 @@ int ibmdem_CloudEvolutionStepMS(ibmdem_ctx* h) {
   { PhaseScope t(c, P_WEIGHTS); launch_weights(c, true); }
   { PhaseScope t(c, P_IMAGES); launch_img_update(c); }
   { PhaseScope t(c, P_WEIGHTS); launch_weights(c, false); }
-  {
-    PhaseScope t(c, P_PLAN);
-    int rc = plan(h);
-    if (rc) return rc;
-  }
+  // the spread plan follows the new weights when a spread next needs it: of
+  // coupleInterval sub-steps only the last one's plan is ever used
   c.listsBuilt = c.weightsLocal = c.weightsGhost = true;
+  c.planReady = c.spreadValid = false;
   return launch_status(h);
 }
 

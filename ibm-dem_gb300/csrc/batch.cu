@@ -81,7 +81,8 @@ struct ibmdem_batch {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   std::vector<long long> launchesPerStep;
-  std::vector<unsigned long long> keys;  // member state the graph was captured for
+  std::vector<unsigned long long> keys;  // member state the captured step leaves
+  bool stationary = true;  // the captured step leaves the state it was captured from
   bool dirty = true;
   std::string err = "ok";
 };
@@ -155,6 +156,8 @@ int capture_batch(ibmdem_batch* b) {
   // a pending asynchronous field read-out is waited for on the member's own
   // stream (the graph is ordered after it), not inside the capture
   for (ibmdem_ctx* m : b->cases) wait_fields_read(m->c);
+  std::vector<unsigned long long> pre(n);
+  for (int i = 0; i < n; ++i) pre[i] = state_key(b->cases[i]->c);
   e = cudaStreamBeginCapture(b->origin, cudaStreamCaptureModeRelaxed);
   if (e != cudaSuccess) return batch_error(b, IBMDEM_ECUDA, "begin capture: %s", cudaGetErrorString(e));
   cudaEventRecord(b->fork, b->origin);
@@ -198,6 +201,7 @@ int capture_batch(ibmdem_batch* b) {
   b->graph = g;
   b->keys.resize(n);
   for (int i = 0; i < n; ++i) b->keys[i] = state_key(b->cases[i]->c);
+  b->stationary = b->keys == pre;
   b->dirty = false;
   return IBMDEM_OK;
 }
@@ -217,15 +221,21 @@ int launch_batch(ibmdem_batch* b, int nsteps) {
     cudaStreamWaitEvent(b->origin, b->inputs[i], 0);
   }
   for (int s = 0; s < nsteps; ++s) {
+    // a step that changes the host state it was captured from (the first one
+    // after a member's state changed) is replayed once, then captured again
+    // from the state it left; the replays are ordered on the origin stream
+    if (b->dirty) {
+      int rc = capture_batch(b);
+      if (rc) return rc;
+    }
     cudaError_t e = cudaGraphLaunch(b->exec, b->origin);
     if (e != cudaSuccess) return batch_error(b, IBMDEM_ECUDA, "graph launch: %s", cudaGetErrorString(e));
+    for (size_t i = 0; i < b->cases.size(); ++i) b->cases[i]->c.launches += b->launchesPerStep[i];
+    if (!b->stationary) b->dirty = true;
   }
   // and each case's own stream after the batch
   cudaEventRecord(b->done, b->origin);
-  for (size_t i = 0; i < b->cases.size(); ++i) {
-    cudaStreamWaitEvent(b->cases[i]->c.stream, b->done, 0);
-    b->cases[i]->c.launches += b->launchesPerStep[i] * nsteps;
-  }
+  for (size_t i = 0; i < b->cases.size(); ++i) cudaStreamWaitEvent(b->cases[i]->c.stream, b->done, 0);
   return IBMDEM_OK;
 }
 
@@ -339,24 +349,40 @@ int admit(ibmdem_server* s, Request* r) {
   r->parts = nullptr;
   r->bodies = nullptr;
   r->u = r->v = r->w = nullptr;
-  if (!cu(cudaStreamBeginCapture(r->stream, cudaStreamCaptureModeRelaxed), "begin capture"))
-    return fail(s, r, IBMDEM_ECUDA);
-  long long l0 = c.launches;
-  rc = ibmdem_step(r->ctx, 1);
-  long long perStep = c.launches - l0;
-  cudaGraph_t g = nullptr;
-  cudaError_t e = cudaStreamEndCapture(r->stream, &g);
-  if (rc || e != cudaSuccess) {
-    if (g) cudaGraphDestroy(g);
-    if (!rc) cu(e, "end capture");
-    return fail(s, r, rc ? rc : IBMDEM_ECUDA);
+  // capture one step and queue the rest as replays; a step that leaves another
+  // host state than it was captured from is replayed once and captured again
+  int left = r->nsteps;
+  for (int attempt = 0; left > 0; ++attempt) {
+    const unsigned long long pre = state_key(c);
+    if (!cu(cudaStreamBeginCapture(r->stream, cudaStreamCaptureModeRelaxed), "begin capture"))
+      return fail(s, r, IBMDEM_ECUDA);
+    long long l0 = c.launches;
+    rc = ibmdem_step(r->ctx, 1);
+    long long perStep = c.launches - l0;
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(r->stream, &g);
+    if (rc || e != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      if (!rc) cu(e, "end capture");
+      return fail(s, r, rc ? rc : IBMDEM_ECUDA);
+    }
+    if (r->exec) cudaGraphExecDestroy(r->exec);  // freed once its queued replays finish
+    if (r->graph) cudaGraphDestroy(r->graph);
+    r->exec = nullptr;
+    r->graph = g;
+    if (!cu(cudaGraphInstantiate(&r->exec, g, 0), "graph instantiate")) return fail(s, r, IBMDEM_ECUDA);
+    c.launches = l0;
+    const bool stationary = state_key(c) == pre;
+    if (!stationary && attempt > 0) {
+      fmt_err(r->err, "the step does not return to the host state it was captured from");
+      return fail(s, r, IBMDEM_EINVAL);
+    }
+    const int k = stationary ? left : 1;
+    for (int q = 0; q < k; ++q)
+      if (!cu(cudaGraphLaunch(r->exec, r->stream), "graph launch")) return fail(s, r, IBMDEM_ECUDA);
+    c.launches += perStep * k;
+    left -= k;
   }
-  r->graph = g;
-  if (!cu(cudaGraphInstantiate(&r->exec, g, 0), "graph instantiate")) return fail(s, r, IBMDEM_ECUDA);
-  c.launches = l0;
-  for (int k = 0; k < r->nsteps; ++k)
-    if (!cu(cudaGraphLaunch(r->exec, r->stream), "graph launch")) return fail(s, r, IBMDEM_ECUDA);
-  c.launches += perStep * r->nsteps;
   if (!cu(cudaEventRecord(r->done, r->stream), "event record")) return fail(s, r, IBMDEM_ECUDA);
   s->running.push_back(r);
   return IBMDEM_OK;

@@ -352,7 +352,9 @@ int ibmdem_measure_fp64_rate(int32_t device, double* gops);
 int64_t ibmdem_launch_count(const ibmdem_ctx* ctx);
 /* Counters of the current lists: [0]=npLocal [1]=np [2]=pairs
  * [3]=touched u nodes [4]=touched v nodes [5]=touched w nodes
- * [6]=spread contributions. */
+ * [6]=spread contributions.  [3..6] are those of the spread plan the next
+ * spread uses; the plan is built here if the weights changed since the last
+ * one (a sub-step leaves it to the next spread). */
 int ibmdem_get_counters(ibmdem_ctx* ctx, int64_t* out, int32_t n);
 
 #ifdef __cplusplus
