@@ -130,18 +130,16 @@ __device__ inline void window_start(const int4& wn, int comp, int& sx, int& sy, 
 // A node (component c, interior (i,j,k)) receives from every parcel whose
 // c-window covers it.  Windows start at cell-1 on the unshifted axes and at
 // cell-1 or cell on the shifted axis, so the candidates live in a 4x3x3 block
-// of cells (4 along axis c).  The cell lists hold each cell's parcels in part
-// order; the hits are merged into part order by a branch-free insertion into a
-// register-resident sorted list.  Each plan
-// entry keeps the contributing root parcel (images share their source's
-// fdrag*vol) and its weight, so spreading streams the plan sequentially.
-constexpr int kMaxHits = 16;
+// of cells (4 along axis c).  Each plan entry keeps the contributing root
+// parcel (images share their source's fdrag*vol) and its weight, so spreading
+// streams the plan sequentially.
 
-// mark the interior nodes touched by any parcel window
-__global__ void k_touch(Geom g, const Counters* cnt, const int4* win, uint8_t* flags) {
+// mark the interior nodes touched by any parcel window; the windows are read in
+// cell order, so that a warp's stores fall on neighbouring nodes
+__global__ void k_touch(Geom g, const Counters* cnt, const int4* winC, uint8_t* flags) {
   int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= cnt->np) return;
-  int4 wn = win[e];
+  int4 wn = winC[e];
   for (int comp = 0; comp < 3; ++comp) {
     int sx, sy, sz;
     window_start(wn, comp, sx, sy, sz);
@@ -216,12 +214,20 @@ __global__ void k_set_runs(Counters* cnt, const int* total, long long capRuns) {
   cnt->nRuns = (int)min((long long)t, capRuns);
 }
 
-// One pass per touched node: scan the candidate cells, append the hits to the
-// thread's shared-memory column and insertion-sort them (a node has 7 hits on
-// average), then reserve the block's contribution range with one atomic (the
-// 256 nodes of a block own one contiguous range, which the spread relies on)
-// and write (root | comp << 30, weight).  Nodes with more than kMaxHits hits
-// rescan into their own range and sort it in place.
+// The fill works on sub-groups: up to kSubMax consecutive touched nodes of one
+// grid row (same component, j and k), taken from a warp's 32 runs.  The warp
+// gathers the parcels of the row's candidate cells once, keeps those whose
+// window covers the row in y and z and reaches the sub-group in x, and sorts
+// them by part index.  A kept parcel covers the three nodes sx..sx+2 of the
+// row, so each node's contributors in part order are the sorted list filtered
+// by sx in [i-2, i]: one ballot per node.  The entries (parcel << 7 | slot)
+// are staged per warp in shared memory; the block reserves its contribution
+// range with one atomic (the 256 runs of a block own one contiguous range in
+// run order, which the spread relies on) and writes (root | comp << 30,
+// weight) with consecutive lanes on consecutive entries.  A sub-group with more
+// than kLCap kept parcels is split into single nodes; a single node with more
+// than kLCap contributors, or a warp whose entries exceed its staging, is
+// written straight into the plan range after the reservation.
 __device__ inline void node_coords(const Geom& g, uint32_t key, int& comp, int& i, int& j, int& k) {
   const uint32_t c = g.fdNint.div(key);
   const uint32_t node = key - c * (uint32_t)g.nint;
@@ -233,124 +239,280 @@ __device__ inline void node_coords(const Geom& g, uint32_t key, int& comp, int& 
   k = (int)kk + 1;
 }
 
-__global__ void __launch_bounds__(kBlock) k_plan_fill(Geom g, Counters* cnt, const uint32_t* __restrict__ runKey,
-                                                      const int* __restrict__ cellStart,
-                                                      const int* __restrict__ cellItems,
-                                                      const int4* __restrict__ win, const int4* __restrict__ winC,
-                                                      const double* __restrict__ W,
-                                                      const int* __restrict__ imgSrc, int* runStart, int* runCnt,
-                                                      uint32_t* planRoot, double* planW,
-                                                      unsigned long long* cursor, long long capContrib) {
-  __shared__ int warpSum[kBlock / 32];
+constexpr int kSubMax = 8;      // nodes per sub-group
+constexpr int kLCap = 64;       // kept parcels per sub-group (two per lane)
+constexpr int kStageCap = 512;  // staged entries per warp
+constexpr int kPlanWarps = kBlock / 32;
+constexpr unsigned kFull = 0xffffffffu;
+
+// Gather the parcels of the candidate cells of nodes iFirst..iLast of row
+// (comp, j, k) whose window covers the row and reaches [iFirst, iLast]; the
+// first kLCap go to key (part index) and aux (sx - iFirst + 2 | (dz*3+dy) << 8).
+// Returns how many there are (all lanes).
+__device__ inline int gather_row(const Geom& g, int comp, int iFirst, int iLast, int j, int k,
+                                 const int* __restrict__ cellStart, const int* __restrict__ cellItems,
+                                 const int4* __restrict__ winC, uint32_t* key, uint32_t* aux, int lane) {
+  const int xlo = iFirst - (comp == 0 ? 2 : 1), xhi = iLast + 1;
+  const int ylo = j - (comp == 1 ? 2 : 1), zlo = k - (comp == 2 ? 2 : 1);
+  const int ny = comp == 1 ? 4 : 3, nr = ny * (comp == 2 ? 4 : 3);  // candidate cell rows (<= 12)
+  int q0 = 0, len = 0;
+  if (lane < nr) {
+    const int cy = ylo + lane % ny, cz = zlo + lane / ny;
+    const int c0 = cell_id(g, xlo, cy, cz);
+    q0 = cellStart[c0 - 1];
+    len = cellStart[c0 + (xhi - xlo)] - q0;
+  }
+  int inc = len;  // inclusive prefix over lanes 0..15 (rows past nr are empty)
+#pragma unroll
+  for (int o = 1; o < 16; o <<= 1) {
+    const int y = __shfl_up_sync(kFull, inc, o);
+    if (lane >= o) inc += y;
+  }
+  const int excl = inc - len;
+  const int total = __shfl_sync(kFull, inc, 15);
+  const unsigned lt = (1u << lane) - 1u;
+  int m = 0;
+  for (int f0 = 0; f0 < total; f0 += 32) {
+    const int f = f0 + lane;
+    // the last row whose first candidate is at or before f
+    int row = 0;
+#pragma unroll
+    for (int step = 8; step; step >>= 1) {
+      const int probe = __shfl_sync(kFull, excl, row + step);
+      if (probe <= f) row += step;
+    }
+    const int rq = __shfl_sync(kFull, q0, row);
+    const int rx = __shfl_sync(kFull, excl, row);
+    bool keep = false;
+    uint32_t pk = 0, pa = 0;
+    if (f < total) {
+      const int q = rq + (f - rx);
+      int sx, sy, sz;
+      window_start(winC[q], comp, sx, sy, sz);
+      const int dy = j - sy, dz = k - sz;
+      keep = (unsigned)dy <= 2u && (unsigned)dz <= 2u && sx <= iLast && sx + 2 >= iFirst;
+      if (keep) {
+        pk = (uint32_t)cellItems[q];
+        pa = (uint32_t)(sx - iFirst + 2) | (uint32_t)(dz * 3 + dy) << 8;
+      }
+    }
+    const unsigned mk = __ballot_sync(kFull, keep);
+    if (keep) {
+      const int at = m + __popc(mk & lt);
+      if (at < kLCap) {
+        key[at] = pk;
+        aux[at] = pa;
+      }
+    }
+    m += __popc(mk);
+  }
+  return m;
+}
+
+// Contributors of one node straight into out[0..), part order (a node with more
+// than kLCap of them; one lane).  Returns how many.
+__device__ inline int scan_node_into(const Geom& g, int comp, int i, int j, int k, const int* __restrict__ cellStart,
+                                     const int* __restrict__ cellItems, const int4* __restrict__ winC,
+                                     uint32_t* out) {
+  const int alo = i - (comp == 0 ? 2 : 1), ahi = i + 1;
+  const int blo = j - (comp == 1 ? 2 : 1), bhi = j + 1;
+  const int clo = k - (comp == 2 ? 2 : 1), chi = k + 1;
+  int t = 0;
+  for (int cz = clo; cz <= chi; ++cz)
+    for (int cy = blo; cy <= bhi; ++cy) {
+      const int c0 = cell_id(g, alo, cy, cz);
+      const int q0 = cellStart[c0 - 1], q1 = cellStart[c0 + (ahi - alo)];
+      for (int q = q0; q < q1; ++q) {
+        int sx, sy, sz;
+        window_start(winC[q], comp, sx, sy, sz);
+        const int dx = i - sx, dy = j - sy, dz = k - sz;
+        if ((unsigned)dx > 2u || (unsigned)dy > 2u || (unsigned)dz > 2u) continue;
+        out[t++] = ((uint32_t)cellItems[q] << 7) | (uint32_t)(comp * 27 + dz * 9 + dy * 3 + dx);
+      }
+    }
+  for (int a = 1; a < t; ++a) {
+    const uint32_t v = out[a];
+    int at = a;
+    while (at > 0 && out[at - 1] > v) {
+      out[at] = out[at - 1];
+      --at;
+    }
+    out[at] = v;
+  }
+  return t;
+}
+
+// The warp's sub-groups in lane order: entries (parcel << 7 | slot) to
+// out[pos] for pos < outCap, each lane's node count and offset.  With direct
+// set, out is the warp's plan range and oversized nodes are scanned into it;
+// otherwise they only count (*needDirect is set).  Returns the warp's total.
+__device__ inline int fill_subgroups(const Geom& g, unsigned starts, int nValid, int comp, int i, int j, int k,
+                                     const int* __restrict__ cellStart, const int* __restrict__ cellItems,
+                                     const int4* __restrict__ winC, uint32_t* key, uint32_t* aux, uint32_t* out,
+                                     int outCap, bool direct, int lane, int& myCnt, int& myOff, bool& needDirect) {
+  const unsigned lt = (1u << lane) - 1u;
+  int off = 0;
+  unsigned rest = starts;
+  while (rest) {
+    const int l0 = __ffs(rest) - 1;
+    rest &= rest - 1u;
+    int l1 = (rest ? __ffs(rest) - 1 : nValid) - 1;
+    const int sc = __shfl_sync(kFull, comp, l0);
+    const int sj = __shfl_sync(kFull, j, l0), sk = __shfl_sync(kFull, k, l0);
+    const int iFirst = __shfl_sync(kFull, i, l0);
+    int m = gather_row(g, sc, iFirst, __shfl_sync(kFull, i, l1), sj, sk, cellStart, cellItems, winC, key, aux, lane);
+    if (m > kLCap && l1 > l0) {
+      // too many for one list: the first node alone, the rest as a sub-group of its own
+      rest |= 1u << (l0 + 1);
+      l1 = l0;
+      m = gather_row(g, sc, iFirst, iFirst, sj, sk, cellStart, cellItems, winC, key, aux, lane);
+    }
+    if (m > kLCap) {
+      // one node with more than kLCap contributors (m counts exactly them)
+      if (direct && lane == l0) scan_node_into(g, sc, iFirst, sj, sk, cellStart, cellItems, winC, out + off);
+      if (lane == l0) {
+        myCnt = m;
+        myOff = off;
+      }
+      needDirect = true;
+      off += m;
+      __syncwarp();
+      continue;
+    }
+    __syncwarp();
+    // part order: rank of each kept parcel among the others (part indices are distinct)
+    uint32_t ek[2], ea[2];
+    int rk[2];
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      const int e = lane + 32 * u;
+      ek[u] = e < m ? key[e] : 0xffffffffu;
+      ea[u] = e < m ? aux[e] : 0u;
+      rk[u] = 0;
+    }
+    for (int f = 0; f < m; ++f) {
+      const uint32_t kf = key[f];
+      rk[0] += kf < ek[0];
+      rk[1] += kf < ek[1];
+    }
+    __syncwarp();
+#pragma unroll
+    for (int u = 0; u < 2; ++u)
+      if (lane + 32 * u < m) {
+        key[rk[u]] = ek[u];
+        aux[rk[u]] = ea[u];
+      }
+    __syncwarp();
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      const int e = lane + 32 * u;
+      ek[u] = e < m ? key[e] : 0u;
+      ea[u] = e < m ? aux[e] : 0u;
+    }
+    __syncwarp();
+    const int sx0 = iFirst - 2;
+    const int two = m > 32 ? 2 : 1;
+    for (int n = l0; n <= l1; ++n) {
+      const int in = __shfl_sync(kFull, i, n);
+      int c = 0;
+      for (int u = 0; u < two; ++u) {
+        const int sx = sx0 + (int)(ea[u] & 0xffu);
+        const bool hit = lane + 32 * u < m && sx <= in && sx + 2 >= in;
+        const unsigned mh = __ballot_sync(kFull, hit);
+        if (hit) {
+          const int at = off + c + __popc(mh & lt);
+          if (at < outCap)
+            out[at] = (ek[u] << 7) | (uint32_t)(sc * 27 + 3 * (int)(ea[u] >> 8) + (in - sx));
+        }
+        c += __popc(mh);
+      }
+      if (lane == n) {
+        myCnt = c;
+        myOff = off;
+      }
+      off += c;
+    }
+  }
+  return off;
+}
+
+__global__ void __launch_bounds__(kBlock, 6) k_plan_fill(Geom g, Counters* cnt, const uint32_t* __restrict__ runKey,
+                                                         const int* __restrict__ cellStart,
+                                                         const int* __restrict__ cellItems,
+                                                         const int4* __restrict__ winC,
+                                                         const double* __restrict__ W,
+                                                         const int* __restrict__ imgSrc, int* runStart, int* runCnt,
+                                                         uint32_t* planRoot, double* planW,
+                                                         unsigned long long* cursor, long long capContrib) {
+  __shared__ int warpSum[kPlanWarps];
   __shared__ long long blockBase;
-  // each thread's hits, column-major (hits[h * kBlock + thread]: conflict-free)
-  __shared__ uint32_t hits[kMaxHits * kBlock];
-  uint32_t* hit = hits + threadIdx.x;
+  __shared__ uint32_t sKey[kPlanWarps][kLCap], sAux[kPlanWarps][kLCap];
+  __shared__ uint32_t sStage[kPlanWarps][kStageCap];
   const long long nRuns = cnt->nRuns;
   const int npLocal = cnt->npLocal;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t* key = sKey[warp];
+  uint32_t* aux = sAux[warp];
+  uint32_t* stage = sStage[warp];
   for (long long r0 = (long long)blockIdx.x * kBlock; r0 < nRuns; r0 += (long long)gridDim.x * kBlock) {
     const long long r = r0 + threadIdx.x;
     const bool has = r < nRuns;
+    const uint32_t rkey = has ? runKey[r] : 0u;
     int comp = 0, i = 1, j = 1, k = 1;
-    if (has) node_coords(g, runKey[r], comp, i, j, k);
-    const int alo = i - (comp == 0 ? 2 : 1), ahi = i + 1;
-    const int blo = j - (comp == 1 ? 2 : 1), bhi = j + 1;
-    const int clo = k - (comp == 2 ? 2 : 1), chi = k + 1;
-    int nh = 0;
-    if (has)
-      for (int cz = clo; cz <= chi; ++cz)
-        for (int cy = blo; cy <= bhi; ++cy) {
-          const int c0 = cell_id(g, alo, cy, cz);
-          const int q0 = cellStart[c0 - 1], q1 = cellStart[c0 + (ahi - alo)];
-          for (int q = q0; q < q1; ++q) {
-            // windows in cell order: no dependent gather per candidate
-            int sx, sy, sz;
-            window_start(winC[q], comp, sx, sy, sz);
-            const int dx = i - sx, dy = j - sy, dz = k - sz;
-            if ((unsigned)dx > 2u || (unsigned)dy > 2u || (unsigned)dz > 2u) continue;
-            if (nh < kMaxHits)
-              hit[nh * kBlock] = ((uint32_t)cellItems[q] << 7) | (uint32_t)(comp * 27 + dz * 9 + dy * 3 + dx);
-            ++nh;
-          }
-        }
-    // part order: insertion sort of the (few) hits in place
-    if (nh <= kMaxHits)
-      for (int a = 1; a < nh; ++a) {
-        const uint32_t v = hit[a * kBlock];
-        int at = a;
-        while (at > 0 && hit[(at - 1) * kBlock] > v) {
-          hit[at * kBlock] = hit[(at - 1) * kBlock];
-          --at;
-        }
-        hit[at * kBlock] = v;
-      }
-    // block-exclusive prefix of nh and one reservation for the block
-    int x = nh;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      int y = __shfl_up_sync(0xffffffffu, x, o);
-      if (lane >= o) x += y;
-    }
-    if (lane == 31) warpSum[warp] = x;
+    if (has) node_coords(g, rkey, comp, i, j, k);
+    // sub-groups: consecutive nodes of one row, split every kSubMax nodes
+    const uint32_t rowKey = rkey - (uint32_t)(i - 1);
+    const uint32_t prevRow = __shfl_up_sync(kFull, rowKey, 1);
+    const int prevI = __shfl_up_sync(kFull, i, 1);
+    const unsigned valid = __ballot_sync(kFull, has);  // lanes 0..nValid-1
+    const int nValid = __popc(valid);
+    bool start = lane == 0 || rowKey != prevRow || i != prevI + 1;
+    unsigned starts = __ballot_sync(kFull, start && has);
+    const unsigned upTo = lane == 31 ? kFull : (2u << lane) - 1u;
+    const int lastStart = 31 - __clz(starts & upTo);
+    start = start || (lane - lastStart) % kSubMax == 0;
+    starts = __ballot_sync(kFull, start && has);
+
+    int myCnt = 0, myOff = 0;
+    bool needDirect = false;
+    const int total = fill_subgroups(g, starts, nValid, comp, i, j, k, cellStart, cellItems, winC, key, aux, stage,
+                                     kStageCap, false, lane, myCnt, myOff, needDirect);
+    if (total > kStageCap) needDirect = true;
+    // one reservation for the block, warps in run order
+    if (lane == 0) warpSum[warp] = total;
     __syncthreads();
-    int pre = 0, tot = 0;
+    long long pre = 0, tot = 0;
 #pragma unroll
-    for (int w = 0; w < kBlock / 32; ++w) {
+    for (int w = 0; w < kPlanWarps; ++w) {
       pre += w < warp ? warpSum[w] : 0;
       tot += warpSum[w];
     }
     if (threadIdx.x == 0) blockBase = (long long)atomicAdd(cursor, (unsigned long long)tot);
     __syncthreads();
-    const long long o = blockBase + pre + x - nh;
+    const long long o = blockBase + pre;
     if (has) {
-      runStart[r] = (int)o;
-      runCnt[r] = nh;
-      if (o + nh > capContrib) {
-        set_err(cnt, E_PLANCAP, (int)r);
-      } else if (nh <= kMaxHits) {
-        for (int t = 0; t < nh; ++t) {
-          const uint32_t v = hit[t * kBlock];
-          const int p = (int)(v >> 7);
-          const int slot = (int)(v & 127u);
-          const uint32_t root = (uint32_t)(p < npLocal ? p : imgSrc[p - npLocal]);
-          planRoot[o + t] = root | ((uint32_t)comp << 30);
-          const int sc = slot / 27;
-          planW[o + t] = W[(size_t)p * kWStride + sc * 28 + (slot - sc * 27)];
-        }
-      } else {
-        int t = 0;
-        for (int cz = clo; cz <= chi; ++cz)
-          for (int cy = blo; cy <= bhi; ++cy) {
-            const int c0 = cell_id(g, alo, cy, cz);
-            const int q0 = cellStart[c0 - 1], q1 = cellStart[c0 + (ahi - alo)];
-            for (int q = q0; q < q1; ++q) {
-              const int p = cellItems[q];
-              int sx, sy, sz;
-              window_start(win[p], comp, sx, sy, sz);
-              const int dx = i - sx, dy = j - sy, dz = k - sz;
-              if ((unsigned)dx > 2u || (unsigned)dy > 2u || (unsigned)dz > 2u) continue;
-              planRoot[o + t++] = ((uint32_t)p << 7) | (uint32_t)(comp * 27 + dz * 9 + dy * 3 + dx);
-            }
-          }
-        for (int a = 1; a < nh; ++a) {
-          const uint32_t v = planRoot[o + a];
-          int at = a;
-          while (at > 0 && planRoot[o + at - 1] > v) {
-            planRoot[o + at] = planRoot[o + at - 1];
-            --at;
-          }
-          planRoot[o + at] = v;
-        }
-        for (int a = 0; a < nh; ++a) {
-          const uint32_t v = planRoot[o + a];
-          const int p = (int)(v >> 7);
-          const int slot = (int)(v & 127u);
-          const uint32_t root = (uint32_t)(p < npLocal ? p : imgSrc[p - npLocal]);
-          planRoot[o + a] = root | ((uint32_t)comp << 30);
-          const int sc = slot / 27;
-          planW[o + a] = W[(size_t)p * kWStride + sc * 28 + (slot - sc * 27)];
-        }
+      runStart[r] = (int)(o + myOff);
+      runCnt[r] = myCnt;
+    }
+    if (o + total > capContrib) {
+      if (lane == 0 && total > 0) set_err(cnt, E_PLANCAP, (int)(r0 + 32 * warp));
+    } else {
+      if (needDirect) {
+        // again, with the entries written straight into the warp's range
+        int c2 = 0, o2 = 0;
+        bool nd = false;
+        fill_subgroups(g, starts, nValid, comp, i, j, k, cellStart, cellItems, winC, key, aux, planRoot + o,
+                       total, true, lane, c2, o2, nd);
+        __syncwarp();
+      }
+      for (int t = lane; t < total; t += 32) {
+        const uint32_t v = needDirect ? planRoot[o + t] : stage[t];
+        const int p = (int)(v >> 7);
+        const int slot = (int)(v & 127u);
+        const int sc = slot / 27;
+        const uint32_t root = (uint32_t)(p < npLocal ? p : imgSrc[p - npLocal]);
+        planRoot[o + t] = root | ((uint32_t)sc << 30);
+        planW[o + t] = W[(size_t)p * kWStride + sc * 28 + (slot - sc * 27)];
       }
     }
     __syncthreads();
@@ -631,11 +793,12 @@ static void flag_touched_nodes(Ctx& c) {
   cudaStream_t s = c.stream;
   const long long nvec = (3 * c.g.nint + 15) / 16;
   cudaMemsetAsync(c.touch, 0, nvec * 16, s);
-  k_touch<<<nblocks(c.cap), kBlock, 0, s>>>(c.g, c.dCnt, c.win, c.touch);
+  k_win_by_cell<<<nblocks(c.cap), kBlock, 0, s>>>(c.dCnt, c.cellItems, c.win, c.winC);
+  k_touch<<<nblocks(c.cap), kBlock, 0, s>>>(c.g, c.dCnt, c.winC, c.touch);
   const long long nb = nblocks(nvec);
   k_flag_count<<<(unsigned)nb, kBlock, 0, s>>>(reinterpret_cast<const uint4*>(c.touch), nvec, c.iTmpA);
   scan_exclusive(c.iTmpA, c.iTmpA, nb, nullptr, c.dTotal, c.scanScratch, s, &c.launches);
-  c.launches += 2;
+  c.launches += 3;
 }
 
 long long count_touched_nodes(Ctx& c) {
@@ -657,12 +820,11 @@ void build_spread_plan(Ctx& c) {
   k_set_runs<<<1, 1, 0, s>>>(c.dCnt, c.dTotal, c.capRuns);
   k_flag_emit<<<(unsigned)nb, kBlock, 0, s>>>(fv4, nvec, nflags, c.iTmpA, c.runKey, c.capRuns);
   cudaMemsetAsync(c.planAlloc, 0, sizeof(unsigned long long), s);
-  k_win_by_cell<<<nblocks(c.cap), kBlock, 0, s>>>(c.dCnt, c.cellItems, c.win, c.winC);
-  k_plan_fill<<<gs_blocks(c.capRuns), kBlock, 0, s>>>(c.g, c.dCnt, c.runKey, c.cellStart, c.cellItems, c.win, c.winC,
-                                                      c.W, c.imgSrc, c.runStart, c.runCnt, c.planRoot, c.planW,
+  k_plan_fill<<<gs_blocks(c.capRuns), kBlock, 0, s>>>(c.g, c.dCnt, c.runKey, c.cellStart, c.cellItems, c.winC, c.W,
+                                                      c.imgSrc, c.runStart, c.runCnt, c.planRoot, c.planW,
                                                       c.planAlloc, c.capContrib);
   k_plan_total<<<1, 1, 0, s>>>(c.dCnt, c.planAlloc);
-  c.launches += 5;
+  c.launches += 4;
   c.planReady = true;
   c.spreadValid = false;
 }
