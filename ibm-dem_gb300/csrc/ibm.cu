@@ -258,9 +258,10 @@ __device__ inline int gather_row(const Geom& g, int comp, int iFirst, int iLast,
   int q0 = 0, len = 0;
   if (lane < nr) {
     const int cy = ylo + lane % ny, cz = zlo + lane / ny;
-    const int c0 = cell_id(g, xlo, cy, cz);
-    q0 = cellStart[c0 - 1];
-    len = cellStart[c0 + (xhi - xlo)] - q0;
+    // cell_id(g, xlo, cy, cz) - 1 in 32 bits (the cell count fits an int)
+    const int c0 = ((cz + 1) * g.nj + (cy + 1)) * g.ni + (xlo + 1);
+    q0 = cellStart[c0];
+    len = cellStart[c0 + 1 + (xhi - xlo)] - q0;
   }
   int inc = len;  // inclusive prefix over lanes 0..15 (rows past nr are empty)
 #pragma unroll
@@ -390,10 +391,15 @@ __device__ inline int fill_subgroups(const Geom& g, unsigned starts, int nValid,
       ea[u] = e < m ? aux[e] : 0u;
       rk[u] = 0;
     }
-    for (int f = 0; f < m; ++f) {
-      const uint32_t kf = key[f];
-      rk[0] += kf < ek[0];
-      rk[1] += kf < ek[1];
+    if (m <= 32) {
+#pragma unroll 4
+      for (int f = 0; f < m; ++f) rk[0] += __shfl_sync(kFull, ek[0], f) < ek[0];
+    } else {
+      for (int f = 0; f < m; ++f) {
+        const uint32_t kf = key[f];
+        rk[0] += kf < ek[0];
+        rk[1] += kf < ek[1];
+      }
     }
     __syncwarp();
 #pragma unroll
