@@ -138,8 +138,10 @@ int check_params(const ibmdem_params* p) {
   if (p->nx < 4 || p->ny < 4 || p->nz < 4 || p->coupleInterval < 1 || p->Ns < 0 || !(p->dx > 0) || !(p->dy > 0) ||
       !(p->dz > 0) || !(p->dt > 0))
     return IBMDEM_EINVAL;
-  for (int f = 0; f < 6; ++f)
-    if (p->bType[f] != 0) return IBMDEM_EUNSUPPORTED;  // periodic faces only
+  // per axis: both faces periodic (0) or both solid walls (1)
+  for (int d = 0; d < 3; ++d)
+    if (p->bType[2 * d] != p->bType[2 * d + 1] || (p->bType[2 * d] != 0 && p->bType[2 * d] != 1))
+      return IBMDEM_EUNSUPPORTED;
   long long ncell = (long long)(p->nx + 4) * (p->ny + 4) * (p->nz + 4);
   long long nint = (long long)p->nx * p->ny * p->nz;
   if (ncell >= (1ll << 31) || 3 * nint >= (1ll << 32)) return IBMDEM_EUNSUPPORTED;
@@ -166,6 +168,11 @@ void init_geom(Geom& g, const ibmdem_params* p) {
   }
   g.hprod = p->dx * p->dy * p->dz;
   g.unit_h = (p->dx == 1.0 && p->dy == 1.0 && p->dz == 1.0) ? 1 : 0;
+  g.anyWall = 0;
+  for (int d = 0; d < 3; ++d) {
+    g.wall[d] = p->bType[2 * d] == 1 ? 1 : 0;
+    g.anyWall |= g.wall[d];
+  }
   g.dt = p->dt;
   g.dtDEM = p->dt / p->coupleInterval;
   g.rhof = p->rhof;
@@ -300,7 +307,7 @@ int check_device(ibmdem_ctx* h) {
   // clear so that the context stays usable after the report
   CU(cudaMemsetAsync(&c.dCnt->err, 0, sizeof(int), c.stream));
   if (e & E_RANGE) return set_error(h, IBMDEM_ERANGE, "parcel %d left the grid and its halo", info);
-  if (e & E_IMGCAP) return set_error(h, IBMDEM_ECAPACITY, "periodic images exceed capacity %d (%d)", c.capImg, info);
+  if (e & E_IMGCAP) return set_error(h, IBMDEM_ECAPACITY, "images exceed capacity %d (%d)", c.capImg, info);
   if (e & E_PAIRCAP)
     return set_error(h, IBMDEM_ECAPACITY, "contact pairs exceed capacity %lld (%d)", c.capPairs, info);
   if (e & E_PARTNER) return set_error(h, IBMDEM_ECAPACITY, "body %d has more than %d near bodies", info, c.maxPartners);
@@ -465,7 +472,7 @@ int ibmdem_destroy(ibmdem_ctx* h) {
   cudaStreamSynchronize(c.stream);
   free_parcel_buffers(c);
   void* ps[] = {c.u, c.v, c.w, c.u0, c.v0, c.w0, c.fx, c.fy, c.fz, c.cellStart, c.dCnt, c.dTotal, c.dBodies,
-                c.bodyStart, c.bodyR2, c.partnerCnt, c.partners};
+                c.bodyStart, c.bodyR2, c.partnerCnt, c.partners, c.dProbes};
   for (void* p : ps) dfree(c, p);
   // the frees are ordered on the context's stream; let them complete before
   // the stream may be destroyed by its owner
@@ -634,6 +641,12 @@ int ibmdem_get_parcels(ibmdem_ctx* h, ibmdem_parcel* parts, int32_t cap, int32_t
   CU(cudaStreamSynchronize(c.stream));
   CU(cudaMemcpyAsync(hi.data(), c.recI[c.cur], sizeof(int) * hi.size(), cudaMemcpyDeviceToHost, c.stream));
   CU(cudaStreamSynchronize(c.stream));
+  // images made across a solid wall carry pType 1 (ZJS_MPI_DEM.F90:200)
+  std::vector<int> shift(std::max(n - nl, 0));
+  if (!shift.empty()) {
+    CU(cudaMemcpyAsync(shift.data(), c.imgShift, sizeof(int) * shift.size(), cudaMemcpyDeviceToHost, c.stream));
+    CU(cudaStreamSynchronize(c.stream));
+  }
   for (int i = 0; i < n; ++i) {
     ibmdem_parcel& p = parts[i];
     std::memset(&p, 0, sizeof p);
@@ -656,7 +669,7 @@ int ibmdem_get_parcels(ibmdem_ctx* h, ibmdem_parcel* parts, int32_t cap, int32_t
     p.MSIdx = hi[(size_t)I_MSIDX * c.cap + i];
     p.cellIdx = hi[(size_t)I_CELL * c.cap + i];
     p.localIdx = i + 1;
-    p.pType = -1;
+    p.pType = (i >= nl && ((shift[i - nl] >> kWallImgBit) & 1)) ? 1 : -1;
   }
   return IBMDEM_OK;
 }
@@ -829,6 +842,45 @@ int ibmdem_CalculateCollisionForce(ibmdem_ctx* h) {
   return launch_status(h);
 }
 
+int ibmdem_CalculateSolidBoundaryCollisionForce(ibmdem_ctx* h) {
+  CHECK_CTX();
+  Ctx& c = h->c;
+  REQUIRE(c.listsBuilt, "lists are not built");
+  launch_wall_force(c);
+  return launch_status(h);
+}
+
+int ibmdem_set_wall_probes(ibmdem_ctx* h, int32_t n, const ibmdem_wall_probe* probes) {
+  CHECK_CTX();
+  Ctx& c = h->c;
+  if (n < 0 || n > IBMDEM_MAX_WALL_PROBES || (n > 0 && !probes))
+    return set_error(h, IBMDEM_EINVAL, "%d wall probes (at most %d)", n, IBMDEM_MAX_WALL_PROBES);
+  std::vector<ibmdem_wall_probe> hp(probes, probes + n);
+  for (int q = 0; q < n; ++q) {
+    if (hp[q].face < 1 || hp[q].face > 6 || !c.g.wall[(hp[q].face - 1) / 2])
+      return set_error(h, IBMDEM_EINVAL, "wall probe %d: face %d is not a solid wall", q, hp[q].face);
+    hp[q].force[0] = hp[q].force[1] = hp[q].force[2] = 0.0;
+  }
+  if (!c.dProbes && dalloc(c, c.dProbes, IBMDEM_MAX_WALL_PROBES) != cudaSuccess)
+    return set_error(h, IBMDEM_ENOMEM, "wall probes");
+  if (n) CU(cudaMemcpyAsync(c.dProbes, hp.data(), sizeof(ibmdem_wall_probe) * n, cudaMemcpyHostToDevice, c.stream));
+  CU(cudaStreamSynchronize(c.stream));
+  c.nProbe = n;
+  return launch_status(h);
+}
+
+int ibmdem_get_wall_probes(ibmdem_ctx* h, ibmdem_wall_probe* probes, int32_t cap, int32_t* n_out) {
+  CHECK_CTX();
+  Ctx& c = h->c;
+  if (n_out) *n_out = c.nProbe;
+  const int n = std::min<int>(c.nProbe, std::max(cap, 0));
+  if (probes && n > 0) {
+    CU(cudaMemcpyAsync(probes, c.dProbes, sizeof(ibmdem_wall_probe) * n, cudaMemcpyDeviceToHost, c.stream));
+    CU(cudaStreamSynchronize(c.stream));
+  }
+  return check_device(h);
+}
+
 int ibmdem_UpdateFluidVelocityOnLagrangianPoints(ibmdem_ctx* h) {
   CHECK_CTX();
   Ctx& c = h->c;
@@ -981,7 +1033,11 @@ int ibmdem_CloudEvolutionStepMS(ibmdem_ctx* h) {
   CHECK_CTX();
   Ctx& c = h->c;
   REQUIRE(c.listsBuilt && c.weightsLocal && c.weightsGhost, "lists and weights are not built");
-  { PhaseScope t(c, P_FORCE); launch_collision_force(c); }
+  {
+    PhaseScope t(c, P_FORCE);
+    launch_collision_force(c);
+    launch_wall_force(c);
+  }
   { PhaseScope t(c, P_BODYSUM); launch_body_sums(c); }
   { PhaseScope t(c, P_BODYMOVE); launch_evolution(c); }
   { PhaseScope t(c, P_MARKERS); launch_marker_update(c, true, true); }

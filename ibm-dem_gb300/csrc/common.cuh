@@ -80,11 +80,17 @@ struct Geom {
   double err[3];    // di*1e-20 (AdjustParcelPosition)
   double hprod;     // dx*dy*dz
   int unit_h;       // dx == dy == dz == 1: /h, *dx*dy*dz are exact identities
+  int wall[3];      // 1: the axis is bounded by two solid walls (bType 1), 0: periodic
+  int anyWall;
   double dt, dtDEM, rhof, eta, cut2, knCoeff, di;
   double g[3];
   FastDiv fdNint, fdN0, fdN1;  // interior nodes per component, nx, ny
   FastDiv fdNi, fdNj;          // nx + 4, ny + 4 (cells with the halo)
 };
+
+// image shift codes (imgShift): 2 bits per axis, and this bit for an image
+// made across a solid wall (pType 1: never a contact partner)
+constexpr int kWallImgBit = 6;
 
 struct Counters {
   int npLocal, np, nImg, nActive, nPairs, nRuns, nContrib, nLast;

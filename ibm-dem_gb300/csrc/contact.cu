@@ -93,10 +93,18 @@ __global__ void k_compact_active(const Counters* cnt, const int* flag, const int
 // the 32 lanes take 32 consecutive stencil cells (kk, jj, ii order), count
 // their hits, and a warp prefix places them, so the list keeps the reference's
 // order (stencil cell, then the cell's part order).  FILL = false counts.
+// A partner must have pType -1 (ZJS_UPDATE_LIST_DEM.F90:272): images made
+// across a solid wall (pType 1) never are.
+__device__ inline bool partner_type_ok(const Geom& g, const Counters* cnt, const int* imgShift, int j) {
+  if (!g.anyWall) return true;
+  const int q = j - cnt->npLocal;
+  return q < 0 || !((imgShift[q] >> kWallImgBit) & 1);
+}
+
 template <bool FILL>
 __global__ void k_pair_scan(Recs R, Geom g, const Counters* cnt, const int* activeList, const int* nActive,
-                            const int* cellStart, const int* cellItems, int* pairCnt, const int* pairStart,
-                            int* pairIdx, long long capPairs, Counters* cntw) {
+                            const int* cellStart, const int* cellItems, const int* imgShift, int* pairCnt,
+                            const int* pairStart, int* pairIdx, long long capPairs, Counters* cntw) {
   const int lane = threadIdx.x & 31;
   const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
   const int na = *nActive;
@@ -127,7 +135,7 @@ __global__ void k_pair_scan(Recs R, Geom g, const Counters* cnt, const int* acti
         const double xij2 = xi1 - R.D(D_X + 1, jjx);
         const double xij3 = xi2 - R.D(D_X + 2, jjx);
         const double distSqr = xij1 * xij1 + xij2 * xij2 + xij3 * xij3;
-        if (distSqr < g.cut2 && jjx != ii) ++mine;
+        if (distSqr < g.cut2 && jjx != ii && partner_type_ok(g, cnt, imgShift, jjx)) ++mine;
       }
       int x = mine;
 #pragma unroll
@@ -144,7 +152,7 @@ __global__ void k_pair_scan(Recs R, Geom g, const Counters* cnt, const int* acti
           const double xij2 = xi1 - R.D(D_X + 1, jjx);
           const double xij3 = xi2 - R.D(D_X + 2, jjx);
           const double distSqr = xij1 * xij1 + xij2 * xij2 + xij3 * xij3;
-          if (distSqr < g.cut2 && jjx != ii) {
+          if (distSqr < g.cut2 && jjx != ii && partner_type_ok(g, cnt, imgShift, jjx)) {
             if (at < capPairs) pairIdx[at] = jjx;
             else set_err(cntw, E_PAIRCAP, (int)at);
             ++at;
@@ -208,7 +216,127 @@ __global__ void k_collision_force(Recs R, Geom g, const Counters* cnt, const int
   R.D(D_FCOL + 2, ii) = fc3;
 }
 
+// ---- CalculateSolidBoundaryCollisionForce (ZJS_COLLISION_DEM.F90:76-148) ----
+// plane of face f (0..5 = -x,+x,-y,+y,-z,+z): pointBound and normBound
+// (ZJS_INIT_DEM.F90:120-137)
+struct WallHit {
+  double dist, cp1, cp2, cp3, kn, deltan;
+  double n1, n2, n3;
+};
+__device__ inline WallHit wall_contact(const Geom& g, int f, double x1, double x2, double x3, double m,
+                                       double radeff) {
+  WallHit w;
+  const int d = f >> 1;
+  const bool hi = f & 1;
+  const double p1 = hi ? g.end[0] : g.start[0], p2 = hi ? g.end[1] : g.start[1], p3 = hi ? g.end[2] : g.start[2];
+  const double s = hi ? -1.0 : 1.0;
+  w.n1 = d == 0 ? s : 0.0;
+  w.n2 = d == 1 ? s : 0.0;
+  w.n3 = d == 2 ? s : 0.0;
+  const double r1 = x1 - p1, r2 = x2 - p2, r3 = x3 - p3;
+  w.dist = r1 * w.n1 + r2 * w.n2 + r3 * w.n3;
+  w.cp1 = x1 - w.dist * w.n1;
+  w.cp2 = x2 - w.dist * w.n2;
+  w.cp3 = x3 - w.dist * w.n3;
+  w.deltan = radeff - w.dist;
+  w.kn = g.knCoeff / (0.1 * g.di) * m;
+  return w;
+}
+
+// Local parcels in the first or last interior cell layer feel every solid
+// wall, faces in order, after their pair forces; flag marks the parcels with a
+// wall contact (for the probe sums).
+__global__ void k_wall_force(Recs R, Geom g, const Counters* cnt, int* flag) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= cnt->npLocal) return;
+  int a, b, cc;
+  cell_coords(g, R.I(I_CELL, m), a, b, cc);
+  int hit = 0;
+  if (a == 1 || a == g.n[0] || b == 1 || b == g.n[1] || cc == 1 || cc == g.n[2]) {
+    const double x1 = R.D(D_X, m), x2 = R.D(D_X + 1, m), x3 = R.D(D_X + 2, m);
+    const double v1 = R.D(D_V, m), v2 = R.D(D_V + 1, m), v3 = R.D(D_V + 2, m);
+    const double meff = R.D(D_M, m), rij = R.D(D_RADEFF, m);
+    double fc1 = R.D(D_FCOL, m), fc2 = R.D(D_FCOL + 1, m), fc3 = R.D(D_FCOL + 2, m);
+    for (int f = 0; f < 6; ++f) {
+      if (!g.wall[f >> 1]) continue;
+      const WallHit w = wall_contact(g, f, x1, x2, x3, meff, rij);
+      const double etan = g.eta * sqrt(meff * w.kn);
+      const double vnij = w.n1 * v1 + w.n2 * v2 + w.n3 * v3;
+      if (w.deltan > 0) {
+        fc1 = fc1 + w.n1 * (w.kn * w.deltan - etan * vnij);
+        fc2 = fc2 + w.n2 * (w.kn * w.deltan - etan * vnij);
+        fc3 = fc3 + w.n3 * (w.kn * w.deltan - etan * vnij);
+        hit = 1;
+      }
+    }
+    R.D(D_FCOL, m) = fc1;
+    R.D(D_FCOL + 1, m) = fc2;
+    R.D(D_FCOL + 2, m) = fc3;
+  }
+  if (flag) flag[m] = hit;
+}
+
+__global__ void k_wall_list(const Counters* cnt, const int* flag, const int* pos, int* list) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m < cnt->npLocal && flag[m]) list[pos[m]] = m;
+}
+
+// WallProbeCollision (ZJS_COLLISION_DEM.F90:150-179); a NaN angle sum counts as
+// inside, as the reference's comparison is false for it
+__device__ inline bool probe_contains(const ibmdem_wall_probe& pr, double cp1, double cp2, double cp3) {
+  double theta = 0.0;
+  for (int q = 0; q < 4; ++q) {
+    const int qj = q + 1 > 3 ? q + 1 - 4 : q + 1;
+    const double ni1 = pr.points[q][0] - cp1, ni2 = pr.points[q][1] - cp2, ni3 = pr.points[q][2] - cp3;
+    const double nj1 = pr.points[qj][0] - cp1, nj2 = pr.points[qj][1] - cp2, nj3 = pr.points[qj][2] - cp3;
+    double t = (ni1 * nj1 + ni2 * nj2 + ni3 * nj3) /
+               (sqrt(ni1 * ni1 + ni2 * ni2 + ni3 * ni3) * sqrt(nj1 * nj1 + nj2 * nj2 + nj3 * nj3));
+    theta = theta + acos(t);
+  }
+  const double pi = acos(-1.0);
+  return !(fabs(theta - 2 * pi) > 0.001 * pi);
+}
+
+// one thread per probe: the normal spring forces of the listed parcels whose
+// contact point on the probe's face lies inside it, in part order
+__global__ void k_probe_sum(Recs R, Geom g, const int* list, const int* nList, ibmdem_wall_probe* probes, int nProbe) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nProbe) return;
+  ibmdem_wall_probe pr = probes[q];
+  const int f = pr.face - 1;
+  double s1 = 0.0, s2 = 0.0, s3 = 0.0;
+  const int n = *nList;
+  for (int t = 0; t < n; ++t) {
+    const int m = list[t];
+    const WallHit w = wall_contact(g, f, R.D(D_X, m), R.D(D_X + 1, m), R.D(D_X + 2, m), R.D(D_M, m),
+                                   R.D(D_RADEFF, m));
+    if (!(w.deltan > 0)) continue;
+    if (!probe_contains(pr, w.cp1, w.cp2, w.cp3)) continue;
+    s1 = s1 + w.n1 * w.kn * w.deltan;
+    s2 = s2 + w.n2 * w.kn * w.deltan;
+    s3 = s3 + w.n3 * w.kn * w.deltan;
+  }
+  probes[q].force[0] = s1;
+  probes[q].force[1] = s2;
+  probes[q].force[2] = s3;
+}
+
 }  // namespace
+
+void launch_wall_force(Ctx& c) {
+  if (!c.g.anyWall) return;
+  cudaStream_t s = c.stream;
+  const int nbl = nblocks(c.capLocal);
+  const bool probes = c.nProbe > 0;
+  k_wall_force<<<nbl, kBlock, 0, s>>>(c.rec(), c.g, c.dCnt, probes ? c.iTmpA : nullptr);
+  c.launches++;
+  if (!probes) return;
+  // the contact lists are built, so their scratch (iTmpA/B, activeList) is free here
+  scan_exclusive(c.iTmpA, c.iTmpB, c.capLocal, &c.dCnt->npLocal, c.dTotal + 3, c.scanScratch, s, &c.launches);
+  k_wall_list<<<nbl, kBlock, 0, s>>>(c.dCnt, c.iTmpA, c.iTmpB, c.activeList);
+  k_probe_sum<<<1, 64, 0, s>>>(c.rec(), c.g, c.activeList, c.dTotal + 3, c.dProbes, c.nProbe);
+  c.launches += 2;
+}
 
 void rebuild_collision_lists(Ctx& c) {
   cudaStream_t s = c.stream;
@@ -234,11 +362,13 @@ void rebuild_collision_lists(Ctx& c) {
   cudaMemsetAsync(c.pairCnt, 0, sizeof(int) * (c.capLocal + 1), s);
   const int nbw = gs_blocks(32ll * c.capLocal);
   k_pair_scan<false><<<nbw, kBlock, 0, s>>>(c.rec(), c.g, c.dCnt, c.activeList, &c.dCnt->nActive, c.cellStart,
-                                            c.cellItems, c.pairCnt, nullptr, nullptr, c.capPairs, c.dCnt);
+                                            c.cellItems, c.imgShift, c.pairCnt, nullptr, nullptr, c.capPairs,
+                                            c.dCnt);
   scan_exclusive(c.pairCnt, c.pairStart, c.capLocal + 1, nullptr, c.dTotal, c.scanScratch, s, &c.launches);
   k_set_pair_total<<<1, 1, 0, s>>>(c.dCnt, c.dTotal, c.capPairs);
   k_pair_scan<true><<<nbw, kBlock, 0, s>>>(c.rec(), c.g, c.dCnt, c.activeList, &c.dCnt->nActive, c.cellStart,
-                                           c.cellItems, c.pairCnt, c.pairStart, c.pairIdx, c.capPairs, c.dCnt);
+                                           c.cellItems, c.imgShift, c.pairCnt, c.pairStart, c.pairIdx, c.capPairs,
+                                           c.dCnt);
   c.launches += 4;
 }
 

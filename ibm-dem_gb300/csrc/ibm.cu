@@ -536,19 +536,56 @@ __global__ void k_plan_total(Counters* cnt, const unsigned long long* cursor) {
   cnt->nContrib = (int)*cursor;
 }
 
-// write a value at an interior node and at all its periodic halo mirrors
-__device__ inline void put_mirrored(double* F, const Geom& g, int i, int j, int k, double val) {
-  int ox[2] = {0, 0}, oy[2] = {0, 0}, oz[2] = {0, 0};
-  int nxo = 1, nyo = 1, nzo = 1;
-  if (i <= kHalo) ox[nxo++] = g.n[0];
-  else if (i > g.n[0] - kHalo) ox[nxo++] = -g.n[0];
-  if (j <= kHalo) oy[nyo++] = g.n[1];
-  else if (j > g.n[1] - kHalo) oy[nyo++] = -g.n[1];
-  if (k <= kHalo) oz[nzo++] = g.n[2];
-  else if (k > g.n[2] - kHalo) oz[nzo++] = -g.n[2];
-  for (int c = 0; c < nzo; ++c)
-    for (int b = 0; b < nyo; ++b)
-      for (int a = 0; a < nxo; ++a) F[field_off(g, i + ox[a], j + oy[b], k + oz[c])] = val;
+// Write the new value of interior node (i,j,k) of component comp where the
+// fluid solver's halo refill puts it (FillGhostRegionForFluid,
+// boundary.F90:122-147): per axis the node itself and, within the 2-cell halo
+// of a face, its copy beyond the opposite face (periodic) or its mirror beyond
+// that face with the sign flipped (solid wall, DealWithBoundaryFluid,
+// boundary.F90:211-245).  Boundary() (fluid.F90:240-249) then zeroes the
+// wall-normal component on the wall face and beyond it.
+template <bool WALLS>
+__device__ inline void put_mirrored(double* F, const Geom& g, int comp, int i, int j, int k, double val) {
+  if (!WALLS) {
+    int ox[2] = {0, 0}, oy[2] = {0, 0}, oz[2] = {0, 0};
+    int nxo = 1, nyo = 1, nzo = 1;
+    if (i <= kHalo) ox[nxo++] = g.n[0];
+    else if (i > g.n[0] - kHalo) ox[nxo++] = -g.n[0];
+    if (j <= kHalo) oy[nyo++] = g.n[1];
+    else if (j > g.n[1] - kHalo) oy[nyo++] = -g.n[1];
+    if (k <= kHalo) oz[nzo++] = g.n[2];
+    else if (k > g.n[2] - kHalo) oz[nzo++] = -g.n[2];
+    for (int c = 0; c < nzo; ++c)
+      for (int b = 0; b < nyo; ++b)
+        for (int a = 0; a < nxo; ++a) F[field_off(g, i + ox[a], j + oy[b], k + oz[c])] = val;
+    return;
+  }
+  int pos[3][2], neg[3][2], cnt[3];
+  const int id[3] = {i, j, k};
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    pos[d][0] = id[d];
+    neg[d][0] = 0;
+    cnt[d] = 1;
+    const int n = g.n[d];
+    if (id[d] <= kHalo) {
+      pos[d][1] = g.wall[d] ? 1 - id[d] : id[d] + n;
+      neg[d][1] = g.wall[d];
+      cnt[d] = 2;
+    } else if (id[d] > n - kHalo) {
+      pos[d][1] = g.wall[d] ? 2 * n + 1 - id[d] : id[d] - n;
+      neg[d][1] = g.wall[d];
+      cnt[d] = 2;
+    }
+  }
+  const int nc = g.n[comp];
+  for (int c = 0; c < cnt[2]; ++c)
+    for (int b = 0; b < cnt[1]; ++b)
+      for (int a = 0; a < cnt[0]; ++a) {
+        const int p[3] = {pos[0][a], pos[1][b], pos[2][c]};
+        double v = (neg[0][a] ^ neg[1][b] ^ neg[2][c]) ? -val : val;
+        if (g.wall[comp] && (p[comp] <= 1 || p[comp] >= nc + 1)) v = 0.0;
+        F[field_off(g, p[0], p[1], p[2])] = v;
+      }
 }
 
 __device__ inline void node_of(const Geom& g, uint32_t key, int& comp, int& i, int& j, int& k) {
@@ -570,6 +607,7 @@ struct Fields {
 // start of FirstOrderForwardEuler's particle side (fluid.F90:255-263): fdrag=0,
 // fx=fy=fz=0; with `frozen`, also restore the fluid where the last spread
 // changed it.
+template <bool WALLS>
 __global__ void k_mdf_reset(Recs R, Geom g, Counters* cnt, Fields fl, const uint32_t* lastNodes, double* fCur,
                             int frozen) {
   const long long nLast = cnt->nLast, nRuns = cnt->nRuns, nl = cnt->npLocal;
@@ -580,7 +618,7 @@ __global__ void k_mdf_reset(Recs R, Geom g, Counters* cnt, Fields fl, const uint
       node_of(g, lastNodes[t], comp, i, j, k);
       long long off = field_off(g, i, j, k);
       fl.F(comp)[off] = 0.0;
-      if (frozen) put_mirrored(fl.U(comp), g, i, j, k, fl.U0(comp)[off]);
+      if (frozen) put_mirrored<WALLS>(fl.U(comp), g, comp, i, j, k, fl.U0(comp)[off]);
     }
     if (t < nRuns) fCur[t] = 0.0;
     if (t < nl) {
@@ -654,7 +692,7 @@ constexpr int kLenBins = 64;
 // part order -- the reference's fx = fx - fdrag*vol*weight, term by term --
 // then applies the post-guess update with the periodic mirrors (MODE 0) or
 // keeps fx and fxOld for a separate VelocityPostGuess (MODE 1).
-template <int MODE>
+template <int MODE, bool WALLS>
 __global__ void __launch_bounds__(kBlock) k_spread(Geom g, const Counters* cnt, const int* __restrict__ runStart,
                                                    const int* __restrict__ runCnt,
                                                    const uint32_t* __restrict__ runKey,
@@ -748,7 +786,7 @@ __global__ void __launch_bounds__(kBlock) k_spread(Geom g, const Counters* cnt, 
       const double f = fres[threadIdx.x];
       fl.F(comp)[off] = f;
       if (MODE == 0) {
-        put_mirrored(fl.U(comp), g, i, j, k, uOld + g.dt * (f - fo));
+        put_mirrored<WALLS>(fl.U(comp), g, comp, i, j, k, uOld + g.dt * (f - fo));
         fCur[myR] = f;
       } else {
         fPrev[myR] = fo;
@@ -762,6 +800,7 @@ constexpr size_t kSpreadSmem = sizeof(double) * kSpreadBuf;
 
 
 // VelocityPostGuess (fluid.F90:135-153) + halo refill, per touched node
+template <bool WALLS>
 __global__ void k_post_guess(Geom g, const Counters* cnt, const uint32_t* runKey, Fields fl, const double* fCur,
                              const double* fPrev) {
   const long long nRuns = cnt->nRuns;
@@ -770,7 +809,7 @@ __global__ void k_post_guess(Geom g, const Counters* cnt, const uint32_t* runKey
     node_of(g, runKey[r], comp, i, j, k);
     double* U = fl.U(comp);
     long long off = field_off(g, i, j, k);
-    put_mirrored(U, g, i, j, k, U[off] + g.dt * (fCur[r] - fPrev[r]));
+    put_mirrored<WALLS>(U, g, comp, i, j, k, U[off] + g.dt * (fCur[r] - fPrev[r]));
   }
 }
 
@@ -837,8 +876,8 @@ void build_spread_plan(Ctx& c) {
 
 void launch_mdf_reset(Ctx& c, bool frozen) {
   long long n = std::max<long long>(c.capRuns, c.capLocal);
-  k_mdf_reset<<<gs_blocks(n), kBlock, 0, c.stream>>>(c.rec(), c.g, c.dCnt, fields_of(c), c.lastNodes, c.fCur,
-                                                   frozen ? 1 : 0);
+  auto k = c.g.anyWall ? k_mdf_reset<true> : k_mdf_reset<false>;
+  k<<<gs_blocks(n), kBlock, 0, c.stream>>>(c.rec(), c.g, c.dCnt, fields_of(c), c.lastNodes, c.fCur, frozen ? 1 : 0);
   c.launches++;
   c.spreadValid = true;
 }
@@ -852,22 +891,22 @@ void launch_interp(Ctx& c) {
   c.launches++;
 }
 
+// the spread with the post-guess fused (MODE 0) or keeping fx and fxOld for a
+// separate VelocityPostGuess (MODE 1); the halo writes know about walls only
+// when the case has some
 void launch_spread(Ctx& c, bool fused_post_guess) {
-  cudaFuncSetAttribute(k_spread<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSpreadSmem);
-  cudaFuncSetAttribute(k_spread<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSpreadSmem);
-  if (fused_post_guess)
-    k_spread<0><<<gs_blocks(c.capRuns), kBlock, kSpreadSmem, c.stream>>>(c.g, c.dCnt, c.runStart, c.runCnt, c.runKey,
-                                                              c.planRoot, c.planW, c.fv, c.cap, fields_of(c), c.fCur,
-                                                              c.fPrev);
-  else
-    k_spread<1><<<gs_blocks(c.capRuns), kBlock, kSpreadSmem, c.stream>>>(c.g, c.dCnt, c.runStart, c.runCnt, c.runKey,
-                                                              c.planRoot, c.planW, c.fv, c.cap, fields_of(c), c.fCur,
-                                                              c.fPrev);
+  const bool w = c.g.anyWall;
+  auto k = fused_post_guess ? (w ? k_spread<0, true> : k_spread<0, false>)
+                            : (w ? k_spread<1, true> : k_spread<1, false>);
+  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSpreadSmem);
+  k<<<gs_blocks(c.capRuns), kBlock, kSpreadSmem, c.stream>>>(c.g, c.dCnt, c.runStart, c.runCnt, c.runKey, c.planRoot,
+                                                            c.planW, c.fv, c.cap, fields_of(c), c.fCur, c.fPrev);
   c.launches++;
 }
 
 void launch_post_guess(Ctx& c) {
-  k_post_guess<<<gs_blocks(c.capRuns), kBlock, 0, c.stream>>>(c.g, c.dCnt, c.runKey, fields_of(c), c.fCur, c.fPrev);
+  auto k = c.g.anyWall ? k_post_guess<true> : k_post_guess<false>;
+  k<<<gs_blocks(c.capRuns), kBlock, 0, c.stream>>>(c.g, c.dCnt, c.runKey, fields_of(c), c.fCur, c.fPrev);
   c.launches++;
 }
 

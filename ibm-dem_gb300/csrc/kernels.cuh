@@ -60,6 +60,10 @@ struct Ctx {
   int* partners = nullptr;
   int maxPartners = 64;
 
+  // wall probes (ibmdem_set_wall_probes): device copy with the force sums
+  ibmdem_wall_probe* dProbes = nullptr;
+  int nProbe = 0;
+
   // contact lists
   int* activeList = nullptr;  // [capLocal]
   int* pairCnt = nullptr;     // [capLocal]
@@ -133,6 +137,9 @@ void launch_img_update(Ctx& c);
 // contact.cu
 void rebuild_collision_lists(Ctx& c);
 void launch_collision_force(Ctx& c);
+// CalculateSolidBoundaryCollisionForce: wall forces into fcol (after the pair
+// forces) and the probe sums; nothing without walls
+void launch_wall_force(Ctx& c);
 // ibm.cu
 void launch_weights(Ctx& c, bool locals);
 void build_spread_plan(Ctx& c);

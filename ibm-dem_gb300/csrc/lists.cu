@@ -47,9 +47,15 @@ __global__ void k_set_local_counts(Counters* cnt, const int* total) {
   cnt->nImg = 0;
 }
 
-// ---- periodic images -------------------------------------------------------
-// shift variant code per axis: 0 none, 1 = +L (near the low face), 2 = -L
-// (near the high face); class order of the face loop:
+// ---- periodic and wall images -------------------------------------------------
+// Variant code per axis: 0 none; 1 = the image the face loop makes beyond the
+// high face, 2 = beyond the low face.  On a periodic axis those are the parcels
+// near the low face shifted by +L (1) and near the high face shifted by -L (2)
+// (ZJS_UPDATE_LIST_DEM.F90:147-151).  Across solid walls there is no rank to
+// send to, and UpdateFullInfoForSolidOutletBoundary (ZJS_MPI_DEM.F90:173-210)
+// mirrors the parcels near the receiving face about it instead: near the high
+// face about the high wall (1), near the low face about the low wall (2), the
+// normal velocity negated, pType 1.  Class order of the face loop:
 //   0: (+,0,0)  1: (-,0,0)
 //   2..4:  sy=+ with sx = 0,+,-     5..7:  sy=- with sx = 0,+,-
 //   8..16: sz=+ with (sy,sx) in {0,+,-}^2 (sy major)   17..25: sz=-
@@ -67,8 +73,9 @@ __device__ inline unsigned image_mask(const Geom& g, int a, int b, int c) {
   int id[3] = {a, b, c};
   for (int d = 0; d < 3; ++d) {
     cnt[d] = 0;
-    if (id[d] >= 1 && id[d] <= kHalo) opt[d][cnt[d]++] = 1;
-    if (id[d] >= g.n[d] - kHalo + 1 && id[d] <= g.n[d]) opt[d][cnt[d]++] = 2;
+    const bool lo = id[d] >= 1 && id[d] <= kHalo, hi = id[d] >= g.n[d] - kHalo + 1 && id[d] <= g.n[d];
+    if (g.wall[d] ? hi : lo) opt[d][cnt[d]++] = 1;
+    if (g.wall[d] ? lo : hi) opt[d][cnt[d]++] = 2;
   }
   unsigned m = 0;
   for (int iz = -1; iz < cnt[2]; ++iz)
@@ -96,6 +103,13 @@ __device__ inline void class_shift(int cls, int& fx, int& fy, int& fz) {
     fz = fy = 0;
     fx = cls == 0 ? 1 : 2;
   }
+}
+
+// coordinate d of the image of class code s (1, 2) of x: a periodic shift, or
+// x(dim) = 2*coordMirror - x(dim) across a wall (ZJS_MPI_DEM.F90:198)
+__device__ inline double image_coord(const Geom& g, int d, int s, double x) {
+  if (g.wall[d]) return 2.0 * (s == 1 ? g.end[d] : g.start[d]) - x;
+  return s == 1 ? x + g.len[d] : x + (-g.len[d]);
 }
 
 __device__ inline unsigned local_mask(const Recs& R, const Geom& g, int m) {
@@ -163,17 +177,22 @@ __global__ void k_img_emit(Recs R, Geom g, Counters* cnt, const int* offs, long 
     R.I(I_GIDX, e) = R.I(I_GIDX, m);
     R.I(I_MSIDX, e) = R.I(I_MSIDX, m);
     int id[3];
+    int wallImg = 0;
     for (int d = 0; d < 3; ++d) {
       double x = R.D(D_X + d, m);
-      // x(dim) = x(dim) + coordShift (ZJS_UPDATE_LIST_DEM.F90:149)
-      if (sh[d] == 1) x = x + g.len[d];
-      if (sh[d] == 2) x = x + (-g.len[d]);
+      if (sh[d]) {
+        x = image_coord(g, d, sh[d], x);
+        if (g.wall[d]) {
+          R.D(D_V + d, e) = -R.D(D_V + d, m);
+          wallImg = 1;
+        }
+      }
       R.D(D_X + d, e) = x;
       id[d] = cell_of(g, d, x);
     }
     R.I(I_CELL, e) = cell_id(g, id[0], id[1], id[2]);
     imgSrc[pos] = m;
-    imgShift[pos] = fx | (fy << 2) | (fz << 4);
+    imgShift[pos] = fx | (fy << 2) | (fz << 4) | (wallImg << kWallImgBit);
   }
 }
 
@@ -188,7 +207,8 @@ __global__ void k_set_image_counts(Counters* cnt, const int* total, int capImg) 
   cnt->np = cnt->npLocal + n;
 }
 
-// ---- UpdateParcelInfoInGhostRegion (ZJS_UPDATE_LIST_DEM.F90:179-246) -------
+// ---- UpdateParcelInfoInGhostRegion (ZJS_UPDATE_LIST_DEM.F90:179-246; across
+// walls UpdatePartInfoForSolidOutletBoundary, ZJS_MPI_DEM.F90:222-269) -------
 __global__ void k_img_update(Recs R, Geom g, const Counters* cnt, const int* imgSrc, const int* imgShift) {
   int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= cnt->nImg) return;
@@ -200,10 +220,11 @@ __global__ void k_img_update(Recs R, Geom g, const Counters* cnt, const int* img
   for (int d = 0; d < 3; ++d) {
     int s = (code >> (2 * d)) & 3;
     double x = R.D(D_X + d, m);
-    if (s == 1) x = x + g.len[d];
-    if (s == 2) x = x + (-g.len[d]);
+    const double v = R.D(D_V + d, m);
+    if (s) x = image_coord(g, d, s, x);
     R.D(D_X + d, e) = x;
-    R.D(D_V + d, e) = R.D(D_V + d, m);
+    // across a wall the normal velocity is negated (ZJS_MPI_DEM.F90:256); fdrag is copied as is
+    R.D(D_V + d, e) = (s && g.wall[d]) ? -v : v;
     R.D(D_FDRAG + d, e) = R.D(D_FDRAG + d, m);
   }
   R.D(D_WSUM, e) = R.D(D_WSUM, m);

@@ -11,6 +11,7 @@ import os
 
 import numpy as np
 
+from . import records
 from .records import MULTISPHERE, PARAMS, PARCEL, PARTICLE, UPARAMS, field_shape, ufield_shape
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
@@ -23,6 +24,7 @@ EXPORTS = [
     "ibmdem_set_bodies", "ibmdem_get_bodies", "ibmdem_get_cell_lists", "ibmdem_get_collision_lists",
     "ibmdem_RebuildAllListOrNot", "ibmdem_UpdateLocalCellWeightListDEM", "ibmdem_UpdateGhostCellWeightListDEM",
     "ibmdem_UpdateParcelInfoInGhostRegion", "ibmdem_CalculateCollisionForce",
+    "ibmdem_CalculateSolidBoundaryCollisionForce", "ibmdem_set_wall_probes", "ibmdem_get_wall_probes",
     "ibmdem_UpdateFluidVelocityOnLagrangianPoints", "ibmdem_UpdateMomentumSourceTerm", "ibmdem_VelocityPostGuess",
     "ibmdem_AssembleLocalForceMS", "ibmdem_EvolutionMS", "ibmdem_ResetVelocityAndPositionLagrangianPoints",
     "ibmdem_AdjustParcelPosition", "ibmdem_InitializationDEM", "ibmdem_MultiDirectForcing",
@@ -44,7 +46,8 @@ EXPORTS = [
 
 SUBROUTINES = [
     "RebuildAllListOrNot", "UpdateLocalCellWeightListDEM", "UpdateGhostCellWeightListDEM",
-    "UpdateParcelInfoInGhostRegion", "CalculateCollisionForce", "UpdateFluidVelocityOnLagrangianPoints",
+    "UpdateParcelInfoInGhostRegion", "CalculateCollisionForce", "CalculateSolidBoundaryCollisionForce",
+    "UpdateFluidVelocityOnLagrangianPoints",
     "UpdateMomentumSourceTerm", "VelocityPostGuess", "AssembleLocalForceMS", "EvolutionMS",
     "ResetVelocityAndPositionLagrangianPoints", "AdjustParcelPosition", "InitializationDEM", "MultiDirectForcing",
     "CloudEvolutionStepMS", "CloudEvolutionMS",
@@ -90,6 +93,8 @@ def load(path=LIB_PATH):
     lib.ibmdem_measure_fp64_rate.argtypes = [i32, P(ctypes.c_double)]
     for name in SUBROUTINES:
         getattr(lib, "ibmdem_" + name).argtypes = [vp]
+    lib.ibmdem_set_wall_probes.argtypes = [vp, i32, vp]
+    lib.ibmdem_get_wall_probes.argtypes = [vp, vp, i32, P(i32)]
     dp = P(ctypes.c_double)
     lib.ibmdem_case_bytes.argtypes = [vp, i32, vp, i32, P(i64)]
     lib.ibmdem_batch_create.argtypes = [i32, P(vp)]
@@ -251,6 +256,20 @@ class Case:
         self._chk(self.lib.ibmdem_get_collision_lists(self.h, start.ctypes.data, idx.ctypes.data, ctypes.byref(nl),
                                                       ctypes.byref(npairs)), "pairs")
         return start, idx
+
+    def set_wall_probes(self, probes):
+        """Wall collision probes (records.WALL_PROBE) on solid-wall faces."""
+        probes = np.ascontiguousarray(probes, dtype=records.WALL_PROBE)
+        self._chk(self.lib.ibmdem_set_wall_probes(self.h, len(probes), probes.ctypes.data), "set_wall_probes")
+
+    def get_wall_probes(self):
+        """The probes with the force sums of the last wall-force call."""
+        n = ctypes.c_int32()
+        self._chk(self.lib.ibmdem_get_wall_probes(self.h, None, 0, ctypes.byref(n)), "get_wall_probes")
+        out = np.zeros(n.value, records.WALL_PROBE)
+        self._chk(self.lib.ibmdem_get_wall_probes(self.h, out.ctypes.data, n.value, ctypes.byref(n)),
+                  "get_wall_probes")
+        return out
 
     def counters(self):
         out = np.zeros(7, np.int64)

@@ -36,14 +36,23 @@ PARAMS = np.dtype([
 ])
 assert PARAMS.itemsize == 144
 
+# type WallColProbe (ZJS_VARS.F90:92-94): a quadrilateral on a wall face (1..6)
+WALL_PROBE = np.dtype([("face", "<i4"), ("pad_", "<i4"), ("points", "<f8", (4, 3)), ("force", "<f8", 3)])
+assert WALL_PROBE.itemsize == 128
+MAX_WALL_PROBES = 60
+
 
 def make_params(nx, ny, nz, h=1.0, dt=1e-3, coupleInterval=1, Ns=5, rhof=1e3, knCoeff=1e4,
-                ResistCoeff=0.9, collisionBuffer=0.1, gravity=(0.0, 0.0, -9.81), collisionDist=None):
-    """Case parameters; collisionDist defaults to dx*0.75*2 (ZJS_INIT_DEM.F90:413)."""
+                ResistCoeff=0.9, collisionBuffer=0.1, gravity=(0.0, 0.0, -9.81), collisionDist=None,
+                walls=""):
+    """Case parameters; collisionDist defaults to dx*0.75*2 (ZJS_INIT_DEM.F90:413).
+
+    `walls` names the axes bounded by two solid walls (bType 1), e.g. "z";
+    the others are periodic (bType 0)."""
     p = np.zeros((), PARAMS)
     p["nx"], p["ny"], p["nz"] = nx, ny, nz
     p["coupleInterval"], p["Ns"] = coupleInterval, Ns
-    p["bType"] = 0
+    p["bType"] = [1 if "xxyyzz"[f] in walls else 0 for f in range(6)]
     p["dx"] = p["dy"] = p["dz"] = h
     p["dt"], p["rhof"], p["knCoeff"], p["ResistCoeff"] = dt, rhof, knCoeff, ResistCoeff
     p["collisionDist"] = h * 0.75 * 2 if collisionDist is None else collisionDist

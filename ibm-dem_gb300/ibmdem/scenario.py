@@ -194,6 +194,124 @@ def kolmogorov_field(p, amp=0.05):
     return [u, np.zeros(shape), np.zeros(shape)]
 
 
+def fill_halo(p, fields):
+    """The fluid solver's boundary treatment of u, v, w (in place): the halo refill
+    of FillGhostRegionForFluid (boundary.F90:122-147) face by face -- periodic
+    copies, or beyond a solid wall the mirrored cells with all components
+    negated (DealWithBoundaryFluid, boundary.F90:211-245) -- then Boundary()
+    (fluid.F90:240-249), which zeroes the wall-normal velocity on the wall face
+    and beyond.  A field handed to the library should already satisfy this."""
+    n = [int(p["nx"]), int(p["ny"]), int(p["nz"])]
+    bt = [int(b) for b in p["bType"]]
+
+    def ax(d):  # array axis of grid axis d (arrays are (k, j, i))
+        return 2 - d
+
+    def sl(d, lo, hi, e_lo):  # index tuple: axis d in [lo, hi] (Fortran), others per e_lo
+        idx = [slice(None)] * 3
+        for e in range(3):
+            if e == d:
+                idx[ax(e)] = slice(lo + 1, hi + 2)
+            elif e > d:  # not yet filled: interior only
+                idx[ax(e)] = slice(2, n[e] + 2)
+            else:
+                idx[ax(e)] = slice(None)
+        return tuple(idx)
+
+    for side in range(6):
+        recv = side ^ 1
+        d = recv // 2
+        wall = bt[recv] == 1
+        src_side = recv if wall else side
+        s_lo = 1 if src_side % 2 == 0 else n[d] - 1
+        src = sl(d, s_lo, s_lo + 1, None)
+        if not wall:
+            r_lo = -1 if recv % 2 == 0 else n[d] + 1
+            dst = sl(d, r_lo, r_lo + 1, None)
+            for f in fields:
+                f[dst] = f[src]
+        else:
+            # filled outward from the wall: source cell t -> halo cell t beyond
+            for f in fields:
+                block = -np.flip(f[src], axis=ax(d)) if recv % 2 == 0 else -f[src]
+                if recv % 2 == 0:
+                    f[sl(d, -1, 0, None)] = block          # halo(0) = -f(1), halo(-1) = -f(2)
+                else:
+                    f[sl(d, n[d] + 1, n[d] + 2, None)] = np.flip(block, axis=ax(d))
+    for side in range(6):
+        if bt[side] != 1:
+            continue
+        d = side // 2
+        idx = [slice(None)] * 3
+        idx[ax(d)] = slice(0, 3) if side % 2 == 0 else slice(n[d] + 2, n[d] + 4)
+        fields[d][tuple(idx)] = 0.0
+    return fields
+
+
+def walled_case(nx, ny, nz, nbodies, d, seed=0, h=1.0, walls="z", vel_std=0.01, n_modes=16, amp=0.05,
+                rho_p=1.14e3, n_markers=None, touching=2, **param_kw):
+    """Spheres between solid walls on the axes in `walls` (the others periodic):
+    `touching` bodies rest against the low wall of the first walled axis (their
+    nearest markers within the contact distance of the wall, moving towards it),
+    the rest are placed at random clear of the walls.  The Fourier field is
+    given the wall conditions by fill_halo.  Returns (params, parcels, bodies,
+    (u, v, w))."""
+    p = make_params(nx, ny, nz, h=h, walls=walls, **param_kw)
+    rng = np.random.default_rng(seed)
+    L = np.array([nx * h, ny * h, nz * h])
+    R = 0.5 * d * h
+    wa = ["xyz".index(a) for a in walls]
+    centres = []
+    for b in range(touching):
+        # clear of the other walls and of each other
+        for _ in range(100_000):
+            c = rng.uniform(0, 1, 3) * L
+            for a in wa[1:]:
+                c[a] = rng.uniform(R + 1.5 * h, L[a] - R - 1.5 * h)
+            # lowest markers at radius R - 0.3h sit 0.4h from the wall (< radeff = 0.75h)
+            c[wa[0]] = (R - 0.3 * h) + 0.4 * h
+            dd = [c - q for q in centres]
+            for v in dd:
+                for e in range(3):
+                    if e not in wa:
+                        v[e] -= L[e] * round(v[e] / L[e])
+            if all(float(v @ v) > (2 * R + 0.5 * h) ** 2 for v in dd):
+                break
+        centres.append(c)
+    tries = 0
+    while len(centres) < nbodies:
+        tries += 1
+        if tries > 1_000_000:
+            raise RuntimeError("could not place the bodies")
+        c = rng.uniform(0, 1, 3) * L
+        if any(c[a] < R + 1.5 * h or c[a] > L[a] - R - 1.5 * h for a in wa):
+            continue
+        ok = True
+        for q in centres:
+            dd = c - q
+            for e in range(3):
+                if e not in wa:
+                    dd[e] -= L[e] * round(dd[e] / L[e])
+            if float(dd @ dd) <= (2 * R + 0.5 * h) ** 2:
+                ok = False
+                break
+        if ok:
+            centres.append(c)
+    centres = np.array(centres)
+    vel = rng.standard_normal((nbodies, 3)) * vel_std
+    vel[:touching, wa[0]] = -abs(vel[:touching, wa[0]]) - 0.01
+    parts, bodies = sphere_bodies(centres, d * h, h, rho_p, vel, n_markers=n_markers)
+    per = np.array([0 if e in wa else 1 for e in range(3)], bool)
+    x = parts["x"].copy()
+    xw = wrap_coord(x, L)
+    x[:, per] = xw[:, per]
+    parts["x"] = x
+    field = fourier_field(p, n_modes, amp, seed) if n_modes > 0 else [np.zeros(field_shape(p)) for _ in range(3)]
+    field = [np.array(f, dtype=np.float64, copy=True) for f in field]
+    fill_halo(p, field)
+    return p, parts, bodies, field
+
+
 def _capped_bodies(n_cells, d, nb, max_fraction):
     cap = int(max_fraction * n_cells / (math.pi / 6.0 * d ** 3))
     return max(1, min(nb, cap))

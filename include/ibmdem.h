@@ -61,6 +61,20 @@ typedef struct ibmdem_multisphere {
   double I, rad, rho, vol, m;
 } ibmdem_multisphere;
 
+/* Wall collision probe, type WallColProbe (ZJS_VARS.F90:92-94, set up by
+ * SetWallProbe, ZJS_INIT_DEM.F90:496-506): a quadrilateral on a solid wall
+ * face.  CalculateSolidBoundaryCollisionForce sums the normal spring force
+ * n*kn*deltan of every local parcel whose wall contact point lies inside it
+ * (WallProbeCollision, ZJS_COLLISION_DEM.F90:150-179), in part order; the sum
+ * restarts at every call. */
+#define IBMDEM_MAX_WALL_PROBES 60  /* maxNumWallProbe (10) per face, 6 faces */
+typedef struct ibmdem_wall_probe {
+  int32_t face;          /* 1..6 = -x,+x,-y,+y,-z,+z; the face has bType 1 */
+  int32_t pad_;
+  double points[4][3];   /* corners in order, points(1:3,1:4)             */
+  double force[3];       /* the last call's summed normal force (output)  */
+} ibmdem_wall_probe;
+
 /* Case parameters: the reference hard-codes these in source
  * (vars.F90, ZJS_VARS.F90:48-50, ZJS_INIT_DEM.F90:187-194,
  *  initialization.F90:251-259, fluid.F90:257, couplesolverCylinder.F90:12-13). */
@@ -68,7 +82,8 @@ typedef struct ibmdem_params {
   int32_t nx, ny, nz;        /* interior cells of the (single-rank) domain   */
   int32_t coupleInterval;    /* DEM sub-steps per fluid step                 */
   int32_t Ns;                /* multi-direct-forcing iterations (ref: 5)     */
-  int32_t bType[6];          /* face types -x,+x,-y,+y,-z,+z: 0 = periodic   */
+  int32_t bType[6];          /* face types -x,+x,-y,+y,-z,+z: 0 = periodic,
+                                1 = solid wall; both faces of an axis alike  */
   int32_t pad_;
   double dx, dy, dz;         /* cell sizes                                   */
   double dt;                 /* fluid time step                              */
@@ -115,7 +130,8 @@ int ibmdem_get_fluid_async(ibmdem_ctx* ctx, double* u, double* v, double* w,
                            double* fx, double* fy, double* fz, void* copy_stream);
 /* Local parcels part(1:npLocal) (ZJS_VARS.F90:20); pType is set to -1. */
 int ibmdem_set_parcels(ibmdem_ctx* ctx, int32_t np, const ibmdem_parcel* parts);
-/* Copy out part(1:np): locals first, then periodic images (np_out gets np,
+/* Copy out part(1:np): locals first, then the images, periodic (pType -1) and
+ * mirrored across solid walls (pType 1) (np_out gets np,
  * nlocal_out gets npLocal).  cap = capacity of `parts` in records. */
 int ibmdem_get_parcels(ibmdem_ctx* ctx, ibmdem_parcel* parts, int32_t cap,
                        int32_t* np_out, int32_t* nlocal_out);
@@ -140,17 +156,30 @@ int ibmdem_get_collision_lists(ibmdem_ctx* ctx, int32_t* start, int32_t* idx,
 int ibmdem_RebuildAllListOrNot(ibmdem_ctx* ctx);
 /* ZJS_UPDATE_LIST_DEM.F90:323-370: delta weights of local parcels. */
 int ibmdem_UpdateLocalCellWeightListDEM(ibmdem_ctx* ctx);
-/* ZJS_UPDATE_LIST_DEM.F90:372-416: delta weights of periodic images. */
+/* ZJS_UPDATE_LIST_DEM.F90:372-416: delta weights of the images. */
 int ibmdem_UpdateGhostCellWeightListDEM(ibmdem_ctx* ctx);
-/* ZJS_UPDATE_LIST_DEM.F90:179-246: refresh image copies (x + shift, v, fdrag). */
+/* ZJS_UPDATE_LIST_DEM.F90:179-246: refresh image copies (x + shift, v, fdrag;
+ * across a wall: x mirrored, the normal v negated, ZJS_MPI_DEM.F90:222-269). */
 int ibmdem_UpdateParcelInfoInGhostRegion(ibmdem_ctx* ctx);
 /* ZJS_COLLISION_DEM.F90:21-74: spring-dashpot contact force fcol. */
 int ibmdem_CalculateCollisionForce(ibmdem_ctx* ctx);
+/* ZJS_COLLISION_DEM.F90:76-148: parcel-wall spring-dashpot added to fcol for
+ * local parcels in the first or last cell layer, faces -x..+z in order, and the
+ * probe sums.  Without walls it does nothing.  The reference also appends a
+ * line per probe hit to its log file; this library writes no files. */
+int ibmdem_CalculateSolidBoundaryCollisionForce(ibmdem_ctx* ctx);
+/* Replace the wall probes (SetWallProbe, ZJS_INIT_DEM.F90:496-506); at most
+ * IBMDEM_MAX_WALL_PROBES, each on a face with bType 1, else IBMDEM_EINVAL. */
+int ibmdem_set_wall_probes(ibmdem_ctx* ctx, int32_t n, const ibmdem_wall_probe* probes);
+/* Copy out the probes with their last force sums (synchronises). */
+int ibmdem_get_wall_probes(ibmdem_ctx* ctx, ibmdem_wall_probe* probes, int32_t cap, int32_t* n_out);
 /* ZJS_VOLUMEFRACTION_DEM.F90:2-36: interpolation and direct forcing. */
 int ibmdem_UpdateFluidVelocityOnLagrangianPoints(ibmdem_ctx* ctx);
 /* ZJS_VOLUMEFRACTION_DEM.F90:38-67: deterministic spreading into fx,fy,fz. */
 int ibmdem_UpdateMomentumSourceTerm(ibmdem_ctx* ctx);
-/* fluid.F90:135-153 + the periodic halo refill of u,v,w (boundary.F90:122-147). */
+/* fluid.F90:135-153 + the halo refill of u,v,w (boundary.F90:122-147; beyond a
+ * wall the mirrored values negated, boundary.F90:211-245) + Boundary()
+ * (fluid.F90:240-249): zero wall-normal velocity on the wall and beyond. */
 int ibmdem_VelocityPostGuess(ibmdem_ctx* ctx);
 /* ZJS_MS_DEM.F90:494-519 (== AssembleForceMS on one rank, :385-432). */
 int ibmdem_AssembleLocalForceMS(ibmdem_ctx* ctx);

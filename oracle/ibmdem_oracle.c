@@ -7,9 +7,13 @@
  * path; this file restates its source, citing file:line for each routine, and
  * is pinned by the analytic checks in tests/test_oracle_*.py.
  *
- * Scope: one MPI rank owning the whole domain, every face periodic
- * (bType = 0).  On one rank the reference's MPI_SENDRECV calls for periodic
- * faces send to the rank itself; they are restated as the copies they perform.
+ * Scope: one MPI rank owning the whole domain; each axis either periodic
+ * (bType = 0 on both faces) or bounded by two solid walls (bType = 1).  On one
+ * rank the reference's MPI_SENDRECV calls for periodic faces send to the rank
+ * itself; they are restated as the copies they perform.  A wall face has no
+ * neighbour rank (neighCpu = -1), so the reference takes its
+ * UpdateFullInfoForSolidOutletBoundary / UpdatePartInfoForSolidOutletBoundary
+ * and DealWithBoundaryFluid branches there.
  *
  * Floating point: compile with -ffp-contract=off (gfortran on x86-64 without
  * -march emits no FMA).  Every expression keeps the Fortran left-to-right
@@ -55,6 +59,11 @@ struct orc_case {
   double di, dj, dk;
   double start[3], end[3], len[3];
   double coordShift[6];
+  double coordMirror[6]; /* wall coordinates (ZJS_INIT_DEM.F90:145-150) */
+  double pointBound[6][3], normBound[6][3]; /* wall planes (ZJS_INIT_DEM.F90:120-137) */
+  /* wall probes (type WallColProbe, ZJS_VARS.F90:92-94), in the caller's order */
+  int nProbe;
+  ibmdem_wall_probe probe[IBMDEM_MAX_WALL_PROBES];
   double dtDEM, eta, cut2;
   /* parcels part(1:np); locals are part(1:npLocal) */
   Parcel* part;
@@ -149,8 +158,9 @@ static void* xrealloc(void* p, size_t n) {
 
 orc_case* orc_create(const ibmdem_params* p) {
   if (!p || p->nx < 4 || p->ny < 4 || p->nz < 4) return NULL;
-  for (int f = 0; f < 6; ++f)
-    if (p->bType[f] != 0) return NULL; /* periodic faces only */
+  /* per axis: both faces periodic or both solid walls */
+  for (int d = 0; d < 3; ++d)
+    if (p->bType[2 * d] != p->bType[2 * d + 1] || (p->bType[2 * d] != 0 && p->bType[2 * d] != 1)) return NULL;
   orc_case* c = (orc_case*)calloc(1, sizeof(orc_case));
   c->p = *p;
   c->n[0] = p->nx;
@@ -186,6 +196,20 @@ orc_case* orc_create(const ibmdem_params* p) {
   c->coordShift[3] = -c->len[1];
   c->coordShift[4] = c->len[2];
   c->coordShift[5] = -c->len[2];
+  /* walls at the domain's faces: 0 and lGlo on one rank */
+  for (int d = 0; d < 3; ++d) {
+    c->coordMirror[2 * d] = c->start[d];
+    c->coordMirror[2 * d + 1] = c->end[d];
+  }
+  for (int f = 0; f < 6; ++f)
+    for (int d = 0; d < 3; ++d) {
+      c->pointBound[f][d] = (f % 2 == 0) ? c->start[d] : c->end[d];
+      c->normBound[f][d] = 0.0;
+    }
+  for (int d = 0; d < 3; ++d) {
+    c->normBound[2 * d][d] = 1.0;
+    c->normBound[2 * d + 1][d] = -1.0;
+  }
   /* InitParameters (ZJS_INIT_DEM.F90:184-195): dtDEM = dt/coupleInterval */
   c->dtDEM = p->dt / p->coupleInterval;
   c->eta = orc_eta(p->ResistCoeff);
@@ -408,6 +432,26 @@ static int RebuildParcelInCellListForGhostRegionDEM(orc_case* c) {
     int idxRecv = (idx % 2 == 0) ? idx + 1 : idx - 1;
     int nSend = c->npSend[idx];
     int dim = idx / 2;
+    if (c->p.bType[idxRecv] == 1) {
+      /* no rank beyond the wall (neighCpu = -1): UpdateFullInfoForSolidOutletBoundary
+       * (ZJS_MPI_DEM.F90:173-210) mirrors the parcels near face idxRecv itself */
+      int nRecv = c->npSend[idxRecv];
+      c->npRecv[idxRecv] = nRecv;
+      int rc = ensure_parts(c, c->np + nRecv);
+      if (rc) return rc;
+      for (int i = 0; i < nRecv; ++i) {
+        Parcel* d = &c->part[c->np + i];
+        *d = c->part[c->partSendIdx[idxRecv][i]];
+        d->x[dim] = 2 * c->coordMirror[idxRecv] - d->x[dim];
+        d->v[dim] = -d->v[dim];
+        d->pType = 1;
+      }
+      rc = PutParcelsIntoCellsDEM(c, c->np, c->np + nRecv, dim + 1);
+      if (rc) return rc;
+      c->startIdxRecv[idxRecv] = c->np;
+      c->np += nRecv;
+      continue;
+    }
     /* periodic: shift the copies (ZJS_UPDATE_LIST_DEM.F90:147-151) */
     for (int i = 0; i < nSend; ++i) c->partSend[idxSend][i].x[dim] = c->partSend[idxSend][i].x[dim] + c->coordShift[idxSend];
     /* receive into part(np+1 : np+nRecv): fields of ZJS_MPI_DEM.F90:82-95 */
@@ -633,6 +677,22 @@ int orc_UpdateParcelInfoInGhostRegion(orc_case* c) {
       s->wsum = o->wsum;
       memcpy(s->fdrag, o->fdrag, sizeof s->fdrag);
     }
+    if (c->p.bType[idxRecv] == 1) {
+      /* UpdatePartInfoForSolidOutletBoundary (ZJS_MPI_DEM.F90:222-269) */
+      int nRecv = c->npSend[idxRecv];
+      for (int i = 0; i < nRecv; ++i) {
+        Parcel* d = &c->part[c->startIdxRecv[idxRecv] + i];
+        const Parcel* o = &c->part[c->partSendIdx[idxRecv][i]];
+        memcpy(d->x, o->x, sizeof d->x);
+        memcpy(d->v, o->v, sizeof d->v);
+        memcpy(d->fdrag, o->fdrag, sizeof d->fdrag);
+        d->wsum = o->wsum;
+        d->x[dim] = 2 * c->coordMirror[idxRecv] - d->x[dim];
+        d->v[dim] = -d->v[dim];
+        d->pType = 1;
+      }
+      continue;
+    }
     for (int i = 0; i < nSend; ++i) c->partSend[idxSend][i].x[dim] = c->partSend[idxSend][i].x[dim] + c->coordShift[idxSend];
     int nRecv = c->npRecv[idxRecv];
     for (int i = 0; i < nRecv; ++i) {
@@ -686,6 +746,106 @@ int orc_CalculateCollisionForce(orc_case* c) {
       pi->fcol[2] = pi->fcol[2] + f3;
     }
   }
+  return 0;
+}
+
+/* WallProbeCollision (ZJS_COLLISION_DEM.F90:150-179): the contact point is
+ * inside the quadrilateral when the angles it sees the four edges under sum
+ * to 2 pi (within 0.001 pi); a NaN angle sum counts as inside, as the
+ * reference's comparison is false for it. */
+static int WallProbeCollision(double cp1, double cp2, double cp3, const ibmdem_wall_probe* prob) {
+  double theta = 0.0;
+  for (int i = 0; i < 4; ++i) {
+    int idxi = i, idxj = i + 1;
+    if (idxj > 3) idxj = idxj - 4;
+    double ni1 = prob->points[idxi][0] - cp1;
+    double ni2 = prob->points[idxi][1] - cp2;
+    double ni3 = prob->points[idxi][2] - cp3;
+    double nj1 = prob->points[idxj][0] - cp1;
+    double nj2 = prob->points[idxj][1] - cp2;
+    double nj3 = prob->points[idxj][2] - cp3;
+    double thetai = (ni1 * nj1 + ni2 * nj2 + ni3 * nj3) /
+                    (sqrt(ni1 * ni1 + ni2 * ni2 + ni3 * ni3) * sqrt(nj1 * nj1 + nj2 * nj2 + nj3 * nj3));
+    thetai = acos(thetai);
+    theta = theta + thetai;
+  }
+  double pi = acos(-1.0);
+  return fabs(theta - 2 * pi) > 0.001 * pi ? 0 : 1;
+}
+
+/* CalculateSolidBoundaryCollisionForce (ZJS_COLLISION_DEM.F90:76-148): the
+ * parcel-plane spring-dashpot for local parcels in the first or last interior
+ * cell layer, face by face, added to fcol after the pair forces; the normal
+ * spring part is summed into every probe of the face that contains the contact
+ * point, in part order.  The per-hit log line the reference appends to its
+ * log file is not written. */
+int orc_CalculateSolidBoundaryCollisionForce(orc_case* c) {
+  if (!c->listsBuilt) return fail(c, IBMDEM_ESTATE, "lists not built");
+  for (int q = 0; q < c->nProbe; ++q) memset(c->probe[q].force, 0, sizeof c->probe[q].force);
+  const double eta = c->eta;
+  const double knCoeff = c->p.knCoeff, di = c->di;
+  for (int i = 0; i < c->npLocal; ++i) {
+    Parcel* pi = &c->part[i];
+    int cellIdx1, cellIdx2, cellIdx3;
+    map1Dto3D(c, pi->cellIdx, &cellIdx1, &cellIdx2, &cellIdx3);
+    double xij1 = pi->x[0], xij2 = pi->x[1], xij3 = pi->x[2];
+    if (!(cellIdx1 == c->SG[0] || cellIdx1 == c->EG[0] || cellIdx2 == c->SG[1] || cellIdx2 == c->EG[1] ||
+          cellIdx3 == c->SG[2] || cellIdx3 == c->EG[2]))
+      continue;
+    for (int j = 0; j < 6; ++j) {
+      if (c->p.bType[j] != 1) continue;
+      double p1 = c->pointBound[j][0], p2 = c->pointBound[j][1], p3 = c->pointBound[j][2];
+      double n1 = c->normBound[j][0], n2 = c->normBound[j][1], n3 = c->normBound[j][2];
+      double r1 = xij1 - p1, r2 = xij2 - p2, r3 = xij3 - p3;
+      double dist = r1 * n1 + r2 * n2 + r3 * n3;
+      double cp1 = xij1 - dist * n1;
+      double cp2 = xij2 - dist * n2;
+      double cp3 = xij3 - dist * n3;
+      double meff = pi->m;
+      double rij = pi->radeff;
+      double deltan = rij - dist;
+      double kn = knCoeff / (0.1 * di) * meff;
+      double etan = eta * sqrt(meff * kn);
+      double vnij = n1 * pi->v[0] + n2 * pi->v[1] + n3 * pi->v[2];
+      if (deltan > 0) {
+        double f1 = n1 * (kn * deltan - etan * vnij);
+        double f2 = n2 * (kn * deltan - etan * vnij);
+        double f3 = n3 * (kn * deltan - etan * vnij);
+        double fn1 = n1 * kn * deltan;
+        double fn2 = n2 * kn * deltan;
+        double fn3 = n3 * kn * deltan;
+        pi->fcol[0] = pi->fcol[0] + f1;
+        pi->fcol[1] = pi->fcol[1] + f2;
+        pi->fcol[2] = pi->fcol[2] + f3;
+        for (int k = 0; k < c->nProbe; ++k) {
+          ibmdem_wall_probe* pr = &c->probe[k];
+          if (pr->face != j + 1) continue;
+          if (WallProbeCollision(cp1, cp2, cp3, pr)) {
+            pr->force[0] = pr->force[0] + fn1;
+            pr->force[1] = pr->force[1] + fn2;
+            pr->force[2] = pr->force[2] + fn3;
+          }
+        }
+      }
+    }
+  }
+  return 0;
+}
+
+int orc_set_wall_probes(orc_case* c, int32_t n, const ibmdem_wall_probe* probes) {
+  if (n < 0 || n > IBMDEM_MAX_WALL_PROBES || (n > 0 && !probes)) return fail(c, IBMDEM_EINVAL, "probe count");
+  for (int q = 0; q < n; ++q)
+    if (probes[q].face < 1 || probes[q].face > 6 || c->p.bType[probes[q].face - 1] != 1)
+      return fail(c, IBMDEM_EINVAL, "probe %d is not on a wall face", q);
+  memcpy(c->probe, probes, (size_t)n * sizeof *probes);
+  for (int q = 0; q < n; ++q) memset(c->probe[q].force, 0, sizeof c->probe[q].force);
+  c->nProbe = n;
+  return 0;
+}
+
+int orc_get_wall_probes(orc_case* c, ibmdem_wall_probe* probes, int32_t cap, int32_t* n_out) {
+  if (n_out) *n_out = c->nProbe;
+  if (probes) memcpy(probes, c->probe, (size_t)(cap < c->nProbe ? cap : c->nProbe) * sizeof *probes);
   return 0;
 }
 
@@ -764,24 +924,79 @@ int orc_UpdateMomentumSourceTerm(orc_case* c) {
   return 0;
 }
 
-/* FillGhostRegionForFluid for u,v,w on one periodic rank
- * (boundary.F90:122-147 with the send/recv boxes of boundary.F90:2-108):
- * every halo cell holds the value of its periodic image. */
-static inline int wrapi(int i, int n) { return i < 1 ? i + n : (i > n ? i - n : i); }
+/* FillGhostRegionForFluid (boundary.F90:122-147) for u,v,w on one rank, with
+ * the send/recv boxes of BuildMPIRecvAndSendIndexForFluid (boundary.F90:2-108):
+ * face by face, the halo beyond face sideRecv takes the cells next to face
+ * sideSend (periodic), or, beyond a wall, the mirrored cells next to sideRecv
+ * with all three components negated (DealWithBoundaryFluid, boundary.F90:211-245). */
+static void face_box(const orc_case* c, int side, int recv, int wall, int lo[3], int hi[3], int inc[3]) {
+  int d = side / 2, high = side % 2;
+  for (int e = 0; e < 3; ++e) {
+    inc[e] = 1;
+    if (e < d) { /* axes filled by earlier faces: halo included */
+      lo[e] = c->LG[e];
+      hi[e] = c->UG[e];
+    } else {
+      lo[e] = c->SG[e];
+      hi[e] = c->EG[e];
+    }
+  }
+  if (!recv) {
+    lo[d] = high ? c->EG[d] - HALO + 1 : c->SG[d];
+    hi[d] = high ? c->EG[d] : c->SG[d] + HALO - 1;
+  } else if (!wall) {
+    lo[d] = high ? c->EG[d] + 1 : c->LG[d];
+    hi[d] = high ? c->UG[d] : c->SG[d] - 1;
+  } else { /* walls fill outward from the face */
+    lo[d] = high ? c->UG[d] : c->SG[d] - 1;
+    hi[d] = high ? c->EG[d] + 1 : c->LG[d];
+    inc[d] = -1;
+  }
+}
 static void FillGhostRegionForFluid(orc_case* c) {
   double* f[3] = {c->u, c->v, c->w};
+  for (int i = 0; i < 6; ++i) {
+    int sideSend = i, sideRecv = (i % 2 == 0) ? i + 1 : i - 1;
+    int wall = c->p.bType[sideRecv] == 1;
+    int from = wall ? sideRecv : sideSend; /* DealWithBoundaryFluid reads sendIdxFluid(:,sideRecv) */
+    int slo[3], shi[3], sinc[3], rlo[3], rhi[3], rinc[3];
+    face_box(c, from, 0, 0, slo, shi, sinc);
+    face_box(c, sideRecv, 1, wall, rlo, rhi, rinc);
+    int d = sideRecv / 2;
+    int nr = (rhi[d] - rlo[d]) * rinc[d] + 1;
+    /* the boxes differ only along d; walk both in (k, j, i) order */
 #pragma omp parallel for schedule(static) num_threads(g_threads)
-  for (int k = c->LG[2]; k <= c->UG[2]; ++k)
-    for (int j = c->LG[1]; j <= c->UG[1]; ++j)
-      for (int i = c->LG[0]; i <= c->UG[0]; ++i) {
-        if (i >= c->SG[0] && i <= c->EG[0] && j >= c->SG[1] && j <= c->EG[1] && k >= c->SG[2] && k <= c->EG[2]) continue;
-        int64_t dst = fidx(c, i, j, k), src = fidx(c, wrapi(i, c->n[0]), wrapi(j, c->n[1]), wrapi(k, c->n[2]));
-        for (int q = 0; q < 3; ++q) f[q][dst] = f[q][src];
-      }
+    for (int k = slo[2]; k <= shi[2]; ++k)
+      for (int j = slo[1]; j <= shi[1]; ++j)
+        for (int ii = slo[0]; ii <= shi[0]; ++ii) {
+          int src[3] = {ii, j, k}, dst[3] = {ii, j, k};
+          int t = src[d] - slo[d];
+          dst[d] = rlo[d] + t * rinc[d];
+          if (t >= nr) continue;
+          int64_t a = fidx(c, dst[0], dst[1], dst[2]), s0 = fidx(c, src[0], src[1], src[2]);
+          for (int q = 0; q < 3; ++q) f[q][a] = wall ? -f[q][s0] : f[q][s0];
+        }
+  }
 }
 
-/* VelocityPostGuess (fluid.F90:135-153) followed by the halo refill done by
- * FirstOrderForwardEuler (fluid.F90:280). */
+/* Boundary (fluid.F90:240-249): the wall-normal velocity on the wall face and
+ * in the halo beyond it is zero. */
+static void Boundary(orc_case* c) {
+  double* f[3] = {c->u, c->v, c->w};
+  for (int side = 0; side < 6; ++side) {
+    if (c->p.bType[side] != 1) continue;
+    int d = side / 2;
+    int lo[3] = {c->LG[0], c->LG[1], c->LG[2]}, hi[3] = {c->UG[0], c->UG[1], c->UG[2]};
+    if (side % 2 == 0) hi[d] = c->SG[d];
+    else lo[d] = c->EG[d] + 1;
+    for (int k = lo[2]; k <= hi[2]; ++k)
+      for (int j = lo[1]; j <= hi[1]; ++j)
+        for (int i = lo[0]; i <= hi[0]; ++i) f[d][fidx(c, i, j, k)] = 0.0;
+  }
+}
+
+/* VelocityPostGuess (fluid.F90:135-153) followed by the halo refill and the
+ * wall condition done by FirstOrderForwardEuler (fluid.F90:275-277). */
 int orc_VelocityPostGuess(orc_case* c) {
   const double dt = c->p.dt;
 #pragma omp parallel for schedule(static) num_threads(g_threads)
@@ -794,6 +1009,7 @@ int orc_VelocityPostGuess(orc_case* c) {
         c->w[f] = c->w[f] + dt * (c->fz[f] - c->fzOld[f]);
       }
   FillGhostRegionForFluid(c);
+  Boundary(c);
   return 0;
 }
 
@@ -993,6 +1209,7 @@ int orc_MultiDirectForcing(orc_case* c) {
 int orc_CloudEvolutionStepMS(orc_case* c) {
   int rc;
   if ((rc = orc_CalculateCollisionForce(c))) return rc;
+  if ((rc = orc_CalculateSolidBoundaryCollisionForce(c))) return rc;
   if ((rc = orc_AssembleLocalForceMS(c))) return rc;
   if ((rc = orc_EvolutionMS(c))) return rc;
   if ((rc = orc_ResetVelocityAndPositionLagrangianPoints(c))) return rc;

@@ -13,7 +13,7 @@
  * pinned only by analytic and self-consistency checks (tests/test_oracle_*.py).
  *
  * The entry points mirror the reference subroutines one-for-one and operate on
- * one single-rank, triply periodic case.  Record layouts are the C-ABI ones
+ * one single-rank case, each axis periodic or between two solid walls.  Record layouts are the C-ABI ones
  * from include/ibmdem.h.
  */
 #ifndef IBMDEM_ORACLE_H
@@ -49,6 +49,9 @@ int orc_UpdateLocalCellWeightListDEM(orc_case* c);
 int orc_UpdateGhostCellWeightListDEM(orc_case* c);
 int orc_UpdateParcelInfoInGhostRegion(orc_case* c);
 int orc_CalculateCollisionForce(orc_case* c);
+int orc_CalculateSolidBoundaryCollisionForce(orc_case* c);
+int orc_set_wall_probes(orc_case* c, int32_t n, const ibmdem_wall_probe* probes);
+int orc_get_wall_probes(orc_case* c, ibmdem_wall_probe* probes, int32_t cap, int32_t* n_out);
 int orc_UpdateFluidVelocityOnLagrangianPoints(orc_case* c);
 int orc_UpdateMomentumSourceTerm(orc_case* c);
 int orc_VelocityPostGuess(orc_case* c);

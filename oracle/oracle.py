@@ -51,7 +51,7 @@ def _load():
     lib.orc_get_collision_lists.argtypes = [vp, vp, vp, P(i32), P(i32)]
     lib.orc_get_weights.argtypes = [vp, i32, vp, vp]
     for name in ("RebuildAllListOrNot", "UpdateLocalCellWeightListDEM", "UpdateGhostCellWeightListDEM",
-                 "UpdateParcelInfoInGhostRegion", "CalculateCollisionForce",
+                 "UpdateParcelInfoInGhostRegion", "CalculateCollisionForce", "CalculateSolidBoundaryCollisionForce",
                  "UpdateFluidVelocityOnLagrangianPoints", "UpdateMomentumSourceTerm", "VelocityPostGuess",
                  "AssembleLocalForceMS", "EvolutionMS", "ResetVelocityAndPositionLagrangianPoints",
                  "AdjustParcelPosition", "InitializationDEM", "MultiDirectForcing", "CloudEvolutionStepMS",
@@ -59,6 +59,8 @@ def _load():
         getattr(lib, "orc_" + name).argtypes = [vp]
         getattr(lib, "orc_" + name).restype = ctypes.c_int
     lib.orc_step.argtypes = [vp, i32]
+    lib.orc_set_wall_probes.argtypes = [vp, i32, vp]
+    lib.orc_get_wall_probes.argtypes = [vp, vp, i32, P(i32)]
     lib.orc_eta.restype = ctypes.c_double
     lib.orc_eta.argtypes = [ctypes.c_double]
     lib.orc_CalculateDragForce.argtypes = [ctypes.c_double, ctypes.c_double, vp, ctypes.c_double,
@@ -194,9 +196,23 @@ class OracleCase:
     def step(self, n=1):
         self._chk(self.lib.orc_step(self.h, int(n)), "step")
 
+    def set_wall_probes(self, probes):
+        from ibmdem import records
+        probes = np.ascontiguousarray(probes, dtype=records.WALL_PROBE)
+        self._chk(self.lib.orc_set_wall_probes(self.h, len(probes), probes.ctypes.data), "set_wall_probes")
+
+    def get_wall_probes(self):
+        from ibmdem import records
+        n = ctypes.c_int32()
+        self._chk(self.lib.orc_get_wall_probes(self.h, None, 0, ctypes.byref(n)), "get_wall_probes")
+        out = np.zeros(n.value, records.WALL_PROBE)
+        self._chk(self.lib.orc_get_wall_probes(self.h, out.ctypes.data, n.value, ctypes.byref(n)), "get_wall_probes")
+        return out
+
 
 _SUBROUTINES = ("RebuildAllListOrNot", "UpdateLocalCellWeightListDEM", "UpdateGhostCellWeightListDEM",
-                "UpdateParcelInfoInGhostRegion", "CalculateCollisionForce", "UpdateFluidVelocityOnLagrangianPoints",
+                "UpdateParcelInfoInGhostRegion", "CalculateCollisionForce", "CalculateSolidBoundaryCollisionForce",
+                "UpdateFluidVelocityOnLagrangianPoints",
                 "UpdateMomentumSourceTerm", "VelocityPostGuess", "AssembleLocalForceMS", "EvolutionMS",
                 "ResetVelocityAndPositionLagrangianPoints", "AdjustParcelPosition", "InitializationDEM",
                 "MultiDirectForcing", "CloudEvolutionStepMS", "CloudEvolutionMS")
