@@ -469,6 +469,7 @@ int ibmdem_destroy(ibmdem_ctx* h) {
   if (!h) return IBMDEM_EINVAL;
   Ctx& c = h->c;
   cudaSetDevice(c.device);
+  output_release(c);
   cudaStreamSynchronize(c.stream);
   free_parcel_buffers(c);
   void* ps[] = {c.u, c.v, c.w, c.u0, c.v0, c.w0, c.fx, c.fy, c.fz, c.cellStart, c.dCnt, c.dTotal, c.dBodies,

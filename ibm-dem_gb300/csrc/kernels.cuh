@@ -8,6 +8,8 @@
 
 namespace ibmdem {
 
+struct OutputState;  // output.cu: snapshot buffers and the file writer thread
+
 struct Ctx {
   ibmdem_params p{};
   Geom g{};
@@ -59,6 +61,8 @@ struct Ctx {
   int* partnerCnt = nullptr;
   int* partners = nullptr;
   int maxPartners = 64;
+
+  OutputState* out = nullptr;  // ibmdem_output_async
 
   // wall probes (ibmdem_set_wall_probes): device copy with the force sums
   ibmdem_wall_probe* dProbes = nullptr;
@@ -155,6 +159,8 @@ void record_written_nodes(Ctx& c);
 // weights in a static device array (no allocation); synchronises c.stream.
 // *bad = the lowest index of a point outside the box, or -1.
 cudaError_t interpolate_points_noalloc(Ctx& c, int n, const double* x, double* ulp, int* bad);
+// output.cu: wait for the writer thread and free the snapshot buffers
+void output_release(Ctx& c);
 // bodies.cu
 void launch_body_sums(Ctx& c);
 void launch_evolution(Ctx& c);

@@ -25,6 +25,7 @@ EXPORTS = [
     "ibmdem_RebuildAllListOrNot", "ibmdem_UpdateLocalCellWeightListDEM", "ibmdem_UpdateGhostCellWeightListDEM",
     "ibmdem_UpdateParcelInfoInGhostRegion", "ibmdem_CalculateCollisionForce",
     "ibmdem_CalculateSolidBoundaryCollisionForce", "ibmdem_set_wall_probes", "ibmdem_get_wall_probes",
+    "ibmdem_write_tecplot_markers", "ibmdem_write_body_probes", "ibmdem_output_async", "ibmdem_output_wait",
     "ibmdem_UpdateFluidVelocityOnLagrangianPoints", "ibmdem_UpdateMomentumSourceTerm", "ibmdem_VelocityPostGuess",
     "ibmdem_AssembleLocalForceMS", "ibmdem_EvolutionMS", "ibmdem_ResetVelocityAndPositionLagrangianPoints",
     "ibmdem_AdjustParcelPosition", "ibmdem_InitializationDEM", "ibmdem_MultiDirectForcing",
@@ -94,6 +95,10 @@ def load(path=LIB_PATH):
     for name in SUBROUTINES:
         getattr(lib, "ibmdem_" + name).argtypes = [vp]
     lib.ibmdem_set_wall_probes.argtypes = [vp, i32, vp]
+    lib.ibmdem_write_tecplot_markers.argtypes = [ctypes.c_char_p, i32, vp, vp]
+    lib.ibmdem_write_body_probes.argtypes = [ctypes.c_char_p, i64, i32, vp, ctypes.c_double]
+    lib.ibmdem_output_async.argtypes = [vp, ctypes.c_char_p, ctypes.c_char_p, i64]
+    lib.ibmdem_output_wait.argtypes = [vp]
     lib.ibmdem_get_wall_probes.argtypes = [vp, vp, i32, P(i32)]
     dp = P(ctypes.c_double)
     lib.ibmdem_case_bytes.argtypes = [vp, i32, vp, i32, P(i64)]
@@ -262,6 +267,15 @@ class Case:
         probes = np.ascontiguousarray(probes, dtype=records.WALL_PROBE)
         self._chk(self.lib.ibmdem_set_wall_probes(self.h, len(probes), probes.ctypes.data), "set_wall_probes")
 
+    def output_async(self, tecplot_path=None, probe_dir=None, step=0):
+        """Snapshot the parcels and bodies and write the Tecplot marker file and the
+        body probe lines from a host thread (ibmdem_output_async)."""
+        enc = lambda x: None if x is None else os.fsencode(x)  # noqa: E731
+        self._chk(self.lib.ibmdem_output_async(self.h, enc(tecplot_path), enc(probe_dir), int(step)), "output_async")
+
+    def output_wait(self):
+        self._chk(self.lib.ibmdem_output_wait(self.h), "output_wait")
+
     def get_wall_probes(self):
         """The probes with the force sums of the last wall-force call."""
         n = ctypes.c_int32()
@@ -305,6 +319,26 @@ def _make_method(name):
 
 for _name in SUBROUTINES:
     setattr(Case, _name, _make_method(_name))
+
+
+def write_tecplot_markers(path, parcels, centre=(0.0, 0.0, 0.0)):
+    """OutputCloudTecplot's marker file from host parcel records (no GPU needed)."""
+    lib = load()
+    a = np.ascontiguousarray(parcels, dtype=PARCEL)
+    c = np.ascontiguousarray(centre, dtype=np.float64)
+    rc = lib.ibmdem_write_tecplot_markers(os.fsencode(path), len(a), a.ctypes.data if len(a) else None, c.ctypes.data)
+    if rc != 0:
+        raise IbmDemError(rc, "ibmdem_write_tecplot_markers")
+
+
+def write_body_probes(directory, step, bodies, rhof):
+    """Append the per-body probe lines of fluid.F90:392-397 (no GPU needed)."""
+    lib = load()
+    b = np.ascontiguousarray(bodies, dtype=MULTISPHERE)
+    rc = lib.ibmdem_write_body_probes(os.fsencode(directory), int(step), len(b), b.ctypes.data if len(b) else None,
+                                      float(rhof))
+    if rc != 0:
+        raise IbmDemError(rc, "ibmdem_write_body_probes")
 
 
 def case_bytes(params, parcels, n_bodies):

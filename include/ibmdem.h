@@ -365,6 +365,25 @@ int ibmdem_server_memory(const ibmdem_server* s, int64_t* in_use, int64_t* budge
  * device, so that early requests finish early under load. */
 int ibmdem_server_set_work_limit(ibmdem_server* s, int64_t parcels);
 
+/* ---- output files ------------------------------------------------------ */
+/* OutputCloudTecplot (ZJS_IO_DEM.F90:82-121): the header lines
+ * "variables=x,y,z,u,v,w,index,ugap,vgap,wgap" and "zone i=<n> j=1", then per
+ * parcel x, v, MSIdx, vgap; with n == 0 one point at `centre` with zeros.  The
+ * reference names the file Results/Particle_<trec>_<cpu>.dat. */
+int ibmdem_write_tecplot_markers(const char* path, int32_t n, const ibmdem_parcel* parts, const double* centre);
+/* The per-body line of fluid.F90:392-397 appended to <dir>/<GlobalIdx>.probe:
+ * step, x, v, omega, fdrag/m*rhof, fmom/I*rhof, fcol/m. */
+int ibmdem_write_body_probes(const char* dir, int64_t step, int32_t nMS, const ibmdem_multisphere* ms, double rhof);
+/* Both files of the context's current state (tecplot_path or probe_dir NULL:
+ * that file is skipped).  Device-to-host copies of the local parcels and the
+ * bodies run on a stream of the library's own after the work issued so far,
+ * later work on the context waits for them, and a host thread formats the files;
+ * the call returns at once.  Lines use gfortran's list-directed layout (REAL(8)
+ * items as G25.17E3 fields, INTEGER items in 12 columns). */
+int ibmdem_output_async(ibmdem_ctx* ctx, const char* tecplot_path, const char* probe_dir, int64_t step);
+/* Wait for the files of the last ibmdem_output_async; its status. */
+int ibmdem_output_wait(ibmdem_ctx* ctx);
+
 /* ---- instrumentation -------------------------------------------------- */
 /* Record CUDA events around every phase of the drivers (interpolation,
  * spreading, weights, spread plan, cell lists, contact lists, contact force,
