@@ -470,6 +470,7 @@ int ibmdem_destroy(ibmdem_ctx* h) {
   Ctx& c = h->c;
   cudaSetDevice(c.device);
   output_release(c);
+  fluid_update_release(c);
   cudaStreamSynchronize(c.stream);
   free_parcel_buffers(c);
   void* ps[] = {c.u, c.v, c.w, c.u0, c.v0, c.w0, c.fx, c.fy, c.fz, c.cellStart, c.dCnt, c.dTotal, c.dBodies,
@@ -527,6 +528,9 @@ int ibmdem_set_fluid(ibmdem_ctx* h, const double* u, const double* v, const doub
   if (!u || !v || !w) return set_error(h, IBMDEM_EINVAL, "null field");
   Ctx& c = h->c;
   wait_fields_read(c);
+  // a sparse read-out may still be writing the caller's arrays
+  int ru = fluid_update_join(c);
+  if (ru) return ru;
   size_t nb = sizeof(double) * (size_t)c.g.ncell;
   CU(cudaMemcpyAsync(c.u, u, nb, cudaMemcpyHostToDevice, c.stream));
   CU(cudaMemcpyAsync(c.v, v, nb, cudaMemcpyHostToDevice, c.stream));

@@ -9,6 +9,7 @@
 namespace ibmdem {
 
 struct OutputState;  // output.cu: snapshot buffers and the file writer thread
+struct FluidUpdate;  // readout.cu: the sparse field read-out
 
 struct Ctx {
   ibmdem_params p{};
@@ -63,6 +64,7 @@ struct Ctx {
   int maxPartners = 64;
 
   OutputState* out = nullptr;  // ibmdem_output_async
+  FluidUpdate* upd = nullptr;  // ibmdem_update_fluid_async
 
   // wall probes (ibmdem_set_wall_probes): device copy with the force sums
   ibmdem_wall_probe* dProbes = nullptr;
@@ -161,6 +163,9 @@ void record_written_nodes(Ctx& c);
 cudaError_t interpolate_points_noalloc(Ctx& c, int n, const double* x, double* ulp, int* bad);
 // output.cu: wait for the writer thread and free the snapshot buffers
 void output_release(Ctx& c);
+// readout.cu: finish a pending sparse read-out (its status), and free its buffers
+int fluid_update_join(Ctx& c);
+void fluid_update_release(Ctx& c);
 // bodies.cu
 void launch_body_sums(Ctx& c);
 void launch_evolution(Ctx& c);

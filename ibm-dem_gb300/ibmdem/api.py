@@ -26,6 +26,7 @@ EXPORTS = [
     "ibmdem_UpdateParcelInfoInGhostRegion", "ibmdem_CalculateCollisionForce",
     "ibmdem_CalculateSolidBoundaryCollisionForce", "ibmdem_set_wall_probes", "ibmdem_get_wall_probes",
     "ibmdem_write_tecplot_markers", "ibmdem_write_body_probes", "ibmdem_output_async", "ibmdem_output_wait",
+    "ibmdem_update_fluid_async", "ibmdem_update_fluid_wait", "ibmdem_update_fluid_bytes",
     "ibmdem_UpdateFluidVelocityOnLagrangianPoints", "ibmdem_UpdateMomentumSourceTerm", "ibmdem_VelocityPostGuess",
     "ibmdem_AssembleLocalForceMS", "ibmdem_EvolutionMS", "ibmdem_ResetVelocityAndPositionLagrangianPoints",
     "ibmdem_AdjustParcelPosition", "ibmdem_InitializationDEM", "ibmdem_MultiDirectForcing",
@@ -99,6 +100,9 @@ def load(path=LIB_PATH):
     lib.ibmdem_write_body_probes.argtypes = [ctypes.c_char_p, i64, i32, vp, ctypes.c_double]
     lib.ibmdem_output_async.argtypes = [vp, ctypes.c_char_p, ctypes.c_char_p, i64]
     lib.ibmdem_output_wait.argtypes = [vp]
+    lib.ibmdem_update_fluid_async.argtypes = [vp] + [vp] * 6 + [vp]
+    lib.ibmdem_update_fluid_wait.argtypes = [vp]
+    lib.ibmdem_update_fluid_bytes.argtypes = [vp, P(i64)]
     lib.ibmdem_get_wall_probes.argtypes = [vp, vp, i32, P(i32)]
     dp = P(ctypes.c_double)
     lib.ibmdem_case_bytes.argtypes = [vp, i32, vp, i32, P(i64)]

@@ -128,6 +128,22 @@ int ibmdem_get_fluid(ibmdem_ctx* ctx, double* u, double* v, double* w,
  * they should be pinned for the copies to overlap anything. */
 int ibmdem_get_fluid_async(ibmdem_ctx* ctx, double* u, double* v, double* w,
                            double* fx, double* fy, double* fz, void* copy_stream);
+/* The read-out of ibmdem_get_fluid_async for a caller that keeps its own copy
+ * of the fields, as the Fortran fluid solver does: after MultiDirectForcing the
+ * fields differ from what ibmdem_set_fluid loaded only at the nodes the spread
+ * touched (and their halo images), and fx,fy,fz are zero elsewhere, so only
+ * those nodes' (u, f) pairs are copied -- about 20 bytes per touched node
+ * instead of six fields -- and a host thread writes them into u..fz.  u,v,w
+ * must hold the field last passed to ibmdem_set_fluid and fx,fy,fz what the
+ * previous call left there (zeros before the first); call it after each
+ * MultiDirectForcing.  The copies run on copy_stream after the work issued so
+ * far and the call returns at once; the arrays are complete when
+ * ibmdem_update_fluid_wait returns (ibmdem_set_fluid also waits for them). */
+int ibmdem_update_fluid_async(ibmdem_ctx* ctx, double* u, double* v, double* w,
+                              double* fx, double* fy, double* fz, void* copy_stream);
+int ibmdem_update_fluid_wait(ibmdem_ctx* ctx);
+/* Device-to-host bytes of the last completed ibmdem_update_fluid_async. */
+int ibmdem_update_fluid_bytes(const ibmdem_ctx* ctx, int64_t* bytes);
 /* Local parcels part(1:npLocal) (ZJS_VARS.F90:20); pType is set to -1. */
 int ibmdem_set_parcels(ibmdem_ctx* ctx, int32_t np, const ibmdem_parcel* parts);
 /* Copy out part(1:np): locals first, then the images, periodic (pType -1) and
