@@ -30,14 +30,25 @@ __global__ void __launch_bounds__(kSumWarps * 32) k_body_sums(Recs R, Geom g, ib
                                                               const int* __restrict__ bodyItems) {
   __shared__ double term[kSumWarps][32][13];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int b = blockIdx.x * kSumWarps + warp;
-  if (b >= nMS) return;
-  const double X[3] = {B[b].x[0], B[b].x[1], B[b].x[2]};
+  // two bodies per warp, one per half: the ordered folds of both (12 sums
+  // each) share their FP64 instructions
+  const int half = lane >> 4, hl = lane & 15;
+  const int b = (blockIdx.x * kSumWarps + warp) * 2 + half;
+  const bool hasBody = b < nMS;
+  double X[3] = {0.0, 0.0, 0.0};
+  int q0 = 0, q1 = 0;
+  if (hasBody) {
+    for (int k = 0; k < 3; ++k) X[k] = B[b].x[k];
+    q0 = bodyStart[b];
+    q1 = bodyStart[b + 1];
+  }
   const double rhof = g.rhof;
-  double acc = 0.0;  // lane L < 12 owns sum L: fdrag[0..2], fcol[0..2], fmom[0..2], fmomCol[0..2]
-  const int q0 = bodyStart[b], q1 = bodyStart[b + 1];
-  for (int base = q0; base < q1; base += 32) {
-    const int q = base + lane;
+  double acc = 0.0;  // lane hl < 12 owns sum hl: fdrag[0..2], fcol[0..2], fmom[0..2], fmomCol[0..2]
+  const int rounds = (q1 - q0 + 15) >> 4;
+  const int maxRounds = max(rounds, __shfl_xor_sync(0xffffffffu, rounds, 16));
+  for (int rd = 0; rd < maxRounds; ++rd) {
+    const int base = q0 + 16 * rd;
+    const int q = base + hl;
     if (q < q1) {
       const int m = bodyItems[q];
       const double vol = R.D(D_VOL, m);
@@ -65,15 +76,16 @@ __global__ void __launch_bounds__(kSumWarps * 32) k_body_sums(Recs R, Geom g, ib
       t[11] = rpc[0] * fc[1] - rpc[1] * fc[0];
     }
     __syncwarp();
-    const int n = min(32, q1 - base);
-    if (lane < 12)
-      for (int j = 0; j < n; ++j) acc = acc + term[warp][j][lane];
+    const int n = min(16, q1 - base);
+    if (hl < 12)
+      for (int j = 0; j < n; ++j) acc = acc + term[warp][16 * half + j][hl];
     __syncwarp();
   }
-  if (lane < 3) B[b].fdrag[lane] = acc;
-  else if (lane < 6) B[b].fcol[lane - 3] = acc;
-  else if (lane < 9) B[b].fmom[lane - 6] = acc;
-  else if (lane < 12) B[b].fmomCol[lane - 9] = acc;
+  if (!hasBody) return;
+  if (hl < 3) B[b].fdrag[hl] = acc;
+  else if (hl < 6) B[b].fcol[hl - 3] = acc;
+  else if (hl < 9) B[b].fmom[hl - 6] = acc;
+  else if (hl < 12) B[b].fmomCol[hl - 9] = acc;
 }
 
 // CloudEvolutionMS before AssembleForceMS (couplesolverCylinder.F90:194-204)
@@ -205,8 +217,8 @@ __global__ void k_marker_update(Recs R, Geom g, const Counters* cnt, const ibmde
 
 void launch_body_sums(Ctx& c) {
   if (c.nMS <= 0) return;
-  k_body_sums<<<nblocks(c.nMS, kSumWarps), kSumWarps * 32, 0, c.stream>>>(c.rec(), c.g, c.dBodies, c.nMS,
-                                                                           c.bodyStart, c.bodyItems);
+  k_body_sums<<<nblocks((c.nMS + 1) / 2, kSumWarps), kSumWarps * 32, 0, c.stream>>>(c.rec(), c.g, c.dBodies, c.nMS,
+                                                                                     c.bodyStart, c.bodyItems);
   c.launches++;
 }
 

@@ -254,7 +254,10 @@ __global__ void k_body_keys(Recs R, Counters* cnt, int nMS, uint32_t* keys, uint
   }
   keys[m] = (uint32_t)(b - 1);
   vals[m] = (uint32_t)m;
-  atomicAdd(&bodyCount[b - 1], 1);
+  // a body's markers are mostly neighbours in part order: one atomic per body
+  // and warp instead of one per marker on the same counter
+  const unsigned peers = __match_any_sync(__activemask(), b);
+  if ((int)(threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&bodyCount[b - 1], __popc(peers));
 }
 
 int bits_for(long long n) {
