@@ -22,17 +22,34 @@ __device__ inline float min_image_f(float d, float L) { return d - L * rintf(d /
 
 __global__ void k_body_bound(Recs R, Geom g, const Counters* cnt, const ibmdem_multisphere* B, int nMS,
                              unsigned* r2bits) {
-  int m = blockIdx.x * blockDim.x + threadIdx.x;
-  if (m >= cnt->npLocal) return;
-  int b = R.I(I_MSIDX, m) - 1;
-  if (b < 0 || b >= nMS) return;
-  float d2 = 0.f;
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  int b = -1;
+  unsigned v = 0u;  // squared distance as float bits (non-negative: the order is the integer order)
+  if (m < cnt->npLocal) {
+    b = R.I(I_MSIDX, m) - 1;
+    if (b >= 0 && b < nMS) {
+      float d2 = 0.f;
 #pragma unroll
-  for (int d = 0; d < 3; ++d) {
-    float dd = min_image_f((float)R.D(D_X + d, m) - (float)B[b].x[d], (float)g.len[d]);
-    d2 += dd * dd;
+      for (int d = 0; d < 3; ++d) {
+        float dd = min_image_f((float)R.D(D_X + d, m) - (float)B[b].x[d], (float)g.len[d]);
+        d2 += dd * dd;
+      }
+      v = __float_as_uint(d2);
+    } else {
+      b = -1;
+    }
   }
-  atomicMax(&r2bits[b], __float_as_uint(d2));
+  // a body's markers are mostly neighbours in part order: maximum over each run
+  // of equal bodies in the warp, one atomic per run
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned vo = __shfl_up_sync(0xffffffffu, v, o);
+    const int bo = __shfl_up_sync(0xffffffffu, b, o);
+    if (lane >= o && bo == b) v = max(v, vo);
+  }
+  const int next = __shfl_down_sync(0xffffffffu, b, 1);
+  if (b >= 0 && (lane == 31 || next != b)) atomicMax(&r2bits[b], v);
 }
 
 __global__ void k_body_pairs(const ibmdem_multisphere* B, int nMS, Geom g, const unsigned* r2bits, float reach,

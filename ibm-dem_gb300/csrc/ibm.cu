@@ -615,7 +615,7 @@ __global__ void k_mdf_reset(Recs R, Geom g, Counters* cnt, Fields fl, const uint
   GRID_STRIDE(t, n) {
     if (t < nLast) {
       int comp, i, j, k;
-      node_of(g, lastNodes[t], comp, i, j, k);
+      node_coords(g, lastNodes[t], comp, i, j, k);
       long long off = field_off(g, i, j, k);
       fl.F(comp)[off] = 0.0;
       if (frozen) put_mirrored<WALLS>(fl.U(comp), g, comp, i, j, k, fl.U0(comp)[off]);
