@@ -178,6 +178,12 @@ __global__ void k_img_emit(Recs R, Geom g, Counters* cnt, const int* offs, long 
     R.I(I_MSIDX, e) = R.I(I_MSIDX, m);
     int id[3];
     int wallImg = 0;
+    // MyMPISendAndRecv does not send vgap and wdrag (ZJS_MPI_DEM.F90:17-32); the
+    // slot's leftovers in the reference, zero here (a mirror across a wall copies
+    // the whole record, ZJS_MPI_DEM.F90:194, and takes them back below)
+#pragma unroll
+    for (int d = 0; d < 3; ++d) R.D(D_VGAP + d, e) = 0.0;
+    R.D(D_WDRAG, e) = 0.0;
     for (int d = 0; d < 3; ++d) {
       double x = R.D(D_X + d, m);
       if (sh[d]) {
@@ -191,6 +197,15 @@ __global__ void k_img_emit(Recs R, Geom g, Counters* cnt, const int* offs, long 
       id[d] = cell_of(g, d, x);
     }
     R.I(I_CELL, e) = cell_id(g, id[0], id[1], id[2]);
+    // a chain of mirrors keeps the source's values; a periodic step in it zeroes them
+    bool allWall = true;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) allWall = allWall && (!sh[d] || g.wall[d]);
+    if (allWall) {
+#pragma unroll
+      for (int d = 0; d < 3; ++d) R.D(D_VGAP + d, e) = R.D(D_VGAP + d, m);
+      R.D(D_WDRAG, e) = R.D(D_WDRAG, m);
+    }
     imgSrc[pos] = m;
     imgShift[pos] = fx | (fy << 2) | (fz << 4) | (wallImg << kWallImgBit);
   }

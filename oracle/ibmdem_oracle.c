@@ -32,6 +32,10 @@
  *     CSR with the reference's per-cell insertion order.
  *  4. Halo cells of fx,fy,fz (accumulated and then discarded by the reference)
  *     are not part of the state: VelocityPostGuess reads interior cells only.
+ *  5. A periodic image receives only the fields MyMPISendAndRecv sends; its
+ *     vgap and wdrag keep whatever the slot held before in the reference.  Here
+ *     they are zero, so that a marker that migrates across a periodic face (its
+ *     image becomes the local) has a defined vgap until the next interpolation.
  */
 #include "ibmdem_oracle.h"
 
@@ -476,6 +480,10 @@ static int RebuildParcelInCellListForGhostRegionDEM(orc_case* c) {
       memcpy(d->v, s->v, sizeof d->v);
       memcpy(d->fcol, s->fcol, sizeof d->fcol);
       memcpy(d->fdrag, s->fdrag, sizeof d->fdrag);
+      /* not sent (ZJS_MPI_DEM.F90:82-95): the reference leaves the slot's old
+       * contents there; they are defined as zero here (deviation 5) */
+      memset(d->vgap, 0, sizeof d->vgap);
+      d->wdrag = 0.0;
     }
     rc = PutParcelsIntoCellsDEM(c, c->np, c->np + nRecv, dim + 1);
     if (rc) return rc;
