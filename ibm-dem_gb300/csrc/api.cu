@@ -301,6 +301,7 @@ int check_device(ibmdem_ctx* h) {
   Ctx& c = h->c;
   CU(cudaMemcpyAsync(c.hCnt, c.dCnt, sizeof(Counters), cudaMemcpyDeviceToHost, c.stream));
   CU(cudaStreamSynchronize(c.stream));
+  if (c.planReady && c.hCnt->nRuns > 0) c.runsSeen = c.hCnt->nRuns;
   int e = c.hCnt->err;
   if (!e) return IBMDEM_OK;
   int info = c.hCnt->errInfo;
@@ -908,6 +909,7 @@ static int size_runs(ibmdem_ctx* h) {
   });
   c.bytes -= c.bytesRuns;
   c.capRuns = run_capacity(c, touched);
+  c.runsSeen = touched;
   const size_t b0 = c.bytes;
   cudaError_t e = cudaSuccess;
   for_each_run_buffer(c, [&](auto& q, size_t n) {

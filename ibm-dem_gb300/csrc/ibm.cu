@@ -855,6 +855,17 @@ long long count_touched_nodes(Ctx& c) {
   return total;
 }
 
+// Grid of the plan fill and the spread: one block per kBlock touched nodes of
+// the count the host last read back, plus an eighth (blocks past the device's
+// count return at once; the kernels' grid-stride loops cover growth beyond it).
+// One batch per block, rather than a resident grid looping over batches, lets
+// blocks start as others finish: their load and FP64 phases interleave and no
+// block's run of heavy batches holds up the end of the launch.
+static int run_blocks(const Ctx& c) {
+  const long long n = c.runsSeen > 0 ? std::min(c.capRuns, c.runsSeen + c.runsSeen / 8 + kBlock) : c.capRuns;
+  return std::max(nblocks(n), 1);
+}
+
 void build_spread_plan(Ctx& c) {
   cudaStream_t s = c.stream;
   const long long nflags = 3 * c.g.nint;
@@ -865,7 +876,7 @@ void build_spread_plan(Ctx& c) {
   k_set_runs<<<1, 1, 0, s>>>(c.dCnt, c.dTotal, c.capRuns);
   k_flag_emit<<<(unsigned)nb, kBlock, 0, s>>>(fv4, nvec, nflags, c.iTmpA, c.runKey, c.capRuns);
   cudaMemsetAsync(c.planAlloc, 0, sizeof(unsigned long long), s);
-  k_plan_fill<<<gs_blocks(c.capRuns), kBlock, 0, s>>>(c.g, c.dCnt, c.runKey, c.cellStart, c.cellItems, c.winC, c.W,
+  k_plan_fill<<<run_blocks(c), kBlock, 0, s>>>(c.g, c.dCnt, c.runKey, c.cellStart, c.cellItems, c.winC, c.W,
                                                       c.imgSrc, c.runStart, c.runCnt, c.planRoot, c.planW,
                                                       c.planAlloc, c.capContrib);
   k_plan_total<<<1, 1, 0, s>>>(c.dCnt, c.planAlloc);
@@ -899,7 +910,7 @@ void launch_spread(Ctx& c, bool fused_post_guess) {
   auto k = fused_post_guess ? (w ? k_spread<0, true> : k_spread<0, false>)
                             : (w ? k_spread<1, true> : k_spread<1, false>);
   cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSpreadSmem);
-  k<<<gs_blocks(c.capRuns), kBlock, kSpreadSmem, c.stream>>>(c.g, c.dCnt, c.runStart, c.runCnt, c.runKey, c.planRoot,
+  k<<<run_blocks(c), kBlock, kSpreadSmem, c.stream>>>(c.g, c.dCnt, c.runStart, c.runCnt, c.runKey, c.planRoot,
                                                             c.planW, c.fv, c.cap, fields_of(c), c.fCur, c.fPrev);
   c.launches++;
 }

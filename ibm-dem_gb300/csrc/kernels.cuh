@@ -93,6 +93,7 @@ struct Ctx {
   double* fPrev = nullptr;       // [capRuns]
   uint32_t* lastNodes = nullptr; // [capRuns] nodes written by the last spread
   long long capRuns = 0;
+  long long runsSeen = 0;  // touched nodes the host last read back (sizes the grids of the run kernels)
   bool runsSized = false;  // run arrays allocated for the counted touched nodes
   size_t bytesRuns = 0;
 
