@@ -174,6 +174,11 @@ void init_geom(Geom& g, const ibmdem_params* p) {
     g.anyWall |= g.wall[d];
   }
   g.dt = p->dt;
+  g.rdt = 1.0 / p->dt;
+  g.rdtLo = std::fma(-p->dt, g.rdt, 1.0) / p->dt;  // the remainder 1 - dt*rdt is exact
+  g.divDt = std::isnormal(p->dt) && std::isnormal(g.rdt) && std::fabs(p->dt) < 0x1p200 && std::fabs(p->dt) > 0x1p-200
+                ? 1
+                : 0;
   g.dtDEM = p->dt / p->coupleInterval;
   g.rhof = p->rhof;
   g.eta = eta_of(p->ResistCoeff);

@@ -83,6 +83,8 @@ struct Geom {
   int wall[3];      // 1: the axis is bounded by two solid walls (bType 1), 0: periodic
   int anyWall;
   double dt, dtDEM, rhof, eta, cut2, knCoeff, di;
+  double rdt, rdtLo; // RN(1/dt) and RN(1/dt - rdt), for div_dt
+  int divDt;         // dt and 1/dt normal with exponents within 2^+-200: div_dt may skip the division
   double g[3];
   FastDiv fdNint, fdN0, fdN1;  // interior nodes per component, nx, ny
   FastDiv fdNi, fdNj;          // nx + 4, ny + 4 (cells with the halo)

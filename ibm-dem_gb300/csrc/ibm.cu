@@ -43,6 +43,34 @@ __device__ inline double div3(double x) {
   return __fma_rn(r, c, q0);
 }
 
+// x / dt, correctly rounded, without a division.  With 1/dt split as
+// y + yl (y = RN(1/dt)), q0 = RN(x*y + RN(x*yl)) lies within half an ulp and a
+// few 2^-105 of x/dt, so it is a faithful quotient and its remainder
+// r = x - dt*q0 is exact in one FMA; RN(q0 + r*y) is then RN(x/dt) (Markstein's
+// correction theorem; a plain RN(x*y) can miss x/dt by 1.5 ulp when 1/dt is
+// rounded by a full half ulp, which is why div3's single product is not enough
+// for an arbitrary dt).  The theorem needs r clear of the subnormal range and
+// no overflow: x's exponent is checked with integer ops, and the division is
+// taken outside 2^-723 <= |x| < 2^777 (and for x = 0).
+__device__ inline double div_dt(double x, const Geom& g) {
+  const int ex = (int)((unsigned long long)__double_as_longlong(x) >> 52) & 0x7ff;
+  if (!g.divDt || ex < 300 || ex > 1800) return x / g.dt;
+  const double q0 = __fma_rn(x, g.rdt, __dmul_rn(x, g.rdtLo));
+  const double r = __fma_rn(-q0, g.dt, x);
+  return __fma_rn(r, g.rdt, q0);
+}
+
+// 0.0 + t and 0.0 - t under round-to-nearest, with integer ops in place of an
+// FP64 add: t and -t, except that the sum of opposite zeros is +0.0
+__device__ inline double zero_plus(double t) {
+  const long long b = __double_as_longlong(t);
+  return __longlong_as_double(b == (long long)0x8000000000000000ull ? 0ll : b);
+}
+__device__ inline double zero_minus(double t) {
+  const long long b = __double_as_longlong(t);
+  return __longlong_as_double(b == 0 ? 0ll : b ^ (long long)0x8000000000000000ull);
+}
+
 // one axis of DeltaFunction3D (interpolation.F90:7-30)
 template <int UNIT_H>
 __device__ inline double delta1(double xcp, double h) {
@@ -665,13 +693,13 @@ __global__ void __launch_bounds__(kBlock) k_interp(Recs R, Geom g, const Counter
           t = t * g.h[1];
           t = t * g.h[2];
         }
-        ulp = ulp + t;
+        ulp = (kz | ky | kx) ? ulp + t : zero_plus(t);  // 0.0 + t first
       }
     }
   const double vp = R.D(D_V + comp, m);
   R.D(D_VGAP + comp, m) = ulp - vp;
-  const double relaxfactor = 1.0;
-  double fd = R.D(D_FDRAG + comp, m) + relaxfactor * (ulp - vp) / g.dt;
+  // relaxfactor * (ulp - vp) / dt with relaxfactor = 1: the product is exact
+  double fd = R.D(D_FDRAG + comp, m) + div_dt(ulp - vp, g);
   R.D(D_FDRAG + comp, m) = fd;
   fv[(size_t)comp * cap + m] = fd * R.D(D_VOL, m);
 }
@@ -770,13 +798,16 @@ __global__ void __launch_bounds__(kBlock) k_spread(Geom g, const Counters* cnt, 
     if ((int)threadIdx.x < nHere) {
       const int loc = order[threadIdx.x];
       const int s0 = sStart[loc] - base, n = sLen[loc];
+      // f = 0.0 - p1 - p2 - ..., the first subtraction exact without the FP64 pipe
       double f = 0.0;
       if (staged) {
-        for (int q = s0; q < s0 + n; ++q) f = f - prod[q];
+        if (n > 0) f = zero_minus(prod[s0]);
+        for (int q = s0 + 1; q < s0 + n; ++q) f = f - prod[q];
       } else {
         for (int q = base + s0; q < base + s0 + n; ++q) {
           const uint32_t rc = planRoot[q];
-          f = f - fv[(size_t)(rc >> 30) * cap + (rc & 0x3fffffffu)] * planW[q];
+          const double p = fv[(size_t)(rc >> 30) * cap + (rc & 0x3fffffffu)] * planW[q];
+          f = q == base + s0 ? zero_minus(p) : f - p;
         }
       }
       fres[loc] = f;
