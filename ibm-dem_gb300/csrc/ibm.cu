@@ -616,15 +616,6 @@ __device__ inline void put_mirrored(double* F, const Geom& g, int comp, int i, i
       }
 }
 
-__device__ inline void node_of(const Geom& g, uint32_t key, int& comp, int& i, int& j, int& k) {
-  comp = (int)(key / (uint32_t)g.nint);
-  long long node = (long long)key - (long long)comp * g.nint;
-  i = (int)(node % g.n[0]) + 1;
-  node /= g.n[0];
-  j = (int)(node % g.n[1]) + 1;
-  k = (int)(node / g.n[1]) + 1;
-}
-
 struct Fields {
   double *u, *v, *w, *u0, *v0, *w0, *fx, *fy, *fz;
   __device__ double* U(int c) const { return c == 0 ? u : (c == 1 ? v : w); }
@@ -706,11 +697,11 @@ __global__ void __launch_bounds__(kBlock) k_interp(Recs R, Geom g, const Counter
 
 // UpdateMomentumSourceTerm (ZJS_VOLUMEFRACTION_DEM.F90:38-67) per touched node;
 // MODE 0: fused with VelocityPostGuess + halo refill, 1: spread only.
-// A warp takes 32 consecutive touched nodes, whose plan entries are contiguous:
-// the lanes form the products (fdrag*vol)*weight of the whole range in
-// parallel from coalesced reads, then each lane folds its own node's products
-// in part order -- the reference's fx = fx - fdrag*vol*weight, term by term.
-constexpr int kSpreadBuf = 3072;  // products per block held in shared memory
+// 2560 staged products per block (20 KB) let 8 blocks share an SM (32 registers,
+// about 26 KB of shared memory each) with room left for L1; a block whose range
+// holds more (markers far denser than the usual spacing) folds from global
+// memory instead.
+constexpr int kSpreadBuf = 2560;  // products per block held in shared memory
 constexpr int kStageDepth = 4;    // plan loads in flight per thread while staging
 constexpr int kLenBins = 64;
 // A block takes 256 consecutive touched nodes (one contiguous plan range).
@@ -719,9 +710,11 @@ constexpr int kLenBins = 64;
 // the same warp, so the FP64 lanes fold in step.  Each thread folds its node in
 // part order -- the reference's fx = fx - fdrag*vol*weight, term by term --
 // then applies the post-guess update with the periodic mirrors (MODE 0) or
-// keeps fx and fxOld for a separate VelocityPostGuess (MODE 1).
+// keeps fx and fxOld for a separate VelocityPostGuess (MODE 1).  (Folding the
+// shortest and the longest node in one thread idles fewer FP64 lanes but
+// leaves half the warps without work in the fold, and measured slower.)
 template <int MODE, bool WALLS>
-__global__ void __launch_bounds__(kBlock) k_spread(Geom g, const Counters* cnt, const int* __restrict__ runStart,
+__global__ void __launch_bounds__(kBlock, 8) k_spread(Geom g, const Counters* cnt, const int* __restrict__ runStart,
                                                    const int* __restrict__ runCnt,
                                                    const uint32_t* __restrict__ runKey,
                                                    const uint32_t* __restrict__ planRoot,
@@ -732,18 +725,17 @@ __global__ void __launch_bounds__(kBlock) k_spread(Geom g, const Counters* cnt, 
   __shared__ int order[kBlock];
   __shared__ int sStart[kBlock], sLen[kBlock];
   __shared__ double fres[kBlock];
-  const long long nRuns = cnt->nRuns;
-  for (long long r0 = (long long)blockIdx.x * kBlock; r0 < nRuns; r0 += (long long)gridDim.x * kBlock) {
-    const long long rLast = min(r0 + kBlock, nRuns) - 1;
-    const int nHere = (int)(rLast - r0 + 1);
+  const int nRuns = cnt->nRuns;  // run counts are ints (Counters)
+  for (int r0 = blockIdx.x * kBlock; r0 < nRuns; r0 += gridDim.x * kBlock) {
+    const int nHere = min(kBlock, nRuns - r0);
     // this thread's own node: everything its epilogue needs, loaded up front
-    const long long myR = r0 + threadIdx.x;
+    const int myR = r0 + threadIdx.x;
     const bool has = (int)threadIdx.x < nHere;
     int comp = 0, i = 1, j = 1, k = 1, myLen = 0;
     long long off = 0;
     double uOld = 0.0, fo = 0.0;
     if (has) {
-      node_of(g, runKey[myR], comp, i, j, k);
+      node_coords(g, runKey[myR], comp, i, j, k);
       off = field_off(g, i, j, k);
       myLen = runCnt[myR];
       sStart[threadIdx.x] = runStart[myR];
@@ -837,7 +829,7 @@ __global__ void k_post_guess(Geom g, const Counters* cnt, const uint32_t* runKey
   const long long nRuns = cnt->nRuns;
   GRID_STRIDE(r, nRuns) {
     int comp, i, j, k;
-    node_of(g, runKey[r], comp, i, j, k);
+    node_coords(g, runKey[r], comp, i, j, k);
     double* U = fl.U(comp);
     long long off = field_off(g, i, j, k);
     put_mirrored<WALLS>(U, g, comp, i, j, k, U[off] + g.dt * (fCur[r] - fPrev[r]));
