@@ -285,7 +285,9 @@ __device__ inline int gather_row(const Geom& g, int comp, int iFirst, int iLast,
   const int ny = comp == 1 ? 4 : 3, nr = ny * (comp == 2 ? 4 : 3);  // candidate cell rows (<= 12)
   int q0 = 0, len = 0;
   if (lane < nr) {
-    const int cy = ylo + lane % ny, cz = zlo + lane / ny;
+    // lane / ny for ny = 3 or 4 and lane < 16: (lane * 11) >> 5 is lane / 3 there
+    const int dz = ny == 4 ? lane >> 2 : (lane * 11) >> 5;
+    const int cy = ylo + (lane - dz * ny), cz = zlo + dz;
     // cell_id(g, xlo, cy, cz) - 1 in 32 bits (the cell count fits an int)
     const int c0 = ((cz + 1) * g.nj + (cy + 1)) * g.ni + (xlo + 1);
     q0 = cellStart[c0];
