@@ -446,8 +446,51 @@ __device__ inline int fill_subgroups(const Geom& g, unsigned starts, int nValid,
       ea[u] = e < m ? aux[e] : 0u;
     }
     __syncwarp();
+    if (m <= 32) {
+      // The sub-group's nodes are iFirst + t, t < nn <= kSubMax.  One ballot
+      // per node leaves node t's contributor mask in lane t; a scan over those
+      // lanes gives each node's offset, and each kept parcel then writes its
+      // own (up to three) entries at the node's offset plus its rank among
+      // the node's contributors (lanes are in part order).
+      const int nn = l1 - l0 + 1;
+      const int sxr = (int)(ea[0] & 0xffu) - 2;  // sx - iFirst
+      unsigned myMask = 0u;
+      for (int t = 0; t < nn; ++t) {
+        const unsigned mh = __ballot_sync(kFull, lane < m && (unsigned)(t - sxr) <= 2u);
+        if (lane == t) myMask = mh;
+      }
+      const int cntT = __popc(myMask);
+      int incl = cntT;
+#pragma unroll
+      for (int o = 1; o < kSubMax; o <<= 1) {
+        const int y = __shfl_up_sync(kFull, incl, o);
+        if (lane >= o) incl += y;
+      }
+      const int exclT = incl - cntT;
+      const int subTotal = __shfl_sync(kFull, incl, kSubMax - 1);
+      const uint32_t base = (ek[0] << 7) | (uint32_t)(sc * 27 + 3 * (int)(ea[0] >> 8));
+#pragma unroll
+      for (int dx = 0; dx < 3; ++dx) {
+        const int t = sxr + dx;
+        const int tc = min(max(t, 0), kSubMax - 1);
+        const unsigned M = __shfl_sync(kFull, myMask, tc);
+        const int O = __shfl_sync(kFull, exclT, tc);
+        if (lane < m && t >= 0 && t < nn) {
+          const int at = off + O + __popc(M & lt);
+          if (at < outCap) out[at] = base + (uint32_t)dx;
+        }
+      }
+      const int src = min(max(lane - l0, 0), kSubMax - 1);
+      const int cN = __shfl_sync(kFull, cntT, src), oN = __shfl_sync(kFull, exclT, src);
+      if (lane >= l0 && lane <= l1) {
+        myCnt = cN;
+        myOff = off + oN;
+      }
+      off += subTotal;
+      continue;
+    }
     const int sx0 = iFirst - 2;
-    const int two = m > 32 ? 2 : 1;
+    const int two = 2;
     for (int n = l0; n <= l1; ++n) {
       const int in = __shfl_sync(kFull, i, n);
       int c = 0;
