@@ -248,14 +248,15 @@ __global__ void k_set_runs(Counters* cnt, const int* total, long long capRuns) {
 // window covers the row in y and z and reaches the sub-group in x, and sorts
 // them by part index.  A kept parcel covers the three nodes sx..sx+2 of the
 // row, so each node's contributors in part order are the sorted list filtered
-// by sx in [i-2, i]: one ballot per node.  The entries (parcel << 7 | slot)
-// are staged per warp in shared memory; the block reserves its contribution
-// range with one atomic (the 256 runs of a block own one contiguous range in
-// run order, which the spread relies on) and writes (root | comp << 30,
-// weight) with consecutive lanes on consecutive entries.  A sub-group with more
-// than kLCap kept parcels is split into single nodes; a single node with more
-// than kLCap contributors, or a warp whose entries exceed its staging, is
-// written straight into the plan range after the reservation.
+// by sx in [i-2, i]: one ballot per node, whose mask stays in the node's lane,
+// and each kept parcel writes its own entries from those masks.  The entries
+// (parcel << 7 | slot) are staged per warp in shared memory; the block
+// reserves its contribution range with one atomic (the 256 runs of a block own
+// one contiguous range in run order, which the spread relies on) and writes
+// (root | comp << 30, weight) with consecutive lanes on consecutive entries.  A
+// sub-group with more than kLCap kept parcels is halved until it fits; a
+// single node with more than kLCap contributors, or a warp whose entries exceed
+// its staging, is written straight into the plan range after the reservation.
 __device__ inline void node_coords(const Geom& g, uint32_t key, int& comp, int& i, int& j, int& k) {
   const uint32_t c = g.fdNint.div(key);
   const uint32_t node = key - c * (uint32_t)g.nint;
@@ -267,7 +268,7 @@ __device__ inline void node_coords(const Geom& g, uint32_t key, int& comp, int& 
   k = (int)kk + 1;
 }
 
-constexpr int kSubMax = 8;      // nodes per sub-group
+constexpr int kSubMax = 16;     // nodes per sub-group (a power of two: the node scan)
 constexpr int kLCap = 64;       // kept parcels per sub-group (two per lane)
 constexpr int kStageCap = 512;  // staged entries per warp
 constexpr int kPlanWarps = kBlock / 32;
@@ -392,11 +393,12 @@ __device__ inline int fill_subgroups(const Geom& g, unsigned starts, int nValid,
     const int sj = __shfl_sync(kFull, j, l0), sk = __shfl_sync(kFull, k, l0);
     const int iFirst = __shfl_sync(kFull, i, l0);
     int m = gather_row(g, sc, iFirst, __shfl_sync(kFull, i, l1), sj, sk, cellStart, cellItems, winC, key, aux, lane);
-    if (m > kLCap && l1 > l0) {
-      // too many for one list: the first node alone, the rest as a sub-group of its own
-      rest |= 1u << (l0 + 1);
-      l1 = l0;
-      m = gather_row(g, sc, iFirst, iFirst, sj, sk, cellStart, cellItems, winC, key, aux, lane);
+    while (m > kLCap && l1 > l0) {
+      // too many for one list: the first half now, the second as a sub-group of its own
+      const int mid = l0 + ((l1 - l0 + 1) >> 1);
+      rest |= 1u << mid;
+      l1 = mid - 1;
+      m = gather_row(g, sc, iFirst, __shfl_sync(kFull, i, l1), sj, sk, cellStart, cellItems, winC, key, aux, lane);
     }
     if (m > kLCap) {
       // one node with more than kLCap contributors (m counts exactly them)
@@ -446,71 +448,75 @@ __device__ inline int fill_subgroups(const Geom& g, unsigned starts, int nValid,
       ea[u] = e < m ? aux[e] : 0u;
     }
     __syncwarp();
+    // The sub-group's nodes are iFirst + t, t < nn <= kSubMax.  One ballot per
+    // node (and slot) leaves node t's contributor masks in lane t; a scan over
+    // those lanes gives each node's offset, and each kept parcel then writes
+    // its own (up to three) entries at the node's offset plus its rank among
+    // the node's contributors (slots, then lanes, are in part order).
+    const int nn = l1 - l0 + 1;
+    unsigned mask0 = 0u, mask1 = 0u;
+    const int sxr0 = (int)(ea[0] & 0xffu) - 2;  // sx - iFirst
     if (m <= 32) {
-      // The sub-group's nodes are iFirst + t, t < nn <= kSubMax.  One ballot
-      // per node leaves node t's contributor mask in lane t; a scan over those
-      // lanes gives each node's offset, and each kept parcel then writes its
-      // own (up to three) entries at the node's offset plus its rank among
-      // the node's contributors (lanes are in part order).
-      const int nn = l1 - l0 + 1;
-      const int sxr = (int)(ea[0] & 0xffu) - 2;  // sx - iFirst
-      unsigned myMask = 0u;
       for (int t = 0; t < nn; ++t) {
-        const unsigned mh = __ballot_sync(kFull, lane < m && (unsigned)(t - sxr) <= 2u);
-        if (lane == t) myMask = mh;
+        const unsigned b0 = __ballot_sync(kFull, lane < m && (unsigned)(t - sxr0) <= 2u);
+        if (lane == t) mask0 = b0;
       }
-      const int cntT = __popc(myMask);
-      int incl = cntT;
+    } else {
+      const int sxr1 = (int)(ea[1] & 0xffu) - 2;
+      for (int t = 0; t < nn; ++t) {
+        const unsigned b0 = __ballot_sync(kFull, (unsigned)(t - sxr0) <= 2u);
+        const unsigned b1 = __ballot_sync(kFull, lane + 32 < m && (unsigned)(t - sxr1) <= 2u);
+        if (lane == t) {
+          mask0 = b0;
+          mask1 = b1;
+        }
+      }
+    }
+    const int cntT = __popc(mask0) + __popc(mask1);
+    int incl = cntT;
 #pragma unroll
-      for (int o = 1; o < kSubMax; o <<= 1) {
-        const int y = __shfl_up_sync(kFull, incl, o);
-        if (lane >= o) incl += y;
-      }
-      const int exclT = incl - cntT;
-      const int subTotal = __shfl_sync(kFull, incl, kSubMax - 1);
-      const uint32_t base = (ek[0] << 7) | (uint32_t)(sc * 27 + 3 * (int)(ea[0] >> 8));
+    for (int o = 1; o < kSubMax; o <<= 1) {
+      const int y = __shfl_up_sync(kFull, incl, o);
+      if (lane >= o) incl += y;
+    }
+    const int exclT = incl - cntT;
+    const int subTotal = __shfl_sync(kFull, incl, kSubMax - 1);
+    {
+      const uint32_t entry = (ek[0] << 7) | (uint32_t)(sc * 27 + 3 * (int)(ea[0] >> 8));
 #pragma unroll
       for (int dx = 0; dx < 3; ++dx) {
-        const int t = sxr + dx;
+        const int t = sxr0 + dx;
         const int tc = min(max(t, 0), kSubMax - 1);
-        const unsigned M = __shfl_sync(kFull, myMask, tc);
+        const unsigned M0 = __shfl_sync(kFull, mask0, tc);
         const int O = __shfl_sync(kFull, exclT, tc);
         if (lane < m && t >= 0 && t < nn) {
-          const int at = off + O + __popc(M & lt);
-          if (at < outCap) out[at] = base + (uint32_t)dx;
+          const int at = off + O + __popc(M0 & lt);
+          if (at < outCap) out[at] = entry + (uint32_t)dx;
         }
       }
-      const int src = min(max(lane - l0, 0), kSubMax - 1);
-      const int cN = __shfl_sync(kFull, cntT, src), oN = __shfl_sync(kFull, exclT, src);
-      if (lane >= l0 && lane <= l1) {
-        myCnt = cN;
-        myOff = off + oN;
-      }
-      off += subTotal;
-      continue;
     }
-    const int sx0 = iFirst - 2;
-    const int two = 2;
-    for (int n = l0; n <= l1; ++n) {
-      const int in = __shfl_sync(kFull, i, n);
-      int c = 0;
-      for (int u = 0; u < two; ++u) {
-        const int sx = sx0 + (int)(ea[u] & 0xffu);
-        const bool hit = lane + 32 * u < m && sx <= in && sx + 2 >= in;
-        const unsigned mh = __ballot_sync(kFull, hit);
-        if (hit) {
-          const int at = off + c + __popc(mh & lt);
-          if (at < outCap)
-            out[at] = (ek[u] << 7) | (uint32_t)(sc * 27 + 3 * (int)(ea[u] >> 8) + (in - sx));
+    if (m > 32) {
+      const int sxr1 = (int)(ea[1] & 0xffu) - 2;
+      const uint32_t entry = (ek[1] << 7) | (uint32_t)(sc * 27 + 3 * (int)(ea[1] >> 8));
+#pragma unroll
+      for (int dx = 0; dx < 3; ++dx) {
+        const int t = sxr1 + dx;
+        const int tc = min(max(t, 0), kSubMax - 1);
+        const unsigned M0 = __shfl_sync(kFull, mask0, tc), M1 = __shfl_sync(kFull, mask1, tc);
+        const int O = __shfl_sync(kFull, exclT, tc);
+        if (lane + 32 < m && t >= 0 && t < nn) {
+          const int at = off + O + __popc(M0) + __popc(M1 & lt);
+          if (at < outCap) out[at] = entry + (uint32_t)dx;
         }
-        c += __popc(mh);
       }
-      if (lane == n) {
-        myCnt = c;
-        myOff = off;
-      }
-      off += c;
     }
+    const int src = min(max(lane - l0, 0), kSubMax - 1);
+    const int cN = __shfl_sync(kFull, cntT, src), oN = __shfl_sync(kFull, exclT, src);
+    if (lane >= l0 && lane <= l1) {
+      myCnt = cN;
+      myOff = off + oN;
+    }
+    off += subTotal;
   }
   return off;
 }
