@@ -749,9 +749,10 @@ __global__ void __launch_bounds__(kBlock) k_interp(Recs R, Geom g, const Counter
 // UpdateMomentumSourceTerm (ZJS_VOLUMEFRACTION_DEM.F90:38-67) per touched node;
 // MODE 0: fused with VelocityPostGuess + halo refill, 1: spread only.
 // 2560 staged products per block (20 KB) let 8 blocks share an SM (32 registers,
-// about 26 KB of shared memory each) with room left for L1; a block whose range
-// holds more (markers far denser than the usual spacing) folds from global
-// memory instead.
+// under 24 KB of shared memory each, so that the SM keeps the 196 KB shared
+// memory split and 60 KB of L1, which the kernels that run beside it in a batch
+// of cases rely on); a block whose range holds more (markers far denser than the
+// usual spacing) folds from global memory instead.
 constexpr int kSpreadBuf = 2560;  // products per block held in shared memory
 constexpr int kStageDepth = 4;    // plan loads in flight per thread while staging
 constexpr int kLenBins = 64;
@@ -771,11 +772,12 @@ __global__ void __launch_bounds__(kBlock, 8) k_spread(Geom g, const Counters* cn
                                                    const uint32_t* __restrict__ planRoot,
                                                    const double* __restrict__ planW, const double* __restrict__ fv,
                                                    int cap, Fields fl, double* fCur, double* fPrev) {
+  // prod: the staged products; a node's sum replaces its first product (a node
+  // without products keeps 0), and without staging prod[t] holds node t's sum
   extern __shared__ double prod[];
   __shared__ int bins[kLenBins];
   __shared__ int order[kBlock];
-  __shared__ int sStart[kBlock], sLen[kBlock];
-  __shared__ double fres[kBlock];
+  __shared__ int sStart[kBlock + 1];  // the block's runs are contiguous: run t spans sStart[t]..sStart[t+1]
   const int nRuns = cnt->nRuns;  // run counts are ints (Counters)
   for (int r0 = blockIdx.x * kBlock; r0 < nRuns; r0 += gridDim.x * kBlock) {
     const int nHere = min(kBlock, nRuns - r0);
@@ -789,15 +791,16 @@ __global__ void __launch_bounds__(kBlock, 8) k_spread(Geom g, const Counters* cn
       node_coords(g, runKey[myR], comp, i, j, k);
       off = field_off(g, i, j, k);
       myLen = runCnt[myR];
-      sStart[threadIdx.x] = runStart[myR];
-      sLen[threadIdx.x] = myLen;
+      const int st = runStart[myR];
+      sStart[threadIdx.x] = st;
+      if ((int)threadIdx.x == nHere - 1) sStart[nHere] = st + myLen;
       fo = fCur[myR];
       if (MODE == 0) uOld = fl.U(comp)[off];
     }
     if (threadIdx.x < kLenBins) bins[threadIdx.x] = 0;
     __syncthreads();
     const int base = sStart[0];
-    const int total = sStart[nHere - 1] + sLen[nHere - 1] - base;
+    const int total = sStart[nHere] - base;
     const bool staged = total <= kSpreadBuf;
     if (staged)
       for (int q0 = threadIdx.x; q0 < total; q0 += kStageDepth * kBlock) {
@@ -840,24 +843,27 @@ __global__ void __launch_bounds__(kBlock, 8) k_spread(Geom g, const Counters* cn
     // fold a node of similar length to the warp's other nodes, in part order
     if ((int)threadIdx.x < nHere) {
       const int loc = order[threadIdx.x];
-      const int s0 = sStart[loc] - base, n = sLen[loc];
+      const int s0 = sStart[loc] - base, n = sStart[loc + 1] - sStart[loc];
       // f = 0.0 - p1 - p2 - ..., the first subtraction exact without the FP64 pipe
       double f = 0.0;
       if (staged) {
-        if (n > 0) f = zero_minus(prod[s0]);
-        for (int q = s0 + 1; q < s0 + n; ++q) f = f - prod[q];
+        if (n > 0) {
+          f = zero_minus(prod[s0]);
+          for (int q = s0 + 1; q < s0 + n; ++q) f = f - prod[q];
+          prod[s0] = f;
+        }
       } else {
         for (int q = base + s0; q < base + s0 + n; ++q) {
           const uint32_t rc = planRoot[q];
           const double p = fv[(size_t)(rc >> 30) * cap + (rc & 0x3fffffffu)] * planW[q];
           f = q == base + s0 ? zero_minus(p) : f - p;
         }
+        prod[loc] = f;
       }
-      fres[loc] = f;
     }
     __syncthreads();
     if (has) {
-      const double f = fres[threadIdx.x];
+      const double f = !staged ? prod[threadIdx.x] : (myLen > 0 ? prod[sStart[threadIdx.x] - base] : 0.0);
       fl.F(comp)[off] = f;
       if (MODE == 0) {
         put_mirrored<WALLS>(fl.U(comp), g, comp, i, j, k, uOld + g.dt * (f - fo));
