@@ -126,7 +126,9 @@ __host__ __device__ inline void cell_coords(const Geom& g, int id, int& i, int& 
 }
 // floor((x-xStart)/di)+SG (ZJS_UPDATE_LIST_DEM.F90:41-43)
 __device__ inline int cell_of(const Geom& g, int d, double x) {
-  return (int)floor((x - g.start[d]) / g.h[d]) + 1;
+  // (x - start) / h; with unit spacing the division by 1.0 is an identity
+  const double t = x - g.start[d];
+  return (int)floor(g.unit_h ? t : t / g.h[d]) + 1;
 }
 __device__ inline bool interior(const Geom& g, int i, int j, int k) {
   return i >= 1 && i <= g.n[0] && j >= 1 && j <= g.n[1] && k >= 1 && k <= g.n[2];

@@ -78,8 +78,13 @@ __global__ void k_scan_spine(int* partial, long long nb, int* total) {
   if (threadIdx.x == 0 && total) *total = carry;
 }
 
+// tile slot of element idx: one pad word per 32, so that a thread's
+// kScanItems consecutive elements (and a warp's 32 consecutive loads) fall in
+// distinct banks
+__device__ inline int padded(int idx) { return idx + (idx >> 5); }
+
 __global__ void k_scan_down(const int* in, int* out, long long n_max, const int* n_dev, const int* partial) {
-  __shared__ int tile[kScanTile];
+  __shared__ int tile[kScanTile + kScanTile / 32];
   __shared__ int sh[32];
   long long n = read_n(n_max, n_dev);
   long long base = (long long)blockIdx.x * kScanTile;
@@ -87,28 +92,28 @@ __global__ void k_scan_down(const int* in, int* out, long long n_max, const int*
   for (int it = 0; it < kScanItems; ++it) {
     int idx = it * kScanThreads + threadIdx.x;
     long long e = base + idx;
-    tile[idx] = e < n ? in[e] : 0;
+    tile[padded(idx)] = e < n ? in[e] : 0;
   }
   __syncthreads();
   int v[kScanItems];
   int s = 0;
 #pragma unroll
   for (int q = 0; q < kScanItems; ++q) {
-    v[q] = tile[threadIdx.x * kScanItems + q];
+    v[q] = tile[padded(threadIdx.x * kScanItems + q)];
     s += v[q];
   }
   int tot;
   int run = block_excl_scan(s, sh, &tot) + partial[blockIdx.x];
 #pragma unroll
   for (int q = 0; q < kScanItems; ++q) {
-    tile[threadIdx.x * kScanItems + q] = run;
+    tile[padded(threadIdx.x * kScanItems + q)] = run;
     run += v[q];
   }
   __syncthreads();
   for (int it = 0; it < kScanItems; ++it) {
     int idx = it * kScanThreads + threadIdx.x;
     long long e = base + idx;
-    if (e < n) out[e] = tile[idx];
+    if (e < n) out[e] = tile[padded(idx)];
   }
 }
 
