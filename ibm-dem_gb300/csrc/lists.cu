@@ -118,15 +118,27 @@ __device__ inline unsigned local_mask(const Recs& R, const Geom& g, int m) {
   return image_mask(g, a, b, c);
 }
 
+// a warp's image count per class into wc[0..kClasses) (lane 0 writes); only the
+// classes some lane of the warp has are balloted (most warps have none).
+// Returns the union of the lanes' class masks.
+__device__ inline unsigned warp_class_counts(unsigned mask, int lane, int* wc) {
+  const unsigned wmask = __reduce_or_sync(0xffffffffu, mask);
+  if (lane < kClasses) wc[lane] = 0;
+  __syncwarp();
+  for (unsigned rest = wmask; rest; rest &= rest - 1u) {
+    const int c = __ffs(rest) - 1;
+    const unsigned bal = __ballot_sync(0xffffffffu, (mask >> c) & 1u);
+    if (lane == 0) wc[c] = __popc(bal);
+  }
+  return wmask;
+}
+
 __global__ void k_img_count(Recs R, Geom g, const Counters* cnt, int* blockCls, long long nb) {
   __shared__ int wc[kBlock / 32][kClasses];
   int m = blockIdx.x * blockDim.x + threadIdx.x;
   unsigned mask = m < cnt->npLocal ? local_mask(R, g, m) : 0u;
   int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int c = 0; c < kClasses; ++c) {
-    unsigned bal = __ballot_sync(0xffffffffu, (mask >> c) & 1u);
-    if (lane == 0) wc[warp][c] = __popc(bal);
-  }
+  warp_class_counts(mask, lane, wc[warp]);
   __syncthreads();
   if (threadIdx.x < kClasses) {
     int s = 0;
@@ -143,12 +155,7 @@ __global__ void k_img_emit(Recs R, Geom g, Counters* cnt, const int* offs, long 
   unsigned mask = m < npLocal ? local_mask(R, g, m) : 0u;
   int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   unsigned lt = (1u << lane) - 1u;
-  int rank[kClasses];
-  for (int c = 0; c < kClasses; ++c) {
-    unsigned bal = __ballot_sync(0xffffffffu, (mask >> c) & 1u);
-    rank[c] = __popc(bal & lt);
-    if (lane == 0) wc[warp][c] = __popc(bal);
-  }
+  const unsigned wmask = warp_class_counts(mask, lane, wc[warp]);
   __syncthreads();
   if (threadIdx.x < kClasses) {
     int run = 0;
@@ -159,11 +166,13 @@ __global__ void k_img_emit(Recs R, Geom g, Counters* cnt, const int* offs, long 
     }
   }
   __syncthreads();
-  if (!mask) return;
+  if (!wmask) return;  // the whole warp: no images
   const int cap = R.cap;
-  for (int c = 0; c < kClasses; ++c) {
+  for (unsigned rest = wmask; rest; rest &= rest - 1u) {
+    const int c = __ffs(rest) - 1;
+    const unsigned bal = __ballot_sync(0xffffffffu, (mask >> c) & 1u);
     if (!((mask >> c) & 1u)) continue;
-    int pos = offs[(long long)c * nb + blockIdx.x] + wc[warp][c] + rank[c];
+    int pos = offs[(long long)c * nb + blockIdx.x] + wc[warp][c] + __popc(bal & lt);
     int e = npLocal + pos;
     if (pos >= capImg || e >= cap) {
       set_err(cnt, E_IMGCAP, e);
