@@ -32,7 +32,6 @@ struct Ctx {
   int cur = 0;
   Recs rec() const { return Recs{recD[cur], recI[cur], cap}; }
   Recs recAlt() const { return Recs{recD[cur ^ 1], recI[cur ^ 1], cap}; }
-  void swap_recs() { cur ^= 1; }
 
   int* imgSrc = nullptr;    // [capImg] root local of each image
   int* imgShift = nullptr;  // [capImg] 2-bit shift code per axis

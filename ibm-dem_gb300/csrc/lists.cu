@@ -26,18 +26,43 @@ __global__ void k_compress_flags(Recs R, Geom g, const Counters* cnt, int* flag)
   flag[e] = interior(g, a, b, c) ? 1 : 0;
 }
 
-__global__ void k_compress_gather(Recs A, Recs B, Geom g, const Counters* cnt, const int* flag, const int* pos) {
-  int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= cnt->np || !flag[e]) return;
-  int n = pos[e];
+// The compaction runs in place.  A kept parcel whose slot does not change (all
+// the locals, unless one left the interior) only gets its cell index; the
+// others -- kept parcels behind a dropped one -- go to their new slot through
+// the spare record set in two passes (a new slot can hold a parcel that moves
+// too).  No kept parcel that stays is a destination: a parcel stays only when
+// every parcel before it is kept, and then every later kept parcel lands after it.
+__device__ inline void set_cell(Recs R, const Geom& g, int n) {
+  int a = cell_of(g, 0, R.D(D_X, n));
+  int b = cell_of(g, 1, R.D(D_X + 1, n));
+  int c = cell_of(g, 2, R.D(D_X + 2, n));
+  R.I(I_CELL, n) = cell_id(g, a, b, c);
+}
+
+__device__ inline void copy_record(Recs A, int e, Recs B, int n) {
 #pragma unroll
   for (int f = 0; f < ND; ++f) B.D(f, n) = A.D(f, e);
   B.I(I_GIDX, n) = A.I(I_GIDX, e);
   B.I(I_MSIDX, n) = A.I(I_MSIDX, e);
-  int a = cell_of(g, 0, B.D(D_X, n));
-  int b = cell_of(g, 1, B.D(D_X + 1, n));
-  int c = cell_of(g, 2, B.D(D_X + 2, n));
-  B.I(I_CELL, n) = cell_id(g, a, b, c);
+}
+
+__global__ void k_compress_move(Recs A, Recs B, Geom g, const Counters* cnt, const int* flag, const int* pos) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= cnt->np || !flag[e]) return;
+  const int n = pos[e];
+  if (n == e)
+    set_cell(A, g, e);
+  else
+    copy_record(A, e, B, n);
+}
+
+__global__ void k_compress_back(Recs A, Recs B, Geom g, const Counters* cnt, const int* flag, const int* pos) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= cnt->np || !flag[e]) return;
+  const int n = pos[e];
+  if (n == e) return;
+  copy_record(B, n, A, n);
+  set_cell(A, g, n);
 }
 
 __global__ void k_set_local_counts(Counters* cnt, const int* total) {
@@ -302,10 +327,10 @@ void rebuild_cell_lists(Ctx& c) {
   // CompressDEM: keep parcels (locals and images) whose cell is interior
   k_compress_flags<<<nblocks(c.cap), kBlock, 0, s>>>(c.rec(), c.g, c.dCnt, c.iTmpA);
   scan_exclusive(c.iTmpA, c.iTmpB, c.cap, &c.dCnt->np, c.dTotal, c.scanScratch, s, &c.launches);
-  k_compress_gather<<<nblocks(c.cap), kBlock, 0, s>>>(c.rec(), c.recAlt(), c.g, c.dCnt, c.iTmpA, c.iTmpB);
-  c.swap_recs();
+  k_compress_move<<<nblocks(c.cap), kBlock, 0, s>>>(c.rec(), c.recAlt(), c.g, c.dCnt, c.iTmpA, c.iTmpB);
+  k_compress_back<<<nblocks(c.cap), kBlock, 0, s>>>(c.rec(), c.recAlt(), c.g, c.dCnt, c.iTmpA, c.iTmpB);
   k_set_local_counts<<<1, 1, 0, s>>>(c.dCnt, c.dTotal);
-  c.launches += 3;
+  c.launches += 4;
   // periodic images, class-major in the face-loop order
   long long nbl = nblocks(c.capLocal);
   k_img_count<<<(unsigned)nbl, kBlock, 0, s>>>(c.rec(), c.g, c.dCnt, c.iTmpA, nbl);
