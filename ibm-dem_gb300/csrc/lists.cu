@@ -280,7 +280,12 @@ __global__ void k_img_update(Recs R, Geom g, const Counters* cnt, const int* img
 }
 
 // ---- cell and body lists -----------------------------------------------------
-__global__ void k_cell_keys(Recs R, Geom g, Counters* cnt, uint32_t* keys, uint32_t* vals, int* cellCount) {
+// The cell lists (npPartInCell / partIdxInCell) without a sort: a parcel takes
+// a slot in its cell from the count's atomic, the exclusive scan of the counts
+// gives the cells' starts, the parcels scatter to start + slot, and the parcel
+// that took slot 0 puts its cell's few items back in part order -- the order a
+// stable sort by cell gives.
+__global__ void k_cell_keys(Recs R, Geom g, Counters* cnt, uint32_t* cellOf, int* slot, int* cellCount) {
   int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= cnt->np) return;
   int id = R.I(I_CELL, e);
@@ -288,9 +293,40 @@ __global__ void k_cell_keys(Recs R, Geom g, Counters* cnt, uint32_t* keys, uint3
     set_err(cnt, E_RANGE, e);
     id = 1;
   }
-  keys[e] = (uint32_t)(id - 1);
-  vals[e] = (uint32_t)e;
-  atomicAdd(&cellCount[id - 1], 1);
+  cellOf[e] = (uint32_t)(id - 1);
+  slot[e] = atomicAdd(&cellCount[id - 1], 1);
+}
+
+__global__ void k_cell_scatter(const Counters* cnt, const uint32_t* __restrict__ cellOf, const int* __restrict__ slot,
+                               const int* __restrict__ cellStart, int* cellItems) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= cnt->np) return;
+  cellItems[cellStart[cellOf[e]] + slot[e]] = e;
+}
+
+// Shell sort (Ciura's gaps) of a cell's items: an insertion sort for the usual
+// handful, and no quadratic cost for a cell that holds very many parcels
+__global__ void k_cell_order(const Counters* cnt, const uint32_t* __restrict__ cellOf, const int* __restrict__ slot,
+                             const int* __restrict__ cellStart, int* cellItems) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= cnt->np || slot[e] != 0) return;
+  const uint32_t c = cellOf[e];
+  const int s = cellStart[c], n = cellStart[c + 1] - s;
+  if (n < 2) return;
+  int* a = cellItems + s;
+  constexpr int kGaps[8] = {701, 301, 132, 57, 23, 10, 4, 1};
+  for (int gi = 0; gi < 8; ++gi) {
+    const int gap = kGaps[gi];
+    for (int i = gap; i < n; ++i) {
+      const int v = a[i];
+      int j = i;
+      while (j >= gap && a[j - gap] > v) {
+        a[j] = a[j - gap];
+        j -= gap;
+      }
+      a[j] = v;
+    }
+  }
 }
 
 __global__ void k_body_keys(Recs R, Counters* cnt, int nMS, uint32_t* keys, uint32_t* vals, int* bodyCount) {
@@ -341,15 +377,15 @@ void rebuild_cell_lists(Ctx& c) {
   c.launches += 3;
   // cell lists: stable sort of part indices by cell (npPartInCell/partIdxInCell)
   cudaMemsetAsync(c.cellStart, 0, sizeof(int) * (c.g.ncell + 1), s);
-  k_cell_keys<<<nblocks(c.cap), kBlock, 0, s>>>(c.rec(), c.g, c.dCnt, c.kA, c.vA, c.cellStart);
+  k_cell_keys<<<nblocks(c.cap), kBlock, 0, s>>>(c.rec(), c.g, c.dCnt, c.kA, c.iTmpA, c.cellStart);
   c.launches++;
-  c.planReady = false;  // the sort buffers hold the plan; it is rebuilt after new weights
-  uint32_t *k0 = c.kA, *v0 = c.vA, *k1 = c.kB, *v1 = c.vB;
-  radix_sort_pairs(k0, v0, k1, v1, c.cap, &c.dCnt->np, bits_for(c.g.ncell), c.sortHist, c.scanScratch, s,
-                   &c.launches);
-  cudaMemcpyAsync(c.cellItems, v0, sizeof(int) * c.cap, cudaMemcpyDeviceToDevice, s);
+  c.planReady = false;  // the plan is rebuilt after new weights
   scan_exclusive(c.cellStart, c.cellStart, c.g.ncell, nullptr, c.cellStart + c.g.ncell, c.scanScratch, s,
                  &c.launches);
+  k_cell_scatter<<<nblocks(c.cap), kBlock, 0, s>>>(c.dCnt, c.kA, c.iTmpA, c.cellStart, c.cellItems);
+  k_cell_order<<<nblocks(c.cap), kBlock, 0, s>>>(c.dCnt, c.kA, c.iTmpA, c.cellStart, c.cellItems);
+  c.launches += 2;
+  uint32_t *k0, *v0, *k1, *v1;
   // body lists for AssembleLocalForceMS: locals grouped by body in part order
   if (c.nMS > 0) {
     cudaMemsetAsync(c.bodyStart, 0, sizeof(int) * (c.nMS + 1), s);
