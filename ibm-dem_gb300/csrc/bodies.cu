@@ -24,7 +24,9 @@ namespace {
 // One warp per body.  The 32 lanes evaluate the per-parcel terms of a batch of
 // 32 parcels in parallel (each term is formed exactly as in the reference);
 // lanes 0..11 then fold one sum component each over the batch in part order.
-constexpr int kSumWarps = 8;
+// One warp per block: the few hundred to few thousand body pairs then spread
+// over all SMs.
+constexpr int kSumWarps = 1;
 __global__ void __launch_bounds__(kSumWarps * 32) k_body_sums(Recs R, Geom g, ibmdem_multisphere* B, int nMS,
                                                               const int* __restrict__ bodyStart,
                                                               const int* __restrict__ bodyItems) {
