@@ -231,7 +231,7 @@ void for_each_parcel_buffer(Ctx& c, F&& f) {
   long long scanInts = std::max({scan_scratch_ints(c.capRuns + 1), scan_scratch_ints(sort_hist_ints(std::max<long long>(c.cap, c.capRuns))),
                                  scan_scratch_ints(c.g.ncell + 1), scan_scratch_ints(26ll * nblocks(c.capLocal)),
                                  scan_scratch_ints(nblocks((3 * c.g.nint + 15) / 16))});
-  tmpInts = std::max<long long>(tmpInts, nblocks((3 * c.g.nint + 15) / 16) + 1);
+  tmpInts = std::max<long long>(tmpInts, nblocks((3 * c.g.nint + 127) / 128) + 1);
   f(c.recD[0], (size_t)ND * c.cap);
   f(c.recD[1], (size_t)ND * c.cap);
   f(c.recI[0], (size_t)NI * c.cap);
@@ -248,7 +248,7 @@ void for_each_parcel_buffer(Ctx& c, F&& f) {
   f(c.vA, (size_t)c.cap);
   f(c.kB, (size_t)c.cap);
   f(c.vB, (size_t)c.cap);
-  f(c.touch, (size_t)(((3 * c.g.nint + 15) / 16) * 16));
+  f(c.touch, (size_t)(((3 * c.g.nint + 127) / 128) * 16));  // one bit per node, whole uint4s
   f(c.planRoot, (size_t)c.capContrib);
   f(c.planW, (size_t)c.capContrib);
   f(c.planAlloc, (size_t)1);

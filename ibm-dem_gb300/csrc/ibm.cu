@@ -164,35 +164,37 @@ __device__ inline void window_start(const int4& wn, int comp, int& sx, int& sy, 
 
 // mark the interior nodes touched by any parcel window; the windows are read in
 // cell order, so that a warp's stores fall on neighbouring nodes
-__global__ void k_touch(Geom g, const Counters* cnt, const int4* winC, uint8_t* flags) {
+__global__ void k_touch(Geom g, const Counters* cnt, const int4* winC, unsigned* flags) {
   int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= cnt->np) return;
   int4 wn = winC[e];
   for (int comp = 0; comp < 3; ++comp) {
     int sx, sy, sz;
     window_start(wn, comp, sx, sy, sz);
+    // the window's interior nodes along x: bits ilo..ihi of each row it covers
+    const int ilo = max(sx, 1), ihi = min(sx + 2, g.n[0]);
+    if (ihi < ilo) continue;
+    const unsigned run = (1u << (ihi - ilo + 1)) - 1u;
     for (int kz = 0; kz < 3; ++kz)
-      for (int ky = 0; ky < 3; ++ky)
-        for (int kx = 0; kx < 3; ++kx) {
-          int i = sx + kx, j = sy + ky, k = sz + kz;
-          if (!interior(g, i, j, k)) continue;
-          long long node = ((long long)(k - 1) * g.n[1] + (j - 1)) * g.n[0] + (i - 1);
-          flags[comp * g.nint + node] = 1;
-        }
+      for (int ky = 0; ky < 3; ++ky) {
+        const int j = sy + ky, k = sz + kz;
+        if (j < 1 || j > g.n[1] || k < 1 || k > g.n[2]) continue;
+        const long long b0 = comp * g.nint + ((long long)(k - 1) * g.n[1] + (j - 1)) * g.n[0] + (ilo - 1);
+        const int sh = (int)(b0 & 31);
+        atomicOr(&flags[b0 >> 5], run << sh);
+        if (sh + (ihi - ilo + 1) > 32) atomicOr(&flags[(b0 >> 5) + 1], run >> (32 - sh));
+      }
   }
 }
 
-// compaction of the byte flags into the sorted node-key list (16 flags per thread)
-__device__ inline int nz_bytes(uint32_t w) {
-  return ((w & 0xffu) != 0) + ((w & 0xff00u) != 0) + ((w & 0xff0000u) != 0) + ((w & 0xff000000u) != 0);
-}
+// compaction of the flag bits into the sorted node-key list (128 flags per thread)
 __global__ void k_flag_count(const uint4* flags, long long nvec, int* blockCnt) {
   __shared__ int sh[kBlock / 32];
   long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   int c = 0;
   if (v < nvec) {
     uint4 q = flags[v];
-    c = nz_bytes(q.x) + nz_bytes(q.y) + nz_bytes(q.z) + nz_bytes(q.w);
+    c = __popc(q.x) + __popc(q.y) + __popc(q.z) + __popc(q.w);
   }
   for (int o = 16; o; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
   if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = c;
@@ -212,7 +214,7 @@ __global__ void k_flag_emit(const uint4* flags, long long nvec, long long nflags
     uint4 q = flags[v];
     w4[0] = q.x; w4[1] = q.y; w4[2] = q.z; w4[3] = q.w;
   }
-  int c = nz_bytes(w4[0]) + nz_bytes(w4[1]) + nz_bytes(w4[2]) + nz_bytes(w4[3]);
+  int c = __popc(w4[0]) + __popc(w4[1]) + __popc(w4[2]) + __popc(w4[3]);
   // exclusive prefix of c over the block
   int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   int x = c;
@@ -225,12 +227,17 @@ __global__ void k_flag_emit(const uint4* flags, long long nvec, long long nflags
   int base = blockOff[blockIdx.x];
   for (int w = 0; w < warp; ++w) base += sh[w];
   int pos = base + x - c;
-  long long f0 = v * 16;
-  for (int q = 0; q < 16; ++q) {
-    uint32_t byte = (w4[q >> 2] >> (8 * (q & 3))) & 0xffu;
-    if (byte && f0 + q < nflags) {
-      if (pos < capRuns) keys[pos] = (uint32_t)(f0 + q);
-      ++pos;
+  const long long f0 = v * 128;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    uint32_t w = w4[q];
+    while (w) {
+      const long long f = f0 + 32 * q + (__ffs(w) - 1);
+      w &= w - 1u;
+      if (f < nflags) {
+        if (pos < capRuns) keys[pos] = (uint32_t)f;
+        ++pos;
+      }
     }
   }
 }
@@ -916,10 +923,10 @@ void launch_weights(Ctx& c, bool locals) {
 // touched-node flags, their per-block counts (iTmpA, scanned) and the total (dTotal)
 static void flag_touched_nodes(Ctx& c) {
   cudaStream_t s = c.stream;
-  const long long nvec = (3 * c.g.nint + 15) / 16;
+  const long long nvec = (3 * c.g.nint + 127) / 128;
   cudaMemsetAsync(c.touch, 0, nvec * 16, s);
   k_win_by_cell<<<nblocks(c.cap), kBlock, 0, s>>>(c.dCnt, c.cellItems, c.win, c.winC);
-  k_touch<<<nblocks(c.cap), kBlock, 0, s>>>(c.g, c.dCnt, c.winC, c.touch);
+  k_touch<<<nblocks(c.cap), kBlock, 0, s>>>(c.g, c.dCnt, c.winC, reinterpret_cast<unsigned*>(c.touch));
   const long long nb = nblocks(nvec);
   k_flag_count<<<(unsigned)nb, kBlock, 0, s>>>(reinterpret_cast<const uint4*>(c.touch), nvec, c.iTmpA);
   scan_exclusive(c.iTmpA, c.iTmpA, nb, nullptr, c.dTotal, c.scanScratch, s, &c.launches);
@@ -949,7 +956,7 @@ static int run_blocks(const Ctx& c) {
 void build_spread_plan(Ctx& c) {
   cudaStream_t s = c.stream;
   const long long nflags = 3 * c.g.nint;
-  const long long nvec = (nflags + 15) / 16;
+  const long long nvec = (nflags + 127) / 128;
   flag_touched_nodes(c);
   const uint4* fv4 = reinterpret_cast<const uint4*>(c.touch);
   const long long nb = nblocks(nvec);

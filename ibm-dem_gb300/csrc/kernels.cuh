@@ -81,7 +81,7 @@ struct Ctx {
   int4* winC = nullptr;    // [cap] the same, in cell-list order (spread plan)
   int* cntInt = nullptr;   // [cap] interior contributions per parcel
   double* fv = nullptr;    // [3*cap] fdrag*vol of locals
-  uint8_t* touch = nullptr;      // [3*nint rounded to 16] touched-node flags
+  uint8_t* touch = nullptr;      // touched-node flags: one bit per node, 3*nint rounded up to 128 bits
   uint32_t* planRoot = nullptr;  // [capContrib] contributing root parcel, node-major, part order
   double* planW = nullptr;       // [capContrib] its delta weight
   int* runCnt = nullptr;         // [capRuns] contributions per touched node
