@@ -172,7 +172,7 @@ __global__ void k_img_count(Recs R, Geom g, const Counters* cnt, int* blockCls, 
   }
 }
 
-__global__ void k_img_emit(Recs R, Geom g, Counters* cnt, const int* offs, long long nb, int* imgSrc,
+__global__ void __launch_bounds__(kBlock, 4) k_img_emit(Recs R, Geom g, Counters* cnt, const int* offs, long long nb, int* imgSrc,
                            int* imgShift, int capImg) {
   __shared__ int wc[kBlock / 32][kClasses];
   int m = blockIdx.x * blockDim.x + threadIdx.x;
@@ -206,7 +206,7 @@ __global__ void k_img_emit(Recs R, Geom g, Counters* cnt, const int* offs, long 
     int fx, fy, fz;
     class_shift(c, fx, fy, fz);
     int sh[3] = {fx, fy, fz};
-#pragma unroll
+#pragma unroll 2
     for (int f = 0; f < ND; ++f) R.D(f, e) = R.D(f, m);
     R.I(I_GIDX, e) = R.I(I_GIDX, m);
     R.I(I_MSIDX, e) = R.I(I_MSIDX, m);
