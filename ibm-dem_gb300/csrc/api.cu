@@ -492,6 +492,9 @@ int ibmdem_destroy(ibmdem_ctx* h) {
   }
   for (cudaEvent_t e : c.evFree) cudaEventDestroy(e);
   if (c.fieldsRead) cudaEventDestroy(c.fieldsRead);
+  if (c.upStart) cudaEventDestroy(c.upStart);
+  if (c.upDone) cudaEventDestroy(c.upDone);
+  if (c.upStream) cudaStreamDestroy(c.upStream);
   delete h;
   return IBMDEM_OK;
 }
@@ -529,6 +532,8 @@ int ibmdem_synchronize(ibmdem_ctx* h) {
   return check_device(h);
 }
 
+static int ensure_plan(ibmdem_ctx* h);
+
 int ibmdem_set_fluid(ibmdem_ctx* h, const double* u, const double* v, const double* w) {
   CHECK_CTX();
   if (!u || !v || !w) return set_error(h, IBMDEM_EINVAL, "null field");
@@ -538,9 +543,32 @@ int ibmdem_set_fluid(ibmdem_ctx* h, const double* u, const double* v, const doub
   int ru = fluid_update_join(c);
   if (ru) return ru;
   size_t nb = sizeof(double) * (size_t)c.g.ncell;
-  CU(cudaMemcpyAsync(c.u, u, nb, cudaMemcpyHostToDevice, c.stream));
-  CU(cudaMemcpyAsync(c.v, v, nb, cudaMemcpyHostToDevice, c.stream));
-  CU(cudaMemcpyAsync(c.w, w, nb, cudaMemcpyHostToDevice, c.stream));
+  // With the weights of a new parcel state and no plan for them yet, the
+  // spread plan (which does not read the fluid) is built on the context's
+  // stream while the fields upload on a second one.
+  const bool planBeside = c.weightsLocal && c.weightsGhost && !c.planReady;
+  cudaStream_t up = c.stream;
+  if (planBeside) {
+    if (!c.upStream) CU(cudaStreamCreateWithFlags(&c.upStream, cudaStreamNonBlocking));
+    if (!c.upStart) CU(cudaEventCreateWithFlags(&c.upStart, cudaEventDisableTiming));
+    if (!c.upDone) CU(cudaEventCreateWithFlags(&c.upDone, cudaEventDisableTiming));
+    up = c.upStream;
+    CU(cudaEventRecord(c.upStart, c.stream));  // after all earlier work on the fields
+    CU(cudaStreamWaitEvent(up, c.upStart, 0));
+  }
+  CU(cudaMemcpyAsync(c.u, u, nb, cudaMemcpyHostToDevice, up));
+  CU(cudaMemcpyAsync(c.v, v, nb, cudaMemcpyHostToDevice, up));
+  CU(cudaMemcpyAsync(c.w, w, nb, cudaMemcpyHostToDevice, up));
+  if (planBeside) {
+    CU(cudaEventRecord(c.upDone, up));
+    int rp = ensure_plan(h);
+    // the fields are in place before any later work of the context's stream
+    CU(cudaStreamWaitEvent(c.stream, c.upDone, 0));
+    if (rp) {
+      cudaStreamSynchronize(c.stream);
+      return rp;
+    }
+  }
   CU(cudaMemcpyAsync(c.u0, c.u, nb, cudaMemcpyDeviceToDevice, c.stream));
   CU(cudaMemcpyAsync(c.v0, c.v, nb, cudaMemcpyDeviceToDevice, c.stream));
   CU(cudaMemcpyAsync(c.w0, c.w, nb, cudaMemcpyDeviceToDevice, c.stream));
@@ -768,8 +796,6 @@ int ibmdem_get_collision_lists(ibmdem_ctx* h, int32_t* start, int32_t* idx, int3
   }
   return IBMDEM_OK;
 }
-
-static int ensure_plan(ibmdem_ctx* h);
 
 int ibmdem_get_counters(ibmdem_ctx* h, int64_t* out, int32_t n) {
   CHECK_CTX();

@@ -117,6 +117,10 @@ struct Ctx {
   cudaEvent_t fieldsRead = nullptr;
   bool fieldsReadPending = false;
 
+  // ibmdem_set_fluid: the uploads on their own stream, beside a spread plan build
+  cudaStream_t upStream = nullptr;
+  cudaEvent_t upStart = nullptr, upDone = nullptr;
+
   // state flags
   bool haveFluid = false, haveParcels = false, listsBuilt = false;
   bool weightsLocal = false, weightsGhost = false, planReady = false;

@@ -114,7 +114,10 @@ int ibmdem_synchronize(ibmdem_ctx* ctx);
 /* Fluid velocity u,v,w in the reference layout: Fortran order
  * (lg1:ug1, lg2:ug2, lg3:ug3), i fastest, 2-cell halo (vars.F90:44,
  * allocate.F90:16-18): (nx+4)*(ny+4)*(nz+4) doubles each.  Also stored as the
- * frozen field that ibmdem_step() restores at the start of every step. */
+ * frozen field that ibmdem_step() restores at the start of every step.
+ * Returns when the copies are done.  When the parcels moved since the last
+ * spread (new weights), the spread plan for them is built while the fields
+ * upload, on a second stream of the same device. */
 int ibmdem_set_fluid(ibmdem_ctx* ctx, const double* u, const double* v, const double* w);
 /* Copy out u,v,w and the momentum source fx,fy,fz (vars.F90:63), same layout.
  * Any pointer may be NULL. */
