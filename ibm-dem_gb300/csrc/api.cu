@@ -477,6 +477,7 @@ int ibmdem_destroy(ibmdem_ctx* h) {
   cudaSetDevice(c.device);
   output_release(c);
   fluid_update_release(c);
+  fluid_release(c);
   cudaStreamSynchronize(c.stream);
   free_parcel_buffers(c);
   void* ps[] = {c.u, c.v, c.w, c.u0, c.v0, c.w0, c.fx, c.fy, c.fz, c.cellStart, c.dCnt, c.dTotal, c.dBodies,

@@ -117,6 +117,14 @@ struct Ctx {
   cudaEvent_t fieldsRead = nullptr;
   bool fieldsReadPending = false;
 
+  // fluid stencils (fluid.cu): the fields beyond u,v,w,fx,fy,fz (indexed by
+  // IBMDEM_FLUID_*, allocated on first use), the guess's output (3 fields), the
+  // ordered partial sums of ModifyBulkVelocity, and VelocityGuess's parameters
+  double* ffield[IBMDEM_FLUID_NFIELDS] = {};
+  double* fnew = nullptr;
+  double* fsum = nullptr;
+  double visc = 0.0, CPx = 0.0, CPy = 0.0, CPz = 0.0;
+
   // ibmdem_set_fluid: the uploads on their own stream, beside a spread plan build
   cudaStream_t upStream = nullptr;
   cudaEvent_t upStart = nullptr, upDone = nullptr;
@@ -167,6 +175,8 @@ void record_written_nodes(Ctx& c);
 cudaError_t interpolate_points_noalloc(Ctx& c, int n, const double* x, double* ulp, int* bad);
 // output.cu: wait for the writer thread and free the snapshot buffers
 void output_release(Ctx& c);
+// fluid.cu: free the fluid stencils' fields
+void fluid_release(Ctx& c);
 // readout.cu: finish a pending sparse read-out (its status), and free its buffers
 int fluid_update_join(Ctx& c);
 void fluid_update_release(Ctx& c);

@@ -44,6 +44,9 @@ EXPORTS = [
     "ibmdem_unresolved_step", "ibmdem_unresolved_synchronize", "ibmdem_unresolved_launch_count",
     "ibmdem_CalculateDragForce", "ibmdem_unresolved_timing_enable", "ibmdem_unresolved_get_timing",
     "ibmdem_unresolved_phase_name", "ibmdem_get_fluid_async",
+    "ibmdem_set_fluid_params", "ibmdem_set_fluid_field", "ibmdem_get_fluid_field", "ibmdem_StoreOldVelocity",
+    "ibmdem_VelocityGuess", "ibmdem_FillGhostRegionForFluid", "ibmdem_Boundary", "ibmdem_ModifyBulkVelocity",
+    "ibmdem_VelocityDivergence", "ibmdem_PressureCorrection", "ibmdem_VelocityCorrection",
 ]
 
 SUBROUTINES = [
@@ -88,6 +91,17 @@ def load(path=LIB_PATH):
     lib.ibmdem_launch_count.argtypes = [vp]
     lib.ibmdem_step.argtypes = [vp, i32]
     lib.ibmdem_interpolate_velocity_noalloc.argtypes = [vp, i32, vp, vp]
+    d = ctypes.c_double
+    lib.ibmdem_set_fluid_params.argtypes = [vp, d, d, d, d]
+    lib.ibmdem_set_fluid_field.argtypes = [vp, i32, vp]
+    lib.ibmdem_get_fluid_field.argtypes = [vp, i32, vp]
+    for name in ("StoreOldVelocity", "FillGhostRegionForFluid", "Boundary"):
+        getattr(lib, "ibmdem_" + name).argtypes = [vp]
+    lib.ibmdem_VelocityGuess.argtypes = [vp, d, d, d]
+    lib.ibmdem_VelocityDivergence.argtypes = [vp, d]
+    lib.ibmdem_VelocityCorrection.argtypes = [vp, d]
+    lib.ibmdem_PressureCorrection.argtypes = [vp, vp]
+    lib.ibmdem_ModifyBulkVelocity.argtypes = [vp, i32, i32, i32, d, d, d]
     lib.ibmdem_timing_enable.argtypes = [vp, i32]
     lib.ibmdem_get_timing.argtypes = [vp, vp, vp, i32, i32]
     lib.ibmdem_phase_name.restype = ctypes.c_char_p
@@ -265,6 +279,50 @@ class Case:
         self._chk(self.lib.ibmdem_get_collision_lists(self.h, start.ctypes.data, idx.ctypes.data, ctypes.byref(nl),
                                                       ctypes.byref(npairs)), "pairs")
         return start, idx
+
+    # ---- fluid stencils (ibmdem_VelocityGuess and the others) ----------------
+    def set_fluid_params(self, visc, CPx=0.0, CPy=0.0, CPz=0.0):
+        self._chk(self.lib.ibmdem_set_fluid_params(self.h, visc, CPx, CPy, CPz), "set_fluid_params")
+
+    def set_fluid_field(self, which, a):
+        """One field of records.FLUID_FIELDS (name or IBMDEM_FLUID_* number)."""
+        which = records.FLUID[which] if isinstance(which, str) else int(which)
+        a = np.ascontiguousarray(a, dtype=np.float64).reshape(self.shape)
+        self._chk(self.lib.ibmdem_set_fluid_field(self.h, which, a.ctypes.data), "set_fluid_field")
+
+    def get_fluid_field(self, which):
+        which = records.FLUID[which] if isinstance(which, str) else int(which)
+        out = np.empty(self.shape)
+        self._chk(self.lib.ibmdem_get_fluid_field(self.h, which, out.ctypes.data), "get_fluid_field")
+        return out
+
+    def StoreOldVelocity(self):
+        self._chk(self.lib.ibmdem_StoreOldVelocity(self.h), "StoreOldVelocity")
+
+    def VelocityGuess(self, aRK, bRK, cRK):
+        self._chk(self.lib.ibmdem_VelocityGuess(self.h, aRK, bRK, cRK), "VelocityGuess")
+
+    def FillGhostRegionForFluid(self):
+        self._chk(self.lib.ibmdem_FillGhostRegionForFluid(self.h), "FillGhostRegionForFluid")
+
+    def Boundary(self):
+        self._chk(self.lib.ibmdem_Boundary(self.h), "Boundary")
+
+    def ModifyBulkVelocity(self, swU, swV, swW, bulkU, bulkV, bulkW):
+        self._chk(self.lib.ibmdem_ModifyBulkVelocity(self.h, swU, swV, swW, bulkU, bulkV, bulkW), "ModifyBulkVelocity")
+
+    def VelocityDivergence(self, cRK):
+        self._chk(self.lib.ibmdem_VelocityDivergence(self.h, cRK), "VelocityDivergence")
+
+    def PressureCorrection(self, Pcorr=None):
+        ptr = None
+        if Pcorr is not None:
+            Pcorr = np.ascontiguousarray(Pcorr, dtype=np.float64).reshape(self.shape)
+            ptr = Pcorr.ctypes.data
+        self._chk(self.lib.ibmdem_PressureCorrection(self.h, ptr), "PressureCorrection")
+
+    def VelocityCorrection(self, cRK):
+        self._chk(self.lib.ibmdem_VelocityCorrection(self.h, cRK), "VelocityCorrection")
 
     def set_wall_probes(self, probes):
         """Wall collision probes (records.WALL_PROBE) on solid-wall faces."""

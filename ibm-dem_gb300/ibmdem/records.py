@@ -61,6 +61,12 @@ def make_params(nx, ny, nz, h=1.0, dt=1e-3, coupleInterval=1, Ns=5, rhof=1e3, kn
     return p
 
 
+# fields of the fluid stencils (IBMDEM_FLUID_* of include/ibmdem.h)
+FLUID_FIELDS = ["u", "v", "w", "fx", "fy", "fz", "uold", "vold", "wold", "P", "Pcorr", "velDiv",
+                "Px", "Py", "Pz", "RHSul", "RHSvl", "RHSwl", "omegaX", "omegaY", "omegaZ"]
+FLUID = {name: i for i, name in enumerate(FLUID_FIELDS)}
+
+
 def field_shape(p):
     """(nk, nj, ni) C-order view of a Fortran (lg1:ug1, lg2:ug2, lg3:ug3) array."""
     return (int(p["nz"]) + 4, int(p["ny"]) + 4, int(p["nx"]) + 4)

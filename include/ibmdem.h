@@ -403,6 +403,57 @@ int ibmdem_output_async(ibmdem_ctx* ctx, const char* tecplot_path, const char* p
 /* Wait for the files of the last ibmdem_output_async; its status. */
 int ibmdem_output_wait(ibmdem_ctx* ctx);
 
+/* ---- fluid stencils (fluid.F90:2-249, boundary.F90:122-247) ----------- */
+/* The fluid step of FirstOrderForwardEuler (fluid.F90:251-326) around the
+ * Poisson solve, on the context's fields: the particle side's u,v,w and
+ * fx,fy,fz and the fields below, all in the layout of ibmdem_set_fluid.  The
+ * Poisson solve itself (SetPressureVector, PoissonSolver: PETSc) stays with
+ * the caller: it reads the velocity divergence and hands back Pcorr. */
+enum {
+  IBMDEM_FLUID_U = 0, IBMDEM_FLUID_V, IBMDEM_FLUID_W,
+  IBMDEM_FLUID_FX, IBMDEM_FLUID_FY, IBMDEM_FLUID_FZ,
+  IBMDEM_FLUID_UOLD, IBMDEM_FLUID_VOLD, IBMDEM_FLUID_WOLD,
+  IBMDEM_FLUID_P, IBMDEM_FLUID_PCORR, IBMDEM_FLUID_VELDIV,
+  IBMDEM_FLUID_PX, IBMDEM_FLUID_PY, IBMDEM_FLUID_PZ,       /* PressureGradient */
+  IBMDEM_FLUID_RHSUL, IBMDEM_FLUID_RHSVL, IBMDEM_FLUID_RHSWL, /* last RHS (Runge-Kutta) */
+  IBMDEM_FLUID_OMEGAX, IBMDEM_FLUID_OMEGAY, IBMDEM_FLUID_OMEGAZ,
+  IBMDEM_FLUID_NFIELDS
+};
+/* visc (vars.F90:40) and the constant pressure gradient CPx,CPy,CPz
+ * (vars.F90:53) of VelocityGuess's right-hand side. */
+int ibmdem_set_fluid_params(ibmdem_ctx* ctx, double visc, double CPx, double CPy, double CPz);
+/* One field in or out (host arrays of (nx+4)*(ny+4)*(nz+4) doubles). */
+int ibmdem_set_fluid_field(ibmdem_ctx* ctx, int32_t which, const double* a);
+int ibmdem_get_fluid_field(ibmdem_ctx* ctx, int32_t which, double* a);
+/* uold = u; vold = v; wold = w (fluid.F90:257) */
+int ibmdem_StoreOldVelocity(ibmdem_ctx* ctx);
+/* VelocityGuess(aRK,bRK,cRK) (fluid.F90:108-133) with ConvectionTensor,
+ * ViscousTensor and PressureGradient, bit-identical to the reference's
+ * statements; keeps PressureGradient in PX..PZ and the right-hand side in
+ * RHSUL..RHSWL. */
+int ibmdem_VelocityGuess(ibmdem_ctx* ctx, double aRK, double bRK, double cRK);
+/* FillGhostRegionForFluid (boundary.F90:122-147) on one rank for u, v, w, P,
+ * omegaZ and Pcorr: periodic copies, or across a solid wall the mirrored
+ * layers with u,v,w negated (DealWithBoundaryFluid). */
+int ibmdem_FillGhostRegionForFluid(ibmdem_ctx* ctx);
+/* Boundary (fluid.F90:240-249): zero wall-normal velocity on and beyond each
+ * solid wall. */
+int ibmdem_Boundary(ibmdem_ctx* ctx);
+/* ModifyBulkVelocity (fluid.F90:155-195) with the switches and targets of
+ * DefAveBulk{U,V,W}Switch and bulkU,V,W.  The interior sums are formed in a
+ * fixed order of their own (blocks of consecutive nodes, then the blocks in
+ * order), not the reference's single running sum: deterministic, and within
+ * a few ulps of it. */
+int ibmdem_ModifyBulkVelocity(ibmdem_ctx* ctx, int32_t swU, int32_t swV, int32_t swW, double bulkU, double bulkV,
+                              double bulkW);
+/* VelocityDivergence(cRK) (fluid.F90:93-106) into VELDIV. */
+int ibmdem_VelocityDivergence(ibmdem_ctx* ctx, double cRK);
+/* PressureCorrection (fluid.F90:197-208): P = P + Pcorr; Pcorr (host, may be
+ * NULL to use the PCORR field as it stands) is stored as PCORR first. */
+int ibmdem_PressureCorrection(ibmdem_ctx* ctx, const double* Pcorr);
+/* VelocityCorrection(cRK) (fluid.F90:210-237), then the vorticity. */
+int ibmdem_VelocityCorrection(ibmdem_ctx* ctx, double cRK);
+
 /* ---- instrumentation -------------------------------------------------- */
 /* Record CUDA events around every phase of the drivers (interpolation,
  * spreading, weights, spread plan, cell lists, contact lists, contact force,

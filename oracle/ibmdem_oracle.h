@@ -85,6 +85,22 @@ int orc_u_get_volume_fraction(orc_ucase* u, double* alphaf);
 int orc_u_get_contacts(orc_ucase* u, int32_t* start, int32_t* partner, double* xi, int32_t* ncontacts);
 int orc_u_step(orc_ucase* u, int32_t nsteps);
 
+/* fluid stencils (fluid_oracle.c) */
+typedef struct orc_fluid orc_fluid;
+orc_fluid* orc_fluid_create(const ibmdem_params* p);
+void orc_fluid_destroy(orc_fluid* F);
+void orc_fluid_set_params(orc_fluid* F, double visc, double CPx, double CPy, double CPz);
+int orc_fluid_set_field(orc_fluid* F, int which, const double* a);
+int orc_fluid_get_field(orc_fluid* F, int which, double* a);
+void orc_fluid_StoreOldVelocity(orc_fluid* F);
+void orc_fluid_VelocityGuess(orc_fluid* F, double aRK, double bRK, double cRK);
+void orc_fluid_FillGhostRegionForFluid(orc_fluid* F);
+void orc_fluid_Boundary(orc_fluid* F);
+void orc_fluid_ModifyBulkVelocity(orc_fluid* F, int swU, int swV, int swW, double bulkU, double bulkV, double bulkW);
+void orc_fluid_VelocityDivergence(orc_fluid* F, double cRK);
+void orc_fluid_PressureCorrection(orc_fluid* F);
+void orc_fluid_VelocityCorrection(orc_fluid* F, double cRK);
+
 #ifdef __cplusplus
 }
 #endif

@@ -76,6 +76,19 @@ def _load():
     lib.orc_u_get_volume_fraction.argtypes = [vp, vp]
     lib.orc_u_get_contacts.argtypes = [vp, vp, vp, vp, P(i32)]
     lib.orc_u_step.argtypes = [vp, i32]
+    d = ctypes.c_double
+    lib.orc_fluid_create.restype = vp
+    lib.orc_fluid_create.argtypes = [vp]
+    lib.orc_fluid_destroy.argtypes = [vp]
+    lib.orc_fluid_set_params.argtypes = [vp, d, d, d, d]
+    lib.orc_fluid_set_field.argtypes = [vp, ctypes.c_int, vp]
+    lib.orc_fluid_get_field.argtypes = [vp, ctypes.c_int, vp]
+    for name in ("StoreOldVelocity", "FillGhostRegionForFluid", "Boundary", "PressureCorrection"):
+        getattr(lib, "orc_fluid_" + name).argtypes = [vp]
+    lib.orc_fluid_VelocityGuess.argtypes = [vp, d, d, d]
+    lib.orc_fluid_VelocityDivergence.argtypes = [vp, d]
+    lib.orc_fluid_VelocityCorrection.argtypes = [vp, d]
+    lib.orc_fluid_ModifyBulkVelocity.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, d, d, d]
     _lib = lib
     return lib
 
@@ -299,3 +312,72 @@ class OracleUnresolved:
 
     def step(self, n=1):
         self._chk(self.lib.orc_u_step(self.h, int(n)), "step")
+
+
+class OracleFluid:
+    """The fluid stencils of FirstOrderForwardEuler held by the CPU restatement
+    (fluid_oracle.c): fields indexed by the IBMDEM_FLUID_* numbers of
+    include/ibmdem.h (ibmdem.records.FLUID_FIELDS), in the layout of
+    ibmdem_set_fluid."""
+
+    def __init__(self, params):
+        import sys
+        sys.path.insert(0, os.path.join(os.path.dirname(_HERE), "ibm-dem_gb300"))
+        from ibmdem.records import PARAMS, field_shape
+
+        self.lib = _load()
+        self.params = np.array(params, dtype=PARAMS, copy=True)
+        self.h = self.lib.orc_fluid_create(self.params.ctypes.data)
+        if not self.h:
+            raise RuntimeError("orc_fluid_create failed")
+        self.shape = field_shape(self.params)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.orc_fluid_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_fluid_params(self, visc, CPx=0.0, CPy=0.0, CPz=0.0):
+        self.lib.orc_fluid_set_params(self.h, visc, CPx, CPy, CPz)
+
+    def set_field(self, which, a):
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        assert a.size == int(np.prod(self.shape))
+        if self.lib.orc_fluid_set_field(self.h, int(which), a.ctypes.data):
+            raise RuntimeError("orc_fluid_set_field failed")
+
+    def get_field(self, which):
+        out = np.empty(self.shape, np.float64)
+        if self.lib.orc_fluid_get_field(self.h, int(which), out.ctypes.data):
+            raise RuntimeError("orc_fluid_get_field failed")
+        return out
+
+    def StoreOldVelocity(self):
+        self.lib.orc_fluid_StoreOldVelocity(self.h)
+
+    def VelocityGuess(self, aRK, bRK, cRK):
+        self.lib.orc_fluid_VelocityGuess(self.h, aRK, bRK, cRK)
+
+    def FillGhostRegionForFluid(self):
+        self.lib.orc_fluid_FillGhostRegionForFluid(self.h)
+
+    def Boundary(self):
+        self.lib.orc_fluid_Boundary(self.h)
+
+    def ModifyBulkVelocity(self, swU, swV, swW, bulkU, bulkV, bulkW):
+        self.lib.orc_fluid_ModifyBulkVelocity(self.h, swU, swV, swW, bulkU, bulkV, bulkW)
+
+    def VelocityDivergence(self, cRK):
+        self.lib.orc_fluid_VelocityDivergence(self.h, cRK)
+
+    def PressureCorrection(self):
+        self.lib.orc_fluid_PressureCorrection(self.h)
+
+    def VelocityCorrection(self, cRK):
+        self.lib.orc_fluid_VelocityCorrection(self.h, cRK)
