@@ -95,6 +95,8 @@ def parse():
     ap.add_argument("--unresolved-particles", type=int, default=1_048_576,
                     help="particles of the unresolved CFD-DEM case (0 = skip)")
     ap.add_argument("--unresolved-steps", type=int, default=100)
+    ap.add_argument("--fluid-steps", type=int, default=20,
+                    help="steps of the GPU fluid stencils on the default grid (0 = skip)")
     ap.add_argument("--serve-work-limit", type=int, default=2_000_000,
                     help="markers the running requests may hold together (0 = no limit)")
     return ap.parse_args()
@@ -455,6 +457,122 @@ def run_unresolved(args, device, stream, cpu=True):
     return out
 
 
+# algorithmic bytes per interior node of the fluid stencil kernels (FP64 fields
+# streamed once; the stencil neighbours come through L1/L2)
+FLUID_BYTES = {
+    # u,v,w, P, fx..fz, uold..wold, RHSul..wl read; the guess, Px..Pz, RHSul..wl written;
+    # then the guess copied into u,v,w
+    "guess": 13 * 8 + 9 * 8 + 6 * 8,
+    # u,v,w read, velDiv written; P, Pcorr read, P written; u,v,w, P, Px..Pz read and
+    # u,v,w written, then u,v,w read and omega written; the bulk sums and shift
+    "other": 4 * 8 + 3 * 8 + 7 * 8 + 3 * 8 + 6 * 8 + 3 * 8 + 6 * 8,
+}
+# FP64 operations per interior node of VelocityGuess with unit spacing: 18 flux
+# products (2 adds, 3 multiplies), 9 differences, 9 Laplacians (2 adds, 2
+# multiplies), 3 gradients (a subtraction and a division), 3 right-hand sides
+# (7 adds) and 3 updates (7 operations)
+FLUID_GUESS_FP64 = 18 * 5 + 9 + 9 * 4 + 3 * 2 + 3 * 7 + 3 * 7
+
+
+def run_fluid(args, device, stream, cpu=True):
+    """The fluid step of FirstOrderForwardEuler around the Poisson solve on the GPU
+    (fluid.F90:251-326 without SetPressureVector/PoissonSolver): uold = u,
+    VelocityGuess(1,0,1), ModifyBulkVelocity (u and w switched, the reference's
+    initialization), VelocityDivergence, PressureCorrection with a resident
+    Pcorr, VelocityCorrection, each followed by FillGhostRegionForFluid and
+    Boundary, on the default grid with the workload's Fourier field.
+    Device-timed; the CPU restatement times one step on all host threads."""
+    import torch
+    import numpy as np
+    from ibmdem import api
+
+    p, parts, bodies, field = make_case(args.workload, args.seed, "cuda")
+    g = api.Case(p, None, None, field, device=device, stream=stream)
+    g.set_fluid_params(1e-6, 0.0, 0.0, 0.0)
+
+    def halo():
+        g.FillGhostRegionForFluid()
+        g.Boundary()
+
+    def fstep():
+        g.StoreOldVelocity()
+        g.VelocityGuess(1.0, 0.0, 1.0)
+        halo()
+        g.ModifyBulkVelocity(1, 0, 1, 0.1, 0.0, 0.0)
+        halo()
+        g.VelocityDivergence(1.0)
+        halo()
+        g.PressureCorrection(None)
+        halo()
+        g.VelocityCorrection(1.0)
+        halo()
+
+    for _ in range(3):
+        fstep()
+    g.synchronize()
+    k = args.fluid_steps
+    g.timing(True)
+    g.phase_times(reset=True)
+    l0 = g.launches
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(k):
+        fstep()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    launches = g.launches - l0
+    ph = g.phase_times(reset=True)
+    g.close()
+    nint = int(p["nx"]) * int(p["ny"]) * int(p["nz"])
+    phases = {name: {"ms_per_step": ph[name][0] / k} for name in ("fluid_guess", "fluid_halo", "fluid_other")}
+    guess_ms = phases["fluid_guess"]["ms_per_step"]
+    hbm_peak, peak_kind = measured_peaks()
+    fp64_peak = api.fp64_rate(device)
+    out = {"value": nint * k / (ms / 1e3), "unit": "interior node-steps/s", "steps": k, "ms_per_step": ms / k,
+           "interior_nodes": nint, "gpu_launches": launches, "phases": phases,
+           "roofline": {"kernel": "fluid_guess", "bound": "fp64",
+                        "algorithmic_bytes_per_step": nint * FLUID_BYTES["guess"],
+                        "hbm_achieved_gbs": nint * FLUID_BYTES["guess"] / (guess_ms / 1e3) / 1e9,
+                        "hbm_peak_gbs": hbm_peak, "hbm_peak_kind": peak_kind,
+                        "fp64_achieved_gops": nint * FLUID_GUESS_FP64 / (guess_ms / 1e3) / 1e9,
+                        "fp64_peak_gops": fp64_peak,
+                        "fp64_frac": nint * FLUID_GUESS_FP64 / (guess_ms / 1e3) / 1e9 / fp64_peak if fp64_peak else None},
+           "workload": "%s grid, the workload's Fourier field, visc 1e-6, bulk velocity (u: 0.1, w: 0) switched on "
+                       "as in the reference's initialization; the Poisson solve (PETSc) is outside, Pcorr resident"
+                       % "x".join(str(int(p[a])) for a in ("nx", "ny", "nz")),
+           "timing": "CUDA events on the launching stream"}
+    if cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+
+        O.build()
+        threads = os.cpu_count() or 1
+        O.set_threads(threads)
+        r = O.OracleFluid(p)
+        r.set_fluid_params(1e-6, 0.0, 0.0, 0.0)
+        from ibmdem.records import FLUID
+        host = [np.ascontiguousarray(f.cpu().numpy() if hasattr(f, "cpu") else f) for f in field]
+        for name, a in zip(("u", "v", "w"), host):
+            r.set_field(FLUID[name], a)
+        t0 = time.perf_counter()
+        r.StoreOldVelocity()
+        r.VelocityGuess(1.0, 0.0, 1.0)
+        for call in (lambda: r.ModifyBulkVelocity(1, 0, 1, 0.1, 0.0, 0.0), lambda: r.VelocityDivergence(1.0),
+                     r.PressureCorrection, lambda: r.VelocityCorrection(1.0), None):
+            r.FillGhostRegionForFluid()
+            r.Boundary()
+            if call is not None:
+                call()
+        dt = time.perf_counter() - t0
+        r.close()
+        out["cpu_baseline"] = {"value": nint / dt, "unit": "interior node-steps/s", "cores": threads, "kind": "port",
+                               "sample": "1 step of the same grid and field (CPU restatement; VelocityGuess, the "
+                                         "divergence and the corrections with OpenMP, the halo fills serial)",
+                               "seconds": dt}
+    return out
+
+
 def unresolved_algorithmic(n, nint, contacts):
     """Compulsory bytes and FP64 instructions per launch of the unresolved kernels."""
     return {
@@ -748,6 +866,8 @@ def run_ours(args):
             line["served"] = run_served(args, local, stream)
         if args.unresolved_particles > 0:
             line["unresolved"] = run_unresolved(args, local, stream, cpu=not args.no_cpu_baseline)
+        if args.fluid_steps > 0:
+            line["fluid"] = run_fluid(args, local, stream, cpu=not args.no_cpu_baseline)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

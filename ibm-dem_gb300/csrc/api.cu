@@ -175,12 +175,14 @@ void init_geom(Geom& g, const ibmdem_params* p) {
   }
   g.dt = p->dt;
   g.rdt = 1.0 / p->dt;
+  g.sdt = split_recip(p->dt);
   g.rdtLo = std::fma(-p->dt, g.rdt, 1.0) / p->dt;  // the remainder 1 - dt*rdt is exact
   g.divDt = std::isnormal(p->dt) && std::isnormal(g.rdt) && std::fabs(p->dt) < 0x1p200 && std::fabs(p->dt) > 0x1p-200
                 ? 1
                 : 0;
   g.dtDEM = p->dt / p->coupleInterval;
   g.rhof = p->rhof;
+  g.srhof = split_recip(p->rhof);
   g.eta = eta_of(p->ResistCoeff);
   double cd = p->collisionDist * (1.0 + p->collisionBuffer);
   g.cut2 = cd * cd;
@@ -356,7 +358,8 @@ static cudaEvent_t take_event(Ctx& c) {
   return e;
 }
 static const char* const kPhaseLabels[P_COUNT] = {"interp", "spread", "weights", "plan", "cells", "pairs",
-                                                  "force", "bodysum", "bodymove", "markers", "images", "reset"};
+                                                  "force", "bodysum", "bodymove", "markers", "images", "reset",
+                                                  "fluid_guess", "fluid_halo", "fluid_other"};
 // Every phase is an NVTX range (visible to any attached profiler, a few ns
 // otherwise); with timing on it is also bracketed by CUDA events.
 PhaseScope::PhaseScope(Ctx& ctx, int ph) : c(ctx), phase(ph) {

@@ -17,6 +17,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <cmath>
+
 #include "../../include/ibmdem.h"
 
 namespace ibmdem {
@@ -69,6 +71,28 @@ struct FastDiv {
   }
 };
 
+// A divisor b with its split reciprocal: r = RN(1/b), lo = RN(1/b - r).  x/b
+// correctly rounded is then q0 = RN(x*r + RN(x*lo)) (a faithful quotient, so
+// its remainder x - b*q0 is exact in one FMA) corrected by RN(q0 + rem*r)
+// (Markstein's correction theorem).  ok: b and 1/b normal with exponents
+// within 2^+-200; div_split takes the division outside that and for x outside
+// 2^-723 <= |x| < 2^777 (or x = 0), where the remainder could leave the
+// normal range.
+struct SplitRecip {
+  double b, r, lo;
+  int ok;
+  int one;  // b == 1: x/b is x
+};
+inline SplitRecip split_recip(double b) {
+  SplitRecip s;
+  s.b = b;
+  s.r = 1.0 / b;
+  s.lo = std::fma(-b, s.r, 1.0) / b;  // the remainder 1 - b*r is exact
+  s.ok = std::isnormal(b) && std::isnormal(s.r) && std::fabs(b) < 0x1p200 && std::fabs(b) > 0x1p-200;
+  s.one = b == 1.0;
+  return s;
+}
+
 struct Geom {
   int n[3];
   int ni, nj, nk;
@@ -84,6 +108,7 @@ struct Geom {
   int anyWall;
   double dt, dtDEM, rhof, eta, cut2, knCoeff, di;
   double rdt, rdtLo; // RN(1/dt) and RN(1/dt - rdt), for div_dt
+  SplitRecip sdt, srhof;  // dt and rhof as divisors (div_split)
   int divDt;         // dt and 1/dt normal with exponents within 2^+-200: div_dt may skip the division
   double g[3];
   FastDiv fdNint, fdN0, fdN1;  // interior nodes per component, nx, ny
@@ -109,6 +134,19 @@ struct Recs {
 };
 
 // ---- index helpers -------------------------------------------------------
+#ifdef __CUDACC__
+// x / s.b, correctly rounded (SplitRecip)
+__device__ inline double div_split(double x, const SplitRecip& s) {
+  if (s.one) return x;
+  const int ex = (int)((unsigned long long)__double_as_longlong(x) >> 52) & 0x7ff;
+  if (s.ok && (__double_as_longlong(x) << 1) == 0) return x * s.r;  // +-0 / b: a zero of the quotient's sign
+  if (!s.ok || ex < 300 || ex > 1800) return x / s.b;
+  const double q0 = __fma_rn(x, s.r, __dmul_rn(x, s.lo));
+  const double rem = __fma_rn(-q0, s.b, x);
+  return __fma_rn(rem, s.r, q0);
+}
+#endif
+
 __host__ __device__ inline long long field_off(const Geom& g, int i, int j, int k) {
   return ((long long)(k + 1) * g.nj + (j + 1)) * g.ni + (i + 1);
 }

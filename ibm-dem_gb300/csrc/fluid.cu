@@ -5,7 +5,9 @@
 // Every statement keeps the reference's operations in the reference's order
 // (FP64, no contraction: -fmad=false), so the fields are bit-identical to a
 // serial run of the Fortran, except ModifyBulkVelocity's interior sums, which
-// are formed in a fixed order of their own.  One thread per interior node;
+// are formed in a fixed order of their own.  Divisions by dt, rhof and the
+// Runge-Kutta coefficient are correctly rounded products with a split
+// reciprocal (div_split); by a unit spacing they are skipped.  One thread per interior node;
 // the stencil neighbours come through L1/L2, so each kernel streams its
 // fields about once from HBM.
 #include <algorithm>
@@ -42,9 +44,29 @@ struct FluidPtrs {
   double *nu, *nv, *nw, *Px, *Py, *Pz, *RHSul, *RHSvl, *RHSwl;
 };
 
+// x is zero or its exponent keeps x/4 normal and x*4 finite
+__device__ inline bool scalable(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const int e = (int)(b >> 52) & 0x7ff;
+  return (b << 1) == 0 || (e >= 3 && e <= 2044);
+}
+
+// The reference's difference of two fluxes on opposite faces,
+// 0.5*s1*0.5*t1 - 0.5*s2*0.5*t2 (each product left to right).  When s1, s2,
+// the products and their difference are zero or far from the subnormal and
+// overflow ranges, the factors 0.5*0.5 are an exact scaling by 1/4 that
+// commutes with every rounding, so the value is 0.25*RN(RN(s1*t1) - RN(s2*t2))
+// bit for bit; otherwise the statement is evaluated as written.
+__device__ inline double flux_diff(double s1, double t1, double s2, double t2) {
+  const double p1 = s1 * t1, p2 = s2 * t2, d = p1 - p2;
+  if (scalable(s1) && scalable(s2) && scalable(p1) && scalable(p2) && scalable(d)) return d * 0.25;
+  return 0.5 * s1 * 0.5 * t1 - 0.5 * s2 * 0.5 * t2;
+}
+
 // VelocityGuess (fluid.F90:108-133) with ConvectionTensor (fluid.F90:2-54),
-// ViscousTensor (fluid.F90:56-76) and PressureGradient (fluid.F90:78-91)
-template <bool UNIT>
+// ViscousTensor (fluid.F90:56-76) and PressureGradient (fluid.F90:78-91).
+// A1, C1: aRK == 1, cRK == 1, whose products are identities.
+template <bool UNIT, bool A1, bool C1>
 __global__ void __launch_bounds__(kFBlock) k_velocity_guess(Geom g, FluidPtrs f, double aRK, double bRK, double cRK,
                                                            double visc, double CPx, double CPy, double CPz) {
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -54,32 +76,26 @@ __global__ void __launch_bounds__(kFBlock) k_velocity_guess(Geom g, FluidPtrs f,
   const long long sj = g.ni, sk = (long long)g.ni * g.nj;
   const long long c = field_off(g, i, j, k);
   const double *u = f.u, *v = f.v, *w = f.w;
-  const double dx = g.h[0], dy = g.h[1], dz = g.h[2], dt = g.dt, rhof = g.rhof;
-  // 2nd order centre differences of the fluxes on the control-volume faces
-  const double uuE = 0.5 * (u[c + 1] + u[c]) * 0.5 * (u[c + 1] + u[c]);
-  const double uuW = 0.5 * (u[c - 1] + u[c]) * 0.5 * (u[c - 1] + u[c]);
-  const double uvB = 0.5 * (u[c + sj] + u[c]) * 0.5 * (v[c - 1 + sj] + v[c + sj]);
-  const double uvF = 0.5 * (u[c - sj] + u[c]) * 0.5 * (v[c - 1] + v[c]);
-  const double uwN = 0.5 * (u[c + sk] + u[c]) * 0.5 * (w[c - 1 + sk] + w[c + sk]);
-  const double uwS = 0.5 * (u[c - sk] + u[c]) * 0.5 * (w[c - 1] + w[c]);
-
-  const double vuE = 0.5 * (v[c + 1] + v[c]) * 0.5 * (u[c + 1 - sj] + u[c + 1]);
-  const double vuW = 0.5 * (v[c - 1] + v[c]) * 0.5 * (u[c - sj] + u[c]);
-  const double vvB = 0.5 * (v[c + sj] + v[c]) * 0.5 * (v[c + sj] + v[c]);
-  const double vvF = 0.5 * (v[c - sj] + v[c]) * 0.5 * (v[c - sj] + v[c]);
-  const double vwN = 0.5 * (v[c + sk] + v[c]) * 0.5 * (w[c - sj + sk] + w[c + sk]);
-  const double vwS = 0.5 * (v[c - sk] + v[c]) * 0.5 * (w[c - sj] + w[c]);
-
-  const double wuE = 0.5 * (w[c + 1] + w[c]) * 0.5 * (u[c + 1 - sk] + u[c + 1]);
-  const double wuW = 0.5 * (w[c - 1] + w[c]) * 0.5 * (u[c - sk] + u[c]);
-  const double wvB = 0.5 * (w[c + sj] + w[c]) * 0.5 * (v[c + sj - sk] + v[c + sj]);
-  const double wvF = 0.5 * (w[c - sj] + w[c]) * 0.5 * (v[c - sk] + v[c]);
-  const double wwN = 0.5 * (w[c + sk] + w[c]) * 0.5 * (w[c + sk] + w[c]);
-  const double wwS = 0.5 * (w[c - sk] + w[c]) * 0.5 * (w[c - sk] + w[c]);
-
-  const double TIux = by_h<UNIT>(uuE - uuW, dx), TIuy = by_h<UNIT>(uvB - uvF, dy), TIuz = by_h<UNIT>(uwN - uwS, dz);
-  const double TIvx = by_h<UNIT>(vuE - vuW, dx), TIvy = by_h<UNIT>(vvB - vvF, dy), TIvz = by_h<UNIT>(vwN - vwS, dz);
-  const double TIwx = by_h<UNIT>(wuE - wuW, dx), TIwy = by_h<UNIT>(wvB - wvF, dy), TIwz = by_h<UNIT>(wwN - wwS, dz);
+  const double dx = g.h[0], dy = g.h[1], dz = g.h[2], dt = g.dt;
+  // 2nd order centre differences of the fluxes on the control-volume faces:
+  // uuE - uuW, uvB - uvF, ... (fluid.F90:15-33)
+  const double TIux = by_h<UNIT>(flux_diff(u[c + 1] + u[c], u[c + 1] + u[c], u[c - 1] + u[c], u[c - 1] + u[c]), dx);
+  const double TIuy = by_h<UNIT>(
+      flux_diff(u[c + sj] + u[c], v[c - 1 + sj] + v[c + sj], u[c - sj] + u[c], v[c - 1] + v[c]), dy);
+  const double TIuz = by_h<UNIT>(
+      flux_diff(u[c + sk] + u[c], w[c - 1 + sk] + w[c + sk], u[c - sk] + u[c], w[c - 1] + w[c]), dz);
+  const double TIvx = by_h<UNIT>(
+      flux_diff(v[c + 1] + v[c], u[c + 1 - sj] + u[c + 1], v[c - 1] + v[c], u[c - sj] + u[c]), dx);
+  const double TIvy = by_h<UNIT>(
+      flux_diff(v[c + sj] + v[c], v[c + sj] + v[c], v[c - sj] + v[c], v[c - sj] + v[c]), dy);
+  const double TIvz = by_h<UNIT>(
+      flux_diff(v[c + sk] + v[c], w[c - sj + sk] + w[c + sk], v[c - sk] + v[c], w[c - sj] + w[c]), dz);
+  const double TIwx = by_h<UNIT>(
+      flux_diff(w[c + 1] + w[c], u[c + 1 - sk] + u[c + 1], w[c - 1] + w[c], u[c - sk] + u[c]), dx);
+  const double TIwy = by_h<UNIT>(
+      flux_diff(w[c + sj] + w[c], v[c + sj - sk] + v[c + sj], w[c - sj] + w[c], v[c - sk] + v[c]), dy);
+  const double TIwz = by_h<UNIT>(
+      flux_diff(w[c + sk] + w[c], w[c + sk] + w[c], w[c - sk] + w[c], w[c - sk] + w[c]), dz);
 
   const double TVux = by_h<UNIT>(u[c + 1] + u[c - 1] - 2.0 * u[c], dx * dx) * visc;
   const double TVuy = by_h<UNIT>(u[c + sj] + u[c - sj] - 2.0 * u[c], dy * dy) * visc;
@@ -92,16 +108,17 @@ __global__ void __launch_bounds__(kFBlock) k_velocity_guess(Geom g, FluidPtrs f,
   const double TVwz = by_h<UNIT>(w[c + sk] + w[c - sk] - 2.0 * w[c], dz * dz) * visc;
 
   const double* P = f.P;
-  const double Px = by_h<UNIT>(P[c] - P[c - 1], dx) / rhof;
-  const double Py = by_h<UNIT>(P[c] - P[c - sj], dy) / rhof;
-  const double Pz = by_h<UNIT>(P[c] - P[c - sk], dz) / rhof;
+  const double Px = div_split(by_h<UNIT>(P[c] - P[c - 1], dx), g.srhof);
+  const double Py = div_split(by_h<UNIT>(P[c] - P[c - sj], dy), g.srhof);
+  const double Pz = div_split(by_h<UNIT>(P[c] - P[c - sk], dz), g.srhof);
 
   const double RHSu = -(TIux + TIuy + TIuz) + (TVux + TVuy + TVuz) + CPx + f.fx[c];
   const double RHSv = -(TIvx + TIvy + TIvz) + (TVvx + TVvy + TVvz) + CPy + f.fy[c];
   const double RHSw = -(TIwx + TIwy + TIwz) + (TVwx + TVwy + TVwz) + CPz + f.fz[c];
-  f.nu[c] = f.uold[c] + dt * (aRK * RHSu + bRK * f.RHSul[c] - cRK * Px);
-  f.nv[c] = f.vold[c] + dt * (aRK * RHSv + bRK * f.RHSvl[c] - cRK * Py);
-  f.nw[c] = f.wold[c] + dt * (aRK * RHSw + bRK * f.RHSwl[c] - cRK * Pz);
+  // aRK*RHS and cRK*grad P with a coefficient of 1 are the values themselves
+  f.nu[c] = f.uold[c] + dt * ((A1 ? RHSu : aRK * RHSu) + bRK * f.RHSul[c] - (C1 ? Px : cRK * Px));
+  f.nv[c] = f.vold[c] + dt * ((A1 ? RHSv : aRK * RHSv) + bRK * f.RHSvl[c] - (C1 ? Py : cRK * Py));
+  f.nw[c] = f.wold[c] + dt * ((A1 ? RHSw : aRK * RHSw) + bRK * f.RHSwl[c] - (C1 ? Pz : cRK * Pz));
   f.Px[c] = Px;
   f.Py[c] = Py;
   f.Pz[c] = Pz;
@@ -127,7 +144,7 @@ __global__ void k_copy_interior3(Geom g, const double* nu, const double* nv, con
 // VelocityDivergence (fluid.F90:93-106)
 template <bool UNIT>
 __global__ void k_velocity_divergence(Geom g, const double* u, const double* v, const double* w, double* velDiv,
-                                      double cRK) {
+                                      SplitRecip cRK) {
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (uint32_t)g.nint) return;
   int i, j, k;
@@ -136,7 +153,7 @@ __global__ void k_velocity_divergence(Geom g, const double* u, const double* v, 
   const long long c = field_off(g, i, j, k);
   const double d = by_h<UNIT>(u[c + 1] - u[c], g.h[0]) + by_h<UNIT>(v[c + sj] - v[c], g.h[1]) +
                    by_h<UNIT>(w[c + sk] - w[c], g.h[2]);
-  velDiv[c] = -d / g.dt / cRK * g.rhof;
+  velDiv[c] = div_split(div_split(-d, g.sdt), cRK) * g.rhof;
 }
 
 // PressureCorrection (fluid.F90:197-208)
@@ -149,8 +166,9 @@ __global__ void k_pressure_correction(Geom g, double* P, const double* Pcorr) {
   P[c] = P[c] + Pcorr[c];
 }
 
-// VelocityCorrection (fluid.F90:210-224): the velocity update
-template <bool UNIT>
+// VelocityCorrection (fluid.F90:210-224): the velocity update; C1: cRK == 1,
+// whose products are identities
+template <bool UNIT, bool C1>
 __global__ void k_velocity_correction(Geom g, double* u, double* v, double* w, const double* P, const double* Px,
                                       const double* Py, const double* Pz, double cRK) {
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -159,10 +177,11 @@ __global__ void k_velocity_correction(Geom g, double* u, double* v, double* w, c
   interior_ijk(g, t, i, j, k);
   const long long sj = g.ni, sk = (long long)g.ni * g.nj;
   const long long c = field_off(g, i, j, k);
-  const double dt = g.dt, rhof = g.rhof;
-  u[c] = u[c] + cRK * Px[c] * dt - by_h<UNIT>(cRK * (P[c] - P[c - 1]), g.h[0]) * dt / rhof;
-  v[c] = v[c] + cRK * Py[c] * dt - by_h<UNIT>(cRK * (P[c] - P[c - sj]), g.h[1]) * dt / rhof;
-  w[c] = w[c] + cRK * Pz[c] * dt - by_h<UNIT>(cRK * (P[c] - P[c - sk]), g.h[2]) * dt / rhof;
+  const double dt = g.dt;
+  const double dPx = P[c] - P[c - 1], dPy = P[c] - P[c - sj], dPz = P[c] - P[c - sk];
+  u[c] = u[c] + (C1 ? Px[c] : cRK * Px[c]) * dt - div_split(by_h<UNIT>(C1 ? dPx : cRK * dPx, g.h[0]) * dt, g.srhof);
+  v[c] = v[c] + (C1 ? Py[c] : cRK * Py[c]) * dt - div_split(by_h<UNIT>(C1 ? dPy : cRK * dPy, g.h[1]) * dt, g.srhof);
+  w[c] = w[c] + (C1 ? Pz[c] : cRK * Pz[c]) * dt - div_split(by_h<UNIT>(C1 ? dPz : cRK * dPz, g.h[2]) * dt, g.srhof);
 }
 
 // the vorticity of the corrected field (fluid.F90:225-234)
@@ -186,13 +205,10 @@ __global__ void k_bulk_partial(Geom g, const double* u, const double* v, const d
   __shared__ double sh[3][kFBlock];
   const long long t0 = (long long)blockIdx.x * per;
   const long long t1 = std::min<long long>(t0 + per, g.nint);
-  // thread r sums a contiguous stretch of the block's range, then thread 0
-  // adds the stretches in order
-  const long long len = t1 > t0 ? t1 - t0 : 0;
-  const long long chunk = (len + kFBlock - 1) / kFBlock;
-  const long long a = t0 + threadIdx.x * chunk, b = std::min<long long>(a + chunk, t1);
+  // thread r sums the nodes r, r + kFBlock, ... of the block's range (warps
+  // read consecutive nodes), then threads 0..2 add the 256 sums in order
   double su = 0.0, sv = 0.0, sw = 0.0;
-  for (long long t = a; t < b; ++t) {
+  for (long long t = t0 + threadIdx.x; t < t1; t += kFBlock) {
     int i, j, k;
     interior_ijk(g, (uint32_t)t, i, j, k);
     const long long c = field_off(g, i, j, k);
@@ -436,10 +452,14 @@ int ibmdem_VelocityGuess(ibmdem_ctx* h, double aRK, double bRK, double cRK) {
   f.RHSvl = c.ffield[IBMDEM_FLUID_RHSVL];
   f.RHSwl = c.ffield[IBMDEM_FLUID_RHSWL];
   const unsigned nb = interior_blocks(c);
-  if (c.g.unit_h)
-    k_velocity_guess<true><<<nb, kFBlock, 0, c.stream>>>(c.g, f, aRK, bRK, cRK, c.visc, c.CPx, c.CPy, c.CPz);
-  else
-    k_velocity_guess<false><<<nb, kFBlock, 0, c.stream>>>(c.g, f, aRK, bRK, cRK, c.visc, c.CPx, c.CPy, c.CPz);
+  PhaseScope ps(c, P_FGUESS);
+  const int variant = (c.g.unit_h ? 4 : 0) | (aRK == 1.0 ? 2 : 0) | (cRK == 1.0 ? 1 : 0);
+  decltype(&k_velocity_guess<true, true, true>) kern[8] = {
+      k_velocity_guess<false, false, false>, k_velocity_guess<false, false, true>,
+      k_velocity_guess<false, true, false>,  k_velocity_guess<false, true, true>,
+      k_velocity_guess<true, false, false>,  k_velocity_guess<true, false, true>,
+      k_velocity_guess<true, true, false>,   k_velocity_guess<true, true, true>};
+  kern[variant]<<<nb, kFBlock, 0, c.stream>>>(c.g, f, aRK, bRK, cRK, c.visc, c.CPx, c.CPy, c.CPz);
   k_copy_interior3<<<nb, kFBlock, 0, c.stream>>>(c.g, f.nu, f.nv, f.nw, c.u, c.v, c.w);
   c.launches += 2;
   return fluid_launched(h, "ibmdem_VelocityGuess");
@@ -453,6 +473,7 @@ int ibmdem_FillGhostRegionForFluid(ibmdem_ctx* h) {
   CarriedFields cf{{c.u, c.v, c.w, c.ffield[IBMDEM_FLUID_P], c.ffield[IBMDEM_FLUID_OMEGAZ],
                     c.ffield[IBMDEM_FLUID_PCORR]}};
   const int SG = 1, H = 2;
+  PhaseScope ps(c, P_FHALO);
   for (int s = 0; s < 6; ++s) {
     const int sideSend = s, sideRecv = (s % 2 == 0) ? s + 1 : s - 1;
     const int d = sideRecv / 2;
@@ -490,6 +511,7 @@ int ibmdem_Boundary(ibmdem_ctx* h) {
   Ctx& c = h->c;
   const Geom& g = c.g;
   double* comp[3] = {c.u, c.v, c.w};
+  PhaseScope ps(c, P_FHALO);
   for (int side = 0; side < 6; ++side) {
     const int d = side / 2;
     if (!g.wall[d]) continue;
@@ -514,6 +536,7 @@ int ibmdem_ModifyBulkVelocity(ibmdem_ctx* h, int32_t swU, int32_t swV, int32_t s
   const int nblk = (int)std::min<long long>(kSumBlocks, std::max<long long>(1, (nint + kFBlock - 1) / kFBlock));
   const int per = (int)((nint + nblk - 1) / nblk);
   double* modify = c.fsum + 3 * kSumBlocks;
+  PhaseScope ps(c, P_FOTHER);
   k_bulk_partial<<<nblk, kFBlock, 0, c.stream>>>(c.g, c.u, c.v, c.w, c.fsum, per);
   k_bulk_modify<<<1, 32, 0, c.stream>>>(c.g, c.fsum, nblk, modify, swU, swV, swW, bulkU, bulkV, bulkW);
   k_bulk_apply<<<interior_blocks(c), kFBlock, 0, c.stream>>>(c.g, c.u, c.v, c.w, modify);
@@ -526,10 +549,13 @@ int ibmdem_VelocityDivergence(ibmdem_ctx* h, double cRK) {
   if (rc) return rc;
   Ctx& c = h->c;
   const unsigned nb = interior_blocks(c);
+  PhaseScope ps(c, P_FOTHER);
   if (c.g.unit_h)
-    k_velocity_divergence<true><<<nb, kFBlock, 0, c.stream>>>(c.g, c.u, c.v, c.w, c.ffield[IBMDEM_FLUID_VELDIV], cRK);
+    k_velocity_divergence<true><<<nb, kFBlock, 0, c.stream>>>(c.g, c.u, c.v, c.w, c.ffield[IBMDEM_FLUID_VELDIV],
+                                                             split_recip(cRK));
   else
-    k_velocity_divergence<false><<<nb, kFBlock, 0, c.stream>>>(c.g, c.u, c.v, c.w, c.ffield[IBMDEM_FLUID_VELDIV], cRK);
+    k_velocity_divergence<false><<<nb, kFBlock, 0, c.stream>>>(c.g, c.u, c.v, c.w, c.ffield[IBMDEM_FLUID_VELDIV],
+                                                              split_recip(cRK));
   c.launches++;
   return fluid_launched(h, "ibmdem_VelocityDivergence");
 }
@@ -541,8 +567,11 @@ int ibmdem_PressureCorrection(ibmdem_ctx* h, const double* Pcorr) {
   if (Pcorr && cudaMemcpyAsync(c.ffield[IBMDEM_FLUID_PCORR], Pcorr, sizeof(double) * (size_t)c.g.ncell,
                                cudaMemcpyHostToDevice, c.stream) != cudaSuccess)
     return IBMDEM_ECUDA;
-  k_pressure_correction<<<interior_blocks(c), kFBlock, 0, c.stream>>>(c.g, c.ffield[IBMDEM_FLUID_P],
-                                                                        c.ffield[IBMDEM_FLUID_PCORR]);
+  {
+    PhaseScope ps(c, P_FOTHER);
+    k_pressure_correction<<<interior_blocks(c), kFBlock, 0, c.stream>>>(c.g, c.ffield[IBMDEM_FLUID_P],
+                                                                          c.ffield[IBMDEM_FLUID_PCORR]);
+  }
   c.launches++;
   rc = fluid_launched(h, "ibmdem_PressureCorrection");
   // the caller may reuse Pcorr when this returns
@@ -556,15 +585,15 @@ int ibmdem_VelocityCorrection(ibmdem_ctx* h, double cRK) {
   Ctx& c = h->c;
   const unsigned nb = interior_blocks(c);
   double** F = c.ffield;
+  PhaseScope ps(c, P_FOTHER);
+  auto corr = c.g.unit_h ? (cRK == 1.0 ? k_velocity_correction<true, true> : k_velocity_correction<true, false>)
+                         : (cRK == 1.0 ? k_velocity_correction<false, true> : k_velocity_correction<false, false>);
+  corr<<<nb, kFBlock, 0, c.stream>>>(c.g, c.u, c.v, c.w, F[IBMDEM_FLUID_P], F[IBMDEM_FLUID_PX], F[IBMDEM_FLUID_PY],
+                                     F[IBMDEM_FLUID_PZ], cRK);
   if (c.g.unit_h) {
-    k_velocity_correction<true><<<nb, kFBlock, 0, c.stream>>>(c.g, c.u, c.v, c.w, F[IBMDEM_FLUID_P], F[IBMDEM_FLUID_PX],
-                                                              F[IBMDEM_FLUID_PY], F[IBMDEM_FLUID_PZ], cRK);
     k_vorticity<true><<<nb, kFBlock, 0, c.stream>>>(c.g, c.u, c.v, c.w, F[IBMDEM_FLUID_OMEGAX], F[IBMDEM_FLUID_OMEGAY],
                                                     F[IBMDEM_FLUID_OMEGAZ]);
   } else {
-    k_velocity_correction<false><<<nb, kFBlock, 0, c.stream>>>(c.g, c.u, c.v, c.w, F[IBMDEM_FLUID_P],
-                                                               F[IBMDEM_FLUID_PX], F[IBMDEM_FLUID_PY],
-                                                               F[IBMDEM_FLUID_PZ], cRK);
     k_vorticity<false><<<nb, kFBlock, 0, c.stream>>>(c.g, c.u, c.v, c.w, F[IBMDEM_FLUID_OMEGAX],
                                                      F[IBMDEM_FLUID_OMEGAY], F[IBMDEM_FLUID_OMEGAZ]);
   }

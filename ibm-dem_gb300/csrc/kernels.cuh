@@ -138,7 +138,7 @@ struct Ctx {
 // timed phases (names in api.cu: ibmdem_phase_name)
 enum Phase : int {
   P_INTERP = 0, P_SPREAD, P_WEIGHTS, P_PLAN, P_CELLS, P_PAIRS, P_FORCE, P_BODYSUM, P_BODYMOVE, P_MARKERS,
-  P_IMAGES, P_RESET, P_COUNT
+  P_IMAGES, P_RESET, P_FGUESS, P_FHALO, P_FOTHER, P_COUNT
 };
 // records CUDA events around one phase on the context's stream when timing is on
 struct PhaseScope {

@@ -61,6 +61,9 @@ def test_fluid_stencils_bit_identical(gpu_lib, oracle_mod, walls, h):
             c.Boundary()
         same(g, r)
         for c in (g, r):
+            c.VelocityDivergence(0.6)
+        same(g, r)
+        for c in (g, r):
             c.VelocityDivergence(1.0)
         same(g, r)
         pcorr = np.random.default_rng(7).standard_normal(r.shape)
@@ -75,6 +78,9 @@ def test_fluid_stencils_bit_identical(gpu_lib, oracle_mod, walls, h):
             c.VelocityCorrection(1.0)
             c.FillGhostRegionForFluid()
             c.Boundary()
+        same(g, r)
+        for c in (g, r):
+            c.VelocityCorrection(0.5)
         same(g, r)
     finally:
         g.close()
