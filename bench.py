@@ -535,6 +535,10 @@ def run_fluid(args, device, stream, cpu=True):
                         "algorithmic_bytes_per_step": nint * FLUID_BYTES["guess"],
                         "hbm_achieved_gbs": nint * FLUID_BYTES["guess"] / (guess_ms / 1e3) / 1e9,
                         "hbm_peak_gbs": hbm_peak, "hbm_peak_kind": peak_kind,
+                        "fp64_ops_per_node": FLUID_GUESS_FP64,
+                        "fp64_ops_note": "the reference statement's FP64 operations; the kernel issues about 160 "
+                                         "(exact quarter scalings of the flux products, identity coefficients, "
+                                         "split-reciprocal divisions)",
                         "fp64_achieved_gops": nint * FLUID_GUESS_FP64 / (guess_ms / 1e3) / 1e9,
                         "fp64_peak_gops": fp64_peak,
                         "fp64_frac": nint * FLUID_GUESS_FP64 / (guess_ms / 1e3) / 1e9 / fp64_peak if fp64_peak else None},
