@@ -497,7 +497,8 @@ int ibmdem_destroy(ibmdem_ctx* h) {
   for (cudaEvent_t e : c.evFree) cudaEventDestroy(e);
   if (c.fieldsRead) cudaEventDestroy(c.fieldsRead);
   if (c.upStart) cudaEventDestroy(c.upStart);
-  if (c.upDone) cudaEventDestroy(c.upDone);
+  for (cudaEvent_t e : c.upDone)
+    if (e) cudaEventDestroy(e);
   if (c.upStream) cudaStreamDestroy(c.upStream);
   delete h;
   return IBMDEM_OK;
@@ -551,35 +552,46 @@ int ibmdem_set_fluid(ibmdem_ctx* h, const double* u, const double* v, const doub
   // spread plan (which does not read the fluid) is built on the context's
   // stream while the fields upload on a second one.
   const bool planBeside = c.weightsLocal && c.weightsGhost && !c.planReady;
-  cudaStream_t up = c.stream;
+  double* dst[3] = {c.u, c.v, c.w};
+  double* frozen[3] = {c.u0, c.v0, c.w0};
+  const double* src[3] = {u, v, w};
   if (planBeside) {
+    // The uploads go on a second stream; the context's stream clears the
+    // forcing and builds the plan meanwhile, then copies each component to the
+    // frozen field as soon as it has arrived (only the last copy follows the
+    // last upload).
     if (!c.upStream) CU(cudaStreamCreateWithFlags(&c.upStream, cudaStreamNonBlocking));
     if (!c.upStart) CU(cudaEventCreateWithFlags(&c.upStart, cudaEventDisableTiming));
-    if (!c.upDone) CU(cudaEventCreateWithFlags(&c.upDone, cudaEventDisableTiming));
-    up = c.upStream;
+    for (cudaEvent_t& e : c.upDone)
+      if (!e) CU(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     CU(cudaEventRecord(c.upStart, c.stream));  // after all earlier work on the fields
-    CU(cudaStreamWaitEvent(up, c.upStart, 0));
-  }
-  CU(cudaMemcpyAsync(c.u, u, nb, cudaMemcpyHostToDevice, up));
-  CU(cudaMemcpyAsync(c.v, v, nb, cudaMemcpyHostToDevice, up));
-  CU(cudaMemcpyAsync(c.w, w, nb, cudaMemcpyHostToDevice, up));
-  if (planBeside) {
-    CU(cudaEventRecord(c.upDone, up));
+    CU(cudaStreamWaitEvent(c.upStream, c.upStart, 0));
+    for (int q = 0; q < 3; ++q) {
+      CU(cudaMemcpyAsync(dst[q], src[q], nb, cudaMemcpyHostToDevice, c.upStream));
+      CU(cudaEventRecord(c.upDone[q], c.upStream));
+    }
+    CU(cudaMemsetAsync(c.fx, 0, nb, c.stream));
+    CU(cudaMemsetAsync(c.fy, 0, nb, c.stream));
+    CU(cudaMemsetAsync(c.fz, 0, nb, c.stream));
+    CU(cudaMemsetAsync(&c.dCnt->nLast, 0, sizeof(int), c.stream));
     int rp = ensure_plan(h);
     // the fields are in place before any later work of the context's stream
-    CU(cudaStreamWaitEvent(c.stream, c.upDone, 0));
+    for (int q = 0; q < 3; ++q) {
+      CU(cudaStreamWaitEvent(c.stream, c.upDone[q], 0));
+      CU(cudaMemcpyAsync(frozen[q], dst[q], nb, cudaMemcpyDeviceToDevice, c.stream));
+    }
     if (rp) {
       cudaStreamSynchronize(c.stream);
       return rp;
     }
+  } else {
+    for (int q = 0; q < 3; ++q) CU(cudaMemcpyAsync(dst[q], src[q], nb, cudaMemcpyHostToDevice, c.stream));
+    for (int q = 0; q < 3; ++q) CU(cudaMemcpyAsync(frozen[q], dst[q], nb, cudaMemcpyDeviceToDevice, c.stream));
+    CU(cudaMemsetAsync(c.fx, 0, nb, c.stream));
+    CU(cudaMemsetAsync(c.fy, 0, nb, c.stream));
+    CU(cudaMemsetAsync(c.fz, 0, nb, c.stream));
+    CU(cudaMemsetAsync(&c.dCnt->nLast, 0, sizeof(int), c.stream));
   }
-  CU(cudaMemcpyAsync(c.u0, c.u, nb, cudaMemcpyDeviceToDevice, c.stream));
-  CU(cudaMemcpyAsync(c.v0, c.v, nb, cudaMemcpyDeviceToDevice, c.stream));
-  CU(cudaMemcpyAsync(c.w0, c.w, nb, cudaMemcpyDeviceToDevice, c.stream));
-  CU(cudaMemsetAsync(c.fx, 0, nb, c.stream));
-  CU(cudaMemsetAsync(c.fy, 0, nb, c.stream));
-  CU(cudaMemsetAsync(c.fz, 0, nb, c.stream));
-  CU(cudaMemsetAsync(&c.dCnt->nLast, 0, sizeof(int), c.stream));
   c.haveFluid = true;
   // synchronous for pageable host memory semantics: the caller may reuse u,v,w
   CU(cudaStreamSynchronize(c.stream));

@@ -127,7 +127,7 @@ struct Ctx {
 
   // ibmdem_set_fluid: the uploads on their own stream, beside a spread plan build
   cudaStream_t upStream = nullptr;
-  cudaEvent_t upStart = nullptr, upDone = nullptr;
+  cudaEvent_t upStart = nullptr, upDone[3] = {};  // upDone[q]: component q uploaded
 
   // state flags
   bool haveFluid = false, haveParcels = false, listsBuilt = false;
