@@ -497,6 +497,8 @@ int ibmdem_destroy(ibmdem_ctx* h) {
   for (cudaEvent_t e : c.evFree) cudaEventDestroy(e);
   if (c.fieldsRead) cudaEventDestroy(c.fieldsRead);
   if (c.upStart) cudaEventDestroy(c.upStart);
+  for (cudaEvent_t e : c.compDone)
+    if (e) cudaEventDestroy(e);
   for (cudaEvent_t e : c.upDone)
     if (e) cudaEventDestroy(e);
   if (c.upStream) cudaStreamDestroy(c.upStream);
@@ -606,13 +608,23 @@ int ibmdem_get_fluid_async(ibmdem_ctx* h, double* u, double* v, double* w, doubl
   if (cs == c.stream) return set_error(h, IBMDEM_EINVAL, "copy_stream must differ from the context's stream");
   if (!c.fieldsRead) CU(cudaEventCreateWithFlags(&c.fieldsRead, cudaEventDisableTiming));
   const size_t nb = sizeof(double) * (size_t)c.g.ncell;
-  // the copies start after the work issued so far on the context's stream ...
-  CU(cudaEventRecord(c.fieldsRead, c.stream));
-  CU(cudaStreamWaitEvent(cs, c.fieldsRead, 0));
   double* dst[6] = {u, v, w, fx, fy, fz};
   double* src[6] = {c.u, c.v, c.w, c.fx, c.fy, c.fz};
-  for (int q = 0; q < 6; ++q)
-    if (dst[q]) CU(cudaMemcpyAsync(dst[q], src[q], nb, cudaMemcpyDeviceToHost, cs));
+  if (c.compDoneAt == c.launches) {
+    // right after a MDF loop: each component's velocity and forcing leave as
+    // soon as that component is done, while the next ones are still computed
+    for (int q = 0; q < 3; ++q) {
+      CU(cudaStreamWaitEvent(cs, c.compDone[q], 0));
+      if (dst[q]) CU(cudaMemcpyAsync(dst[q], src[q], nb, cudaMemcpyDeviceToHost, cs));
+      if (dst[q + 3]) CU(cudaMemcpyAsync(dst[q + 3], src[q + 3], nb, cudaMemcpyDeviceToHost, cs));
+    }
+  } else {
+    // the copies start after the work issued so far on the context's stream
+    CU(cudaEventRecord(c.fieldsRead, c.stream));
+    CU(cudaStreamWaitEvent(cs, c.fieldsRead, 0));
+    for (int q = 0; q < 6; ++q)
+      if (dst[q]) CU(cudaMemcpyAsync(dst[q], src[q], nb, cudaMemcpyDeviceToHost, cs));
+  }
   // ... and the next context work that writes the fields waits for them
   CU(cudaEventRecord(c.fieldsRead, cs));
   c.fieldsReadPending = true;
@@ -939,7 +951,7 @@ int ibmdem_UpdateFluidVelocityOnLagrangianPoints(ibmdem_ctx* h) {
   Ctx& c = h->c;
   REQUIRE(c.weightsLocal, "local weights are not computed");
   REQUIRE(c.haveFluid, "no fluid field");
-  launch_interp(c);
+  launch_interp(c, -1);
   return launch_status(h);
 }
 
@@ -996,7 +1008,7 @@ int ibmdem_UpdateMomentumSourceTerm(ibmdem_ctx* h) {
   int rc = ensure_plan(h);
   if (rc) return rc;
   REQUIRE(c.spreadValid, "spreading needs MultiDirectForcing's reset after the weights change");
-  launch_spread(c, false);
+  launch_spread(c, false, -1);
   return launch_status(h);
 }
 
@@ -1057,24 +1069,44 @@ static int mdf(ibmdem_ctx* h, bool frozen) {
     PhaseScope t(c, P_RESET);
     launch_mdf_reset(c, frozen);
   }
-  for (int it = 0; it < c.p.Ns; ++it) {
-    {
-      PhaseScope t(c, P_INTERP);
-      launch_interp(c);
+  // The three velocity components never meet inside the MDF loop (fluid.F90:
+  // 265-285): a marker's component interpolates from that component of the
+  // field, and the spread and the post-guess of a node write that component
+  // only.  For a caller that reads the fields right after (MultiDirectForcing
+  // in a coupled step) the loop runs component by component, so that the
+  // read-out of u and fx can start once the first component is done
+  // (ibmdem_get_fluid_async); the frozen-fluid step keeps the three
+  // components in one launch, which is 3% faster on the device.  The spread
+  // gathers the roots' fdrag*vol, never the images', so either way the images
+  // take their sources' final fdrag once, after the loop.
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  cudaStreamIsCapturing(c.stream, &cap);
+  const bool byComp = !frozen && cap == cudaStreamCaptureStatusNone;
+  for (int comp = byComp ? 0 : -1; comp < (byComp ? 3 : 0); ++comp) {
+    for (int it = 0; it < c.p.Ns; ++it) {
+      {
+        PhaseScope t(c, P_INTERP);
+        launch_interp(c, comp);
+      }
+      {
+        PhaseScope t(c, P_SPREAD);
+        launch_spread(c, true, comp);
+      }
     }
-    {
-      PhaseScope t(c, P_IMAGES);
-      launch_img_update(c);
+    if (byComp) {
+      if (!c.compDone[comp]) cudaEventCreateWithFlags(&c.compDone[comp], cudaEventDisableTiming);
+      cudaEventRecord(c.compDone[comp], c.stream);
     }
-    {
-      PhaseScope t(c, P_SPREAD);
-      launch_spread(c, true);
-    }
+  }
+  {
+    PhaseScope t(c, P_IMAGES);
+    launch_img_update(c);
   }
   {
     PhaseScope t(c, P_RESET);
     record_written_nodes(c);
   }
+  c.compDoneAt = byComp ? c.launches : -1;
   return launch_status(h);
 }
 

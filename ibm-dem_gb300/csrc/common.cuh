@@ -122,7 +122,8 @@ constexpr int kWallImgBit = 6;
 struct Counters {
   int npLocal, np, nImg, nActive, nPairs, nRuns, nContrib, nLast;
   int err, errInfo;
-  int pad[6];
+  int compStart[4];  // first run of each velocity component (and nRuns) in the spread plan
+  int pad[2];
 };
 
 struct Recs {

@@ -622,6 +622,23 @@ __global__ void k_plan_total(Counters* cnt, const unsigned long long* cursor) {
   cnt->nContrib = (int)*cursor;
 }
 
+// the first run of each velocity component in the sorted run keys
+__global__ void k_comp_bounds(Counters* cnt, const uint32_t* runKey, long long nint) {
+  const int n = cnt->nRuns;
+  cnt->compStart[0] = 0;
+  cnt->compStart[3] = n;
+  for (int comp = 1; comp < 3; ++comp) {
+    const uint32_t key = (uint32_t)(comp * nint);
+    int lo = 0, hi = n;  // first run with runKey >= key
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (runKey[mid] < key) lo = mid + 1;
+      else hi = mid;
+    }
+    cnt->compStart[comp] = lo;
+  }
+}
+
 // Write the new value of interior node (i,j,k) of component comp where the
 // fluid solver's halo refill puts it (FillGhostRegionForFluid,
 // boundary.F90:122-147): per axis the node itself and, within the 2-cell halo
@@ -710,10 +727,10 @@ __global__ void k_mdf_reset(Recs R, Geom g, Counters* cnt, Fields fl, const uint
 // blockIdx.y is the velocity component.
 template <int UNIT_H>
 __global__ void __launch_bounds__(kBlock) k_interp(Recs R, Geom g, const Counters* cnt, const double* __restrict__ W,
-                                                   const int4* __restrict__ win, Fields fl, double* fv) {
+                                                   const int4* __restrict__ win, Fields fl, double* fv, int comp0) {
   int m = blockIdx.x * blockDim.x + threadIdx.x;
   if (m >= cnt->npLocal) return;
-  const int comp = blockIdx.y;
+  const int comp = comp0 + blockIdx.y;
   const int cap = R.cap;
   const double* __restrict__ F = fl.U(comp);
   int sx, sy, sz;
@@ -778,7 +795,7 @@ __global__ void __launch_bounds__(kBlock, 8) k_spread(Geom g, const Counters* cn
                                                    const uint32_t* __restrict__ runKey,
                                                    const uint32_t* __restrict__ planRoot,
                                                    const double* __restrict__ planW, const double* __restrict__ fv,
-                                                   int cap, Fields fl, double* fCur, double* fPrev) {
+                                                   int cap, Fields fl, double* fCur, double* fPrev, int onlyComp) {
   // prod: the staged products; a node's sum replaces its first product (a node
   // without products keeps 0), and without staging prod[t] holds node t's sum
   extern __shared__ double prod[];
@@ -786,11 +803,17 @@ __global__ void __launch_bounds__(kBlock, 8) k_spread(Geom g, const Counters* cn
   __shared__ int order[kBlock];
   __shared__ int sStart[kBlock + 1];  // the block's runs are contiguous: run t spans sStart[t]..sStart[t+1]
   const int nRuns = cnt->nRuns;  // run counts are ints (Counters)
-  for (int r0 = blockIdx.x * kBlock; r0 < nRuns; r0 += gridDim.x * kBlock) {
+  // one component's runs [rs, re) (onlyComp >= 0) or all of them; a block
+  // always stages its whole 256-run range (contiguous in the plan) but writes
+  // only its own component's nodes
+  const int rs = onlyComp < 0 ? 0 : cnt->compStart[onlyComp];
+  const int re = onlyComp < 0 ? nRuns : cnt->compStart[onlyComp + 1];
+  for (int r0 = (rs / kBlock + blockIdx.x) * kBlock; r0 < re; r0 += gridDim.x * kBlock) {
     const int nHere = min(kBlock, nRuns - r0);
     // this thread's own node: everything its epilogue needs, loaded up front
     const int myR = r0 + threadIdx.x;
     const bool has = (int)threadIdx.x < nHere;
+    const bool mine = has && myR >= rs && myR < re;
     int comp = 0, i = 1, j = 1, k = 1, myLen = 0;
     long long off = 0;
     double uOld = 0.0, fo = 0.0;
@@ -869,7 +892,7 @@ __global__ void __launch_bounds__(kBlock, 8) k_spread(Geom g, const Counters* cn
       }
     }
     __syncthreads();
-    if (has) {
+    if (mine) {
       const double f = !staged ? prod[threadIdx.x] : (myLen > 0 ? prod[sStart[threadIdx.x] - base] : 0.0);
       fl.F(comp)[off] = f;
       if (MODE == 0) {
@@ -967,7 +990,8 @@ void build_spread_plan(Ctx& c) {
                                                       c.imgSrc, c.runStart, c.runCnt, c.planRoot, c.planW,
                                                       c.planAlloc, c.capContrib);
   k_plan_total<<<1, 1, 0, s>>>(c.dCnt, c.planAlloc);
-  c.launches += 4;
+  k_comp_bounds<<<1, 1, 0, s>>>(c.dCnt, c.runKey, c.g.nint);
+  c.launches += 5;
   c.planReady = true;
   c.spreadValid = false;
 }
@@ -980,25 +1004,28 @@ void launch_mdf_reset(Ctx& c, bool frozen) {
   c.spreadValid = true;
 }
 
-void launch_interp(Ctx& c) {
-  dim3 grid(nblocks(c.capLocal), 3);
+void launch_interp(Ctx& c, int comp) {
+  dim3 grid(nblocks(c.capLocal), comp < 0 ? 3 : 1);
+  const int comp0 = comp < 0 ? 0 : comp;
   if (c.g.unit_h)
-    k_interp<1><<<grid, kBlock, 0, c.stream>>>(c.rec(), c.g, c.dCnt, c.W, c.win, fields_of(c), c.fv);
+    k_interp<1><<<grid, kBlock, 0, c.stream>>>(c.rec(), c.g, c.dCnt, c.W, c.win, fields_of(c), c.fv, comp0);
   else
-    k_interp<0><<<grid, kBlock, 0, c.stream>>>(c.rec(), c.g, c.dCnt, c.W, c.win, fields_of(c), c.fv);
+    k_interp<0><<<grid, kBlock, 0, c.stream>>>(c.rec(), c.g, c.dCnt, c.W, c.win, fields_of(c), c.fv, comp0);
   c.launches++;
 }
 
 // the spread with the post-guess fused (MODE 0) or keeping fx and fxOld for a
 // separate VelocityPostGuess (MODE 1); the halo writes know about walls only
 // when the case has some
-void launch_spread(Ctx& c, bool fused_post_guess) {
+void launch_spread(Ctx& c, bool fused_post_guess, int comp) {
   const bool w = c.g.anyWall;
   auto k = fused_post_guess ? (w ? k_spread<0, true> : k_spread<0, false>)
                             : (w ? k_spread<1, true> : k_spread<1, false>);
   cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSpreadSmem);
-  k<<<run_blocks(c), kBlock, kSpreadSmem, c.stream>>>(c.g, c.dCnt, c.runStart, c.runCnt, c.runKey, c.planRoot,
-                                                            c.planW, c.fv, c.cap, fields_of(c), c.fCur, c.fPrev);
+  // one component: about a third of the runs, plus the block across its start
+  const int grid = comp < 0 ? run_blocks(c) : std::max(1, (run_blocks(c) + 2) / 3 + 1);
+  k<<<grid, kBlock, kSpreadSmem, c.stream>>>(c.g, c.dCnt, c.runStart, c.runCnt, c.runKey, c.planRoot, c.planW, c.fv,
+                                             c.cap, fields_of(c), c.fCur, c.fPrev, comp);
   c.launches++;
 }
 

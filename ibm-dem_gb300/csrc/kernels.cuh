@@ -116,6 +116,10 @@ struct Ctx {
   // that writes them waits for the copies
   cudaEvent_t fieldsRead = nullptr;
   bool fieldsReadPending = false;
+  // the MDF loop's component q finished (u|v|w and fx|fy|fz final) at
+  // compDone[q]; valid while no launch followed the loop (launches == compDoneAt)
+  cudaEvent_t compDone[3] = {};
+  long long compDoneAt = -1;
 
   // fluid stencils (fluid.cu): the fields beyond u,v,w,fx,fy,fz (indexed by
   // IBMDEM_FLUID_*, allocated on first use), the guess's output (3 fields), the
@@ -165,8 +169,9 @@ void build_spread_plan(Ctx& c);
 // c.stream (-1 on a CUDA error)
 long long count_touched_nodes(Ctx& c);
 void launch_mdf_reset(Ctx& c, bool frozen);
-void launch_interp(Ctx& c);
-void launch_spread(Ctx& c, bool fused_post_guess);
+// comp: one velocity component, or -1 for all three
+void launch_interp(Ctx& c, int comp);
+void launch_spread(Ctx& c, bool fused_post_guess, int comp);
 void launch_post_guess(Ctx& c);
 void record_written_nodes(Ctx& c);
 // Interpolation at n <= IBMDEM_PROBE_MAX_POINTS device points with the
