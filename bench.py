@@ -790,7 +790,7 @@ def run_ours(args):
         # the coupled sequence: fluid in, multi-direct forcing, the corrected
         # fluid and forcing out (six whole fields) while the bodies and lists
         # advance, bodies out
-        case._chk(case.lib.ibmdem_set_fluid(case.h, *[a.ctypes.data for a in hin]), "set_fluid")
+        case._chk(case.lib.ibmdem_set_fluid_async(case.h, *[a.ctypes.data for a in hin]), "set_fluid_async")
         case.MultiDirectForcing()
         case._chk(case.lib.ibmdem_get_fluid_async(case.h, *[a.ctypes.data for a in hout],
                                                   ctypes.c_void_p(copy_stream.cuda_stream)), "get_fluid_async")
@@ -848,8 +848,10 @@ def run_ours(args):
             "phases": per_phase,
             "e2e": {"value": e2e_val, "unit": "particle-steps/s", "h2d_bytes_per_step": 3 * fbytes,
                     "d2h_bytes_per_step": 6 * fbytes + nb * MULTISPHERE.itemsize, "steps": args.e2e_steps,
-                    "path": "ibmdem_set_fluid(host u,v,w) + ibmdem_MultiDirectForcing + "
-                            "ibmdem_get_fluid_async(u,v,w,fx,fy,fz; overlaps the next call) + ibmdem_CloudEvolutionMS + "
+                    "path": "ibmdem_set_fluid_async(host u,v,w; each component's forcing loop starts when it "
+                            "has arrived) + ibmdem_MultiDirectForcing (by component) + "
+                            "ibmdem_get_fluid_async(u,v,w,fx,fy,fz; each component leaves when done) + "
+                            "ibmdem_CloudEvolutionMS + "
                             "ibmdem_get_bodies, pinned host buffers",
                     "sparse_readout": {
                         "value": e2e_sparse, "d2h_bytes_per_step": int(upd_bytes.value) + nb * MULTISPHERE.itemsize,

@@ -306,6 +306,7 @@ int alloc_parcels(ibmdem_ctx* h, int np, long long nimg_est) {
 // latch device errors into a status (after a stream synchronise)
 int check_device(ibmdem_ctx* h) {
   Ctx& c = h->c;
+  wait_fields_read(c);  // an upload still pending finishes before the caller may reuse its arrays
   CU(cudaMemcpyAsync(c.hCnt, c.dCnt, sizeof(Counters), cudaMemcpyDeviceToHost, c.stream));
   CU(cudaStreamSynchronize(c.stream));
   if (c.planReady && c.hCnt->nRuns > 0) c.runsSeen = c.hCnt->nRuns;
@@ -541,7 +542,7 @@ int ibmdem_synchronize(ibmdem_ctx* h) {
 
 static int ensure_plan(ibmdem_ctx* h);
 
-int ibmdem_set_fluid(ibmdem_ctx* h, const double* u, const double* v, const double* w) {
+static int set_fluid(ibmdem_ctx* h, const double* u, const double* v, const double* w, bool async) {
   CHECK_CTX();
   if (!u || !v || !w) return set_error(h, IBMDEM_EINVAL, "null field");
   Ctx& c = h->c;
@@ -557,6 +558,31 @@ int ibmdem_set_fluid(ibmdem_ctx* h, const double* u, const double* v, const doub
   double* dst[3] = {c.u, c.v, c.w};
   double* frozen[3] = {c.u0, c.v0, c.w0};
   const double* src[3] = {u, v, w};
+  if (async) {
+    // Everything of the fields on a second stream, component by component:
+    // the upload, then its frozen copy.  The context's stream clears the
+    // forcing and builds the plan meanwhile, and the forcing loop waits for
+    // each component only when it reaches it (mdf).
+    if (!c.upStream) CU(cudaStreamCreateWithFlags(&c.upStream, cudaStreamNonBlocking));
+    if (!c.upStart) CU(cudaEventCreateWithFlags(&c.upStart, cudaEventDisableTiming));
+    for (cudaEvent_t& e : c.upDone)
+      if (!e) CU(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    CU(cudaEventRecord(c.upStart, c.stream));
+    CU(cudaStreamWaitEvent(c.upStream, c.upStart, 0));
+    for (int q = 0; q < 3; ++q) {
+      CU(cudaMemcpyAsync(dst[q], src[q], nb, cudaMemcpyHostToDevice, c.upStream));
+      CU(cudaMemcpyAsync(frozen[q], dst[q], nb, cudaMemcpyDeviceToDevice, c.upStream));
+      CU(cudaEventRecord(c.upDone[q], c.upStream));
+    }
+    c.uploadPending = true;
+    CU(cudaMemsetAsync(c.fx, 0, nb, c.stream));
+    CU(cudaMemsetAsync(c.fy, 0, nb, c.stream));
+    CU(cudaMemsetAsync(c.fz, 0, nb, c.stream));
+    CU(cudaMemsetAsync(&c.dCnt->nLast, 0, sizeof(int), c.stream));
+    c.haveFluid = true;
+    if (planBeside) return ensure_plan(h);
+    return launch_status(h);
+  }
   if (planBeside) {
     // The uploads go on a second stream; the context's stream clears the
     // forcing and builds the plan meanwhile, then copies each component to the
@@ -598,6 +624,14 @@ int ibmdem_set_fluid(ibmdem_ctx* h, const double* u, const double* v, const doub
   // synchronous for pageable host memory semantics: the caller may reuse u,v,w
   CU(cudaStreamSynchronize(c.stream));
   return IBMDEM_OK;
+}
+
+int ibmdem_set_fluid(ibmdem_ctx* h, const double* u, const double* v, const double* w) {
+  return set_fluid(h, u, v, w, false);
+}
+
+int ibmdem_set_fluid_async(ibmdem_ctx* h, const double* u, const double* v, const double* w) {
+  return set_fluid(h, u, v, w, true);
 }
 
 int ibmdem_get_fluid_async(ibmdem_ctx* h, double* u, double* v, double* w, double* fx, double* fy, double* fz,
@@ -1062,7 +1096,8 @@ int ibmdem_InitializationDEM(ibmdem_ctx* h) {
 static int mdf(ibmdem_ctx* h, bool frozen) {
   Ctx& c = h->c;
   REQUIRE(c.haveFluid, "no fluid field");
-  wait_fields_read(c);
+  const bool perCompUpload = !frozen && c.uploadPending;  // ibmdem_set_fluid_async still uploading
+  wait_fields_read(c, !perCompUpload);
   int rc = ensure_plan(h);
   if (rc) return rc;
   {
@@ -1082,7 +1117,9 @@ static int mdf(ibmdem_ctx* h, bool frozen) {
   cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
   cudaStreamIsCapturing(c.stream, &cap);
   const bool byComp = !frozen && cap == cudaStreamCaptureStatusNone;
+  if (!byComp) wait_fields_read(c);
   for (int comp = byComp ? 0 : -1; comp < (byComp ? 3 : 0); ++comp) {
+    if (byComp && perCompUpload) cudaStreamWaitEvent(c.stream, c.upDone[comp], 0);
     for (int it = 0; it < c.p.Ns; ++it) {
       {
         PhaseScope t(c, P_INTERP);
@@ -1106,6 +1143,7 @@ static int mdf(ibmdem_ctx* h, bool frozen) {
     PhaseScope t(c, P_RESET);
     record_written_nodes(c);
   }
+  if (perCompUpload) c.uploadPending = false;  // the stream has waited for the last component
   c.compDoneAt = byComp ? c.launches : -1;
   return launch_status(h);
 }

@@ -132,6 +132,7 @@ struct Ctx {
   // ibmdem_set_fluid: the uploads on their own stream, beside a spread plan build
   cudaStream_t upStream = nullptr;
   cudaEvent_t upStart = nullptr, upDone[3] = {};  // upDone[q]: component q uploaded
+  bool uploadPending = false;  // ibmdem_set_fluid_async: the context's stream has not waited for upDone yet
 
   // state flags
   bool haveFluid = false, haveParcels = false, listsBuilt = false;
@@ -200,10 +201,16 @@ struct ibmdem_ctx {
 };
 
 // order the context's stream after an ibmdem_get_fluid_async still reading the fields
-inline void wait_fields_read(ibmdem::Ctx& c) {
+// and, unless only the read-out matters (uploads = false), after an
+// ibmdem_set_fluid_async still uploading
+inline void wait_fields_read(ibmdem::Ctx& c, bool uploads = true) {
   if (c.fieldsReadPending) {
     cudaStreamWaitEvent(c.stream, c.fieldsRead, 0);
     c.fieldsReadPending = false;
+  }
+  if (uploads && c.uploadPending) {
+    cudaStreamWaitEvent(c.stream, c.upDone[2], 0);  // the uploads run in order on one stream
+    c.uploadPending = false;
   }
 }
 

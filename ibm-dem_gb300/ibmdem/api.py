@@ -44,7 +44,7 @@ EXPORTS = [
     "ibmdem_unresolved_step", "ibmdem_unresolved_synchronize", "ibmdem_unresolved_launch_count",
     "ibmdem_CalculateDragForce", "ibmdem_unresolved_timing_enable", "ibmdem_unresolved_get_timing",
     "ibmdem_unresolved_phase_name", "ibmdem_get_fluid_async",
-    "ibmdem_set_fluid_params", "ibmdem_set_fluid_field", "ibmdem_get_fluid_field", "ibmdem_StoreOldVelocity",
+    "ibmdem_set_fluid_async", "ibmdem_set_fluid_params", "ibmdem_set_fluid_field", "ibmdem_get_fluid_field", "ibmdem_StoreOldVelocity",
     "ibmdem_VelocityGuess", "ibmdem_FillGhostRegionForFluid", "ibmdem_Boundary", "ibmdem_ModifyBulkVelocity",
     "ibmdem_VelocityDivergence", "ibmdem_PressureCorrection", "ibmdem_VelocityCorrection",
 ]
@@ -78,6 +78,7 @@ def load(path=LIB_PATH):
     lib.ibmdem_set_stream.argtypes = [vp, vp]
     lib.ibmdem_synchronize.argtypes = [vp]
     lib.ibmdem_set_fluid.argtypes = [vp, vp, vp, vp]
+    lib.ibmdem_set_fluid_async.argtypes = [vp, vp, vp, vp]
     lib.ibmdem_get_fluid.argtypes = [vp] + [vp] * 6
     lib.ibmdem_get_fluid_async.argtypes = [vp] + [vp] * 6 + [vp]
     lib.ibmdem_set_parcels.argtypes = [vp, i32, vp]

@@ -119,6 +119,13 @@ int ibmdem_synchronize(ibmdem_ctx* ctx);
  * spread (new weights), the spread plan for them is built while the fields
  * upload, on a second stream of the same device. */
 int ibmdem_set_fluid(ibmdem_ctx* ctx, const double* u, const double* v, const double* w);
+/* ibmdem_set_fluid without waiting for the copies: they run on a second stream
+ * of the device, component by component, and the forcing loop of
+ * ibmdem_MultiDirectForcing starts on each velocity component as soon as that
+ * component has arrived.  The caller keeps u,v,w unchanged until the next call
+ * that synchronises the context (a getter such as ibmdem_get_bodies, or
+ * ibmdem_synchronize). */
+int ibmdem_set_fluid_async(ibmdem_ctx* ctx, const double* u, const double* v, const double* w);
 /* Copy out u,v,w and the momentum source fx,fy,fz (vars.F90:63), same layout.
  * Any pointer may be NULL. */
 int ibmdem_get_fluid(ibmdem_ctx* ctx, double* u, double* v, double* w,
