@@ -547,6 +547,7 @@ static int set_fluid(ibmdem_ctx* h, const double* u, const double* v, const doub
   if (!u || !v || !w) return set_error(h, IBMDEM_EINVAL, "null field");
   Ctx& c = h->c;
   wait_fields_read(c);
+  c.compDoneAt = -1;  // the fields change: no read-out may start from the last forcing loop's marks
   // a sparse read-out may still be writing the caller's arrays
   int ru = fluid_update_join(c);
   if (ru) return ru;

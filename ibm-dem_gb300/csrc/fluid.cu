@@ -394,6 +394,7 @@ int ibmdem_set_fluid_field(ibmdem_ctx* h, int32_t which, const double* a) {
     c.err = "ibmdem_set_fluid_field: bad field or null array";
     return IBMDEM_EINVAL;
   }
+  c.compDoneAt = -1;  // the fields change after the last forcing loop
   if (cudaMemcpyAsync(d, a, sizeof(double) * (size_t)c.g.ncell, cudaMemcpyHostToDevice, c.stream) != cudaSuccess ||
       cudaStreamSynchronize(c.stream) != cudaSuccess)
     return IBMDEM_ECUDA;
