@@ -777,7 +777,7 @@ def run_ours(args):
         # the coupled sequence of a caller that keeps its fields: fluid in,
         # multi-direct forcing, the changed nodes of u,v,w and the forcing back
         # into the caller's arrays while the bodies and lists advance, bodies out
-        case._chk(case.lib.ibmdem_set_fluid(case.h, *[a.ctypes.data for a in hin]), "set_fluid")
+        case._chk(case.lib.ibmdem_set_fluid_async(case.h, *[a.ctypes.data for a in hin]), "set_fluid_async")
         case.MultiDirectForcing()
         case._chk(case.lib.ibmdem_update_fluid_async(case.h, *[a.ctypes.data for a in hin + hf],
                                                      ctypes.c_void_p(copy_stream.cuda_stream)), "update_fluid_async")
