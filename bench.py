@@ -474,6 +474,31 @@ FLUID_BYTES = {
 FLUID_GUESS_FP64 = 18 * 5 + 9 + 9 * 4 + 3 * 2 + 3 * 7 + 3 * 7
 
 
+def poisson_counts(n, walls):
+    """HBM bytes and FP64 operations of one PoissonSolver on an n grid (nx, ny,
+    nz) with the walled axes doubled: the passes over the complex grid (the
+    ordered sum and the x forward read velDiv, x/y forward and the z solve
+    read and write the grid, the y and x inverses cover the original z and y,
+    x inverse writes Pcorr) and the radix-2 butterflies (the first stage 4
+    adds, the others a 4-operation complex product and 4 adds) with the
+    eigenvalue scaling (2 multiplies, 2 adds, a division)."""
+    import math
+    ne = [2 * m if w else m for m, w in zip(n, walls)]
+
+    def line(N):
+        lg = int(math.log2(N))
+        return (N // 2) * (4 + 8 * (lg - 1))
+
+    tot = ne[0] * ne[1] * ne[2]
+    nint = n[0] * n[1] * n[2]
+    rows_x_inv = n[1] * n[2]
+    y_inv = ne[0] * n[2]
+    nbytes = (nint * 8 * 2 + tot * 16 + tot * 32 * 2 + y_inv * ne[1] * 32 + rows_x_inv * ne[0] * 16 + nint * 8)
+    ops = (ne[1] * ne[2] * line(ne[0]) + ne[0] * ne[2] * line(ne[1]) + 2 * ne[0] * ne[1] * line(ne[2])
+           + tot * 5 + y_inv * line(ne[1]) + rows_x_inv * line(ne[0]))
+    return nbytes, ops
+
+
 def run_fluid(args, device, stream, cpu=True):
     """The fluid step of FirstOrderForwardEuler around the Poisson solve on the GPU
     (fluid.F90:251-326 without SetPressureVector/PoissonSolver): uold = u,
@@ -523,6 +548,17 @@ def run_fluid(args, device, stream, cpu=True):
     ms = e0.elapsed_time(e1)
     launches = g.launches - l0
     ph = g.phase_times(reset=True)
+    # the Poisson solve alone: velDiv of the last step in, Pcorr out
+    for _ in range(3):
+        g.PoissonSolver()
+    g.synchronize()
+    kp = max(5, k // 2)
+    e0.record(stream)
+    for _ in range(kp):
+        g.PoissonSolver()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    pois_ms = e0.elapsed_time(e1) / kp
     g.close()
     nint = int(p["nx"]) * int(p["ny"]) * int(p["nz"])
     phases = {name: {"ms_per_step": ph[name][0] / k} for name in ("fluid_guess", "fluid_halo", "fluid_other")}
@@ -546,6 +582,19 @@ def run_fluid(args, device, stream, cpu=True):
                        "as in the reference's initialization; the Poisson solve (PETSc) is outside, Pcorr resident"
                        % "x".join(str(int(p[a])) for a in ("nx", "ny", "nz")),
            "timing": "CUDA events on the launching stream"}
+    dims = [int(p[a]) for a in ("nx", "ny", "nz")]
+    pb, pops = poisson_counts(dims, [int(p["bType"][2 * d]) == 1 for d in range(3)])
+    out["poisson"] = {
+        "ms_per_solve": pois_ms, "solves": kp, "value": nint / (pois_ms / 1e3), "unit": "interior node-solves/s",
+        "method": "direct FFT solve of the reference's pinned 7-point system (FP64, hand-written radix-2 lines in "
+                  "shared memory; 8 launches)",
+        "roofline": {"bound": "fp64", "fp64_ops_per_solve": pops,
+                     "fp64_achieved_gops": pops / (pois_ms / 1e3) / 1e9, "fp64_peak_gops": fp64_peak,
+                     "fp64_frac": pops / (pois_ms / 1e3) / 1e9 / fp64_peak if fp64_peak else None,
+                     "hbm_bytes_per_solve": pb, "hbm_achieved_gbs": pb / (pois_ms / 1e3) / 1e9,
+                     "hbm_peak_gbs": hbm_peak},
+        "cpu_baseline": None,
+        "cpu_baseline_note": "the reference solves with PETSc GMRES + hypre, which cannot be built here"}
     if cpu:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         import oracle as O

@@ -360,7 +360,7 @@ static cudaEvent_t take_event(Ctx& c) {
 }
 static const char* const kPhaseLabels[P_COUNT] = {"interp", "spread", "weights", "plan", "cells", "pairs",
                                                   "force", "bodysum", "bodymove", "markers", "images", "reset",
-                                                  "fluid_guess", "fluid_halo", "fluid_other"};
+                                                  "fluid_guess", "fluid_halo", "fluid_other", "fluid_poisson"};
 // Every phase is an NVTX range (visible to any attached profiler, a few ns
 // otherwise); with timing on it is also bracketed by CUDA events.
 PhaseScope::PhaseScope(Ctx& ctx, int ph) : c(ctx), phase(ph) {
@@ -482,6 +482,7 @@ int ibmdem_destroy(ibmdem_ctx* h) {
   output_release(c);
   fluid_update_release(c);
   fluid_release(c);
+  poisson_release(c);
   cudaStreamSynchronize(c.stream);
   free_parcel_buffers(c);
   void* ps[] = {c.u, c.v, c.w, c.u0, c.v0, c.w0, c.fx, c.fy, c.fz, c.cellStart, c.dCnt, c.dTotal, c.dBodies,

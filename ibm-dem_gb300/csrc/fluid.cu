@@ -325,6 +325,8 @@ static int fluid_alloc(Ctx& c) {
   return IBMDEM_OK;
 }
 
+int fluid_fields(Ctx& c) { return fluid_alloc(c); }
+
 void fluid_release(Ctx& c) {
   for (int q = IBMDEM_FLUID_UOLD; q < IBMDEM_FLUID_NFIELDS; ++q)
     if (c.ffield[q]) cudaFreeAsync(c.ffield[q], c.stream);

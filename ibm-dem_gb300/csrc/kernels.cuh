@@ -11,6 +11,15 @@ namespace ibmdem {
 struct OutputState;  // output.cu: snapshot buffers and the file writer thread
 struct FluidUpdate;  // readout.cu: the sparse field read-out
 
+// poisson.cu: the transform grid and tables of the Poisson solve
+struct PoissonPlan {
+  double2* X = nullptr;   // extended complex grid, x fastest
+  double* aux = nullptr;  // twiddles, eigenvalues, ordered sums
+  int ne[3] = {}, logn[3] = {};
+  size_t twOff[3] = {}, lamOff[3] = {}, partOff = 0;
+  long long total = 0;
+};
+
 struct Ctx {
   ibmdem_params p{};
   Geom g{};
@@ -129,6 +138,9 @@ struct Ctx {
   double* fsum = nullptr;
   double visc = 0.0, CPx = 0.0, CPy = 0.0, CPz = 0.0;
 
+  // the Poisson solve (poisson.cu), planned on first use
+  PoissonPlan pois;
+
   // ibmdem_set_fluid: the uploads on their own stream, beside a spread plan build
   cudaStream_t upStream = nullptr;
   cudaEvent_t upStart = nullptr, upDone[3] = {};  // upDone[q]: component q uploaded
@@ -143,7 +155,7 @@ struct Ctx {
 // timed phases (names in api.cu: ibmdem_phase_name)
 enum Phase : int {
   P_INTERP = 0, P_SPREAD, P_WEIGHTS, P_PLAN, P_CELLS, P_PAIRS, P_FORCE, P_BODYSUM, P_BODYMOVE, P_MARKERS,
-  P_IMAGES, P_RESET, P_FGUESS, P_FHALO, P_FOTHER, P_COUNT
+  P_IMAGES, P_RESET, P_FGUESS, P_FHALO, P_FOTHER, P_FPOISSON, P_COUNT
 };
 // records CUDA events around one phase on the context's stream when timing is on
 struct PhaseScope {
@@ -183,6 +195,8 @@ cudaError_t interpolate_points_noalloc(Ctx& c, int n, const double* x, double* u
 void output_release(Ctx& c);
 // fluid.cu: free the fluid stencils' fields
 void fluid_release(Ctx& c);
+int fluid_fields(Ctx& c);     // the fluid stencils' fields, allocated on first use
+void poisson_release(Ctx& c);
 // readout.cu: finish a pending sparse read-out (its status), and free its buffers
 int fluid_update_join(Ctx& c);
 void fluid_update_release(Ctx& c);

@@ -46,7 +46,7 @@ EXPORTS = [
     "ibmdem_unresolved_phase_name", "ibmdem_get_fluid_async",
     "ibmdem_set_fluid_async", "ibmdem_set_fluid_params", "ibmdem_set_fluid_field", "ibmdem_get_fluid_field", "ibmdem_StoreOldVelocity",
     "ibmdem_VelocityGuess", "ibmdem_FillGhostRegionForFluid", "ibmdem_Boundary", "ibmdem_ModifyBulkVelocity",
-    "ibmdem_VelocityDivergence", "ibmdem_PressureCorrection", "ibmdem_VelocityCorrection",
+    "ibmdem_VelocityDivergence", "ibmdem_PressureCorrection", "ibmdem_VelocityCorrection", "ibmdem_PoissonSolver",
 ]
 
 SUBROUTINES = [
@@ -101,6 +101,7 @@ def load(path=LIB_PATH):
     lib.ibmdem_VelocityGuess.argtypes = [vp, d, d, d]
     lib.ibmdem_VelocityDivergence.argtypes = [vp, d]
     lib.ibmdem_VelocityCorrection.argtypes = [vp, d]
+    lib.ibmdem_PoissonSolver.argtypes = [vp]
     lib.ibmdem_PressureCorrection.argtypes = [vp, vp]
     lib.ibmdem_ModifyBulkVelocity.argtypes = [vp, i32, i32, i32, d, d, d]
     lib.ibmdem_timing_enable.argtypes = [vp, i32]
@@ -324,6 +325,11 @@ class Case:
 
     def VelocityCorrection(self, cRK):
         self._chk(self.lib.ibmdem_VelocityCorrection(self.h, cRK), "VelocityCorrection")
+
+    def PoissonSolver(self):
+        """SetPressureVector + PoissonSolver (poisson.F90:110-186): PCORR on the
+        interior from VELDIV."""
+        self._chk(self.lib.ibmdem_PoissonSolver(self.h), "PoissonSolver")
 
     def set_wall_probes(self, probes):
         """Wall collision probes (records.WALL_PROBE) on solid-wall faces."""

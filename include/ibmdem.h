@@ -460,6 +460,15 @@ int ibmdem_VelocityDivergence(ibmdem_ctx* ctx, double cRK);
 int ibmdem_PressureCorrection(ibmdem_ctx* ctx, const double* Pcorr);
 /* VelocityCorrection(cRK) (fluid.F90:210-237), then the vorticity. */
 int ibmdem_VelocityCorrection(ibmdem_ctx* ctx, double cRK);
+/* SetPressureVector + PoissonSolver + GetLocalArray (poisson.F90:110-186):
+ * PCORR on the interior nodes solves the reference's system -- the 7-point
+ * Laplacian of SetPressureCorrectionJacobian (poisson.F90:50-108), periodic
+ * or Neumann behind a solid wall, with the row of interior node (1,1,1)
+ * replaced by PCORR = 0 -- for the right-hand side VELDIV.  Direct FFT solve
+ * (FP64), residual far below the reference's KSP tolerance (1e-10).  The
+ * halo of PCORR is left as it is.  IBMDEM_EUNSUPPORTED when an extent (doubled
+ * along a walled axis) is not a power of two and longer than 2048. */
+int ibmdem_PoissonSolver(ibmdem_ctx* ctx);
 
 /* ---- instrumentation -------------------------------------------------- */
 /* Record CUDA events around every phase of the drivers (interpolation,

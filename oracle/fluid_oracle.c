@@ -334,3 +334,38 @@ void orc_fluid_Boundary(orc_fluid* F) {
         for (int i = lo[0]; i <= hi[0]; ++i) f[fx_(F, i, j, k)] = 0.0;
   }
 }
+
+/* The matrix of SetPressureCorrectionJacobian (poisson.F90:50-108) applied to
+ * p (field layout) into out (interior nodes; the rest left as it is): each
+ * row but global cell 0 -- interior node (1,1,1) -- holds -1/dl^2 for each
+ * neighbour of GlobalNeighCellIndex (initialization.F90:105-170: periodic
+ * wrap, absent behind a face of bType 1) and minus their sum on the
+ * diagonal; the row of cell 0 is the identity (pConstIdx = 1).  Used to check
+ * a solve against the reference's own linear system. */
+void orc_fluid_PressureOperator(orc_fluid* F, const double* p, double* out) {
+  const double dl[3] = {F->dx, F->dy, F->dz};
+  LOOP_INTERIOR {
+    const int64_t c = fx_(F, i, j, k);
+    if (i == 1 && j == 1 && k == 1) {
+      out[c] = p[c];
+      continue;
+    }
+    double vc = 0.0, acc = 0.0;
+    for (int l = 1; l <= 6; ++l) {
+      const int dim = (l + 1) / 2;
+      const int sh = 2 * ((l + 1) % 2) - 1;
+      int ijk[3] = {i, j, k};
+      ijk[dim - 1] += sh;
+      const int n = F->n[dim - 1];
+      if (ijk[dim - 1] < 1 || ijk[dim - 1] > n) {
+        if (F->bType[l - 1] == 1) continue;
+        ijk[dim - 1] = (ijk[dim - 1] + n - 1) % n + 1;
+      }
+      const double value = -1.0 / (dl[dim - 1] * dl[dim - 1]);
+      acc = acc + value * p[fx_(F, ijk[0], ijk[1], ijk[2])];
+      vc = vc + value;
+    }
+    vc = -vc;
+    out[c] = acc + vc * p[c];
+  }
+}

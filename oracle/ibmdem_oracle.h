@@ -100,6 +100,7 @@ void orc_fluid_ModifyBulkVelocity(orc_fluid* F, int swU, int swV, int swW, doubl
 void orc_fluid_VelocityDivergence(orc_fluid* F, double cRK);
 void orc_fluid_PressureCorrection(orc_fluid* F);
 void orc_fluid_VelocityCorrection(orc_fluid* F, double cRK);
+void orc_fluid_PressureOperator(orc_fluid* F, const double* p, double* out);
 
 #ifdef __cplusplus
 }

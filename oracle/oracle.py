@@ -88,6 +88,7 @@ def _load():
     lib.orc_fluid_VelocityGuess.argtypes = [vp, d, d, d]
     lib.orc_fluid_VelocityDivergence.argtypes = [vp, d]
     lib.orc_fluid_VelocityCorrection.argtypes = [vp, d]
+    lib.orc_fluid_PressureOperator.argtypes = [vp, vp, vp]
     lib.orc_fluid_ModifyBulkVelocity.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, d, d, d]
     _lib = lib
     return lib
@@ -381,3 +382,12 @@ class OracleFluid:
 
     def VelocityCorrection(self, cRK):
         self.lib.orc_fluid_VelocityCorrection(self.h, cRK)
+
+    def PressureOperator(self, p):
+        """The reference's pressure-correction matrix (with the pinned row)
+        applied to the field p: the interior of the result, halo zero."""
+        p = np.ascontiguousarray(p, dtype=np.float64)
+        assert p.shape == tuple(self.shape)
+        out = np.zeros(self.shape, np.float64)
+        self.lib.orc_fluid_PressureOperator(self.h, p.ctypes.data, out.ctypes.data)
+        return out
