@@ -13,9 +13,9 @@ struct FluidUpdate;  // readout.cu: the sparse field read-out
 
 // poisson.cu: the transform grid and tables of the Poisson solve
 struct PoissonPlan {
-  double2* X = nullptr;   // extended complex grid, x fastest
+  double2* X = nullptr;   // half spectrum along x of the extended grid, x fastest
   double* aux = nullptr;  // twiddles, eigenvalues, ordered sums
-  int ne[3] = {}, logn[3] = {};
+  int ne[3] = {}, logn[3] = {}, nh = 0;
   size_t twOff[3] = {}, lamOff[3] = {}, partOff = 0;
   long long total = 0;
 };

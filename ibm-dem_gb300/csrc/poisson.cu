@@ -24,7 +24,9 @@
 // The FFTs are FP64 and hand-written: a block holds L lines of one axis in
 // shared memory and transforms them in place (radix-2 Cooley-Tukey for
 // power-of-two lengths, a direct DFT otherwise), so each pass streams the
-// complex grid once.  The z pass does forward transform, division by lambda and
+// complex grid once.  The data are real, so two rows share one complex x
+// transform and only the n'/2 + 1 x columns of the half spectrum are kept and
+// transformed along y and z: half the work and half the grid.  The z pass does forward transform, division by lambda and
 // inverse transform while the lines are in shared memory.  Launches, on the
 // context's stream: the ordered right-hand-side sum (2), x forward, y forward,
 // z solve, y inverse, q_0 (1 block), x inverse writing Pcorr.
@@ -46,13 +48,14 @@ constexpr int kMaxDirect = 2048;           // longest non-power-of-two line (dir
 constexpr size_t kMaxSmem = 160 * 1024;    // dynamic shared memory of one block
 
 struct PoisArgs {
-  double2* X;            // the extended complex grid, x fastest
+  double2* X;            // the half spectrum along x (nh columns) of the extended grid, x fastest
   const double2* tw[3];  // exp(-2 pi i j / ne[d]), j < ne[d]
   const double* lam[3];  // 4 sin^2(pi k / ne[d]) / dl^2
   double* part;          // kPSumBlocks ordered partial sums, then S, then q_0
   int ne[3];             // extended extents (n, or 2n for a walled axis)
   int logn[3];           // log2(ne[d]) for a power of two, else -1
-  int L[3];              // lines per block of each axis
+  int L[3];              // lines per block of each axis (x: pairs of rows)
+  int nh;                // x columns kept: ne[0]/2 + 1 (the rest follow by conjugate symmetry)
   double scale;          // 1 / (ne0 ne1 ne2)
 };
 
@@ -154,32 +157,44 @@ __global__ void k_pois_total(double* part) {
   part[kPSumBlocks] = s;
 }
 
-// x forward: block holds L[0] rows (y', z') of the extended grid, read from
-// the right-hand side with the mirrors of walled axes and the pinned value
+// x forward: a block holds L[0] pairs of rows (y', z') of the extended grid,
+// read from the right-hand side with the mirrors of walled axes and the
+// pinned value.  Rows 2p and 2p+1 are the real and imaginary parts of one
+// complex line; after its transform Z, the rows' spectra are
+// A(k) = (Z(k) + conj Z(N-k))/2 and B(k) = (Z(k) - conj Z(N-k))/(2i), of which
+// k = 0..N/2 are kept.
 __global__ void __launch_bounds__(kPBlock) k_pois_xfwd(Geom g, PoisArgs a, const double* b) {
   extern __shared__ double2 sm[];
-  const int N = a.ne[0], L = a.L[0];
+  const int N = a.ne[0], L = a.L[0], nh = a.nh;
   double2* s = sm;
   double2* tmp = sm + L * N;
   const long long rows = (long long)a.ne[1] * a.ne[2];
-  const long long r0 = (long long)blockIdx.x * L;
+  const long long r0 = 2LL * blockIdx.x * L;
   const double pinned = -a.part[kPSumBlocks];
   for (int e = threadIdx.x; e < L * N; e += blockDim.x) {
     const int l = e / N, xe = e - l * N;
-    const long long r = r0 + l;
-    double v = 0.0;
-    if (r < rows) {
-      const int ye = (int)(r % a.ne[1]), ze = (int)(r / a.ne[1]);
-      const int x = src_of(xe, g.n[0]), y = src_of(ye, g.n[1]), z = src_of(ze, g.n[2]);
-      v = (x | y | z) == 0 ? pinned : b[field_off(g, x + 1, y + 1, z + 1)];
+    const int x = src_of(xe, g.n[0]);
+    double v[2] = {0.0, 0.0};
+    for (int h = 0; h < 2; ++h) {
+      const long long r = r0 + 2 * l + h;
+      if (r < rows) {
+        const int ye = (int)(r % a.ne[1]), ze = (int)(r / a.ne[1]);
+        const int y = src_of(ye, g.n[1]), z = src_of(ze, g.n[2]);
+        v[h] = (x | y | z) == 0 ? pinned : b[field_off(g, x + 1, y + 1, z + 1)];
+      }
     }
-    s[e] = make_double2(v, 0.0);
+    s[e] = make_double2(v[0], v[1]);
   }
   __syncthreads();
   lines_dft(s, tmp, N, a.logn[0], L, a.tw[0], false);
-  for (int e = threadIdx.x; e < L * N; e += blockDim.x) {
-    const int l = e / N;
-    if (r0 + l < rows) a.X[(r0 + l) * N + (e - l * N)] = s[e];
+  for (int e = threadIdx.x; e < L * nh; e += blockDim.x) {
+    const int l = e / nh, k = e - l * nh;
+    const long long ra = r0 + 2 * l;
+    if (ra >= rows) continue;
+    const double2 z = s[l * N + k];
+    const double2 m = s[l * N + (k == 0 ? 0 : N - k)];  // conj(m) = conj Z(N-k)
+    a.X[ra * nh + k] = make_double2(0.5 * (z.x + m.x), 0.5 * (z.y - m.y));
+    if (ra + 1 < rows) a.X[(ra + 1) * nh + k] = make_double2(0.5 * (z.y + m.y), -0.5 * (z.x - m.x));
   }
 }
 
@@ -190,7 +205,7 @@ __global__ void __launch_bounds__(kPBlock) k_pois_xfwd(Geom g, PoisArgs a, const
 // y' for d = 2).
 __global__ void __launch_bounds__(kPBlock) k_pois_lines(PoisArgs a, int d, int mode, int outer) {
   extern __shared__ double2 sm[];
-  const int N = a.ne[d], L = a.L[d], ne0 = a.ne[0];
+  const int N = a.ne[d], L = a.L[d], ne0 = a.nh;  // x columns of the half spectrum
   double2* s = sm;
   double2* tmp = sm + L * N;
   const int groups = (ne0 + L - 1) / L;
@@ -225,43 +240,59 @@ __global__ void __launch_bounds__(kPBlock) k_pois_lines(PoisArgs a, int d, int m
   }
 }
 
-// q_0 = the inverse x transform at x = 0 of row (0, 0): the sum of the row
-// in order (the 1/n' normalisation is in the lambda division)
+// q_0 = the inverse x transform at x = 0 of row (0, 0): the real parts of
+// the full spectrum summed, the conjugate half counted by doubling, in a
+// fixed order (the 1/n' normalisation is in the lambda division)
 __global__ void k_pois_q0(PoisArgs a) {
   if (threadIdx.x != 0) return;
-  double s = 0.0;
-  for (int k = 0; k < a.ne[0]; ++k) s = s + a.X[k].x;
+  const int N = a.ne[0];
+  double s = a.X[0].x, d = 0.0;
+  const int last = (N & 1) ? a.nh - 1 : a.nh - 2;  // the bins with a distinct conjugate
+  for (int k = 1; k <= last; ++k) d = d + a.X[k].x;
+  s = s + 2.0 * d;
+  if (!(N & 1) && N > 1) s = s + a.X[N / 2].x;
   a.part[kPSumBlocks + 1] = s;
 }
 
-// x inverse over the rows of the original grid, writing Pcorr = q - q_0
+// x inverse over pairs of rows of the original grid: Z = A + iB from the two
+// rows' half spectra (the other half by conjugate symmetry), one complex
+// inverse transform, the rows in its real and imaginary parts; Pcorr = q - q_0
 // (exactly 0 at the pinned node)
 __global__ void __launch_bounds__(kPBlock) k_pois_xinv(Geom g, PoisArgs a, double* pc) {
   extern __shared__ double2 sm[];
-  const int N = a.ne[0], L = a.L[0];
+  const int N = a.ne[0], L = a.L[0], nh = a.nh;
   double2* s = sm;
   double2* tmp = sm + L * N;
   const long long rows = (long long)g.n[1] * g.n[2];
-  const long long r0 = (long long)blockIdx.x * L;
+  const long long r0 = 2LL * blockIdx.x * L;
   for (int e = threadIdx.x; e < L * N; e += blockDim.x) {
-    const int l = e / N;
-    const long long r = r0 + l;
-    if (r < rows) {
-      const long long y = r % g.n[1], z = r / g.n[1];
-      s[e] = a.X[(z * a.ne[1] + y) * N + (e - l * N)];
-    } else {
-      s[e] = make_double2(0.0, 0.0);
+    const int l = e / N, k = e - l * N;
+    const bool lo = k < nh;
+    const int kk = lo ? k : N - k;
+    double2 v[2];
+    for (int h = 0; h < 2; ++h) {
+      const long long r = r0 + 2 * l + h;
+      v[h] = make_double2(0.0, 0.0);
+      if (r < rows) {
+        const long long y = r % g.n[1], z = r / g.n[1];
+        v[h] = a.X[(z * a.ne[1] + y) * nh + kk];
+        if (!lo) v[h].y = -v[h].y;
+      }
     }
+    s[e] = make_double2(v[0].x - v[1].y, v[0].y + v[1].x);
   }
   __syncthreads();
   lines_dft(s, tmp, N, a.logn[0], L, a.tw[0], true);
   const double q0 = a.part[kPSumBlocks + 1];
   for (int e = threadIdx.x; e < L * N; e += blockDim.x) {
     const int l = e / N, x = e - l * N;
-    const long long r = r0 + l;
-    if (r < rows && x < g.n[0]) {
+    if (x >= g.n[0]) continue;
+    for (int h = 0; h < 2; ++h) {
+      const long long r = r0 + 2 * l + h;
+      if (r >= rows) break;
       const int y = (int)(r % g.n[1]), z = (int)(r / g.n[1]);
-      pc[field_off(g, x + 1, y + 1, z + 1)] = (x | y | z) == 0 ? 0.0 : s[e].x - q0;
+      const double q = h == 0 ? s[e].x : s[e].y;
+      pc[field_off(g, x + 1, y + 1, z + 1)] = (x | y | z) == 0 ? 0.0 : q - q0;
     }
   }
 }
@@ -330,7 +361,9 @@ static int poisson_plan(Ctx& c) {
     off += (size_t)n;
   }
   p.partOff = off;
-  if (cudaMallocAsync(reinterpret_cast<void**>(&p.X), tot * sizeof(double2), c.stream) != cudaSuccess) {
+  p.nh = p.ne[0] / 2 + 1;
+  const size_t half = (size_t)p.nh * p.ne[1] * p.ne[2];
+  if (cudaMallocAsync(reinterpret_cast<void**>(&p.X), half * sizeof(double2), c.stream) != cudaSuccess) {
     p.X = nullptr;
     c.err = "ibmdem_PoissonSolver: out of device memory for the transform grid";
     return IBMDEM_ENOMEM;
@@ -346,7 +379,7 @@ static int poisson_plan(Ctx& c) {
       cudaStreamSynchronize(c.stream) != cudaSuccess)
     return IBMDEM_ECUDA;
   p.total = (long long)tot;
-  c.bytes += tot * sizeof(double2) + aux * sizeof(double);
+  c.bytes += half * sizeof(double2) + aux * sizeof(double);
   cudaFuncSetAttribute(k_pois_xfwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem);
   cudaFuncSetAttribute(k_pois_lines, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem);
   cudaFuncSetAttribute(k_pois_xinv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem);
@@ -401,21 +434,22 @@ int ibmdem_PoissonSolver(ibmdem_ctx* h) {
   const double* b = c.ffield[IBMDEM_FLUID_VELDIV];
   double* pc = c.ffield[IBMDEM_FLUID_PCORR];
   const long long per = (c.g.nint + kPSumBlocks - 1) / kPSumBlocks;
-  const int groups = (p.ne[0] + a.L[1] - 1) / a.L[1];
-  const int groupsZ = (p.ne[0] + a.L[2] - 1) / a.L[2];
+  a.nh = p.nh;
+  const int groups = (p.nh + a.L[1] - 1) / a.L[1];
+  const int groupsZ = (p.nh + a.L[2] - 1) / a.L[2];
   {
     PhaseScope ps(c, P_FPOISSON);
     k_pois_partial<<<kPSumBlocks, kPBlock, 0, c.stream>>>(c.g, b, a.part, per);
     k_pois_total<<<1, 32, 0, c.stream>>>(a.part);
     const long long rowsE = (long long)p.ne[1] * p.ne[2];
-    k_pois_xfwd<<<(unsigned)((rowsE + a.L[0] - 1) / a.L[0]), kPBlock, smem_of(a, 0), c.stream>>>(c.g, a, b);
+    k_pois_xfwd<<<(unsigned)((rowsE + 2 * a.L[0] - 1) / (2 * a.L[0])), kPBlock, smem_of(a, 0), c.stream>>>(c.g, a, b);
     // y forward over every z', z solve over every y', y inverse over z' < nz
     k_pois_lines<<<(unsigned)((long long)groups * p.ne[2]), kPBlock, smem_of(a, 1), c.stream>>>(a, 1, 0, p.ne[2]);
     k_pois_lines<<<(unsigned)((long long)groupsZ * p.ne[1]), kPBlock, smem_of(a, 2), c.stream>>>(a, 2, 2, p.ne[1]);
     k_pois_lines<<<(unsigned)((long long)groups * c.g.n[2]), kPBlock, smem_of(a, 1), c.stream>>>(a, 1, 1, c.g.n[2]);
     k_pois_q0<<<1, 32, 0, c.stream>>>(a);
     const long long rows = (long long)c.g.n[1] * c.g.n[2];
-    k_pois_xinv<<<(unsigned)((rows + a.L[0] - 1) / a.L[0]), kPBlock, smem_of(a, 0), c.stream>>>(c.g, a, pc);
+    k_pois_xinv<<<(unsigned)((rows + 2 * a.L[0] - 1) / (2 * a.L[0])), kPBlock, smem_of(a, 0), c.stream>>>(c.g, a, pc);
   }
   c.launches += 8;
   const cudaError_t e = cudaGetLastError();

@@ -113,6 +113,8 @@ def test_bulk_velocity_within_tolerance(gpu_lib, oracle_mod):
 
 @pytest.mark.parametrize("dims,walls,h", [
     ((20, 18, 16), "", 1.0),        # direct DFT lines
+    ((21, 15, 9), "", 1.0),         # odd x: no self-conjugate middle column
+    ((21, 15, 9), "y", 0.8),
     ((20, 18, 16), "z", 1.0),
     ((20, 18, 16), "xyz", 0.7),
     ((32, 32, 64), "", 1.0),        # radix-2 lines
