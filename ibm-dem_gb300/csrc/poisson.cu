@@ -22,7 +22,7 @@
 //    diagonal in Fourier space: lambda = sum_d 4 sin^2(pi k_d / n'_d) / dl_d^2.
 //
 // The FFTs are FP64 and hand-written: a block holds L lines of one axis in
-// shared memory and transforms them in place (radix-2 Cooley-Tukey for
+// shared memory and transforms them in place (radix-4 Cooley-Tukey for
 // power-of-two lengths, a direct DFT otherwise), so each pass streams the
 // complex grid once.  The data are real, so two rows share one complex x
 // transform and only the n'/2 + 1 x columns of the half spectrum are kept and
@@ -80,22 +80,51 @@ __device__ void lines_dft(double2* s, double2* tmp, int N, int logN, int L, cons
       }
     }
     __syncthreads();
-    const int half = N >> 1;
-    for (int lm = 0; lm < logN; ++lm) {
-      const int m = 1 << lm;
+    int lm = 0;
+    if (logN & 1) {
+      // an odd number of stages: one radix-2 stage of unit twiddles first
       for (int b = threadIdx.x; b < (tot >> 1); b += blockDim.x) {
-        const int l = b >> (logN - 1), t = b & (half - 1);
-        const int o = t & (m - 1);
-        const int i0 = l * N + ((t >> lm) << (lm + 1)) + o;
-        const double2 a = s[i0];
-        double2 c = s[i0 + m];
-        if (lm > 0) {
-          double2 w = tw[o << (logN - 1 - lm)];
-          if (inv) w.y = -w.y;
-          c = cmul(c, w);
-        }
+        const int i0 = 2 * b;
+        const double2 a = s[i0], c = s[i0 + 1];
         s[i0] = make_double2(a.x + c.x, a.y + c.y);
-        s[i0 + m] = make_double2(a.x - c.x, a.y - c.y);
+        s[i0 + 1] = make_double2(a.x - c.x, a.y - c.y);
+      }
+      __syncthreads();
+      lm = 1;
+    }
+    // radix-4 stages: two radix-2 stages at once.  After the bit reversal the
+    // four blocks of m points of a group of 4m hold the sub-transforms of the
+    // residues 0, 2, 1, 3 (mod 4); with W = exp(-+2 pi i / 4m) the group's
+    // outputs are the 4-point transform of (a0, W^o a2, W^2o a1, W^3o a3):
+    // 3 complex products and 16 adds for 4 points (radix-2: 4 and 16).
+    for (; lm < logN; lm += 2) {
+      const int m = 1 << lm;
+      const int sh = logN - 2 - lm;  // W^j = tw[j << sh]
+      for (int b = threadIdx.x; b < (tot >> 2); b += blockDim.x) {
+        const int l = b >> (logN - 2), t = b & ((N >> 2) - 1);
+        const int o = t & (m - 1);
+        const int i0 = l * N + ((t >> lm) << (lm + 2)) + o;
+        const double2 a0 = s[i0];
+        double2 t2 = s[i0 + m], t1 = s[i0 + 2 * m], t3 = s[i0 + 3 * m];
+        if (lm > 0) {
+          double2 w1 = tw[o << sh], w2 = tw[(2 * o) << sh], w3 = tw[(3 * o) << sh];
+          if (inv) {
+            w1.y = -w1.y;
+            w2.y = -w2.y;
+            w3.y = -w3.y;
+          }
+          t1 = cmul(t1, w1);
+          t2 = cmul(t2, w2);
+          t3 = cmul(t3, w3);
+        }
+        const double2 u0 = make_double2(a0.x + t2.x, a0.y + t2.y), u1 = make_double2(a0.x - t2.x, a0.y - t2.y);
+        const double2 u2 = make_double2(t1.x + t3.x, t1.y + t3.y), u3 = make_double2(t1.x - t3.x, t1.y - t3.y);
+        // forward: X1 = u1 - i u3, X3 = u1 + i u3; inverse: the signs of i swap
+        const double2 ju3 = inv ? make_double2(-u3.y, u3.x) : make_double2(u3.y, -u3.x);
+        s[i0] = make_double2(u0.x + u2.x, u0.y + u2.y);
+        s[i0 + m] = make_double2(u1.x + ju3.x, u1.y + ju3.y);
+        s[i0 + 2 * m] = make_double2(u0.x - u2.x, u0.y - u2.y);
+        s[i0 + 3 * m] = make_double2(u1.x - ju3.x, u1.y - ju3.y);
       }
       __syncthreads();
     }
