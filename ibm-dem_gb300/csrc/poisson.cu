@@ -178,12 +178,22 @@ __global__ void k_pois_partial(Geom g, const double* b, double* part, long long 
   }
 }
 
-// S = the blocks' sums in order; the pinned row's value is -S
+// S = the blocks' sums in a fixed order (lane l adds blocks 32l..32l+31 in
+// order, then lane 0 adds the 32 lane sums in order); the pinned row's value
+// is -S.  One warp.
 __global__ void k_pois_total(double* part) {
-  if (threadIdx.x != 0) return;
+  static_assert(kPSumBlocks == 32 * 32, "one warp of 32 chunks");
+  __shared__ double sh[32];
+  const int l = threadIdx.x;
   double s = 0.0;
-  for (int r = 0; r < kPSumBlocks; ++r) s = s + part[r];
-  part[kPSumBlocks] = s;
+  for (int r = 0; r < 32; ++r) s = s + part[32 * l + r];
+  sh[l] = s;
+  __syncwarp();
+  if (l == 0) {
+    double t = 0.0;
+    for (int r = 0; r < 32; ++r) t = t + sh[r];
+    part[kPSumBlocks] = t;
+  }
 }
 
 // x forward: a block holds L[0] pairs of rows (y', z') of the extended grid,
@@ -241,31 +251,31 @@ __global__ void __launch_bounds__(kPBlock) k_pois_lines(PoisArgs a, int d, int m
   const int grp = (int)(blockIdx.x % groups), o = (int)(blockIdx.x / groups);
   if (o >= outer) return;
   const int x0 = grp * L;
+  const int La = min(L, ne0 - x0);  // the last group holds the columns that are left (nh is odd)
   const long long plane = (long long)ne0 * a.ne[1];
   const long long base = d == 1 ? (long long)o * plane + x0 : (long long)o * ne0 + x0;
   const long long stride = d == 1 ? ne0 : plane;
-  for (int e = threadIdx.x; e < L * N; e += blockDim.x) {
-    const int j = e / L, l = e - j * L;
-    s[l * N + j] = x0 + l < ne0 ? a.X[base + j * stride + l] : make_double2(0.0, 0.0);
+  for (int e = threadIdx.x; e < La * N; e += blockDim.x) {
+    const int j = e / La, l = e - j * La;
+    s[l * N + j] = a.X[base + j * stride + l];
   }
   __syncthreads();
-  lines_dft(s, tmp, N, a.logn[d], L, a.tw[d], mode == 1);
+  lines_dft(s, tmp, N, a.logn[d], La, a.tw[d], mode == 1);
   if (mode == 2) {
     // s[l*N + kz] holds the transform at (kx = x0 + l, ky = o, kz)
     const double ly = a.lam[1][o];
-    for (int e = threadIdx.x; e < L * N; e += blockDim.x) {
+    for (int e = threadIdx.x; e < La * N; e += blockDim.x) {
       const int l = e / N, kz = e - l * N;
-      const int kx = min(x0 + l, ne0 - 1);
-      const double den = a.lam[0][kx] + ly + a.lam[2][kz];
+      const double den = a.lam[0][x0 + l] + ly + a.lam[2][kz];
       const double f = den > 0.0 ? a.scale / den : 0.0;
       s[e] = make_double2(s[e].x * f, s[e].y * f);
     }
     __syncthreads();
-    lines_dft(s, tmp, N, a.logn[d], L, a.tw[d], true);
+    lines_dft(s, tmp, N, a.logn[d], La, a.tw[d], true);
   }
-  for (int e = threadIdx.x; e < L * N; e += blockDim.x) {
-    const int j = e / L, l = e - j * L;
-    if (x0 + l < ne0) a.X[base + j * stride + l] = s[l * N + j];
+  for (int e = threadIdx.x; e < La * N; e += blockDim.x) {
+    const int j = e / La, l = e - j * La;
+    a.X[base + j * stride + l] = s[l * N + j];
   }
 }
 
