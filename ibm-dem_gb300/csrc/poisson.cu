@@ -63,6 +63,51 @@ __device__ inline double2 cmul(double2 a, double2 b) {
   return make_double2(__fma_rn(a.x, b.x, -(a.y * b.y)), __fma_rn(a.x, b.y, a.y * b.x));
 }
 
+// one radix-4 group of 4 points (see lines_dft): the inputs with their
+// twiddles applied, then the 4-point transform stored back
+struct Quad {
+  int i0;
+  double2 a0, t1, t2, t3;
+};
+
+__device__ inline Quad quad_load(const double2* s, int b, int N, int logN, int lm, const double2* tw, bool inv) {
+  const int m = 1 << lm;
+  const int l = b >> (logN - 2), t = b & ((N >> 2) - 1);
+  const int o = t & (m - 1);
+  Quad q;
+  q.i0 = l * N + ((t >> lm) << (lm + 2)) + o;
+  q.a0 = s[q.i0];
+  q.t2 = s[q.i0 + m];
+  q.t1 = s[q.i0 + 2 * m];
+  q.t3 = s[q.i0 + 3 * m];
+  if (lm > 0) {
+    const int sh = logN - 2 - lm;  // W^j = tw[j << sh]
+    double2 w1 = tw[o << sh], w2 = tw[(2 * o) << sh], w3 = tw[(3 * o) << sh];
+    if (inv) {
+      w1.y = -w1.y;
+      w2.y = -w2.y;
+      w3.y = -w3.y;
+    }
+    q.t1 = cmul(q.t1, w1);
+    q.t2 = cmul(q.t2, w2);
+    q.t3 = cmul(q.t3, w3);
+  }
+  return q;
+}
+
+__device__ inline void quad_store(double2* s, const Quad& q, int m, bool inv) {
+  const double2 u0 = make_double2(q.a0.x + q.t2.x, q.a0.y + q.t2.y);
+  const double2 u1 = make_double2(q.a0.x - q.t2.x, q.a0.y - q.t2.y);
+  const double2 u2 = make_double2(q.t1.x + q.t3.x, q.t1.y + q.t3.y);
+  const double2 u3 = make_double2(q.t1.x - q.t3.x, q.t1.y - q.t3.y);
+  // forward: X1 = u1 - i u3, X3 = u1 + i u3; inverse: the signs of i swap
+  const double2 ju3 = inv ? make_double2(-u3.y, u3.x) : make_double2(u3.y, -u3.x);
+  s[q.i0] = make_double2(u0.x + u2.x, u0.y + u2.y);
+  s[q.i0 + m] = make_double2(u1.x + ju3.x, u1.y + ju3.y);
+  s[q.i0 + 2 * m] = make_double2(u0.x - u2.x, u0.y - u2.y);
+  s[q.i0 + 3 * m] = make_double2(u1.x - ju3.x, u1.y - ju3.y);
+}
+
 // L lines of N points in shared memory, s[l*N + j]: the DFT of each line
 // (sign -1; +1 when inv), natural order in and out.  tmp: L*N more points,
 // used by the direct DFT only.
@@ -97,34 +142,21 @@ __device__ void lines_dft(double2* s, double2* tmp, int N, int logN, int L, cons
     // residues 0, 2, 1, 3 (mod 4); with W = exp(-+2 pi i / 4m) the group's
     // outputs are the 4-point transform of (a0, W^o a2, W^2o a1, W^3o a3):
     // 3 complex products and 16 adds for 4 points (radix-2: 4 and 16).
+    // two groups per thread and pass, both loaded before either is stored:
+    // the groups are disjoint, and the second's loads overlap the first's
+    // arithmetic
+    const int nq = tot >> 2, bd = blockDim.x;
     for (; lm < logN; lm += 2) {
       const int m = 1 << lm;
-      const int sh = logN - 2 - lm;  // W^j = tw[j << sh]
-      for (int b = threadIdx.x; b < (tot >> 2); b += blockDim.x) {
-        const int l = b >> (logN - 2), t = b & ((N >> 2) - 1);
-        const int o = t & (m - 1);
-        const int i0 = l * N + ((t >> lm) << (lm + 2)) + o;
-        const double2 a0 = s[i0];
-        double2 t2 = s[i0 + m], t1 = s[i0 + 2 * m], t3 = s[i0 + 3 * m];
-        if (lm > 0) {
-          double2 w1 = tw[o << sh], w2 = tw[(2 * o) << sh], w3 = tw[(3 * o) << sh];
-          if (inv) {
-            w1.y = -w1.y;
-            w2.y = -w2.y;
-            w3.y = -w3.y;
-          }
-          t1 = cmul(t1, w1);
-          t2 = cmul(t2, w2);
-          t3 = cmul(t3, w3);
+      for (int b = threadIdx.x; b < nq; b += 2 * bd) {
+        const Quad qa = quad_load(s, b, N, logN, lm, tw, inv);
+        if (b + bd < nq) {
+          const Quad qb = quad_load(s, b + bd, N, logN, lm, tw, inv);
+          quad_store(s, qa, m, inv);
+          quad_store(s, qb, m, inv);
+        } else {
+          quad_store(s, qa, m, inv);
         }
-        const double2 u0 = make_double2(a0.x + t2.x, a0.y + t2.y), u1 = make_double2(a0.x - t2.x, a0.y - t2.y);
-        const double2 u2 = make_double2(t1.x + t3.x, t1.y + t3.y), u3 = make_double2(t1.x - t3.x, t1.y - t3.y);
-        // forward: X1 = u1 - i u3, X3 = u1 + i u3; inverse: the signs of i swap
-        const double2 ju3 = inv ? make_double2(-u3.y, u3.x) : make_double2(u3.y, -u3.x);
-        s[i0] = make_double2(u0.x + u2.x, u0.y + u2.y);
-        s[i0 + m] = make_double2(u1.x + ju3.x, u1.y + ju3.y);
-        s[i0 + 2 * m] = make_double2(u0.x - u2.x, u0.y - u2.y);
-        s[i0 + 3 * m] = make_double2(u1.x - ju3.x, u1.y - ju3.y);
       }
       __syncthreads();
     }
@@ -244,7 +276,12 @@ __global__ void __launch_bounds__(kPBlock) k_pois_xfwd(Geom g, PoisArgs a, const
 // y' for d = 2).
 __global__ void __launch_bounds__(kPBlock) k_pois_lines(PoisArgs a, int d, int mode, int outer) {
   extern __shared__ double2 sm[];
-  const int N = a.ne[d], L = a.L[d], ne0 = a.nh;  // x columns of the half spectrum
+  // the axis's values by selection (indexing the parameter arrays with d
+  // would copy them to local memory)
+  const bool y = d == 1;
+  const int N = y ? a.ne[1] : a.ne[2], L = y ? a.L[1] : a.L[2], logN = y ? a.logn[1] : a.logn[2];
+  const double2* tw = y ? a.tw[1] : a.tw[2];
+  const int ne0 = a.nh;  // x columns of the half spectrum
   double2* s = sm;
   double2* tmp = sm + L * N;
   const int groups = (ne0 + L - 1) / L;
@@ -253,14 +290,14 @@ __global__ void __launch_bounds__(kPBlock) k_pois_lines(PoisArgs a, int d, int m
   const int x0 = grp * L;
   const int La = min(L, ne0 - x0);  // the last group holds the columns that are left (nh is odd)
   const long long plane = (long long)ne0 * a.ne[1];
-  const long long base = d == 1 ? (long long)o * plane + x0 : (long long)o * ne0 + x0;
-  const long long stride = d == 1 ? ne0 : plane;
+  const long long base = y ? (long long)o * plane + x0 : (long long)o * ne0 + x0;
+  const long long stride = y ? ne0 : plane;
   for (int e = threadIdx.x; e < La * N; e += blockDim.x) {
     const int j = e / La, l = e - j * La;
     s[l * N + j] = a.X[base + j * stride + l];
   }
   __syncthreads();
-  lines_dft(s, tmp, N, a.logn[d], La, a.tw[d], mode == 1);
+  lines_dft(s, tmp, N, logN, La, tw, mode == 1);
   if (mode == 2) {
     // s[l*N + kz] holds the transform at (kx = x0 + l, ky = o, kz)
     const double ly = a.lam[1][o];
@@ -271,7 +308,7 @@ __global__ void __launch_bounds__(kPBlock) k_pois_lines(PoisArgs a, int d, int m
       s[e] = make_double2(s[e].x * f, s[e].y * f);
     }
     __syncthreads();
-    lines_dft(s, tmp, N, a.logn[d], La, a.tw[d], true);
+    lines_dft(s, tmp, N, logN, La, tw, true);
   }
   for (int e = threadIdx.x; e < La * N; e += blockDim.x) {
     const int j = e / La, l = e - j * La;
