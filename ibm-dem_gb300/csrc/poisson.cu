@@ -452,8 +452,15 @@ static int poisson_plan(Ctx& c) {
     return IBMDEM_ENOMEM;
   }
   if (cudaMemcpyAsync(p.aux, h.data(), aux * sizeof(double), cudaMemcpyHostToDevice, c.stream) != cudaSuccess ||
-      cudaStreamSynchronize(c.stream) != cudaSuccess)
+      cudaStreamSynchronize(c.stream) != cudaSuccess) {
+    // no half-built plan: the next call plans again
+    cudaFreeAsync(p.X, c.stream);
+    cudaFreeAsync(p.aux, c.stream);
+    p.X = nullptr;
+    p.aux = nullptr;
+    c.err = "ibmdem_PoissonSolver: the transform tables could not be uploaded";
     return IBMDEM_ECUDA;
+  }
   p.total = (long long)tot;
   c.bytes += half * sizeof(double2) + aux * sizeof(double);
   cudaFuncSetAttribute(k_pois_xfwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem);
