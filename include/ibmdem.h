@@ -473,7 +473,8 @@ int ibmdem_PoissonSolver(ibmdem_ctx* ctx);
 /* ---- instrumentation -------------------------------------------------- */
 /* Record CUDA events around every phase of the drivers (interpolation,
  * spreading, weights, spread plan, cell lists, contact lists, contact force,
- * body sums, body motion, marker motion, image refresh, resets). */
+ * body sums, body motion, marker motion, image refresh, resets, and the fluid
+ * phases: the guess, the halo fills, the other stencils, the Poisson solve). */
 int ibmdem_timing_enable(ibmdem_ctx* ctx, int32_t on);
 /* Accumulated milliseconds and span counts per phase (synchronises); returns
  * the number of phases.  reset != 0 clears the accumulators. */
