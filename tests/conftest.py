@@ -34,6 +34,9 @@ def pytest_collection_modifyitems(config, items):
 def oracle_mod():
     import oracle
     oracle.build()
+    # the restatement's parallel loops have independent outputs: results do
+    # not depend on the thread count
+    oracle.set_threads(os.cpu_count() or 1)
     return oracle
 
 
