@@ -50,8 +50,8 @@ METRIC = "particle-steps/s (contact+IBM) on 1 GB300, batched vs plain; p50/p99 s
 
 
 # DRAM bytes (read + write) per local marker and launch of the main kernels, from
-# one ncu capture of the 512-sphere 256^3 case (profiles/ncu_ibm_kernels_resolved-512-spheres-256cube.md);
-# the bench workload has the same per-marker structure, so traffic scales with markers.
+# one ncu capture of the 512-sphere 256^3 case; the benchmark workload has the
+# same per-marker structure, so traffic scales with markers.
 DRAM_BYTES_PER_MARKER = {"interp": 1189.0, "spread": 1781.0, "weights": 477.0}
 
 
@@ -90,7 +90,7 @@ def parse():
     ap.add_argument("--cpu-steps", type=int, default=1)
     ap.add_argument("--batch-cases", type=int, default=256, help="cases of the batched mix (0 = skip)")
     ap.add_argument("--batch-steps", type=int, default=10)
-    ap.add_argument("--serve-requests", type=int, default=32, help="requests of the served stream (0 = skip)")
+    ap.add_argument("--serve-requests", type=int, default=128, help="requests of the served stream (0 = skip)")
     ap.add_argument("--serve-steps", type=int, default=100)
     ap.add_argument("--unresolved-particles", type=int, default=1_048_576,
                     help="particles of the unresolved CFD-DEM case (0 = skip)")
@@ -252,24 +252,79 @@ def run_reference_unresolved(args, O, threads):
     return 0
 
 
-def algorithmic(counters, phases):
-    """Compulsory bytes and FP64 instructions per launch of the main kernels."""
+def algorithmic(counters):
+    """Per launch of the main kernels: the compulsory HBM bytes of the hot-path
+    scope table, the bytes the implementation moves with its own intermediates
+    (stored weights, the spread plan), and the FP64 instructions it issues.
+
+    Units: M local markers, NP markers with their periodic images, U touched
+    grid nodes summed over the three velocity components, C spread
+    contributions.  Compulsory bytes: interpolation with its weights (a7+a8,
+    one launch = one forcing iteration, all three components) M (48 x,v + 24
+    fdrag read + 48 fdrag,vgap written) + 8 U field gathers; spreading with the
+    post-guess (a10+a11) NP (24 x + 24 fdrag + 8 vol) + 24 U (the old forcing
+    and u read, u and f written); the weights kernel and the plan fill have no
+    row of their own there (their outputs are intermediates of a7/a10): their
+    compulsory bytes are the positions and cells they read.
+
+    FP64 instructions issued (DADD, DMUL, DFMA, square-root steps), counted
+    from the kernels' operations and checked against ncu's
+    sm__sass_thread_inst_executed_op_fp64_pred_on on the 512-sphere case:
+    interpolation 60 per marker and component (27 products, 26 sums, the
+    velocity gap, the division by dt as 4 operations, the fdrag update and
+    fdrag*vol); spreading 2 per contribution less the first subtraction of
+    each node (an integer sign flip), plus 3 per node for the post-guess;
+    weights FP64_WEIGHTS_PER_PARCEL per parcel (18 one-axis kernels with a
+    square root and an exact /3 each, and 108 products)."""
     M = counters["npLocal"]
+    NP = counters["np"]
     C = counters["contributions"]
     U = counters["nodes_u"] + counters["nodes_v"] + counters["nodes_w"]
-    out = {}
-    # interpolation (one launch = one MDF iteration, all 3 components):
-    # 81 weights, window, vol, and per component v, fdrag r/w, vgap w, fdrag*vol w; plus
-    # every touched node read once
-    out["interp"] = {"bytes": M * (81 * 8 + 16 + 8 + 3 * 5 * 8) + 8 * U,
-                     "fp64": M * 3 * (27 * 2 + 12)}
-    # spreading + post-guess: each contribution's index and weight, fdrag*vol of every
-    # parcel once, and per touched node its key, run start, u r/w, f r/w, fx w
-    out["spread"] = {"bytes": C * (4 + 8) + counters["np"] * 24 + U * (4 + 4 + 16 + 16 + 8),
-                     "fp64": C * 2 + U * 3}
-    # delta weights: position, cell, and 81 weights + window written per parcel
-    out["weights"] = {"bytes": counters["np"] * (24 + 4 + 81 * 8 + 16 + 4), "fp64": counters["np"] * 520}
-    return out
+    # per launch; the two weight launches (locals, then images) as one
+    return {
+        "interp": {"compulsory": M * 120 + 8 * U,
+                   "moved": M * (81 * 8 + 16 + 8 + 3 * 5 * 8) + 8 * U,
+                   "fp64": M * 3 * 60, "per_step": 5},
+        "spread": {"compulsory": NP * 56 + 24 * U,
+                   "moved": C * (4 + 8) + NP * 24 + U * (4 + 4 + 16 + 16 + 8),
+                   "fp64": 2 * C - U + 3 * U, "per_step": 5},
+        "weights": {"compulsory": NP * (24 + 4),
+                    "moved": NP * (24 + 4 + 84 * 8 + 16 + 4),
+                    "fp64": NP * FP64_WEIGHTS_PER_PARCEL, "per_step": 1},
+        "plan": {"compulsory": NP * (24 + 4),
+                 "moved": C * 12 + NP * (4 + 16) * 2 + U * 12,
+                 "fp64": 0, "per_step": 1},
+    }
+
+
+# FP64 instructions per parcel of the delta-weight kernel (ncu count, 512-sphere case)
+FP64_WEIGHTS_PER_PARCEL = 480
+
+
+def kernel_rows(alg, phases, hbm_peak, fp64_peak, npLocal):
+    """One roofline row per main kernel from its CUDA-event time per launch."""
+    rows = {}
+    for k, a in alg.items():
+        tot, n = phases.get(k, (0.0, 0))
+        if not n:
+            continue
+        # the weights phase counts its two launches (locals, images) separately
+        n = n // 2 if k == "weights" else n
+        s = tot / n / 1e3
+        gbs = a["compulsory"] / s / 1e9
+        per_marker = DRAM_BYTES_PER_MARKER.get(k)
+        traffic = per_marker * npLocal if per_marker else None
+        fp = a["fp64"] / s / 1e9
+        row = {"ms_per_launch": tot / n, "launches": n, "compulsory_bytes": a["compulsory"],
+               "compulsory_gbs": gbs, "hbm_frac": gbs / hbm_peak, "moved_bytes": a["moved"],
+               "moved_gbs": a["moved"] / s / 1e9, "traffic": traffic,
+               "waste_ratio": traffic / a["compulsory"] if traffic else None,
+               "fp64_issued": a["fp64"], "fp64_gops": fp,
+               "fp64_frac": fp / fp64_peak if fp64_peak and a["fp64"] else None}
+        row["bound"] = "fp64" if (row["fp64_frac"] or 0) > row["hbm_frac"] else (
+            "issue" if k == "plan" else "hbm")
+        rows[k] = row
+    return rows
 
 
 def percentile(xs, q):
@@ -942,32 +997,32 @@ def run_ours(args):
 
     if rank == 0:
         hbm_peak, peak_kind = measured_peaks()
-        alg = algorithmic(counters, phases)
+        alg = algorithmic(counters)
         per_phase = {}
         for k, (tot, n) in phases.items():
             if n:
                 per_phase[k] = {"ms_total": round(tot, 3), "launches": n, "ms_per_launch": tot / n}
+        rows = kernel_rows(alg, phases, hbm_peak, fp64_peak, counters["npLocal"])
         # dominant kernel: the one with the largest share of the timed region
-        dom = max(("interp", "spread", "weights"), key=lambda k: phases.get(k, (0, 0))[0])
-        tot, n = phases[dom]
-        ms_launch = tot / max(n, 1)
-        achieved = alg[dom]["bytes"] / (ms_launch / 1e3) / 1e9
-        fp64_gops = alg[dom]["fp64"] / (ms_launch / 1e3) / 1e9
-        per_marker = DRAM_BYTES_PER_MARKER.get(dom)
-        traffic = per_marker * counters["npLocal"] if per_marker else None
+        dom = max(rows, key=lambda k: phases.get(k, (0, 0))[0])
+        r = rows[dom]
         line = {
             "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": config_of(args.workload, nm),
             "marker_steps_per_s": world * nm * args.steps / (ms_max / 1e3),
-            "roofline": {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                         "frac": achieved / hbm_peak, "peak_kind": peak_kind, "traffic": traffic,
-                         "algorithmic_bytes_per_launch": alg[dom]["bytes"], "ms_per_launch": ms_launch,
-                         "fp64": {"achieved_gops": fp64_gops, "peak_gops": fp64_peak,
-                                  "peak_kind": "measured live (ibmdem_measure_fp64_rate)",
-                                  "frac": fp64_gops / fp64_peak,
-                                  "instr_per_launch": alg[dom]["fp64"]}},
+            "roofline": {"kernel": dom, "bound": r["bound"], "achieved": r["compulsory_gbs"], "peak": hbm_peak,
+                         "unit": "GB/s", "frac": r["hbm_frac"], "peak_kind": peak_kind + " (hbm_gbs)",
+                         "traffic": r["traffic"], "algorithmic_bytes_per_launch": r["compulsory_bytes"],
+                         "bytes_note": "compulsory bytes of the hot-path scope table; the kernel also moves its "
+                                       "own intermediates (moved_bytes: the spread plan, the stored weights)",
+                         "waste_ratio": r["waste_ratio"], "ms_per_launch": r["ms_per_launch"],
+                         "fp64": {"achieved_gops": r["fp64_gops"], "peak_gops": fp64_peak,
+                                  "peak_kind": "measured live (ibmdem_measure_fp64_rate: DFMA issue rate)",
+                                  "frac": r["fp64_frac"], "instr_per_launch": r["fp64_issued"],
+                                  "instr_note": "FP64 instructions the kernel issues"},
+                         "kernels": rows},
             "phases": per_phase,
             "e2e": {"value": e2e_val, "unit": "particle-steps/s", "h2d_bytes_per_step": 3 * fbytes,
                     "d2h_bytes_per_step": 6 * fbytes + nb * MULTISPHERE.itemsize, "steps": args.e2e_steps,

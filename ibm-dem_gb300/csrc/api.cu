@@ -102,7 +102,19 @@ double eta_of(double e) {
   return -2 * std::log(e) / std::sqrt((double)pi2 + std::log(e));
 }
 
+void free_history(Ctx& c) {
+  void* ps[] = {c.histRange[0], c.histRange[1], c.histGid[0], c.histGid[1], c.histXi[0], c.histXi[1], c.pidMap};
+  for (void* p : ps) dfree(c, p);
+  c.histRange[0] = c.histRange[1] = nullptr;
+  c.histGid[0] = c.histGid[1] = nullptr;
+  c.histXi[0] = c.histXi[1] = nullptr;
+  c.pidMap = nullptr;
+  c.bytes -= c.bytesHist;
+  c.bytesHist = 0;
+}
+
 void free_parcel_buffers(Ctx& c) {
+  free_history(c);
   void* ps[] = {c.recD[0], c.recD[1], c.recI[0], c.recI[1], c.imgSrc, c.imgShift, c.cellItems, c.bodyItems,
                 c.iTmpA, c.iTmpB, c.scanScratch, c.sortHist, c.kA, c.vA, c.kB, c.vB, c.activeList, c.pairCnt,
                 c.pairStart, c.pairIdx, c.W, c.win, c.cntInt, c.fv, c.runStart, c.runKey, c.fCur, c.fPrev,
@@ -303,6 +315,32 @@ int alloc_parcels(ibmdem_ctx* h, int np, long long nimg_est) {
   return IBMDEM_OK;
 }
 
+// The tangential history of the friction law for the current capacities,
+// empty: no local has contacts from an earlier call, every parcel id maps to
+// no local, and the next call reads side 0.
+int alloc_history(ibmdem_ctx* h) {
+  Ctx& c = h->c;
+  free_history(c);
+  const size_t b0 = c.bytes;
+  cudaError_t e = cudaSuccess;
+  for (int q = 0; q < 2 && e == cudaSuccess; ++q) {
+    e = dalloc(c, c.histRange[q], (size_t)c.capLocal);
+    if (e == cudaSuccess) e = dalloc(c, c.histGid[q], (size_t)c.capPairs);
+    if (e == cudaSuccess) e = dalloc(c, c.histXi[q], 3 * (size_t)c.capPairs);
+  }
+  if (e == cudaSuccess) e = dalloc(c, c.pidMap, (size_t)c.capLocal);
+  c.bytesHist = c.bytes - b0;
+  c.allocGen++;
+  if (e != cudaSuccess) {
+    free_history(c);
+    return set_error(h, IBMDEM_ENOMEM, "tangential history: %s", cudaGetErrorString(e));
+  }
+  for (int q = 0; q < 2; ++q) CU(cudaMemsetAsync(c.histRange[q], 0, sizeof(int2) * c.capLocal, c.stream));
+  CU(cudaMemsetAsync(c.pidMap, 0xff, sizeof(int) * (size_t)c.capLocal, c.stream));
+  CU(cudaMemsetAsync(&c.dCnt->histSide, 0, sizeof(int), c.stream));
+  return IBMDEM_OK;
+}
+
 // latch device errors into a status (after a stream synchronise)
 int check_device(ibmdem_ctx* h) {
   Ctx& c = h->c;
@@ -363,17 +401,17 @@ static const char* const kPhaseLabels[P_COUNT] = {"interp", "spread", "weights",
                                                   "fluid_guess", "fluid_halo", "fluid_other", "fluid_poisson"};
 // Every phase is an NVTX range (visible to any attached profiler, a few ns
 // otherwise); with timing on it is also bracketed by CUDA events.
-PhaseScope::PhaseScope(Ctx& ctx, int ph) : c(ctx), phase(ph) {
+PhaseScope::PhaseScope(Ctx& ctx, int ph, cudaStream_t stream) : c(ctx), phase(ph), s(stream) {
   nvtxRangePushA(kPhaseLabels[ph]);
   if (!c.timing) return;
   a = take_event(c);
   b = take_event(c);
-  cudaEventRecord(a, c.stream);
+  cudaEventRecord(a, s);
 }
 PhaseScope::~PhaseScope() {
   nvtxRangePop();
   if (!c.timing || !a) return;
-  cudaEventRecord(b, c.stream);
+  cudaEventRecord(b, s);
   c.spans.push_back({phase, a, b});
 }
 static void collect_timing(Ctx& c) {
@@ -688,6 +726,7 @@ int ibmdem_set_parcels(ibmdem_ctx* h, int32_t np, const ibmdem_parcel* parts) {
   long long nimg = count_images(c.g, np, parts);
   int rc = alloc_parcels(h, np, nimg);
   if (rc) return rc;
+  if (c.ktRatio > 0.0 && (rc = alloc_history(h))) return rc;
   std::vector<double> hd((size_t)ND * c.cap, 0.0);
   std::vector<int> hi((size_t)NI * c.cap, 0);
   for (int i = 0; i < np; ++i) {
@@ -710,6 +749,7 @@ int ibmdem_set_parcels(ibmdem_ctx* h, int32_t np, const ibmdem_parcel* parts) {
     for (int f = 0; f < ND; ++f) hd[(size_t)f * c.cap + i] = *src[f];
     hi[(size_t)I_GIDX * c.cap + i] = p.globalIdx;
     hi[(size_t)I_MSIDX * c.cap + i] = p.MSIdx;
+    hi[(size_t)I_PID * c.cap + i] = i;
     int a[3];
     bool in = std::isfinite(p.x[0]) && std::isfinite(p.x[1]) && std::isfinite(p.x[2]);
     for (int d = 0; d < 3; ++d) a[d] = in ? (int)std::floor((p.x[d] - c.g.start[d]) / c.g.h[d]) + 1 : 0;
@@ -951,6 +991,52 @@ int ibmdem_CalculateSolidBoundaryCollisionForce(ibmdem_ctx* h) {
   return launch_status(h);
 }
 
+int ibmdem_set_friction(ibmdem_ctx* h, double ktRatio, double mu) {
+  CHECK_CTX();
+  Ctx& c = h->c;
+  if (!(ktRatio >= 0.0) || !(mu >= 0.0) || !std::isfinite(ktRatio) || !std::isfinite(mu))
+    return set_error(h, IBMDEM_EINVAL, "friction: ktRatio %g and mu %g must be finite and >= 0", ktRatio, mu);
+  CU(cudaStreamSynchronize(c.stream));
+  c.ktRatio = ktRatio;
+  c.mu = mu;
+  if (ktRatio > 0.0 && c.haveParcels) return alloc_history(h);
+  free_history(c);
+  c.allocGen++;
+  return IBMDEM_OK;
+}
+
+int ibmdem_get_friction_history(ibmdem_ctx* h, int32_t* start, int32_t* gid, double* xi, int32_t* nlocal_out,
+                                int32_t* n_out) {
+  CHECK_CTX();
+  Ctx& c = h->c;
+  int rc = check_device(h);
+  if (rc) return rc;
+  const int nl = c.pidMap ? c.hCnt->npLocal : 0;
+  if (nlocal_out) *nlocal_out = nl;
+  if (n_out) *n_out = 0;
+  if (nl == 0) {
+    if (start) start[0] = 0;
+    return IBMDEM_OK;
+  }
+  const int side = c.hCnt->histSide;  // the side the last call wrote
+  std::vector<int2> r(nl);
+  CU(cudaMemcpyAsync(r.data(), c.histRange[side], sizeof(int2) * nl, cudaMemcpyDeviceToHost, c.stream));
+  CU(cudaStreamSynchronize(c.stream));
+  const int first = r[0].x, total = r[nl - 1].y - first;
+  if (n_out) *n_out = total;
+  if (start) {
+    for (int i = 0; i < nl; ++i) start[i] = r[i].x - first;
+    start[nl] = total;
+  }
+  if (gid && total > 0)
+    CU(cudaMemcpyAsync(gid, c.histGid[side] + first, sizeof(int) * total, cudaMemcpyDeviceToHost, c.stream));
+  if (xi && total > 0)
+    CU(cudaMemcpyAsync(xi, c.histXi[side] + 3 * (size_t)first, sizeof(double) * 3 * total, cudaMemcpyDeviceToHost,
+                       c.stream));
+  CU(cudaStreamSynchronize(c.stream));
+  return IBMDEM_OK;
+}
+
 int ibmdem_set_wall_probes(ibmdem_ctx* h, int32_t n, const ibmdem_wall_probe* probes) {
   CHECK_CTX();
   Ctx& c = h->c;
@@ -987,6 +1073,7 @@ int ibmdem_UpdateFluidVelocityOnLagrangianPoints(ibmdem_ctx* h) {
   Ctx& c = h->c;
   REQUIRE(c.weightsLocal, "local weights are not computed");
   REQUIRE(c.haveFluid, "no fluid field");
+  wait_fields_read(c);  // an ibmdem_set_fluid_async upload lands before the fields are read
   launch_interp(c, -1);
   return launch_status(h);
 }
@@ -1100,12 +1187,23 @@ static int mdf(ibmdem_ctx* h, bool frozen) {
   REQUIRE(c.haveFluid, "no fluid field");
   const bool perCompUpload = !frozen && c.uploadPending;  // ibmdem_set_fluid_async still uploading
   wait_fields_read(c, !perCompUpload);
+  // The plan for new weights does not read the fluid, but it is built here, in
+  // order: beside the forcing loop on a second stream it took the loop's SMs
+  // (the fill is issue-bound, the loop FP64-bound at high occupancy) and the
+  // step measured 5% slower.
   int rc = ensure_plan(h);
   if (rc) return rc;
+  // with at least one iteration the first one takes the reset's zeros itself
+  // and only the nodes the last spread wrote outside the new plan are reset
+  const bool firstFlags = c.p.Ns > 0;
   {
     PhaseScope t(c, P_RESET);
-    launch_mdf_reset(c, frozen);
+    if (firstFlags)
+      launch_mdf_stale(c, frozen);
+    else
+      launch_mdf_reset(c, frozen);
   }
+  const int first = 1 | (frozen ? 2 : 0);
   // The three velocity components never meet inside the MDF loop (fluid.F90:
   // 265-285): a marker's component interpolates from that component of the
   // field, and the spread and the post-guess of a node write that component
@@ -1125,11 +1223,11 @@ static int mdf(ibmdem_ctx* h, bool frozen) {
     for (int it = 0; it < c.p.Ns; ++it) {
       {
         PhaseScope t(c, P_INTERP);
-        launch_interp(c, comp);
+        launch_interp(c, comp, it == 0 ? first : 0);
       }
       {
         PhaseScope t(c, P_SPREAD);
-        launch_spread(c, true, comp);
+        launch_spread(c, true, comp, it == 0 ? first : 0);
       }
     }
     if (byComp) {
@@ -1219,11 +1317,14 @@ int ibmdem_interpolate_velocity_noalloc(ibmdem_ctx* h, int32_t n, const double* 
                      IBMDEM_PROBE_MAX_POINTS);
   if (n > 0 && (!x || !ulp)) return set_error(h, IBMDEM_EINVAL, "null point or result array");
   REQUIRE(c.haveFluid, "no fluid field");
+  wait_fields_read(c);  // an ibmdem_set_fluid_async upload lands before the fields are read
   int bad = -1;
   const cudaError_t e = interpolate_points_noalloc(c, n, x, ulp, &bad);
   if (e != cudaSuccess)
     return set_error(h, IBMDEM_ECUDA, "ibmdem_interpolate_velocity_noalloc: %s", cudaGetErrorString(e));
-  if (bad >= 0) return set_error(h, IBMDEM_ERANGE, "point %d lies outside the periodic box", bad);
+  if (bad >= 0)
+    return set_error(h, IBMDEM_ERANGE, "point %d lies outside the box [0,%g) x [0,%g) x [0,%g)", bad, c.g.len[0],
+                     c.g.len[1], c.g.len[2]);
   return IBMDEM_OK;
 }
 

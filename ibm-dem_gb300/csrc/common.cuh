@@ -34,7 +34,9 @@ enum : int {
   D_RADEFF = 15, D_RAD, D_RHO, D_VOL, D_M, D_WDRAG, D_WSUM, ND
 };
 // int fields
-enum : int { I_GIDX = 0, I_MSIDX, I_CELL, NI };
+// I_PID: the parcel's index in the array last given to ibmdem_set_parcels (images
+// carry their root's); it keys the tangential contact history
+enum : int { I_GIDX = 0, I_MSIDX, I_CELL, I_PID, NI };
 
 // device error bits (Counters::err)
 enum : int {
@@ -123,7 +125,8 @@ struct Counters {
   int npLocal, np, nImg, nActive, nPairs, nRuns, nContrib, nLast;
   int err, errInfo;
   int compStart[4];  // first run of each velocity component (and nRuns) in the spread plan
-  int pad[2];
+  int histSide;      // side of the tangential history the last contact-force call wrote
+  int pad;
 };
 
 struct Recs {

@@ -233,6 +233,120 @@ __global__ void k_collision_force(Recs R, Geom g, const Counters* cnt, const int
   R.D(D_FCOL + 2, ii) = fc3;
 }
 
+// The pair forces with tangential friction (ibmdem_set_friction; the
+// reference's law is normal only).  The normal part is the law above, term by
+// term.  For a touching pair (deltan > 0), with u = v_i - v_j the relative
+// marker velocity (marker velocities carry their body's rotation):
+//   vt = u - vn n;  h = the pair's tangential displacement of the last call
+//   (found by the partner's persistent parcel id, I_PID; 0 for a new contact), projected on the
+//   tangent plane, plus dtDEM vt;  kt = ktRatio kn, etat = eta sqrt(meff kt),
+//   ft = -kt h - etat vt, scaled to mu |fn| beyond the Coulomb limit (h then
+//   the sliding value -(ft + etat vt) / kt);  fcol_i += n fn + ft.
+// One thread per local; the history is read from one side and written to the
+// other (k_hist_finish flips the side and maps the parcel ids to the locals).
+__global__ void k_collision_force_friction(Recs R, Geom g, const Counters* cnt, const int* pairStart,
+                                           const int* pairIdx, long long capPairs, double ktRatio, double mu,
+                                           int2* range0, int2* range1, int* gid0, int* gid1, double* xs0,
+                                           double* xs1, const int* pidMap, int nPid) {
+  const int ii = blockIdx.x * blockDim.x + threadIdx.x;
+  if (ii >= cnt->npLocal) return;
+  const int side = cnt->histSide;
+  const int2* oRange = side ? range1 : range0;
+  const int* oGid = side ? gid1 : gid0;
+  const double* oXi = side ? xs1 : xs0;
+  int2* nRange = side ? range0 : range1;
+  int* nGid = side ? gid0 : gid1;
+  double* nXi = side ? xs0 : xs1;
+  double fc1 = 0, fc2 = 0, fc3 = 0;
+  int s = pairStart[ii], e = pairStart[ii + 1];
+  if (e > capPairs) e = (int)capPairs;
+  if (s > e) s = e;
+  nRange[ii] = make_int2(s, e);
+  const int pi = R.I(I_PID, ii);
+  const int o = (pi >= 0 && pi < nPid) ? pidMap[pi] : -1;
+  const int2 orr = o >= 0 ? oRange[o] : make_int2(0, 0);
+  if (s < e) {
+    const double xi0 = R.D(D_X, ii), xi1 = R.D(D_X + 1, ii), xi2 = R.D(D_X + 2, ii);
+    const double vi0 = R.D(D_V, ii), vi1 = R.D(D_V + 1, ii), vi2 = R.D(D_V + 2, ii);
+    const double mi = R.D(D_M, ii), ri = R.D(D_RADEFF, ii);
+    for (int q = s; q < e; ++q) {
+      int j = pairIdx[q];
+      double r1 = xi0 - R.D(D_X, j);
+      double r2 = xi1 - R.D(D_X + 1, j);
+      double r3 = xi2 - R.D(D_X + 2, j);
+      double dist = sqrt(r1 * r1 + r2 * r2 + r3 * r3);
+      double n1 = r1 / dist, n2 = r2 / dist, n3 = r3 / dist;
+      double mj = R.D(D_M, j);
+      double meff = 2 * mi * mj / (mi + mj);
+      double rij = ri + R.D(D_RADEFF, j);
+      double deltan = rij - dist;
+      double kn = g.knCoeff / (0.1 * g.di) * meff;
+      double etan = g.eta * sqrt(meff * kn);
+      double f1 = 0, f2 = 0, f3 = 0;
+      double u1 = vi0 - R.D(D_V, j), u2 = vi1 - R.D(D_V + 1, j), u3 = vi2 - R.D(D_V + 2, j);
+      double vnij = n1 * u1 + n2 * u2 + n3 * u3;
+      double h1 = 0, h2 = 0, h3 = 0;
+      int hg = -1;
+      if (deltan > 0) {
+        const int gj = R.I(I_PID, j);
+        double fn = kn * deltan - etan * vnij;
+        double vt1 = u1 - vnij * n1, vt2 = u2 - vnij * n2, vt3 = u3 - vnij * n3;
+        for (int t = orr.x; t < orr.y; ++t)
+          if (oGid[t] == gj) {
+            h1 = oXi[3 * (size_t)t];
+            h2 = oXi[3 * (size_t)t + 1];
+            h3 = oXi[3 * (size_t)t + 2];
+            break;
+          }
+        double hn = n1 * h1 + n2 * h2 + n3 * h3;
+        h1 = h1 - hn * n1;
+        h2 = h2 - hn * n2;
+        h3 = h3 - hn * n3;
+        h1 = h1 + g.dtDEM * vt1;
+        h2 = h2 + g.dtDEM * vt2;
+        h3 = h3 + g.dtDEM * vt3;
+        double kt = ktRatio * kn;
+        double etat = g.eta * sqrt(meff * kt);
+        double ft1 = -kt * h1 - etat * vt1, ft2 = -kt * h2 - etat * vt2, ft3 = -kt * h3 - etat * vt3;
+        double ftm = sqrt(ft1 * ft1 + ft2 * ft2 + ft3 * ft3);
+        double lim = mu * fabs(fn);
+        if (ftm > lim) {
+          double sc = lim / ftm;
+          ft1 = ft1 * sc;
+          ft2 = ft2 * sc;
+          ft3 = ft3 * sc;
+          h1 = -(ft1 + etat * vt1) / kt;
+          h2 = -(ft2 + etat * vt2) / kt;
+          h3 = -(ft3 + etat * vt3) / kt;
+        }
+        f1 = n1 * fn + ft1;
+        f2 = n2 * fn + ft2;
+        f3 = n3 * fn + ft3;
+        hg = gj;
+      }
+      nGid[q] = hg;
+      nXi[3 * (size_t)q] = h1;
+      nXi[3 * (size_t)q + 1] = h2;
+      nXi[3 * (size_t)q + 2] = h3;
+      fc1 = fc1 + f1;
+      fc2 = fc2 + f2;
+      fc3 = fc3 + f3;
+    }
+  }
+  R.D(D_FCOL, ii) = fc1;
+  R.D(D_FCOL + 1, ii) = fc2;
+  R.D(D_FCOL + 2, ii) = fc3;
+}
+
+// after the friction forces: parcel id -> local of this call, and the side flips
+__global__ void k_hist_finish(Recs R, Counters* cnt, int* pidMap, int nPid) {
+  const int ii = blockIdx.x * blockDim.x + threadIdx.x;
+  if (ii == 0) cnt->histSide ^= 1;
+  if (ii >= cnt->npLocal) return;
+  const int pi = R.I(I_PID, ii);
+  if (pi >= 0 && pi < nPid) pidMap[pi] = ii;
+}
+
 // ---- CalculateSolidBoundaryCollisionForce (ZJS_COLLISION_DEM.F90:76-148) ----
 // plane of face f (0..5 = -x,+x,-y,+y,-z,+z): pointBound and normBound
 // (ZJS_INIT_DEM.F90:120-137)
@@ -390,6 +504,14 @@ void rebuild_collision_lists(Ctx& c) {
 }
 
 void launch_collision_force(Ctx& c) {
+  if (c.ktRatio > 0.0 && c.pidMap) {
+    k_collision_force_friction<<<nblocks(c.capLocal), kBlock, 0, c.stream>>>(
+        c.rec(), c.g, c.dCnt, c.pairStart, c.pairIdx, c.capPairs, c.ktRatio, c.mu, c.histRange[0], c.histRange[1],
+        c.histGid[0], c.histGid[1], c.histXi[0], c.histXi[1], c.pidMap, c.capLocal);
+    k_hist_finish<<<nblocks(c.capLocal), kBlock, 0, c.stream>>>(c.rec(), c.dCnt, c.pidMap, c.capLocal);
+    c.launches += 2;
+    return;
+  }
   k_collision_force<<<nblocks(c.capLocal), kBlock, 0, c.stream>>>(c.rec(), c.g, c.dCnt, c.pairStart, c.pairIdx,
                                                                   c.capPairs);
   c.launches++;

@@ -723,16 +723,41 @@ __global__ void k_mdf_reset(Recs R, Geom g, Counters* cnt, Fields fl, const uint
   }
 }
 
+// The reset of FirstOrderForwardEuler's particle side (fluid.F90:255-263:
+// fdrag = 0, fx = fy = fz = 0, and in a frozen-fluid step the field restored)
+// when the forcing loop runs: the first iteration's kernels take fdrag and
+// fxOld as 0 and the frozen field as the old velocity, and every node the new
+// plan touches is rewritten by the first spread, so only the nodes the last
+// spread wrote and the new plan does not touch (the touched-node bits) are
+// reset here.
+template <bool WALLS>
+__global__ void k_mdf_stale(Geom g, const Counters* cnt, Fields fl, const uint32_t* __restrict__ lastNodes,
+                            const unsigned* __restrict__ touch, int frozen) {
+  const long long nLast = cnt->nLast;
+  GRID_STRIDE(t, nLast) {
+    const uint32_t key = lastNodes[t];
+    if ((touch[key >> 5] >> (key & 31u)) & 1u) continue;
+    int comp, i, j, k;
+    node_coords(g, key, comp, i, j, k);
+    const long long off = field_off(g, i, j, k);
+    fl.F(comp)[off] = 0.0;
+    if (frozen) put_mirrored<WALLS>(fl.U(comp), g, comp, i, j, k, fl.U0(comp)[off]);
+  }
+}
+
 // UpdateFluidVelocityOnLagrangianPoints (ZJS_VOLUMEFRACTION_DEM.F90:2-36);
-// blockIdx.y is the velocity component.
+// blockIdx.y is the velocity component.  first: bit 0, the forcing loop's first iteration (fdrag was just reset to 0);
+// bit 1, the field is read from the frozen copy (the first iteration of a
+// frozen-fluid step, before any spread of this step wrote the working field).
 template <int UNIT_H>
 __global__ void __launch_bounds__(kBlock) k_interp(Recs R, Geom g, const Counters* cnt, const double* __restrict__ W,
-                                                   const int4* __restrict__ win, Fields fl, double* fv, int comp0) {
+                                                   const int4* __restrict__ win, Fields fl, double* fv, int comp0,
+                                                   int first) {
   int m = blockIdx.x * blockDim.x + threadIdx.x;
   if (m >= cnt->npLocal) return;
   const int comp = comp0 + blockIdx.y;
   const int cap = R.cap;
-  const double* __restrict__ F = fl.U(comp);
+  const double* __restrict__ F = (first & 2) ? fl.U0(comp) : fl.U(comp);
   int sx, sy, sz;
   window_start(win[m], comp, sx, sy, sz);
   const double4_32a* Wc = reinterpret_cast<const double4_32a*>(W + (size_t)m * kWStride + comp * 28);
@@ -764,8 +789,10 @@ __global__ void __launch_bounds__(kBlock) k_interp(Recs R, Geom g, const Counter
     }
   const double vp = R.D(D_V + comp, m);
   R.D(D_VGAP + comp, m) = ulp - vp;
-  // relaxfactor * (ulp - vp) / dt with relaxfactor = 1: the product is exact
-  double fd = R.D(D_FDRAG + comp, m) + div_dt(ulp - vp, g);
+  // relaxfactor * (ulp - vp) / dt with relaxfactor = 1: the product is exact;
+  // after the reset fdrag = 0, so 0.0 + q is q (+0 for a -0)
+  const double q = div_dt(ulp - vp, g);
+  const double fd = (first & 1) ? zero_plus(q) : R.D(D_FDRAG + comp, m) + q;
   R.D(D_FDRAG + comp, m) = fd;
   fv[(size_t)comp * cap + m] = fd * R.D(D_VOL, m);
 }
@@ -789,7 +816,7 @@ constexpr int kLenBins = 64;
 // keeps fx and fxOld for a separate VelocityPostGuess (MODE 1).  (Folding the
 // shortest and the longest node in one thread idles fewer FP64 lanes but
 // leaves half the warps without work in the fold, and measured slower.)
-template <int MODE, bool WALLS>
+template <int MODE, bool WALLS, int FIRST = 0>
 __global__ void __launch_bounds__(kBlock, 8) k_spread(Geom g, const Counters* cnt, const int* __restrict__ runStart,
                                                    const int* __restrict__ runCnt,
                                                    const uint32_t* __restrict__ runKey,
@@ -824,8 +851,10 @@ __global__ void __launch_bounds__(kBlock, 8) k_spread(Geom g, const Counters* cn
       const int st = runStart[myR];
       sStart[threadIdx.x] = st;
       if ((int)threadIdx.x == nHere - 1) sStart[nHere] = st + myLen;
-      fo = fCur[myR];
-      if (MODE == 0) uOld = fl.U(comp)[off];
+      // the first iteration: fxOld = 0 (the reset), and in a frozen-fluid step
+      // the node's velocity is the frozen one
+      fo = (FIRST & 1) ? 0.0 : fCur[myR];
+      if (MODE == 0) uOld = (FIRST & 2) ? fl.U0(comp)[off] : fl.U(comp)[off];
     }
     if (threadIdx.x < kLenBins) bins[threadIdx.x] = 0;
     __syncthreads();
@@ -944,8 +973,7 @@ void launch_weights(Ctx& c, bool locals) {
 }
 
 // touched-node flags, their per-block counts (iTmpA, scanned) and the total (dTotal)
-static void flag_touched_nodes(Ctx& c) {
-  cudaStream_t s = c.stream;
+static void flag_touched_nodes(Ctx& c, cudaStream_t s) {
   const long long nvec = (3 * c.g.nint + 127) / 128;
   cudaMemsetAsync(c.touch, 0, nvec * 16, s);
   k_win_by_cell<<<nblocks(c.cap), kBlock, 0, s>>>(c.dCnt, c.cellItems, c.win, c.winC);
@@ -957,7 +985,7 @@ static void flag_touched_nodes(Ctx& c) {
 }
 
 long long count_touched_nodes(Ctx& c) {
-  flag_touched_nodes(c);
+  flag_touched_nodes(c, c.stream);
   int total = 0;
   if (cudaMemcpyAsync(&total, c.dTotal, sizeof total, cudaMemcpyDeviceToHost, c.stream) != cudaSuccess ||
       cudaStreamSynchronize(c.stream) != cudaSuccess)
@@ -980,18 +1008,19 @@ void build_spread_plan(Ctx& c) {
   cudaStream_t s = c.stream;
   const long long nflags = 3 * c.g.nint;
   const long long nvec = (nflags + 127) / 128;
-  flag_touched_nodes(c);
+  flag_touched_nodes(c, s);
   const uint4* fv4 = reinterpret_cast<const uint4*>(c.touch);
   const long long nb = nblocks(nvec);
   k_set_runs<<<1, 1, 0, s>>>(c.dCnt, c.dTotal, c.capRuns);
   k_flag_emit<<<(unsigned)nb, kBlock, 0, s>>>(fv4, nvec, nflags, c.iTmpA, c.runKey, c.capRuns);
   cudaMemsetAsync(c.planAlloc, 0, sizeof(unsigned long long), s);
-  k_plan_fill<<<run_blocks(c), kBlock, 0, s>>>(c.g, c.dCnt, c.runKey, c.cellStart, c.cellItems, c.winC, c.W,
-                                                      c.imgSrc, c.runStart, c.runCnt, c.planRoot, c.planW,
-                                                      c.planAlloc, c.capContrib);
-  k_plan_total<<<1, 1, 0, s>>>(c.dCnt, c.planAlloc);
   k_comp_bounds<<<1, 1, 0, s>>>(c.dCnt, c.runKey, c.g.nint);
-  c.launches += 5;
+  c.launches += 3;
+  k_plan_fill<<<run_blocks(c), kBlock, 0, s>>>(c.g, c.dCnt, c.runKey, c.cellStart, c.cellItems, c.winC, c.W,
+                                                   c.imgSrc, c.runStart, c.runCnt, c.planRoot, c.planW, c.planAlloc,
+                                                   c.capContrib);
+  k_plan_total<<<1, 1, 0, s>>>(c.dCnt, c.planAlloc);
+  c.launches += 2;
   c.planReady = true;
   c.spreadValid = false;
 }
@@ -1004,29 +1033,44 @@ void launch_mdf_reset(Ctx& c, bool frozen) {
   c.spreadValid = true;
 }
 
-void launch_interp(Ctx& c, int comp) {
+void launch_interp(Ctx& c, int comp, int first) {
   dim3 grid(nblocks(c.capLocal), comp < 0 ? 3 : 1);
   const int comp0 = comp < 0 ? 0 : comp;
-  if (c.g.unit_h)
-    k_interp<1><<<grid, kBlock, 0, c.stream>>>(c.rec(), c.g, c.dCnt, c.W, c.win, fields_of(c), c.fv, comp0);
-  else
-    k_interp<0><<<grid, kBlock, 0, c.stream>>>(c.rec(), c.g, c.dCnt, c.W, c.win, fields_of(c), c.fv, comp0);
+  auto k = c.g.unit_h ? k_interp<1> : k_interp<0>;
+  k<<<grid, kBlock, 0, c.stream>>>(c.rec(), c.g, c.dCnt, c.W, c.win, fields_of(c), c.fv, comp0, first);
   c.launches++;
 }
 
 // the spread with the post-guess fused (MODE 0) or keeping fx and fxOld for a
 // separate VelocityPostGuess (MODE 1); the halo writes know about walls only
 // when the case has some
-void launch_spread(Ctx& c, bool fused_post_guess, int comp) {
+void launch_spread(Ctx& c, bool fused_post_guess, int comp, int first) {
   const bool w = c.g.anyWall;
-  auto k = fused_post_guess ? (w ? k_spread<0, true> : k_spread<0, false>)
-                            : (w ? k_spread<1, true> : k_spread<1, false>);
+  using K = void (*)(Geom, const Counters*, const int*, const int*, const uint32_t*, const uint32_t*, const double*,
+                     const double*, int, Fields, double*, double*, int);
+  K k;
+  if (!fused_post_guess)
+    k = w ? k_spread<1, true> : k_spread<1, false>;
+  else if (first == 3)
+    k = w ? k_spread<0, true, 3> : k_spread<0, false, 3>;
+  else if (first == 1)
+    k = w ? k_spread<0, true, 1> : k_spread<0, false, 1>;
+  else
+    k = w ? k_spread<0, true> : k_spread<0, false>;
   cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSpreadSmem);
   // one component: about a third of the runs, plus the block across its start
   const int grid = comp < 0 ? run_blocks(c) : std::max(1, (run_blocks(c) + 2) / 3 + 1);
   k<<<grid, kBlock, kSpreadSmem, c.stream>>>(c.g, c.dCnt, c.runStart, c.runCnt, c.runKey, c.planRoot, c.planW, c.fv,
                                              c.cap, fields_of(c), c.fCur, c.fPrev, comp);
   c.launches++;
+}
+
+void launch_mdf_stale(Ctx& c, bool frozen) {
+  auto k = c.g.anyWall ? k_mdf_stale<true> : k_mdf_stale<false>;
+  k<<<gs_blocks(c.capRuns), kBlock, 0, c.stream>>>(c.g, c.dCnt, fields_of(c), c.lastNodes,
+                                                   reinterpret_cast<const unsigned*>(c.touch), frozen ? 1 : 0);
+  c.launches++;
+  c.spreadValid = true;
 }
 
 void launch_post_guess(Ctx& c) {

@@ -78,6 +78,18 @@ struct Ctx {
   ibmdem_wall_probe* dProbes = nullptr;
   int nProbe = 0;
 
+  // tangential friction of the marker contacts (ibmdem_set_friction), off while
+  // ktRatio == 0.  History of the last contact-force call on side
+  // Counters::histSide: per local of that call the range of its contacts, per
+  // contact the partner's parcel id (I_PID; -1: not touching) and the
+  // tangential displacement; pidMap takes a parcel id to that call's local.
+  double ktRatio = 0.0, mu = 0.0;
+  int2* histRange[2] = {};  // [capLocal]
+  int* histGid[2] = {};     // [capPairs]
+  double* histXi[2] = {};   // [3*capPairs]
+  int* pidMap = nullptr;    // [capLocal]
+  size_t bytesHist = 0;
+
   // contact lists
   int* activeList = nullptr;  // [capLocal]
   int* pairCnt = nullptr;     // [capLocal]
@@ -157,12 +169,15 @@ enum Phase : int {
   P_INTERP = 0, P_SPREAD, P_WEIGHTS, P_PLAN, P_CELLS, P_PAIRS, P_FORCE, P_BODYSUM, P_BODYMOVE, P_MARKERS,
   P_IMAGES, P_RESET, P_FGUESS, P_FHALO, P_FOTHER, P_FPOISSON, P_COUNT
 };
-// records CUDA events around one phase on the context's stream when timing is on
+// records CUDA events around one phase on the context's stream (or `s`) when
+// timing is on
 struct PhaseScope {
   Ctx& c;
   int phase;
+  cudaStream_t s;
   cudaEvent_t a = nullptr, b = nullptr;
-  PhaseScope(Ctx& ctx, int ph);
+  PhaseScope(Ctx& ctx, int ph) : PhaseScope(ctx, ph, ctx.stream) {}
+  PhaseScope(Ctx& ctx, int ph, cudaStream_t stream);
   ~PhaseScope();
 };
 
@@ -171,20 +186,27 @@ void rebuild_cell_lists(Ctx& c);
 void launch_img_update(Ctx& c);
 // contact.cu
 void rebuild_collision_lists(Ctx& c);
+// the pair forces into fcol; with friction on, also the tangential history
 void launch_collision_force(Ctx& c);
 // CalculateSolidBoundaryCollisionForce: wall forces into fcol (after the pair
 // forces) and the probe sums; nothing without walls
 void launch_wall_force(Ctx& c);
 // ibm.cu
 void launch_weights(Ctx& c, bool locals);
+// The spread plan for the current weights, on the context's stream.
 void build_spread_plan(Ctx& c);
 // number of touched (component, node) pairs for the current weights; synchronises
 // c.stream (-1 on a CUDA error)
 long long count_touched_nodes(Ctx& c);
 void launch_mdf_reset(Ctx& c, bool frozen);
-// comp: one velocity component, or -1 for all three
-void launch_interp(Ctx& c, int comp);
-void launch_spread(Ctx& c, bool fused_post_guess, int comp);
+// comp: one velocity component, or -1 for all three.  first: bit 0, the first
+// iteration of a forcing loop whose reset is launch_mdf_stale (fdrag and fxOld
+// taken as 0); bit 1, the old velocity read from the frozen field
+void launch_interp(Ctx& c, int comp, int first = 0);
+void launch_spread(Ctx& c, bool fused_post_guess, int comp, int first = 0);
+// the forcing loop's reset when its first iteration takes the first flags:
+// only the nodes the last spread wrote and the current plan does not touch
+void launch_mdf_stale(Ctx& c, bool frozen);
 void launch_post_guess(Ctx& c);
 void record_written_nodes(Ctx& c);
 // Interpolation at n <= IBMDEM_PROBE_MAX_POINTS device points with the

@@ -44,6 +44,7 @@ __device__ inline void copy_record(Recs A, int e, Recs B, int n) {
   for (int f = 0; f < ND; ++f) B.D(f, n) = A.D(f, e);
   B.I(I_GIDX, n) = A.I(I_GIDX, e);
   B.I(I_MSIDX, n) = A.I(I_MSIDX, e);
+  B.I(I_PID, n) = A.I(I_PID, e);
 }
 
 __global__ void k_compress_move(Recs A, Recs B, Geom g, const Counters* cnt, const int* flag, const int* pos) {
@@ -210,6 +211,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_img_emit(Recs R, Geom g, Counters
     for (int f = 0; f < ND; ++f) R.D(f, e) = R.D(f, m);
     R.I(I_GIDX, e) = R.I(I_GIDX, m);
     R.I(I_MSIDX, e) = R.I(I_MSIDX, m);
+    R.I(I_PID, e) = R.I(I_PID, m);
     int id[3];
     int wallImg = 0;
     // MyMPISendAndRecv does not send vgap and wdrag (ZJS_MPI_DEM.F90:17-32); the

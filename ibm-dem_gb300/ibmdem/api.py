@@ -47,6 +47,7 @@ EXPORTS = [
     "ibmdem_set_fluid_async", "ibmdem_set_fluid_params", "ibmdem_set_fluid_field", "ibmdem_get_fluid_field", "ibmdem_StoreOldVelocity",
     "ibmdem_VelocityGuess", "ibmdem_FillGhostRegionForFluid", "ibmdem_Boundary", "ibmdem_ModifyBulkVelocity",
     "ibmdem_VelocityDivergence", "ibmdem_PressureCorrection", "ibmdem_VelocityCorrection", "ibmdem_PoissonSolver",
+    "ibmdem_set_friction", "ibmdem_get_friction_history",
 ]
 
 SUBROUTINES = [
@@ -93,6 +94,8 @@ def load(path=LIB_PATH):
     lib.ibmdem_step.argtypes = [vp, i32]
     lib.ibmdem_interpolate_velocity_noalloc.argtypes = [vp, i32, vp, vp]
     d = ctypes.c_double
+    lib.ibmdem_set_friction.argtypes = [vp, d, d]
+    lib.ibmdem_get_friction_history.argtypes = [vp, vp, vp, vp, P(i32), P(i32)]
     lib.ibmdem_set_fluid_params.argtypes = [vp, d, d, d, d]
     lib.ibmdem_set_fluid_field.argtypes = [vp, i32, vp]
     lib.ibmdem_get_fluid_field.argtypes = [vp, i32, vp]
@@ -281,6 +284,22 @@ class Case:
         self._chk(self.lib.ibmdem_get_collision_lists(self.h, start.ctypes.data, idx.ctypes.data, ctypes.byref(nl),
                                                       ctypes.byref(npairs)), "pairs")
         return start, idx
+
+    def set_friction(self, ktRatio, mu):
+        """Tangential friction of the marker contacts (0 = off, the reference's law)."""
+        self._chk(self.lib.ibmdem_set_friction(self.h, float(ktRatio), float(mu)), "set_friction")
+
+    def get_friction_history(self):
+        """(start, partner globalIdx, displacement) of the last contact-force call."""
+        nl, n = ctypes.c_int32(), ctypes.c_int32()
+        self._chk(self.lib.ibmdem_get_friction_history(self.h, None, None, None, ctypes.byref(nl), ctypes.byref(n)),
+                  "get_friction_history")
+        start = np.zeros(nl.value + 1, np.int32)
+        gid = np.empty(n.value, np.int32)
+        xi = np.empty((n.value, 3))
+        self._chk(self.lib.ibmdem_get_friction_history(self.h, start.ctypes.data, gid.ctypes.data, xi.ctypes.data,
+                                                       ctypes.byref(nl), ctypes.byref(n)), "get_friction_history")
+        return start, gid, xi
 
     # ---- fluid stencils (ibmdem_VelocityGuess and the others) ----------------
     def set_fluid_params(self, visc, CPx=0.0, CPy=0.0, CPz=0.0):

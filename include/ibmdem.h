@@ -189,6 +189,27 @@ int ibmdem_UpdateGhostCellWeightListDEM(ibmdem_ctx* ctx);
 int ibmdem_UpdateParcelInfoInGhostRegion(ibmdem_ctx* ctx);
 /* ZJS_COLLISION_DEM.F90:21-74: spring-dashpot contact force fcol. */
 int ibmdem_CalculateCollisionForce(ibmdem_ctx* ctx);
+/* Tangential friction of the marker contacts, off while ktRatio == 0 (the
+ * default).  No counterpart in the reference, whose contact law is normal only
+ * (ZJS_COLLISION_DEM.F90:53-57); with friction off CalculateCollisionForce is
+ * the reference's law exactly.  With ktRatio > 0 each touching pair also
+ * carries a tangential spring kt = ktRatio*kn with damping
+ * etat = eta*sqrt(meff*kt) and a Coulomb limit mu*|fn|: its tangential
+ * displacement is kept from one contact-force call to the next, keyed by the
+ * parcel ids of both parcels -- a parcel's index in the array last given to
+ * ibmdem_set_parcels, which its periodic images share -- so it survives list
+ * rebuilds, migrations and periodic images,
+ * projected on the new tangent plane and advanced by dtDEM times the tangential
+ * relative velocity; beyond the limit the force is scaled to it and the
+ * displacement reset to the sliding value.  fcol += n*fn + ft per pair.  The
+ * history is dropped by this call and by ibmdem_set_parcels. */
+int ibmdem_set_friction(ibmdem_ctx* ctx, double ktRatio, double mu);
+/* The tangential history the last contact-force call left, as CSR over the
+ * locals: start[nlocal+1], the partner's parcel id per contact (-1: listed but
+ * not touching) and 3 displacement components per contact.  Pass NULL to query
+ * the sizes.  nlocal is 0 while friction is off. */
+int ibmdem_get_friction_history(ibmdem_ctx* ctx, int32_t* start, int32_t* gid, double* xi, int32_t* nlocal_out,
+                                int32_t* n_out);
 /* ZJS_COLLISION_DEM.F90:76-148: parcel-wall spring-dashpot added to fcol for
  * local parcels in the first or last cell layer, faces -x..+z in order, and the
  * probe sums.  Without walls it does nothing.  The reference also appends a
@@ -237,8 +258,11 @@ int ibmdem_step(ibmdem_ctx* ctx, int32_t nsteps);
  * [0, nx*dx) x [0, ny*dy) x [0, nz*dz); ulp: device array of n (u, v, w).
  * Allocates nothing: the per-point weights live in a fixed static device array
  * of IBMDEM_PROBE_MAX_POINTS points, and a larger n returns IBMDEM_ERANGE.
- * The call synchronises the context's stream and returns IBMDEM_ERANGE when a
- * point lies outside the box.  Calls that overlap in time on one device (from
+ * That array (about 11.3 MB) is part of the library's device module, so every
+ * device on which the library's kernels are loaded holds it until the process
+ * exits, whether or not this function is ever called.  Each call waits for its
+ * result (it synchronises the context's stream) and returns IBMDEM_ERANGE when
+ * a point lies outside the box.  Calls that overlap in time on one device (from
  * several threads or contexts) share that array and race.  The first call on a
  * device looks the array up (which may load the module): make it before any
  * stream capture.  No counterpart in the reference. */

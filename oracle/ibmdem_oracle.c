@@ -96,6 +96,18 @@ struct orc_case {
   int wCap;
   /* fields, Fortran layout with halo */
   double *u, *v, *w, *fx, *fy, *fz, *fxOld, *fyOld, *fzOld, *u0, *v0, *w0;
+  /* tangential friction of the marker contacts (orc_set_friction); off while
+   * ktRatio == 0.  No counterpart in the reference, whose contact law is normal
+   * only (ZJS_COLLISION_DEM.F90:53-57).  History of the last contact-force call:
+   * per local of that call its persistent id (the record padding, set by
+   * orc_set_parcels) and the range of its contacts, per contact the partner's
+   * id (-1: not touching) and the tangential displacement; hMap takes an id to
+   * that call's local. */
+  double ktRatio, mu;
+  int hN;
+  int32_t *hGidLocal, *hStart, *hGid, *hMap;
+  double* hXi;
+  int hMapN;
   char err[256];
 };
 
@@ -255,7 +267,32 @@ void orc_destroy(orc_case* c) {
   free(c->neighCellWeight);
   double* f[] = {c->u, c->v, c->w, c->fx, c->fy, c->fz, c->fxOld, c->fyOld, c->fzOld, c->u0, c->v0, c->w0};
   for (int q = 0; q < 12; ++q) free(f[q]);
+  free(c->hGidLocal);
+  free(c->hStart);
+  free(c->hGid);
+  free(c->hMap);
+  free(c->hXi);
   free(c);
+}
+
+/* drop the tangential history: the next contact-force call starts from none */
+static void clear_history(orc_case* c) {
+  free(c->hGidLocal);
+  free(c->hStart);
+  free(c->hGid);
+  free(c->hMap);
+  free(c->hXi);
+  c->hGidLocal = c->hStart = c->hGid = c->hMap = NULL;
+  c->hXi = NULL;
+  c->hN = c->hMapN = 0;
+}
+
+int orc_set_friction(orc_case* c, double ktRatio, double mu) {
+  if (!(ktRatio >= 0.0) || !(mu >= 0.0)) return fail(c, IBMDEM_EINVAL, "ktRatio and mu must be >= 0");
+  c->ktRatio = ktRatio;
+  c->mu = mu;
+  clear_history(c);
+  return 0;
 }
 
 static int ensure_parts(orc_case* c, int need) {
@@ -319,9 +356,16 @@ int orc_set_parcels(orc_case* c, int32_t np, const ibmdem_parcel* parts) {
   int rc = ensure_parts(c, np);
   if (rc) return rc;
   memcpy(c->part, parts, (size_t)np * sizeof(Parcel));
-  for (int i = 0; i < np; ++i) c->part[i].pType = -1;
+  /* the record's padding holds the parcel's persistent id (its index here),
+   * which record copies carry to migrated locals and periodic images: the key
+   * of the tangential contact history */
+  for (int i = 0; i < np; ++i) {
+    c->part[i].pType = -1;
+    c->part[i].pad_ = i;
+  }
   c->np = c->npLocal = np;
   c->listsBuilt = 0;
+  clear_history(c);
   return 0;
 }
 int orc_get_parcels(orc_case* c, ibmdem_parcel* parts, int32_t cap, int32_t* np_out, int32_t* nlocal_out) {
@@ -719,9 +763,150 @@ int orc_UpdateParcelInfoInGhostRegion(orc_case* c) {
 /* ------------------------------------------------------------------ */
 /* contacts                                                            */
 
+/* CalculateCollisionForce with tangential friction (orc_set_friction; not in
+ * the reference).  The normal part is the reference's law below, term by term.
+ * For a touching pair (deltan > 0) with relative marker velocity
+ * u = v_i - v_j (marker velocities include their body's rotation):
+ *   vt = u - vn n (vn as the normal law forms it);
+ *   h  = the pair's tangential displacement of the last call (keyed by the
+ *        persistent ids of both parcels, 0 when new), projected on the tangent
+ *        plane, h - (n.h) n, then h + dtDEM vt;
+ *   kt = ktRatio kn, etat = eta sqrt(meff kt), ft = -kt h - etat vt;
+ *   Coulomb: when |ft| > mu |fn| (fn = kn deltan - etan vn), ft is scaled to
+ *        mu |fn| and h reset to the sliding value -(ft + etat vt) / kt;
+ *   fcol_i += n fn + ft, component by component.
+ * A listed pair that does not touch keeps no history. */
+static int collision_force_friction(orc_case* c) {
+  const double eta = c->eta, knCoeff = c->p.knCoeff, di = c->di, dtDEM = c->dtDEM;
+  const double ktRatio = c->ktRatio, mu = c->mu;
+  const int nl = c->npLocal;
+  const int64_t npairs = c->neighPartStart[nl];
+  int32_t* nGid = (int32_t*)malloc((size_t)(npairs ? npairs : 1) * sizeof(int32_t));
+  double* nXi = (double*)malloc((size_t)(npairs ? npairs : 1) * 3 * sizeof(double));
+  int32_t* nStart = (int32_t*)malloc((size_t)(nl + 1) * sizeof(int32_t));
+  int32_t* nGidLocal = (int32_t*)malloc((size_t)(nl ? nl : 1) * sizeof(int32_t));
+  if (!nGid || !nXi || !nStart || !nGidLocal) {
+    free(nGid);
+    free(nXi);
+    free(nStart);
+    free(nGidLocal);
+    return fail(c, IBMDEM_ENOMEM, "tangential history");
+  }
+  memcpy(nStart, c->neighPartStart, (size_t)(nl + 1) * sizeof(int32_t));
+#pragma omp parallel for schedule(dynamic, 256) num_threads(g_threads)
+  for (int ii = 0; ii < nl; ++ii) {
+    Parcel* pi = &c->part[ii];
+    const int gi = pi->pad_;
+    nGidLocal[ii] = gi;
+    const int o = (gi >= 0 && gi < c->hMapN) ? c->hMap[gi] : -1;
+    const int os = o >= 0 ? c->hStart[o] : 0, oe = o >= 0 ? c->hStart[o + 1] : 0;
+    pi->fcol[0] = 0;
+    pi->fcol[1] = 0;
+    pi->fcol[2] = 0;
+    for (int q = c->neighPartStart[ii]; q < c->neighPartStart[ii + 1]; ++q) {
+      const Parcel* pj = &c->part[c->neighPartIdx[q] - 1];
+      double r1 = pi->x[0] - pj->x[0];
+      double r2 = pi->x[1] - pj->x[1];
+      double r3 = pi->x[2] - pj->x[2];
+      double dist = sqrt(r1 * r1 + r2 * r2 + r3 * r3);
+      double n1 = r1 / dist, n2 = r2 / dist, n3 = r3 / dist;
+      double meff = 2 * pi->m * pj->m / (pi->m + pj->m);
+      double rij = pi->radeff + pj->radeff;
+      double deltan = rij - dist;
+      double kn = knCoeff / (0.1 * di) * meff;
+      double etan = eta * sqrt(meff * kn);
+      double f1 = 0, f2 = 0, f3 = 0;
+      double u1 = pi->v[0] - pj->v[0], u2 = pi->v[1] - pj->v[1], u3 = pi->v[2] - pj->v[2];
+      double vnij = n1 * u1 + n2 * u2 + n3 * u3;
+      double h1 = 0, h2 = 0, h3 = 0;
+      int hg = -1;
+      if (deltan > 0) {
+        double fn = kn * deltan - etan * vnij;
+        double vt1 = u1 - vnij * n1, vt2 = u2 - vnij * n2, vt3 = u3 - vnij * n3;
+        for (int t = os; t < oe; ++t)
+          if (c->hGid[t] == pj->pad_) {
+            h1 = c->hXi[3 * (size_t)t];
+            h2 = c->hXi[3 * (size_t)t + 1];
+            h3 = c->hXi[3 * (size_t)t + 2];
+            break;
+          }
+        double hn = n1 * h1 + n2 * h2 + n3 * h3;
+        h1 = h1 - hn * n1;
+        h2 = h2 - hn * n2;
+        h3 = h3 - hn * n3;
+        h1 = h1 + dtDEM * vt1;
+        h2 = h2 + dtDEM * vt2;
+        h3 = h3 + dtDEM * vt3;
+        double kt = ktRatio * kn;
+        double etat = eta * sqrt(meff * kt);
+        double ft1 = -kt * h1 - etat * vt1, ft2 = -kt * h2 - etat * vt2, ft3 = -kt * h3 - etat * vt3;
+        double ftm = sqrt(ft1 * ft1 + ft2 * ft2 + ft3 * ft3);
+        double lim = mu * fabs(fn);
+        if (ftm > lim) {
+          double sc = lim / ftm;
+          ft1 = ft1 * sc;
+          ft2 = ft2 * sc;
+          ft3 = ft3 * sc;
+          h1 = -(ft1 + etat * vt1) / kt;
+          h2 = -(ft2 + etat * vt2) / kt;
+          h3 = -(ft3 + etat * vt3) / kt;
+        }
+        f1 = n1 * fn + ft1;
+        f2 = n2 * fn + ft2;
+        f3 = n3 * fn + ft3;
+        hg = pj->pad_;
+      }
+      nGid[q] = hg;
+      nXi[3 * (size_t)q] = h1;
+      nXi[3 * (size_t)q + 1] = h2;
+      nXi[3 * (size_t)q + 2] = h3;
+      pi->fcol[0] = pi->fcol[0] + f1;
+      pi->fcol[1] = pi->fcol[1] + f2;
+      pi->fcol[2] = pi->fcol[2] + f3;
+    }
+  }
+  int maxg = -1;
+  for (int ii = 0; ii < nl; ++ii) maxg = nGidLocal[ii] > maxg ? nGidLocal[ii] : maxg;
+  int32_t* map = (int32_t*)malloc((size_t)(maxg + 2) * sizeof(int32_t));
+  if (!map) {
+    free(nGid);
+    free(nXi);
+    free(nStart);
+    free(nGidLocal);
+    return fail(c, IBMDEM_ENOMEM, "tangential history");
+  }
+  for (int g = 0; g <= maxg + 1; ++g) map[g] = -1;
+  for (int ii = 0; ii < nl; ++ii)
+    if (nGidLocal[ii] >= 0) map[nGidLocal[ii]] = ii;
+  clear_history(c);
+  c->hN = nl;
+  c->hGidLocal = nGidLocal;
+  c->hStart = nStart;
+  c->hGid = nGid;
+  c->hXi = nXi;
+  c->hMap = map;
+  c->hMapN = maxg + 2;
+  return 0;
+}
+
+/* the tangential history of the last contact-force call as CSR over that
+ * call's locals: start[nl+1], partner id (-1: not touching) and 3
+ * displacement components per contact; pass NULL to query the sizes */
+int orc_get_friction_history(orc_case* c, int32_t* start, int32_t* gid, double* xi, int32_t* nl_out,
+                             int32_t* n_out) {
+  if (nl_out) *nl_out = c->hN;
+  if (n_out) *n_out = c->hN ? c->hStart[c->hN] : 0;
+  if (!c->hN) return 0;
+  if (start) memcpy(start, c->hStart, (size_t)(c->hN + 1) * sizeof(int32_t));
+  if (gid) memcpy(gid, c->hGid, (size_t)c->hStart[c->hN] * sizeof(int32_t));
+  if (xi) memcpy(xi, c->hXi, (size_t)c->hStart[c->hN] * 3 * sizeof(double));
+  return 0;
+}
+
 /* CalculateCollisionForce (ZJS_COLLISION_DEM.F90:21-74) */
 int orc_CalculateCollisionForce(orc_case* c) {
   if (!c->listsBuilt) return fail(c, IBMDEM_ESTATE, "lists not built");
+  if (c->ktRatio > 0.0) return collision_force_friction(c);
   const double eta = c->eta;
   const double knCoeff = c->p.knCoeff, di = c->di;
 #pragma omp parallel for schedule(dynamic, 256) num_threads(g_threads)

@@ -49,6 +49,11 @@ int orc_UpdateLocalCellWeightListDEM(orc_case* c);
 int orc_UpdateGhostCellWeightListDEM(orc_case* c);
 int orc_UpdateParcelInfoInGhostRegion(orc_case* c);
 int orc_CalculateCollisionForce(orc_case* c);
+/* tangential friction of the marker contacts, off while ktRatio == 0 (not in
+ * the reference); drops the tangential history */
+int orc_set_friction(orc_case* c, double ktRatio, double mu);
+int orc_get_friction_history(orc_case* c, int32_t* start, int32_t* gid, double* xi, int32_t* nl_out,
+                             int32_t* n_out);
 int orc_CalculateSolidBoundaryCollisionForce(orc_case* c);
 int orc_set_wall_probes(orc_case* c, int32_t n, const ibmdem_wall_probe* probes);
 int orc_get_wall_probes(orc_case* c, ibmdem_wall_probe* probes, int32_t cap, int32_t* n_out);

@@ -59,6 +59,8 @@ def _load():
         getattr(lib, "orc_" + name).argtypes = [vp]
         getattr(lib, "orc_" + name).restype = ctypes.c_int
     lib.orc_step.argtypes = [vp, i32]
+    lib.orc_set_friction.argtypes = [vp, ctypes.c_double, ctypes.c_double]
+    lib.orc_get_friction_history.argtypes = [vp, vp, vp, vp, P(i32), P(i32)]
     lib.orc_set_wall_probes.argtypes = [vp, i32, vp]
     lib.orc_get_wall_probes.argtypes = [vp, vp, i32, P(i32)]
     lib.orc_eta.restype = ctypes.c_double
@@ -209,6 +211,19 @@ class OracleCase:
 
     def step(self, n=1):
         self._chk(self.lib.orc_step(self.h, int(n)), "step")
+
+    def set_friction(self, ktRatio, mu):
+        self._chk(self.lib.orc_set_friction(self.h, float(ktRatio), float(mu)), "set_friction")
+
+    def get_friction_history(self):
+        nl, n = ctypes.c_int32(), ctypes.c_int32()
+        self.lib.orc_get_friction_history(self.h, None, None, None, ctypes.byref(nl), ctypes.byref(n))
+        start = np.zeros(nl.value + 1, np.int32)
+        gid = np.empty(n.value, np.int32)
+        xi = np.empty((n.value, 3))
+        self.lib.orc_get_friction_history(self.h, start.ctypes.data, gid.ctypes.data, xi.ctypes.data,
+                                          ctypes.byref(nl), ctypes.byref(n))
+        return start, gid, xi
 
     def set_wall_probes(self, probes):
         from ibmdem import records

@@ -143,7 +143,9 @@ def run(case):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit("usage: python make_golden.py <directory of the reference sources holding CYLINDER_LP1125.dat>")
+    ref = sys.argv[1]
     np.savez_compressed(os.path.join(HERE, "sphere_contact.npz"), **run(sphere_case()))
     np.savez_compressed(os.path.join(HERE, "cylinders.npz"),
                         **run(cylinder_case(os.path.join(ref, "CYLINDER_LP1125.dat"))))
