@@ -274,8 +274,9 @@ def algorithmic(counters):
     velocity gap, the division by dt as 4 operations, the fdrag update and
     fdrag*vol); spreading 2 per contribution less the first subtraction of
     each node (an integer sign flip), plus 3 per node for the post-guess;
-    weights FP64_WEIGHTS_PER_PARCEL per parcel (18 one-axis kernels with a
-    square root and an exact /3 each, and 108 products)."""
+    weights FP64_WEIGHTS_PER_PARCEL per parcel (ncu's count: 18 one-axis
+    kernels with a square root and an exact /3 each, 108 products, and the
+    window's coordinates)."""
     M = counters["npLocal"]
     NP = counters["np"]
     C = counters["contributions"]
@@ -298,7 +299,7 @@ def algorithmic(counters):
 
 
 # FP64 instructions per parcel of the delta-weight kernel (ncu count, 512-sphere case)
-FP64_WEIGHTS_PER_PARCEL = 480
+FP64_WEIGHTS_PER_PARCEL = 516
 
 
 def kernel_rows(alg, phases, hbm_peak, fp64_peak, npLocal):
@@ -366,6 +367,7 @@ def run_batched(args, device, stream):
         c.synchronize()
     b = api.Batch(cases, device=device)
     lanes = b.autotune(trial_steps=2)
+    _, fused, interp_block = b.config()
     b.step(1)
     b.synchronize()
     l0 = sum(c.launches for c in cases)
@@ -379,7 +381,8 @@ def run_batched(args, device, stream):
         c.close()
     return {"value": nbodies * k / batch_s, "unit": "particle-steps/s", "plain_value": nbodies * k / plain_s,
             "ratio_vs_plain": plain_s / batch_s, "steps": k, "cases": len(cases), "bodies": nbodies,
-            "markers": nmark, "lanes": lanes, "ms_per_step": batch_s / k * 1e3, "plain_ms_per_step": plain_s / k * 1e3,
+            "markers": nmark, "lanes": lanes, "shared_forcing_launches": bool(fused), "interp_block": interp_block,
+            "ms_per_step": batch_s / k * 1e3, "plain_ms_per_step": plain_s / k * 1e3,
             "gpu_launches": batch_launch, "plain_gpu_launches": plain_launch, "graph_launches": k,
             "workload": f"{len(cases)} cases: grid in {{32,64,96,128}}^3, d in {{8,12,16}}h, bodies log-uniform "
                         f"8..512 capped at 25% solid fraction, 32-mode Fourier field, seed {args.seed}+i",

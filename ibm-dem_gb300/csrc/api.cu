@@ -1182,11 +1182,10 @@ int ibmdem_InitializationDEM(ibmdem_ctx* h) {
   return rc;
 }
 
-static int mdf(ibmdem_ctx* h, bool frozen) {
+// The forcing loop's set-up: the plan for the current weights and the reset.
+// *first gets the first iteration's flags for launch_interp / launch_spread.
+static int mdf_begin(ibmdem_ctx* h, bool frozen, int* first) {
   Ctx& c = h->c;
-  REQUIRE(c.haveFluid, "no fluid field");
-  const bool perCompUpload = !frozen && c.uploadPending;  // ibmdem_set_fluid_async still uploading
-  wait_fields_read(c, !perCompUpload);
   // The plan for new weights does not read the fluid, but it is built here, in
   // order: beside the forcing loop on a second stream it took the loop's SMs
   // (the fill is issue-bound, the loop FP64-bound at high occupancy) and the
@@ -1203,7 +1202,32 @@ static int mdf(ibmdem_ctx* h, bool frozen) {
     else
       launch_mdf_reset(c, frozen);
   }
-  const int first = 1 | (frozen ? 2 : 0);
+  *first = 1 | (frozen ? 2 : 0);
+  return IBMDEM_OK;
+}
+
+// After the forcing loop: the images take their sources' final fdrag (the
+// spread gathers the roots' fdrag*vol, never the images'), and the nodes the
+// last spread wrote are kept for the next reset.
+static void mdf_end(Ctx& c) {
+  {
+    PhaseScope t(c, P_IMAGES);
+    launch_img_update(c);
+  }
+  {
+    PhaseScope t(c, P_RESET);
+    record_written_nodes(c);
+  }
+}
+
+static int mdf(ibmdem_ctx* h, bool frozen) {
+  Ctx& c = h->c;
+  REQUIRE(c.haveFluid, "no fluid field");
+  const bool perCompUpload = !frozen && c.uploadPending;  // ibmdem_set_fluid_async still uploading
+  wait_fields_read(c, !perCompUpload);
+  int first = 0;
+  int rc = mdf_begin(h, frozen, &first);
+  if (rc) return rc;
   // The three velocity components never meet inside the MDF loop (fluid.F90:
   // 265-285): a marker's component interpolates from that component of the
   // field, and the spread and the post-guess of a node write that component
@@ -1211,9 +1235,7 @@ static int mdf(ibmdem_ctx* h, bool frozen) {
   // in a coupled step) the loop runs component by component, so that the
   // read-out of u and fx can start once the first component is done
   // (ibmdem_get_fluid_async); the frozen-fluid step keeps the three
-  // components in one launch, which is 3% faster on the device.  The spread
-  // gathers the roots' fdrag*vol, never the images', so either way the images
-  // take their sources' final fdrag once, after the loop.
+  // components in one launch, which is 3% faster on the device.
   cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
   cudaStreamIsCapturing(c.stream, &cap);
   const bool byComp = !frozen && cap == cudaStreamCaptureStatusNone;
@@ -1235,18 +1257,39 @@ static int mdf(ibmdem_ctx* h, bool frozen) {
       cudaEventRecord(c.compDone[comp], c.stream);
     }
   }
-  {
-    PhaseScope t(c, P_IMAGES);
-    launch_img_update(c);
-  }
-  {
-    PhaseScope t(c, P_RESET);
-    record_written_nodes(c);
-  }
+  mdf_end(c);
   if (perCompUpload) c.uploadPending = false;  // the stream has waited for the last component
   c.compDoneAt = byComp ? c.launches : -1;
   return launch_status(h);
 }
+
+}  // extern "C"
+
+// A frozen-fluid step whose forcing loop a batch runs for all its members in
+// shared launches (batch.cu): the part before the loop, and the part after it.
+int step_before_forcing(ibmdem_ctx* h) {
+  CHECK_CTX();
+  Ctx& c = h->c;
+  REQUIRE(c.haveFluid, "no fluid field");
+  REQUIRE(c.p.Ns > 0, "no forcing iterations");
+  wait_fields_read(c);
+  int first = 0;
+  int rc = mdf_begin(h, true, &first);
+  if (rc) return rc;
+  return launch_status(h);
+}
+
+int step_after_forcing(ibmdem_ctx* h) {
+  CHECK_CTX();
+  Ctx& c = h->c;
+  mdf_end(c);
+  c.compDoneAt = -1;
+  int rc = launch_status(h);
+  if (rc) return rc;
+  return ibmdem_CloudEvolutionMS(h);
+}
+
+extern "C" {
 
 int ibmdem_MultiDirectForcing(ibmdem_ctx* h) {
   CHECK_CTX();

@@ -11,6 +11,13 @@
 // same in a batch as alone.  The number of chains is a tuning knob
 // (ibmdem_batch_autotune times a few and keeps the fastest): many chains give
 // small cases room to overlap, few chains keep large cases from contending.
+// Optionally (ibmdem_batch_set_fused) the forcing loop -- two thirds of a step's
+// work -- runs for all members at once: the chains build every member's plan
+// and reset, join, one interpolation and one spread launch per iteration cover
+// all members (each block looks its member up in a descriptor table and runs
+// the per-case block code on that member's state), and the chains fork again
+// for the images and CloudEvolutionMS.  The autotuner also decides between the
+// two and picks the interpolation's block size.
 //
 // Server.  Requests wait in a first-in first-out queue and are admitted while
 // the summed device footprint of the running cases (ibmdem_case_bytes) stays
@@ -84,6 +91,15 @@ struct ibmdem_batch {
   std::vector<unsigned long long> keys;  // member state the captured step leaves
   bool stationary = true;  // the captured step leaves the state it was captured from
   bool dirty = true;
+  // the forcing loop of all members in shared launches (ibmdem_batch_set_fused)
+  int fused = 0;
+  int interpBlock = kBlock;
+  void* dDesc = nullptr;
+  size_t descBytes = 0;
+  ForcingBatch fb;
+  cudaEvent_t fork2 = nullptr;
+  std::vector<cudaEvent_t> joins2;
+  bool capturedFused = false;
   std::string err = "ok";
 };
 
@@ -112,13 +128,16 @@ cudaError_t ensure_streams(ibmdem_batch* b, int nLanes) {
   if (!b->origin) e = cudaStreamCreateWithFlags(&b->origin, cudaStreamNonBlocking);
   if (e == cudaSuccess && !b->fork) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
   if (e == cudaSuccess && !b->done) e = cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming);
+  if (e == cudaSuccess && !b->fork2) e = cudaEventCreateWithFlags(&b->fork2, cudaEventDisableTiming);
   while (e == cudaSuccess && (int)b->laneStreams.size() < nLanes) {
     cudaStream_t s = nullptr;
-    cudaEvent_t j = nullptr;
+    cudaEvent_t j = nullptr, j2 = nullptr;
     e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&j, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&j2, cudaEventDisableTiming);
     if (s) b->laneStreams.push_back(s);
     if (j) b->joins.push_back(j);
+    if (j2) b->joins2.push_back(j2);
   }
   while (e == cudaSuccess && b->inputs.size() < b->cases.size()) {
     cudaEvent_t q = nullptr;
@@ -156,6 +175,27 @@ int capture_batch(ibmdem_batch* b) {
   // a pending asynchronous field read-out is waited for on the member's own
   // stream (the graph is ordered after it), not inside the capture
   for (ibmdem_ctx* m : b->cases) wait_fields_read(m->c);
+  // The forcing loop in shared launches needs every member to run the same
+  // number of forcing iterations; the members' descriptor table is uploaded
+  // here, before the capture.
+  bool useFused = b->fused != 0;
+  for (ibmdem_ctx* m : b->cases)
+    useFused = useFused && m->c.p.Ns > 0 && m->c.p.Ns == b->cases[0]->c.p.Ns && m->c.runsSized;
+  if (useFused) {
+    std::vector<Ctx*> members(n);
+    for (int i = 0; i < n; ++i) members[i] = &b->cases[i]->c;
+    const size_t need = forcing_desc_bytes(members, b->interpBlock);
+    if (b->descBytes < need) {
+      if (b->dDesc) cudaFree(b->dDesc);
+      b->dDesc = nullptr;
+      b->descBytes = 0;
+      e = cudaMalloc(&b->dDesc, need);
+      if (e != cudaSuccess) return batch_error(b, IBMDEM_ENOMEM, "batch table: %s", cudaGetErrorString(e));
+      b->descBytes = need;
+    }
+    e = forcing_desc_upload(members, b->dDesc, b->interpBlock, b->origin, &b->fb);
+    if (e != cudaSuccess) return batch_error(b, IBMDEM_ECUDA, "batch table: %s", cudaGetErrorString(e));
+  }
   std::vector<unsigned long long> pre(n);
   for (int i = 0; i < n; ++i) pre[i] = state_key(b->cases[i]->c);
   e = cudaStreamBeginCapture(b->origin, cudaStreamCaptureModeRelaxed);
@@ -164,27 +204,55 @@ int capture_batch(ibmdem_batch* b) {
   for (int k = 0; k < nl; ++k) cudaStreamWaitEvent(b->laneStreams[k], b->fork, 0);
   int rc = IBMDEM_OK;
   int failed = -1;
-  for (int i : order) {
+  // one member's part of the step on its chain: the whole step, or the part
+  // before (part 1) or after (part 2) the shared forcing loop
+  auto member_part = [&](int i, int part) {
     Ctx& c = b->cases[i]->c;
     cudaStream_t own = c.stream;
     bool timing = c.timing;
     c.stream = b->laneStreams[laneOf[i]];
     c.timing = false;
     long long l0 = c.launches;
-    rc = ibmdem_step(b->cases[i], 1);
-    b->launchesPerStep[i] = c.launches - l0;
+    int r = part == 0 ? ibmdem_step(b->cases[i], 1)
+                      : (part == 1 ? step_before_forcing(b->cases[i]) : step_after_forcing(b->cases[i]));
+    b->launchesPerStep[i] += c.launches - l0;
     c.launches = l0;  // counted again per replay
     c.stream = own;
     c.timing = timing;
-    if (rc) {
+    return r;
+  };
+  auto join_lanes = [&](std::vector<cudaEvent_t>& ev) {
+    for (int k = 0; k < nl; ++k) {
+      cudaEventRecord(ev[k], b->laneStreams[k]);
+      cudaStreamWaitEvent(b->origin, ev[k], 0);
+    }
+  };
+  for (int i : order) {
+    if ((rc = member_part(i, useFused ? 1 : 0))) {
       failed = i;
       break;
     }
   }
-  for (int k = 0; k < nl; ++k) {
-    cudaEventRecord(b->joins[k], b->laneStreams[k]);
-    cudaStreamWaitEvent(b->origin, b->joins[k], 0);
+  if (useFused && !rc) {
+    // every member's plan and reset done: the forcing iterations of all of
+    // them, two launches each, then their images and CloudEvolutionMS
+    join_lanes(b->joins);
+    const int Ns = b->cases[0]->c.p.Ns;
+    for (int it = 0; it < Ns; ++it) launch_forcing_batch(b->fb, it == 0 ? 3 : 0, b->origin);
+    b->launchesPerStep[0] += 2ll * Ns;
+    cudaEventRecord(b->fork2, b->origin);
+    for (int k = 0; k < nl; ++k) cudaStreamWaitEvent(b->laneStreams[k], b->fork2, 0);
+    for (int i : order) {
+      if ((rc = member_part(i, 2))) {
+        failed = i;
+        break;
+      }
+    }
+    join_lanes(b->joins2);
+  } else {
+    join_lanes(b->joins);
   }
+  b->capturedFused = useFused;
   cudaGraph_t g = nullptr;
   e = cudaStreamEndCapture(b->origin, &g);
   if (rc || e != cudaSuccess) {
@@ -430,8 +498,11 @@ int ibmdem_batch_destroy(ibmdem_batch* b) {
   drop_graph(b);
   for (cudaStream_t s : b->laneStreams) cudaStreamDestroy(s);
   for (cudaEvent_t e : b->joins) cudaEventDestroy(e);
+  for (cudaEvent_t e : b->joins2) cudaEventDestroy(e);
   for (cudaEvent_t e : b->inputs) cudaEventDestroy(e);
   if (b->fork) cudaEventDestroy(b->fork);
+  if (b->fork2) cudaEventDestroy(b->fork2);
+  if (b->dDesc) cudaFree(b->dDesc);
   if (b->done) cudaEventDestroy(b->done);
   if (b->origin) cudaStreamDestroy(b->origin);
   delete b;
@@ -457,6 +528,24 @@ int ibmdem_batch_set_lanes(ibmdem_batch* b, int32_t lanes) {
     b->lanes = lanes;
     drop_graph(b);
   }
+  return IBMDEM_OK;
+}
+
+int ibmdem_batch_set_fused(ibmdem_batch* b, int32_t fused, int32_t interp_block) {
+  if (!b || (fused != 0 && fused != 1) || (interp_block != 128 && interp_block != 256)) return IBMDEM_EINVAL;
+  if (fused != b->fused || interp_block != b->interpBlock) {
+    b->fused = fused;
+    b->interpBlock = interp_block;
+    drop_graph(b);
+  }
+  return IBMDEM_OK;
+}
+
+int ibmdem_batch_get_config(const ibmdem_batch* b, int32_t* lanes, int32_t* fused, int32_t* interp_block) {
+  if (!b) return IBMDEM_EINVAL;
+  if (lanes) *lanes = b->lanes;
+  if (fused) *fused = b->fused;
+  if (interp_block) *interp_block = b->interpBlock;
   return IBMDEM_OK;
 }
 
@@ -492,39 +581,66 @@ int ibmdem_batch_autotune(ibmdem_batch* b, int32_t trial_steps, int32_t* lanes_o
     return IBMDEM_OK;
   }
   cudaSetDevice(b->device);
-  std::vector<int> cands;
-  for (int k : {n, 128, 64, 32, 16, 8, 4, 2, 1})
-    if (k <= n && std::find(cands.begin(), cands.end(), k) == cands.end()) cands.push_back(k);
   cudaEvent_t t0 = nullptr, t1 = nullptr;
   cudaEventCreate(&t0);
   cudaEventCreate(&t1);
-  int best = n;
-  float bestMs = 0.f;
-  int rc = IBMDEM_OK;
-  for (int k : cands) {
-    b->lanes = k;
+  // one trial: capture the configuration, a warm-up step, then trial_steps timed
+  auto trial = [&](int lanes, int fused, int block, float* ms) {
+    b->lanes = lanes;
+    b->fused = fused;
+    b->interpBlock = block;
     drop_graph(b);
-    rc = launch_batch(b, 1);  // capture + warm-up
-    if (rc) break;
+    int rc = launch_batch(b, 1);
+    if (rc) return rc;
     cudaEventRecord(t0, b->origin);
     rc = launch_batch(b, trial_steps);
-    if (rc) break;
+    if (rc) return rc;
     cudaEventRecord(t1, b->origin);
-    if (cudaEventSynchronize(t1) != cudaSuccess) {
-      rc = batch_error(b, IBMDEM_ECUDA, "autotune trial failed");
-      break;
-    }
+    if (cudaEventSynchronize(t1) != cudaSuccess) return batch_error(b, IBMDEM_ECUDA, "autotune trial failed");
+    cudaEventElapsedTime(ms, t0, t1);
+    return IBMDEM_OK;
+  };
+  // first the chain count with each member's own forcing launches, then the
+  // shared forcing launches (both interpolation block sizes) around the best
+  // chain counts
+  std::vector<int> cands;
+  for (int k : {n, 128, 64, 32, 16, 8, 4, 2, 1})
+    if (k <= n && std::find(cands.begin(), cands.end(), k) == cands.end()) cands.push_back(k);
+  int best = n, bestFused = 0, bestBlock = kBlock;
+  float bestMs = 0.f;
+  bool any = false;
+  int rc = IBMDEM_OK;
+  std::vector<std::pair<float, int>> own;
+  for (int k : cands) {
     float ms = 0.f;
-    cudaEventElapsedTime(&ms, t0, t1);
-    if (k == cands.front() || ms < bestMs) {
+    if ((rc = trial(k, 0, kBlock, &ms))) break;
+    own.push_back({ms, k});
+    if (!any || ms < bestMs) {
       bestMs = ms;
       best = k;
+      any = true;
     }
+  }
+  if (!rc) {
+    std::sort(own.begin(), own.end());
+    for (size_t q = 0; q < own.size() && q < 2 && !rc; ++q)
+      for (int block : {kBlock, 128}) {
+        float ms = 0.f;
+        if ((rc = trial(own[q].second, 1, block, &ms))) break;
+        if (ms < bestMs) {
+          bestMs = ms;
+          best = own[q].second;
+          bestFused = 1;
+          bestBlock = block;
+        }
+      }
   }
   cudaEventDestroy(t0);
   cudaEventDestroy(t1);
   if (rc) return rc;
   b->lanes = best;
+  b->fused = bestFused;
+  b->interpBlock = bestBlock;
   drop_graph(b);
   if (lanes_out) *lanes_out = best;
   return IBMDEM_OK;

@@ -750,12 +750,9 @@ __global__ void k_mdf_stale(Geom g, const Counters* cnt, Fields fl, const uint32
 // bit 1, the field is read from the frozen copy (the first iteration of a
 // frozen-fluid step, before any spread of this step wrote the working field).
 template <int UNIT_H>
-__global__ void __launch_bounds__(kBlock) k_interp(Recs R, Geom g, const Counters* cnt, const double* __restrict__ W,
-                                                   const int4* __restrict__ win, Fields fl, double* fv, int comp0,
-                                                   int first) {
-  int m = blockIdx.x * blockDim.x + threadIdx.x;
-  if (m >= cnt->npLocal) return;
-  const int comp = comp0 + blockIdx.y;
+__device__ __forceinline__ void interp_one(const Recs& R, const Geom& g, const double* __restrict__ W,
+                                           const int4* __restrict__ win, const Fields& fl, double* fv, int comp,
+                                           int first, int m) {
   const int cap = R.cap;
   const double* __restrict__ F = (first & 2) ? fl.U0(comp) : fl.U(comp);
   int sx, sy, sz;
@@ -797,6 +794,15 @@ __global__ void __launch_bounds__(kBlock) k_interp(Recs R, Geom g, const Counter
   fv[(size_t)comp * cap + m] = fd * R.D(D_VOL, m);
 }
 
+template <int UNIT_H>
+__global__ void __launch_bounds__(kBlock) k_interp(Recs R, Geom g, const Counters* cnt, const double* __restrict__ W,
+                                                   const int4* __restrict__ win, Fields fl, double* fv, int comp0,
+                                                   int first) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= cnt->npLocal) return;
+  interp_one<UNIT_H>(R, g, W, win, fl, fv, comp0 + blockIdx.y, first, m);
+}
+
 // UpdateMomentumSourceTerm (ZJS_VOLUMEFRACTION_DEM.F90:38-67) per touched node;
 // MODE 0: fused with VelocityPostGuess + halo refill, 1: spread only.
 // 2560 staged products per block (20 KB) let 8 blocks share an SM (32 registers,
@@ -816,26 +822,23 @@ constexpr int kLenBins = 64;
 // keeps fx and fxOld for a separate VelocityPostGuess (MODE 1).  (Folding the
 // shortest and the longest node in one thread idles fewer FP64 lanes but
 // leaves half the warps without work in the fold, and measured slower.)
-template <int MODE, bool WALLS, int FIRST = 0>
-__global__ void __launch_bounds__(kBlock, 8) k_spread(Geom g, const Counters* cnt, const int* __restrict__ runStart,
-                                                   const int* __restrict__ runCnt,
-                                                   const uint32_t* __restrict__ runKey,
-                                                   const uint32_t* __restrict__ planRoot,
-                                                   const double* __restrict__ planW, const double* __restrict__ fv,
-                                                   int cap, Fields fl, double* fCur, double* fPrev, int onlyComp) {
-  // prod: the staged products; a node's sum replaces its first product (a node
-  // without products keeps 0), and without staging prod[t] holds node t's sum
-  extern __shared__ double prod[];
-  __shared__ int bins[kLenBins];
-  __shared__ int order[kBlock];
-  __shared__ int sStart[kBlock + 1];  // the block's runs are contiguous: run t spans sStart[t]..sStart[t+1]
+// The chunks of 256 runs of block `blk` among `nBlk` blocks; the shared-memory
+// buffers come from the kernel (prod: kSpreadBuf doubles, bins, order and
+// sStart as in k_spread).
+template <int MODE, bool WALLS, int FIRST>
+__device__ __forceinline__ void spread_chunks(const Geom& g, const Counters* cnt, const int* __restrict__ runStart,
+                                              const int* __restrict__ runCnt, const uint32_t* __restrict__ runKey,
+                                              const uint32_t* __restrict__ planRoot,
+                                              const double* __restrict__ planW, const double* __restrict__ fv,
+                                              int cap, const Fields& fl, double* fCur, double* fPrev, int onlyComp,
+                                              int blk, int nBlk, double* prod, int* bins, int* order, int* sStart) {
   const int nRuns = cnt->nRuns;  // run counts are ints (Counters)
   // one component's runs [rs, re) (onlyComp >= 0) or all of them; a block
   // always stages its whole 256-run range (contiguous in the plan) but writes
   // only its own component's nodes
   const int rs = onlyComp < 0 ? 0 : cnt->compStart[onlyComp];
   const int re = onlyComp < 0 ? nRuns : cnt->compStart[onlyComp + 1];
-  for (int r0 = (rs / kBlock + blockIdx.x) * kBlock; r0 < re; r0 += gridDim.x * kBlock) {
+  for (int r0 = (rs / kBlock + blk) * kBlock; r0 < re; r0 += nBlk * kBlock) {
     const int nHere = min(kBlock, nRuns - r0);
     // this thread's own node: everything its epilogue needs, loaded up front
     const int myR = r0 + threadIdx.x;
@@ -935,8 +938,110 @@ __global__ void __launch_bounds__(kBlock, 8) k_spread(Geom g, const Counters* cn
     __syncthreads();
   }
 }
+
+template <int MODE, bool WALLS, int FIRST = 0>
+__global__ void __launch_bounds__(kBlock, 8) k_spread(Geom g, const Counters* cnt, const int* __restrict__ runStart,
+                                                   const int* __restrict__ runCnt,
+                                                   const uint32_t* __restrict__ runKey,
+                                                   const uint32_t* __restrict__ planRoot,
+                                                   const double* __restrict__ planW, const double* __restrict__ fv,
+                                                   int cap, Fields fl, double* fCur, double* fPrev, int onlyComp) {
+  // prod: the staged products; a node's sum replaces its first product (a node
+  // without products keeps 0), and without staging prod[t] holds node t's sum
+  extern __shared__ double prod[];
+  __shared__ int bins[kLenBins];
+  __shared__ int order[kBlock];
+  __shared__ int sStart[kBlock + 1];  // the block's runs are contiguous: run t spans sStart[t]..sStart[t+1]
+  spread_chunks<MODE, WALLS, FIRST>(g, cnt, runStart, runCnt, runKey, planRoot, planW, fv, cap, fl, fCur, fPrev,
+                                    onlyComp, blockIdx.x, gridDim.x, prod, bins, order, sStart);
+}
 constexpr size_t kSpreadSmem = sizeof(double) * kSpreadBuf;
 
+
+// ---- the forcing loop of many cases in shared launches ----------------------
+// A batch of independent cases runs each forcing iteration as two launches for
+// all of its members (interpolation, then spreading with the post-guess)
+// instead of two per member.  Every block finds its member in a table of block
+// owners that follows the members' descriptors, copies the member's
+// descriptor into shared memory, and runs the same per-block code as the
+// per-case kernels on that member's state, so each member's results are the
+// ones it gets alone.
+struct MemberDesc {
+  Geom g;
+  Recs R;
+  Fields fl;
+  const Counters* cnt;
+  const double* W;
+  const int4* win;
+  double* fv;
+  const int* runStart;
+  const int* runCnt;
+  const uint32_t* runKey;
+  const uint32_t* planRoot;
+  const double* planW;
+  double* fCur;
+  double* fPrev;
+  int interpBlocks, interpStart;  // blocks per velocity component; first block (3 * interpBlocks per member)
+  int spreadBlocks, spreadStart;
+};
+
+// The table after the descriptors: the member of every interpolation block,
+// then of every spread block (one load instead of a search per block).
+__device__ inline int member_of(const MemberDesc* __restrict__ D, int n, int b, bool spread, int interpTotal) {
+  const int* __restrict__ owner = reinterpret_cast<const int*>(D + n);
+  return owner[spread ? interpTotal + b : b];
+}
+
+// copy member `mi`'s descriptor into shared memory (the whole block takes part)
+__device__ inline void load_member(const MemberDesc* __restrict__ D, int mi, unsigned char* raw) {
+  const int* src = reinterpret_cast<const int*>(D + mi);
+  int* dst = reinterpret_cast<int*>(raw);
+  for (int i = threadIdx.x; i < (int)(sizeof(MemberDesc) / sizeof(int)); i += blockDim.x) dst[i] = src[i];
+}
+
+template <int BS>
+__global__ void __launch_bounds__(BS) k_interp_batch(const MemberDesc* __restrict__ D, int n, int first) {
+  __shared__ __align__(16) unsigned char raw[sizeof(MemberDesc)];
+  __shared__ int sMember;
+  if (threadIdx.x == 0) sMember = member_of(D, n, blockIdx.x, false, 0);
+  __syncthreads();
+  load_member(D, sMember, raw);
+  __syncthreads();
+  const MemberDesc& d = *reinterpret_cast<const MemberDesc*>(raw);
+  const int local = blockIdx.x - d.interpStart;
+  const int comp = local / d.interpBlocks;
+  const int m = (local - comp * d.interpBlocks) * BS + threadIdx.x;
+  if (comp > 2 || m >= d.cnt->npLocal) return;
+  if (d.g.unit_h)
+    interp_one<1>(d.R, d.g, d.W, d.win, d.fl, d.fv, comp, first, m);
+  else
+    interp_one<0>(d.R, d.g, d.W, d.win, d.fl, d.fv, comp, first, m);
+}
+
+// ANYWALL: some member has solid walls (their halo writes take the general
+// path); a batch of periodic cases gets the periodic path only
+template <int FIRST, bool ANYWALL>
+__global__ void __launch_bounds__(kBlock, 8) k_spread_batch(const MemberDesc* __restrict__ D, int n,
+                                                           int interpTotal) {
+  extern __shared__ double prod[];
+  __shared__ int bins[kLenBins];
+  __shared__ int order[kBlock];
+  __shared__ int sStart[kBlock + 1];
+  __shared__ __align__(16) unsigned char raw[sizeof(MemberDesc)];
+  __shared__ int sMember;
+  if (threadIdx.x == 0) sMember = member_of(D, n, blockIdx.x, true, interpTotal);
+  __syncthreads();
+  load_member(D, sMember, raw);
+  __syncthreads();
+  const MemberDesc& d = *reinterpret_cast<const MemberDesc*>(raw);
+  const int lb = blockIdx.x - d.spreadStart;
+  if (ANYWALL && d.g.anyWall)
+    spread_chunks<0, true, FIRST>(d.g, d.cnt, d.runStart, d.runCnt, d.runKey, d.planRoot, d.planW, d.fv, d.R.cap,
+                                  d.fl, d.fCur, d.fPrev, -1, lb, d.spreadBlocks, prod, bins, order, sStart);
+  else
+    spread_chunks<0, false, FIRST>(d.g, d.cnt, d.runStart, d.runCnt, d.runKey, d.planRoot, d.planW, d.fv, d.R.cap,
+                                   d.fl, d.fCur, d.fPrev, -1, lb, d.spreadBlocks, prod, bins, order, sStart);
+}
 
 // VelocityPostGuess (fluid.F90:135-153) + halo refill, per touched node
 template <bool WALLS>
@@ -1071,6 +1176,79 @@ void launch_mdf_stale(Ctx& c, bool frozen) {
                                                    reinterpret_cast<const unsigned*>(c.touch), frozen ? 1 : 0);
   c.launches++;
   c.spreadValid = true;
+}
+
+// blocks of a member: per velocity component for the interpolation, in all
+// for the spread (the per-case launches' grids)
+static int interp_blocks_of(const Ctx& c, int interpBlock) { return nblocks(std::max(c.capLocal, 1), interpBlock); }
+
+size_t forcing_desc_bytes(const std::vector<Ctx*>& members, int interpBlock) {
+  size_t blocks = 0;
+  for (const Ctx* c : members) blocks += 3 * (size_t)interp_blocks_of(*c, interpBlock) + run_blocks(*c);
+  return sizeof(MemberDesc) * std::max<size_t>(members.size(), 1) + sizeof(int) * blocks;
+}
+
+cudaError_t forcing_desc_upload(const std::vector<Ctx*>& members, void* dDesc, int interpBlock, cudaStream_t s,
+                                ForcingBatch* fb) {
+  const size_t n = members.size();
+  std::vector<MemberDesc> h(n);
+  int ib = 0, sb = 0;
+  for (size_t q = 0; q < n; ++q) {
+    Ctx& c = *members[q];
+    MemberDesc& d = h[q];
+    d.g = c.g;
+    d.R = c.rec();
+    d.fl = fields_of(c);
+    d.cnt = c.dCnt;
+    d.W = c.W;
+    d.win = c.win;
+    d.fv = c.fv;
+    d.runStart = c.runStart;
+    d.runCnt = c.runCnt;
+    d.runKey = c.runKey;
+    d.planRoot = c.planRoot;
+    d.planW = c.planW;
+    d.fCur = c.fCur;
+    d.fPrev = c.fPrev;
+    d.interpBlocks = interp_blocks_of(c, interpBlock);
+    d.interpStart = ib;
+    ib += 3 * d.interpBlocks;
+    d.spreadBlocks = run_blocks(c);
+    d.spreadStart = sb;
+    sb += d.spreadBlocks;
+  }
+  std::vector<int> owner((size_t)ib + sb);
+  for (size_t q = 0; q < n; ++q) {
+    std::fill(owner.begin() + h[q].interpStart, owner.begin() + h[q].interpStart + 3 * h[q].interpBlocks, (int)q);
+    std::fill(owner.begin() + ib + h[q].spreadStart,
+              owner.begin() + ib + h[q].spreadStart + h[q].spreadBlocks, (int)q);
+  }
+  fb->desc = dDesc;
+  fb->n = (int)n;
+  fb->interpBlocksTotal = ib;
+  fb->spreadBlocksTotal = sb;
+  fb->interpBlock = interpBlock;
+  fb->anyWall = false;
+  for (Ctx* c : members) fb->anyWall = fb->anyWall || c->g.anyWall;
+  char* base = static_cast<char*>(dDesc);
+  cudaError_t e = cudaMemcpyAsync(base, h.data(), sizeof(MemberDesc) * n, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess && !owner.empty())
+    e = cudaMemcpyAsync(base + sizeof(MemberDesc) * n, owner.data(), sizeof(int) * owner.size(),
+                        cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  return e;
+}
+
+void launch_forcing_batch(const ForcingBatch& fb, int first, cudaStream_t s) {
+  const MemberDesc* D = static_cast<const MemberDesc*>(fb.desc);
+  if (fb.interpBlock == 128)
+    k_interp_batch<128><<<fb.interpBlocksTotal, 128, 0, s>>>(D, fb.n, first);
+  else
+    k_interp_batch<kBlock><<<fb.interpBlocksTotal, kBlock, 0, s>>>(D, fb.n, first);
+  auto k = first == 3 ? (fb.anyWall ? k_spread_batch<3, true> : k_spread_batch<3, false>)
+                      : (fb.anyWall ? k_spread_batch<0, true> : k_spread_batch<0, false>);
+  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSpreadSmem);
+  k<<<fb.spreadBlocksTotal, kBlock, kSpreadSmem, s>>>(D, fb.n, fb.interpBlocksTotal);
 }
 
 void launch_post_guess(Ctx& c) {

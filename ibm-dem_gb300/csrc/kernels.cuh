@@ -208,6 +208,25 @@ void launch_spread(Ctx& c, bool fused_post_guess, int comp, int first = 0);
 // only the nodes the last spread wrote and the current plan does not touch
 void launch_mdf_stale(Ctx& c, bool frozen);
 void launch_post_guess(Ctx& c);
+// The forcing loop of many frozen-fluid cases in shared launches (a batch):
+// the members' descriptor table on the device and its grids.
+struct ForcingBatch {
+  void* desc = nullptr;
+  int n = 0;
+  int interpBlocksTotal = 0, spreadBlocksTotal = 0;
+  int interpBlock = kBlock;
+  bool anyWall = false;
+};
+// Bytes of the table for these members: their descriptors and the owner of
+// every block of the two launches.
+size_t forcing_desc_bytes(const std::vector<Ctx*>& members, int interpBlock);
+// Fill the table at dDesc (forcing_desc_bytes bytes) for the members' current
+// buffers and plan sizes; synchronises s (never call it while capturing).
+cudaError_t forcing_desc_upload(const std::vector<Ctx*>& members, void* dDesc, int interpBlock, cudaStream_t s,
+                                ForcingBatch* fb);
+// One forcing iteration of every member: the interpolation for all, then the
+// spread with the post-guess; first as for launch_interp (0 or 3).
+void launch_forcing_batch(const ForcingBatch& fb, int first, cudaStream_t s);
 void record_written_nodes(Ctx& c);
 // Interpolation at n <= IBMDEM_PROBE_MAX_POINTS device points with the
 // weights in a static device array (no allocation); synchronises c.stream.
@@ -249,6 +268,13 @@ inline void wait_fields_read(ibmdem::Ctx& c, bool uploads = true) {
     c.uploadPending = false;
   }
 }
+
+// A frozen-fluid step (ibmdem_step) in two parts around its forcing loop, for
+// a batch that runs the loop of all its members in shared launches
+// (launch_forcing_batch): the plan and the reset before, the image update and
+// CloudEvolutionMS after.  Both are stream-ordered on the context's stream.
+int step_before_forcing(ibmdem_ctx* h);
+int step_after_forcing(ibmdem_ctx* h);
 
 // ibmdem_create with the context's allocations and work ordered on `stream`
 int create_on_stream(const ibmdem_params* p, int device, cudaStream_t stream, ibmdem_ctx** out);

@@ -47,7 +47,7 @@ EXPORTS = [
     "ibmdem_set_fluid_async", "ibmdem_set_fluid_params", "ibmdem_set_fluid_field", "ibmdem_get_fluid_field", "ibmdem_StoreOldVelocity",
     "ibmdem_VelocityGuess", "ibmdem_FillGhostRegionForFluid", "ibmdem_Boundary", "ibmdem_ModifyBulkVelocity",
     "ibmdem_VelocityDivergence", "ibmdem_PressureCorrection", "ibmdem_VelocityCorrection", "ibmdem_PoissonSolver",
-    "ibmdem_set_friction", "ibmdem_get_friction_history",
+    "ibmdem_set_friction", "ibmdem_get_friction_history", "ibmdem_batch_set_fused", "ibmdem_batch_get_config",
 ]
 
 SUBROUTINES = [
@@ -134,6 +134,8 @@ def load(path=LIB_PATH):
     lib.ibmdem_batch_step.argtypes = [vp, i32]
     lib.ibmdem_batch_synchronize.argtypes = [vp, P(i32)]
     lib.ibmdem_batch_autotune.argtypes = [vp, i32, P(i32)]
+    lib.ibmdem_batch_set_fused.argtypes = [vp, i32, i32]
+    lib.ibmdem_batch_get_config.argtypes = [vp, P(i32), P(i32), P(i32)]
     lib.ibmdem_server_create.argtypes = [i32, i64, i32, P(vp)]
     lib.ibmdem_server_destroy.argtypes = [vp]
     lib.ibmdem_server_last_error.restype = ctypes.c_char_p
@@ -470,6 +472,16 @@ class Batch:
 
     def set_lanes(self, lanes):
         self._chk(self.lib.ibmdem_batch_set_lanes(self.h, int(lanes)), "batch_set_lanes")
+
+    def set_fused(self, fused, interp_block=256):
+        """All members' forcing loops in shared launches (see ibmdem_batch_set_fused)."""
+        self._chk(self.lib.ibmdem_batch_set_fused(self.h, int(bool(fused)), int(interp_block)), "batch_set_fused")
+
+    def config(self):
+        """(lanes, fused, interp_block) the next step runs with."""
+        v = [ctypes.c_int32() for _ in range(3)]
+        self._chk(self.lib.ibmdem_batch_get_config(self.h, *(ctypes.byref(x) for x in v)), "batch_get_config")
+        return tuple(x.value for x in v)
 
     def step(self, n=1):
         self._chk(self.lib.ibmdem_batch_step(self.h, int(n)), "batch_step")

@@ -379,8 +379,19 @@ int ibmdem_batch_step(ibmdem_batch* b, int32_t nsteps);
 /* Waits for the batch and checks every member for device errors; the first
  * failing member's index goes to *failed_case (-1 if none). */
 int ibmdem_batch_synchronize(ibmdem_batch* b, int32_t* failed_case);
+/* The forcing loop (the interpolation and the spread of every iteration) of all
+ * members in shared launches: fused = 1 gives one interpolation launch
+ * (interp_block threads per block, 128 or 256) and one spread launch per
+ * iteration for the whole batch, instead of two per member; each member's
+ * results are the same.  Members must share Ns (else the batch keeps each
+ * member's own launches).  Default: fused = 0, interp_block = 256. */
+int ibmdem_batch_set_fused(ibmdem_batch* b, int32_t fused, int32_t interp_block);
+int ibmdem_batch_get_config(const ibmdem_batch* b, int32_t* lanes, int32_t* fused, int32_t* interp_block);
 /* Times trial_steps batch steps for several lane counts (all, 128, 64, ..., 1)
- * and keeps the fastest in *lanes_out.  The trials advance every member. */
+ * with each member's own forcing launches, then the shared forcing launches
+ * (both block sizes) on the two best lane counts, keeps the fastest
+ * configuration (ibmdem_batch_get_config) and returns its lane count in
+ * *lanes_out.  The trials advance every member. */
 int ibmdem_batch_autotune(ibmdem_batch* b, int32_t trial_steps, int32_t* lanes_out);
 
 /* A request server on one device.  Requests wait first-in first-out and are

@@ -81,13 +81,48 @@ def test_batch_matches_each_case_alone(gpu_lib, lanes):
         case.close()
 
 
+@pytest.mark.parametrize("lanes,interp_block", [(0, 256), (2, 128), (1, 256)])
+def test_batch_shared_forcing_launches_match_alone(gpu_lib, lanes, interp_block):
+    """The forcing loops of all members in shared launches (one interpolation and
+    one spread per iteration for the whole batch): each member exactly as alone,
+    periodic and walled members mixed."""
+    cs = mixed_cases()
+    cs.append(scenario.walled_case(24, 20, 28, 2, 8.0, seed=4, walls="z", n_modes=6, touching=0))
+    assert len({int(c[0]["Ns"]) for c in cs}) == 1
+    steps = 3
+    ref = [alone(c, steps) for c in cs]
+    members = [make_case(c) for c in cs]
+    b = api.Batch(members, lanes=lanes)
+    b.set_fused(True, interp_block)
+    assert b.config()[1:] == (1, interp_block)
+    b.step(1)
+    b.step(steps - 1)
+    b.synchronize()
+    for case, r in zip(members, ref):
+        assert_same(snapshot(case), r)
+    # back to each member's own launches: still the same as alone
+    b.set_fused(False)
+    b.step(1)
+    b.synchronize()
+    for case, c in zip(members, cs):
+        assert_same(snapshot(case), alone(c, steps + 1))
+    b.close()
+    for case in members:
+        case.close()
+
+
 def test_batch_autotune_and_recapture(gpu_lib):
     cs = mixed_cases()[:3]
     members = [make_case(c) for c in cs]
     b = api.Batch(members)
     lanes = b.autotune(trial_steps=1)
     assert 1 <= lanes <= len(cs)
-    n_auto = 2 * len({len(cs), 2, 1})  # each candidate: one warm-up + one trial step
+    assert b.config()[0] == lanes and b.config()[2] in (128, 256)
+    # each trial: one warm-up + one trial step; every lane count with the
+    # members' own launches, then the two best with shared launches and both
+    # interpolation block sizes
+    n_lanes = len({len(cs), 2, 1})
+    n_auto = 2 * (n_lanes + 2 * min(2, n_lanes))
     b.step(2)
     b.synchronize()
     # a member changed outside the batch is re-captured: reload case 0 and rebuild it
