@@ -41,22 +41,24 @@ def fibonacci_sphere(n):
 def rsa_centres(L, nb, d, rng, max_tries=2_000_000):
     """Random sequential addition with minimum-image centre distance > d."""
     L = np.asarray(L, dtype=np.float64)
-    out = np.empty((0, 3))
+    out = np.empty((nb, 3))
+    placed = 0
     tries = 0
     batch = 256
-    while out.shape[0] < nb:
+    while placed < nb:
         cand = rng.random((batch, 3)) * L
         for c in cand:
             tries += 1
             if tries > max_tries:
                 raise RuntimeError(f"RSA could not place {nb} spheres of diameter {d}")
-            if out.shape[0]:
-                dv = out - c
+            if placed:
+                dv = out[:placed] - c
                 dv -= L * np.round(dv / L)
                 if np.min(np.einsum("ij,ij->i", dv, dv)) <= d * d:
                     continue
-            out = np.vstack([out, c])
-            if out.shape[0] == nb:
+            out[placed] = c
+            placed += 1
+            if placed == nb:
                 break
     return out
 
@@ -82,12 +84,11 @@ def sphere_bodies(centres, d, h, rho_p, vel, n_markers=None):
     bodies = np.zeros(nb, MULTISPHERE)
     vol_p = PI32 * h / 3 / n * (12 * rad_sphere * rad_sphere + h * h)
     eye = np.eye(3).reshape(9)
-    for b in range(nb):
-        sl = slice(b * n, (b + 1) * n)
-        parts["x"][sl] = rad_sphere * tpl + centres[b]
-        parts["v"][sl] = vel[b]
-        parts["MSIdx"][sl] = b + 1
-        parts["globalIdx"][sl] = np.arange(1, n + 1)
+    # body b's markers are parcels b*n .. b*n+n-1
+    parts["x"] = ((rad_sphere * tpl)[None, :, :] + centres[:, None, :]).reshape(nb * n, 3)
+    parts["v"] = np.repeat(np.asarray(vel, dtype=np.float64).reshape(nb, 3), n, axis=0)
+    parts["MSIdx"] = np.repeat(np.arange(1, nb + 1), n)
+    parts["globalIdx"] = np.tile(np.arange(1, n + 1), nb)
     parts["radeff"] = h * 0.75
     parts["rad"] = 0.0
     parts["rho"] = rho_p
