@@ -929,8 +929,6 @@ def run_ours(args):
     counters = case.counters()
     case.step(1)
     case.synchronize()
-    case.timing(True)
-    case.phase_times(reset=True)
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
@@ -945,8 +943,16 @@ def run_ours(args):
     case.synchronize()
     ms = e0.elapsed_time(e1)
     launches = case.launches - launches0
+    # per-phase times: a second pass of the same steps with CUDA events around
+    # every phase (kept out of the timed pass above)
+    case.timing(True)
+    case.phase_times(reset=True)
+    for _ in range(args.steps):
+        case.step(1)
+    case.synchronize()
     phases = case.phase_times(reset=True)
     case.timing(False)
+    ms_phased = sum(t for t, _ in phases.values())
     ms_max = max_over_ranks(ms)
     value = world * nb * args.steps / (ms_max / 1e3)
 
@@ -1041,6 +1047,8 @@ def run_ours(args):
                                   "instr_note": "FP64 instructions the kernel issues"},
                          "kernels": rows},
             "phases": per_phase,
+            "phases_note": "a second pass of the same steps with CUDA events around every phase: "
+                           "ms_per_step_phased %.3f" % (ms_phased / args.steps),
             "e2e": {"value": e2e_val, "unit": "particle-steps/s", "h2d_bytes_per_step": 3 * fbytes,
                     "d2h_bytes_per_step": 6 * fbytes + nb * MULTISPHERE.itemsize, "steps": args.e2e_steps,
                     "path": "ibmdem_set_fluid_async(host u,v,w; each component's forcing loop starts when it "

@@ -1296,8 +1296,11 @@ int ibmdem_MultiDirectForcing(ibmdem_ctx* h) {
   return mdf(h, false);
 }
 
-int ibmdem_CloudEvolutionStepMS(ibmdem_ctx* h) {
-  CHECK_CTX();
+}  // extern "C"
+
+// CloudEvolutionStepMS whose AssembleLocalForceMS forms the sums `sums` only
+// (launch_body_sums); ibmdem_CloudEvolutionStepMS forms all of them.
+static int cloud_step(ibmdem_ctx* h, int sums) {
   Ctx& c = h->c;
   REQUIRE(c.listsBuilt && c.weightsLocal && c.weightsGhost, "lists and weights are not built");
   {
@@ -1305,7 +1308,7 @@ int ibmdem_CloudEvolutionStepMS(ibmdem_ctx* h) {
     launch_collision_force(c);
     launch_wall_force(c);
   }
-  { PhaseScope t(c, P_BODYSUM); launch_body_sums(c); }
+  { PhaseScope t(c, P_BODYSUM); launch_body_sums(c, sums); }
   { PhaseScope t(c, P_BODYMOVE); launch_evolution(c); }
   { PhaseScope t(c, P_MARKERS); launch_marker_update(c, true, true); }
   { PhaseScope t(c, P_IMAGES); launch_img_update(c); }
@@ -1321,15 +1324,32 @@ int ibmdem_CloudEvolutionStepMS(ibmdem_ctx* h) {
   return launch_status(h);
 }
 
+extern "C" {
+
+int ibmdem_CloudEvolutionStepMS(ibmdem_ctx* h) {
+  CHECK_CTX();
+  return cloud_step(h, SUMS_ALL);
+}
+
+// Each AssembleLocalForceMS of the reference forms all twelve body sums, but
+// within CloudEvolutionMS (couplesolverCylinder.F90:189-217) only some of
+// them are read before the next call overwrites them: the first call's fdrag
+// and fmom (for fhydro, fmomHydro), each sub-step's fcol and fmomCol (for
+// EvolutionMS).  The fdrag and fmom the caller sees at the end are those of
+// the last call, whose markers sit where the first call's did when there is
+// one sub-step (the sums are then the first call's, bit for bit) and have
+// moved when there are more.  So the first call forms fdrag and fmom, the
+// sub-steps fcol and fmomCol, and the last of several sub-steps all twelve.
 int ibmdem_CloudEvolutionMS(ibmdem_ctx* h) {
   CHECK_CTX();
   Ctx& c = h->c;
   REQUIRE(c.listsBuilt, "lists are not built");
   { PhaseScope t(c, P_BODYMOVE); launch_cloud_pre(c); }
-  { PhaseScope t(c, P_BODYSUM); launch_body_sums(c); }
+  { PhaseScope t(c, P_BODYSUM); launch_body_sums(c, SUMS_HYDRO); }
   { PhaseScope t(c, P_BODYMOVE); launch_cloud_post(c); }
-  for (int s = 0; s < c.p.coupleInterval; ++s) {
-    int rc = ibmdem_CloudEvolutionStepMS(h);
+  const int K = c.p.coupleInterval;
+  for (int s = 0; s < K; ++s) {
+    int rc = cloud_step(h, K > 1 && s == K - 1 ? SUMS_ALL : SUMS_COL);
     if (rc) return rc;
   }
   return launch_status(h);

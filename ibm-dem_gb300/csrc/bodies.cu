@@ -3,9 +3,9 @@
 // AssembleLocalForceMS (ZJS_MS_DEM.F90:494-519) sums, per body and in part
 // order, fdrag*vol*rhof, fcol, (x-X) x (fdrag*vol) and (x-X) x fcol.  Every
 // body's locals are listed in part order (bodyItems, built with the cell
-// lists); a warp per body forms the per-parcel terms in parallel and folds
-// each of the 12 sums sequentially in that order, so the sums are
-// bit-identical to the reference's serial loop.
+// lists); lanes of a warp form the per-parcel terms in parallel and fold each
+// of the 12 sums sequentially in that order, so the sums are bit-identical to
+// the reference's serial loop.
 // CloudEvolutionMS / EvolutionMS / ResetVelocityAndPositionLagrangianPoints /
 // AdjustParcelPosition follow couplesolverCylinder.F90:2-74,189-217 and
 // ZJS_EVOLUTION_DEM.F90:121-150 statement by statement.
@@ -21,21 +21,27 @@ namespace ibmdem {
 
 namespace {
 
-// One warp per body.  The 32 lanes evaluate the per-parcel terms of a batch of
-// 32 parcels in parallel (each term is formed exactly as in the reference);
-// lanes 0..11 then fold one sum component each over the batch in part order.
-// One warp per block: the few hundred to few thousand body pairs then spread
-// over all SMs.
+// Two bodies a warp, one per half.  Each round a half forms the per-parcel
+// terms of its body's next 16 parcels (one a lane, every term exactly as in
+// the reference) into shared memory, then lane s < NS of the half folds sum s
+// over those 16 in part order.  WHICH selects the sums: 1 = fdrag and fmom
+// (the hydrodynamic ones), 2 = fcol and fmomCol, 3 = all twelve.  (Four bodies
+// a warp, with 8 or 32 parcels a round, measured slower: the fold is a
+// dependent chain per sum.)  One warp per block: the body pairs spread over
+// all SMs.
 constexpr int kSumWarps = 1;
+constexpr int kSumBatch = 16;  // parcels per round, one per lane of a half
+template <int WHICH>
 __global__ void __launch_bounds__(kSumWarps * 32) k_body_sums(Recs R, Geom g, ibmdem_multisphere* B, int nMS,
                                                               const int* __restrict__ bodyStart,
                                                               const int* __restrict__ bodyItems) {
-  __shared__ double term[kSumWarps][32][13];
+  constexpr int NS = WHICH == 3 ? 12 : 6;  // sums per body
+  constexpr int G = kSumBatch;             // lanes per body
+  constexpr int SH = 4;                    // log2(G)
+  __shared__ double term[kSumWarps][32 / G][kSumBatch][NS + 1];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  // two bodies per warp, one per half: the ordered folds of both (12 sums
-  // each) share their FP64 instructions
-  const int half = lane >> 4, hl = lane & 15;
-  const int b = (blockIdx.x * kSumWarps + warp) * 2 + half;
+  const int grp = lane >> SH, hl = lane & (G - 1);
+  const int b = (blockIdx.x * kSumWarps + warp) * (32 / G) + grp;
   const bool hasBody = b < nMS;
   double X[3] = {0.0, 0.0, 0.0};
   int q0 = 0, q1 = 0;
@@ -45,49 +51,69 @@ __global__ void __launch_bounds__(kSumWarps * 32) k_body_sums(Recs R, Geom g, ib
     q1 = bodyStart[b + 1];
   }
   const double rhof = g.rhof;
-  double acc = 0.0;  // lane hl < 12 owns sum hl: fdrag[0..2], fcol[0..2], fmom[0..2], fmomCol[0..2]
-  const int rounds = (q1 - q0 + 15) >> 4;
-  const int maxRounds = max(rounds, __shfl_xor_sync(0xffffffffu, rounds, 16));
+  double acc = 0.0;  // lane hl < NS owns sum hl
+  int maxRounds = (q1 - q0 + kSumBatch - 1) / kSumBatch;
+#pragma unroll
+  for (int o = G; o < 32; o <<= 1) maxRounds = max(maxRounds, __shfl_xor_sync(0xffffffffu, maxRounds, o));
+  double(*T)[NS + 1] = term[warp][grp];
   for (int rd = 0; rd < maxRounds; ++rd) {
-    const int base = q0 + 16 * rd;
+    const int base = q0 + kSumBatch * rd;
     const int q = base + hl;
     if (q < q1) {
       const int m = bodyItems[q];
-      const double vol = R.D(D_VOL, m);
-      double fd[3], fc[3], rpc[3], fv[3];
+      double rpc[3];
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
-        fd[k] = R.D(D_FDRAG + k, m);
-        fc[k] = R.D(D_FCOL + k, m);
         const double x = R.D(D_X + k, m);
         rpc[k] = x - body_ref(g, k, x, X[k]);
-        fv[k] = fd[k] * vol;
       }
-      double* t = term[warp][lane];
+      double* t = T[hl];
+      // terms in output order: WHICH 3 is fdrag, fcol, fmom, fmomCol; WHICH 1
+      // fdrag, fmom; WHICH 2 fcol, fmomCol
+      if (WHICH & 1) {
+        const double vol = R.D(D_VOL, m);
+        double fd[3], fv[3];
 #pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        t[k] = fd[k] * vol * rhof;
-        t[3 + k] = fc[k];
+        for (int k = 0; k < 3; ++k) {
+          fd[k] = R.D(D_FDRAG + k, m);
+          fv[k] = fd[k] * vol;
+          t[k] = fd[k] * vol * rhof;
+        }
+        // CrossMultiplication (ZJS_AUXILIARY_DEM.F90:20-30)
+        double* tm = t + (WHICH == 3 ? 6 : 3);
+        tm[0] = rpc[1] * fv[2] - rpc[2] * fv[1];
+        tm[1] = -rpc[0] * fv[2] + rpc[2] * fv[0];
+        tm[2] = rpc[0] * fv[1] - rpc[1] * fv[0];
       }
-      // CrossMultiplication (ZJS_AUXILIARY_DEM.F90:20-30)
-      t[6] = rpc[1] * fv[2] - rpc[2] * fv[1];
-      t[7] = -rpc[0] * fv[2] + rpc[2] * fv[0];
-      t[8] = rpc[0] * fv[1] - rpc[1] * fv[0];
-      t[9] = rpc[1] * fc[2] - rpc[2] * fc[1];
-      t[10] = -rpc[0] * fc[2] + rpc[2] * fc[0];
-      t[11] = rpc[0] * fc[1] - rpc[1] * fc[0];
+      if (WHICH & 2) {
+        double fc[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) fc[k] = R.D(D_FCOL + k, m);
+        double* tc = t + (WHICH == 3 ? 3 : 0);
+        double* tcm = t + (WHICH == 3 ? 9 : 3);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) tc[k] = fc[k];
+        tcm[0] = rpc[1] * fc[2] - rpc[2] * fc[1];
+        tcm[1] = -rpc[0] * fc[2] + rpc[2] * fc[0];
+        tcm[2] = rpc[0] * fc[1] - rpc[1] * fc[0];
+      }
     }
     __syncwarp();
-    const int n = min(16, q1 - base);
-    if (hl < 12)
-      for (int j = 0; j < n; ++j) acc = acc + term[warp][16 * half + j][hl];
+    const int n = min(kSumBatch, q1 - base);
+    if (hl < NS)
+      for (int j = 0; j < n; ++j) acc = acc + T[j][hl];
     __syncwarp();
   }
-  if (!hasBody) return;
-  if (hl < 3) B[b].fdrag[hl] = acc;
-  else if (hl < 6) B[b].fcol[hl - 3] = acc;
-  else if (hl < 9) B[b].fmom[hl - 6] = acc;
-  else if (hl < 12) B[b].fmomCol[hl - 9] = acc;
+  if (!hasBody || hl >= NS) return;
+  const int which = hl / 3, k = hl - 3 * which;
+  double* out;
+  if (WHICH == 3)
+    out = which == 0 ? B[b].fdrag : which == 1 ? B[b].fcol : which == 2 ? B[b].fmom : B[b].fmomCol;
+  else if (WHICH == 1)
+    out = which == 0 ? B[b].fdrag : B[b].fmom;
+  else
+    out = which == 0 ? B[b].fcol : B[b].fmomCol;
+  out[k] = acc;
 }
 
 // CloudEvolutionMS before AssembleForceMS (couplesolverCylinder.F90:194-204)
@@ -217,10 +243,13 @@ __global__ void k_marker_update(Recs R, Geom g, const Counters* cnt, const ibmde
 
 }  // namespace
 
-void launch_body_sums(Ctx& c) {
+void launch_body_sums(Ctx& c, int which) {
   if (c.nMS <= 0) return;
-  k_body_sums<<<nblocks((c.nMS + 1) / 2, kSumWarps), kSumWarps * 32, 0, c.stream>>>(c.rec(), c.g, c.dBodies, c.nMS,
-                                                                                     c.bodyStart, c.bodyItems);
+  const int perWarp = 2;
+  auto k = which == SUMS_ALL ? k_body_sums<3> : which == SUMS_HYDRO ? k_body_sums<1> : k_body_sums<2>;
+  k<<<nblocks((c.nMS + perWarp - 1) / perWarp, kSumWarps), kSumWarps * 32, 0, c.stream>>>(c.rec(), c.g, c.dBodies,
+                                                                                         c.nMS, c.bodyStart,
+                                                                                         c.bodyItems);
   c.launches++;
 }
 

@@ -242,7 +242,10 @@ void poisson_release(Ctx& c);
 int fluid_update_join(Ctx& c);
 void fluid_update_release(Ctx& c);
 // bodies.cu
-void launch_body_sums(Ctx& c);
+// AssembleLocalForceMS: all twelve sums, or only the hydrodynamic (fdrag,
+// fmom) or only the collision ones (fcol, fmomCol)
+enum { SUMS_HYDRO = 1, SUMS_COL = 2, SUMS_ALL = 3 };
+void launch_body_sums(Ctx& c, int which = SUMS_ALL);
 void launch_evolution(Ctx& c);
 void launch_cloud_pre(Ctx& c);
 void launch_cloud_post(Ctx& c);
