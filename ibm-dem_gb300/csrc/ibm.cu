@@ -810,7 +810,8 @@ __global__ void __launch_bounds__(kBlock) k_interp(Recs R, Geom g, const Counter
 // memory split and 60 KB of L1, which the kernels that run beside it in a batch
 // of cases rely on); a block whose range holds more (markers far denser than the
 // usual spacing) folds from global memory instead.
-constexpr int kSpreadBuf = 2560;  // products per block held in shared memory
+constexpr int kSpreadBlock = kBlock;  // touched nodes (threads) per spread block: one plan-fill block
+constexpr int kSpreadBuf = 10 * kSpreadBlock;  // products per block held in shared memory
 constexpr int kStageDepth = 4;    // plan loads in flight per thread while staging
 constexpr int kLenBins = 64;
 // A block takes 256 consecutive touched nodes (one contiguous plan range).
@@ -838,8 +839,8 @@ __device__ __forceinline__ void spread_chunks(const Geom& g, const Counters* cnt
   // only its own component's nodes
   const int rs = onlyComp < 0 ? 0 : cnt->compStart[onlyComp];
   const int re = onlyComp < 0 ? nRuns : cnt->compStart[onlyComp + 1];
-  for (int r0 = (rs / kBlock + blk) * kBlock; r0 < re; r0 += nBlk * kBlock) {
-    const int nHere = min(kBlock, nRuns - r0);
+  for (int r0 = (rs / kSpreadBlock + blk) * kSpreadBlock; r0 < re; r0 += nBlk * kSpreadBlock) {
+    const int nHere = min(kSpreadBlock, nRuns - r0);
     // this thread's own node: everything its epilogue needs, loaded up front
     const int myR = r0 + threadIdx.x;
     const bool has = (int)threadIdx.x < nHere;
@@ -865,22 +866,22 @@ __device__ __forceinline__ void spread_chunks(const Geom& g, const Counters* cnt
     const int total = sStart[nHere] - base;
     const bool staged = total <= kSpreadBuf;
     if (staged)
-      for (int q0 = threadIdx.x; q0 < total; q0 += kStageDepth * kBlock) {
+      for (int q0 = threadIdx.x; q0 < total; q0 += kStageDepth * kSpreadBlock) {
         // kStageDepth independent plan loads and gathers in flight per thread
         uint32_t rc[kStageDepth];
         double w[kStageDepth], a[kStageDepth];
 #pragma unroll
         for (int u = 0; u < kStageDepth; ++u) {
-          const int q = q0 + u * kBlock;
+          const int q = q0 + u * kSpreadBlock;
           rc[u] = q < total ? planRoot[base + q] : 0u;
           w[u] = q < total ? planW[base + q] : 0.0;
         }
 #pragma unroll
         for (int u = 0; u < kStageDepth; ++u)
-          a[u] = q0 + u * kBlock < total ? fv[(size_t)(rc[u] >> 30) * cap + (rc[u] & 0x3fffffffu)] : 0.0;
+          a[u] = q0 + u * kSpreadBlock < total ? fv[(size_t)(rc[u] >> 30) * cap + (rc[u] & 0x3fffffffu)] : 0.0;
 #pragma unroll
         for (int u = 0; u < kStageDepth; ++u)
-          if (q0 + u * kBlock < total) prod[q0 + u * kBlock] = a[u] * w[u];
+          if (q0 + u * kSpreadBlock < total) prod[q0 + u * kSpreadBlock] = a[u] * w[u];
       }
     const int bin = min(myLen, kLenBins - 1);
     if (has) atomicAdd(&bins[bin], 1);
@@ -940,7 +941,7 @@ __device__ __forceinline__ void spread_chunks(const Geom& g, const Counters* cnt
 }
 
 template <int MODE, bool WALLS, int FIRST = 0>
-__global__ void __launch_bounds__(kBlock, 8) k_spread(Geom g, const Counters* cnt, const int* __restrict__ runStart,
+__global__ void __launch_bounds__(kSpreadBlock, 2048 / kSpreadBlock) k_spread(Geom g, const Counters* cnt, const int* __restrict__ runStart,
                                                    const int* __restrict__ runCnt,
                                                    const uint32_t* __restrict__ runKey,
                                                    const uint32_t* __restrict__ planRoot,
@@ -950,8 +951,8 @@ __global__ void __launch_bounds__(kBlock, 8) k_spread(Geom g, const Counters* cn
   // without products keeps 0), and without staging prod[t] holds node t's sum
   extern __shared__ double prod[];
   __shared__ int bins[kLenBins];
-  __shared__ int order[kBlock];
-  __shared__ int sStart[kBlock + 1];  // the block's runs are contiguous: run t spans sStart[t]..sStart[t+1]
+  __shared__ int order[kSpreadBlock];
+  __shared__ int sStart[kSpreadBlock + 1];  // the block's runs are contiguous: run t spans sStart[t]..sStart[t+1]
   spread_chunks<MODE, WALLS, FIRST>(g, cnt, runStart, runCnt, runKey, planRoot, planW, fv, cap, fl, fCur, fPrev,
                                     onlyComp, blockIdx.x, gridDim.x, prod, bins, order, sStart);
 }
@@ -1021,12 +1022,12 @@ __global__ void __launch_bounds__(BS) k_interp_batch(const MemberDesc* __restric
 // ANYWALL: some member has solid walls (their halo writes take the general
 // path); a batch of periodic cases gets the periodic path only
 template <int FIRST, bool ANYWALL>
-__global__ void __launch_bounds__(kBlock, 8) k_spread_batch(const MemberDesc* __restrict__ D, int n,
-                                                           int interpTotal) {
+__global__ void __launch_bounds__(kSpreadBlock, 2048 / kSpreadBlock) k_spread_batch(const MemberDesc* __restrict__ D,
+                                                                                   int n, int interpTotal) {
   extern __shared__ double prod[];
   __shared__ int bins[kLenBins];
-  __shared__ int order[kBlock];
-  __shared__ int sStart[kBlock + 1];
+  __shared__ int order[kSpreadBlock];
+  __shared__ int sStart[kSpreadBlock + 1];
   __shared__ __align__(16) unsigned char raw[sizeof(MemberDesc)];
   __shared__ int sMember;
   if (threadIdx.x == 0) sMember = member_of(D, n, blockIdx.x, true, interpTotal);
@@ -1104,9 +1105,9 @@ long long count_touched_nodes(Ctx& c) {
 // One batch per block, rather than a resident grid looping over batches, lets
 // blocks start as others finish: their load and FP64 phases interleave and no
 // block's run of heavy batches holds up the end of the launch.
-static int run_blocks(const Ctx& c) {
+static int run_blocks(const Ctx& c, int per = kBlock) {
   const long long n = c.runsSeen > 0 ? std::min(c.capRuns, c.runsSeen + c.runsSeen / 8 + kBlock) : c.capRuns;
-  return std::max(nblocks(n), 1);
+  return std::max(nblocks(n, per), 1);
 }
 
 void build_spread_plan(Ctx& c) {
@@ -1164,8 +1165,9 @@ void launch_spread(Ctx& c, bool fused_post_guess, int comp, int first) {
     k = w ? k_spread<0, true> : k_spread<0, false>;
   cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSpreadSmem);
   // one component: about a third of the runs, plus the block across its start
-  const int grid = comp < 0 ? run_blocks(c) : std::max(1, (run_blocks(c) + 2) / 3 + 1);
-  k<<<grid, kBlock, kSpreadSmem, c.stream>>>(c.g, c.dCnt, c.runStart, c.runCnt, c.runKey, c.planRoot, c.planW, c.fv,
+  const int nb = run_blocks(c, kSpreadBlock);
+  const int grid = comp < 0 ? nb : std::max(1, (nb + 2) / 3 + 1);
+  k<<<grid, kSpreadBlock, kSpreadSmem, c.stream>>>(c.g, c.dCnt, c.runStart, c.runCnt, c.runKey, c.planRoot, c.planW, c.fv,
                                              c.cap, fields_of(c), c.fCur, c.fPrev, comp);
   c.launches++;
 }
@@ -1184,7 +1186,7 @@ static int interp_blocks_of(const Ctx& c, int interpBlock) { return nblocks(std:
 
 size_t forcing_desc_bytes(const std::vector<Ctx*>& members, int interpBlock) {
   size_t blocks = 0;
-  for (const Ctx* c : members) blocks += 3 * (size_t)interp_blocks_of(*c, interpBlock) + run_blocks(*c);
+  for (const Ctx* c : members) blocks += 3 * (size_t)interp_blocks_of(*c, interpBlock) + run_blocks(*c, kSpreadBlock);
   return sizeof(MemberDesc) * std::max<size_t>(members.size(), 1) + sizeof(int) * blocks;
 }
 
@@ -1213,7 +1215,7 @@ cudaError_t forcing_desc_upload(const std::vector<Ctx*>& members, void* dDesc, i
     d.interpBlocks = interp_blocks_of(c, interpBlock);
     d.interpStart = ib;
     ib += 3 * d.interpBlocks;
-    d.spreadBlocks = run_blocks(c);
+    d.spreadBlocks = run_blocks(c, kSpreadBlock);
     d.spreadStart = sb;
     sb += d.spreadBlocks;
   }
@@ -1248,7 +1250,7 @@ void launch_forcing_batch(const ForcingBatch& fb, int first, cudaStream_t s) {
   auto k = first == 3 ? (fb.anyWall ? k_spread_batch<3, true> : k_spread_batch<3, false>)
                       : (fb.anyWall ? k_spread_batch<0, true> : k_spread_batch<0, false>);
   cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSpreadSmem);
-  k<<<fb.spreadBlocksTotal, kBlock, kSpreadSmem, s>>>(D, fb.n, fb.interpBlocksTotal);
+  k<<<fb.spreadBlocksTotal, kSpreadBlock, kSpreadSmem, s>>>(D, fb.n, fb.interpBlocksTotal);
 }
 
 void launch_post_guess(Ctx& c) {
