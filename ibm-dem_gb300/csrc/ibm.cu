@@ -71,13 +71,40 @@ __device__ inline double zero_minus(double t) {
   return __longlong_as_double(b == 0 ? 0ll : b ^ (long long)0x8000000000000000ull);
 }
 
-// one axis of DeltaFunction3D (interpolation.F90:7-30)
+// one axis of DeltaFunction3D (interpolation.F90:7-30): the three points of a
+// window.  Each point is the reference's expression for its distance r:
+//   r <= 0.5:        (1 + sqrt(1 - 3 r r)) / 3
+//   0.5 < r <= 1.5:  ((5 - 3 r - sqrt(1 - 3 (1 - r)(1 - r))) / 3) / 2
+//   else             0
+// The outer points of a window sit at u + 1/2 and u - 3/2 cells from the
+// parcel (u its offset in the middle cell), so 1 - r is 1/2 - u and u - 1/2:
+// when both differences are exact (Sterbenz, away from the origin) the two
+// square roots have the same argument, bit for bit, and the second is not
+// issued.  The arguments are compared, so the sharing never changes a bit.
+// delta1 is one point.
 template <int UNIT_H>
 __device__ inline double delta1(double xcp, double h) {
   double r = fabs(UNIT_H ? xcp : xcp / h);
   if (r <= 0.5) return div3(1.0 + sqrt(1.0 - 3.0 * r * r));
   if (r <= 1.5) return div3(5.0 - 3.0 * r - sqrt(1.0 - 3.0 * ((1.0 - r) * (1.0 - r)))) * 0.5;
   return 0.0;
+}
+template <int UNIT_H>
+__device__ inline void delta_triple(const double x[3], double h, double w[3]) {
+  w[1] = delta1<UNIT_H>(x[1], h);
+  const double r0 = fabs(UNIT_H ? x[0] : x[0] / h), r2 = fabs(UNIT_H ? x[2] : x[2] / h);
+  if (r0 > 0.5 && r0 <= 1.5 && r2 > 0.5 && r2 <= 1.5) {
+    // both outer points in the middle branch
+    const double a0 = 1.0 - 3.0 * ((1.0 - r0) * (1.0 - r0));
+    const double a2 = 1.0 - 3.0 * ((1.0 - r2) * (1.0 - r2));
+    const double s0 = sqrt(a0);
+    const double s2 = __double_as_longlong(a2) == __double_as_longlong(a0) ? s0 : sqrt(a2);
+    w[0] = div3(5.0 - 3.0 * r0 - s0) * 0.5;
+    w[2] = div3(5.0 - 3.0 * r2 - s2) * 0.5;
+  } else {
+    w[0] = delta1<UNIT_H>(x[0], h);
+    w[2] = delta1<UNIT_H>(x[2], h);
+  }
 }
 
 template <int UNIT_H>
@@ -101,16 +128,17 @@ __global__ void __launch_bounds__(kBlock) k_weights(Recs R, Geom g, Counters* cn
       if (!UNIT_H) xc = xc * h;
       dl[q] = xp - xc;
     }
-#pragma unroll
-    for (int q = 0; q < 3; ++q) wu[d][q] = delta1<UNIT_H>(dl[q], h);
+    delta_triple<UNIT_H>(dl, h, wu[d]);
     // half-cell shifted component: deltax + 0.5d0*di
     double s0 = dl[0] + g.halfh[d], s3 = dl[3] + g.halfh[d];
     double r0 = fabs(UNIT_H ? s0 : s0 / h), r3 = fabs(UNIT_H ? s3 : s3 / h);
     int st = r0 < 1.5 ? 0 : 1;
     if (r0 < 1.5 && r3 < 1.5) set_err(cnt, E_WINDOW, e);
     flags |= st << d;
+    double xs[3];
 #pragma unroll
-    for (int q = 0; q < 3; ++q) ws[d][q] = delta1<UNIT_H>((st ? dl[q + 1] : dl[q]) + g.halfh[d], h);
+    for (int q = 0; q < 3; ++q) xs[q] = (st ? dl[q + 1] : dl[q]) + g.halfh[d];
+    delta_triple<UNIT_H>(xs, h, ws[d]);
   }
   int total = 0;
   double4_32a* out = reinterpret_cast<double4_32a*>(W + (size_t)e * kWStride);
@@ -1327,13 +1355,14 @@ __global__ void __launch_bounds__(kBlock) k_probe_weights(Geom g, int n, const d
       if (!UNIT_H) xc = xc * h;
       dl[q] = xp[d] - xc;
     }
-#pragma unroll
-    for (int q = 0; q < 3; ++q) wu[d][q] = delta1<UNIT_H>(dl[q], h);
+    delta_triple<UNIT_H>(dl, h, wu[d]);
     const double s0 = dl[0] + g.halfh[d];
     const int st = fabs(UNIT_H ? s0 : s0 / h) < 1.5 ? 0 : 1;
     flags |= st << d;
+    double xs[3];
 #pragma unroll
-    for (int q = 0; q < 3; ++q) ws[d][q] = delta1<UNIT_H>((st ? dl[q + 1] : dl[q]) + g.halfh[d], h);
+    for (int q = 0; q < 3; ++q) xs[q] = (st ? dl[q + 1] : dl[q]) + g.halfh[d];
+    delta_triple<UNIT_H>(xs, h, ws[d]);
   }
   double4_32a* out = reinterpret_cast<double4_32a*>(W + (size_t)e * kWStride);
 #pragma unroll
