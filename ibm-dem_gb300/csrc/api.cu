@@ -124,6 +124,7 @@ void free_parcel_buffers(Ctx& c) {
   c.bytesParcels = c.bytesRuns = 0;
   c.capRuns = 0;
   c.runsSized = false;
+  c.touchState = 0;
   c.recD[0] = c.recD[1] = nullptr;
   c.recI[0] = c.recI[1] = nullptr;
   c.imgSrc = c.imgShift = c.cellItems = c.bodyItems = c.iTmpA = c.iTmpB = c.scanScratch = c.sortHist = nullptr;
@@ -765,6 +766,7 @@ int ibmdem_set_parcels(ibmdem_ctx* h, int32_t np, const ibmdem_parcel* parts) {
   CU(cudaStreamSynchronize(c.stream));
   c.haveParcels = true;
   c.listsBuilt = c.weightsLocal = c.weightsGhost = c.planReady = c.spreadValid = false;
+  c.touchState = 0;
   return IBMDEM_OK;
 }
 
@@ -937,6 +939,7 @@ int ibmdem_RebuildAllListOrNot(ibmdem_ctx* h) {
   rebuild_collision_lists(c);
   c.listsBuilt = true;
   c.weightsLocal = c.weightsGhost = c.planReady = c.spreadValid = false;
+  c.touchState = 0;
   return launch_status(h);
 }
 

@@ -107,9 +107,45 @@ __device__ inline void delta_triple(const double x[3], double h, double w[3]) {
   }
 }
 
+__device__ inline void window_start(const int4& wn, int comp, int& sx, int& sy, int& sz) {
+  sx = wn.x - 1 + (comp == 0 ? (wn.w & 1) : 0);
+  sy = wn.y - 1 + (comp == 1 ? ((wn.w >> 1) & 1) : 0);
+  sz = wn.z - 1 + (comp == 2 ? ((wn.w >> 2) & 1) : 0);
+}
+
+// Mark the interior nodes of parcel window wn in the touched-node bits, all
+// three components: bits ilo..ihi of each row the window covers, one atomic
+// OR per row (and word).
+__device__ inline void mark_window(const Geom& g, const int4& wn, unsigned* flags) {
+  for (int comp = 0; comp < 3; ++comp) {
+    int sx, sy, sz;
+    window_start(wn, comp, sx, sy, sz);
+    const int ilo = max(sx, 1), ihi = min(sx + 2, g.n[0]);
+    if (ihi < ilo) continue;
+    const unsigned run = (1u << (ihi - ilo + 1)) - 1u;
+    for (int kz = 0; kz < 3; ++kz)
+      for (int ky = 0; ky < 3; ++ky) {
+        const int j = sy + ky, k = sz + kz;
+        if (j < 1 || j > g.n[1] || k < 1 || k > g.n[2]) continue;
+        const long long b0 = comp * g.nint + ((long long)(k - 1) * g.n[1] + (j - 1)) * g.n[0] + (ilo - 1);
+        const int sh = (int)(b0 & 31);
+        atomicOr(&flags[b0 >> 5], run << sh);
+        if (sh + (ihi - ilo + 1) > 32) atomicOr(&flags[(b0 >> 5) + 1], run >> (32 - sh));
+      }
+  }
+}
+
+// mark the windows of all parcels, read in cell order so that a warp's ORs
+// fall on neighbouring nodes (when the weights did not mark them)
+__global__ void k_touch(Geom g, const Counters* cnt, const int4* winC, unsigned* flags) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= cnt->np) return;
+  mark_window(g, winC[e], flags);
+}
+
 template <int UNIT_H>
 __global__ void __launch_bounds__(kBlock) k_weights(Recs R, Geom g, Counters* cnt, int locals, double* W,
-                                                    int4* win, int* cntInt) {
+                                                    int4* win, int* cntInt, unsigned* touch) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   int e = locals ? t : cnt->npLocal + t;
   if (locals ? (e >= cnt->npLocal) : (e >= cnt->np)) return;
@@ -172,15 +208,14 @@ __global__ void __launch_bounds__(kBlock) k_weights(Recs R, Geom g, Counters* cn
 #pragma unroll
     for (int q = 0; q < 7; ++q) out[comp * 7 + q] = make_double4_32a(wc[4 * q], wc[4 * q + 1], wc[4 * q + 2], wc[4 * q + 3]);
   }
-  win[e] = make_int4(a[0], a[1], a[2], flags);
+  const int4 wn = make_int4(a[0], a[1], a[2], flags);
+  win[e] = wn;
   cntInt[e] = total;
+  // the touched-node bits of the spread plan, set here where the windows are
+  // made (the atomics go out beside the FP64 work)
+  mark_window(g, wn, touch);
 }
 
-__device__ inline void window_start(const int4& wn, int comp, int& sx, int& sy, int& sz) {
-  sx = wn.x - 1 + (comp == 0 ? (wn.w & 1) : 0);
-  sy = wn.y - 1 + (comp == 1 ? ((wn.w >> 1) & 1) : 0);
-  sz = wn.z - 1 + (comp == 2 ? ((wn.w >> 2) & 1) : 0);
-}
 
 // ---- spread plan -------------------------------------------------------------
 // A node (component c, interior (i,j,k)) receives from every parcel whose
@@ -190,30 +225,6 @@ __device__ inline void window_start(const int4& wn, int comp, int& sx, int& sy, 
 // parcel (images share their source's fdrag*vol) and its weight, so spreading
 // streams the plan sequentially.
 
-// mark the interior nodes touched by any parcel window; the windows are read in
-// cell order, so that a warp's stores fall on neighbouring nodes
-__global__ void k_touch(Geom g, const Counters* cnt, const int4* winC, unsigned* flags) {
-  int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= cnt->np) return;
-  int4 wn = winC[e];
-  for (int comp = 0; comp < 3; ++comp) {
-    int sx, sy, sz;
-    window_start(wn, comp, sx, sy, sz);
-    // the window's interior nodes along x: bits ilo..ihi of each row it covers
-    const int ilo = max(sx, 1), ihi = min(sx + 2, g.n[0]);
-    if (ihi < ilo) continue;
-    const unsigned run = (1u << (ihi - ilo + 1)) - 1u;
-    for (int kz = 0; kz < 3; ++kz)
-      for (int ky = 0; ky < 3; ++ky) {
-        const int j = sy + ky, k = sz + kz;
-        if (j < 1 || j > g.n[1] || k < 1 || k > g.n[2]) continue;
-        const long long b0 = comp * g.nint + ((long long)(k - 1) * g.n[1] + (j - 1)) * g.n[0] + (ilo - 1);
-        const int sh = (int)(b0 & 31);
-        atomicOr(&flags[b0 >> 5], run << sh);
-        if (sh + (ihi - ilo + 1) > 32) atomicOr(&flags[(b0 >> 5) + 1], run >> (32 - sh));
-      }
-  }
-}
 
 // compaction of the flag bits into the sorted node-key list (128 flags per thread)
 __global__ void k_flag_count(const uint4* flags, long long nvec, int* blockCnt) {
@@ -234,7 +245,7 @@ __global__ void k_flag_count(const uint4* flags, long long nvec, int* blockCnt) 
   }
 }
 __global__ void k_flag_emit(const uint4* flags, long long nvec, long long nflags, const int* blockOff,
-                            uint32_t* keys, long long capRuns) {
+                            uint32_t* keys, long long capRuns, Counters* cnt, long long nint) {
   __shared__ int sh[kBlock / 32];
   long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   uint32_t w4[4] = {0, 0, 0, 0};
@@ -256,6 +267,22 @@ __global__ void k_flag_emit(const uint4* flags, long long nvec, long long nflags
   for (int w = 0; w < warp; ++w) base += sh[w];
   int pos = base + x - c;
   const long long f0 = v * 128;
+  // the first run of velocity components 1 and 2: the flags set below their
+  // first node, counted by the thread whose 128 flags hold that node
+#pragma unroll
+  for (int comp = 1; comp < 3; ++comp) {
+    const long long first = comp * nint;
+    if (first >= f0 && first < f0 + 128) {
+      const int b = (int)(first - f0);
+      int below = 0;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int nb = min(max(b - 32 * q, 0), 32);
+        below += __popc(nb == 32 ? w4[q] : (w4[q] & ((1u << nb) - 1u)));
+      }
+      cnt->compStart[comp] = min(pos + below, cnt->nRuns);
+    }
+  }
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
     uint32_t w = w4[q];
@@ -274,6 +301,8 @@ __global__ void k_flag_emit(const uint4* flags, long long nvec, long long nflags
 __global__ void k_set_runs(Counters* cnt, const int* total, long long capRuns) {
   const int t = *total;
   if (t > capRuns) set_err(cnt, E_PLANCAP, t);
+  cnt->compStart[0] = 0;
+  cnt->compStart[3] = (int)min((long long)t, capRuns);
   cnt->nRuns = (int)min((long long)t, capRuns);
 }
 
@@ -650,22 +679,6 @@ __global__ void k_plan_total(Counters* cnt, const unsigned long long* cursor) {
   cnt->nContrib = (int)*cursor;
 }
 
-// the first run of each velocity component in the sorted run keys
-__global__ void k_comp_bounds(Counters* cnt, const uint32_t* runKey, long long nint) {
-  const int n = cnt->nRuns;
-  cnt->compStart[0] = 0;
-  cnt->compStart[3] = n;
-  for (int comp = 1; comp < 3; ++comp) {
-    const uint32_t key = (uint32_t)(comp * nint);
-    int lo = 0, hi = n;  // first run with runKey >= key
-    while (lo < hi) {
-      const int mid = (lo + hi) >> 1;
-      if (runKey[mid] < key) lo = mid + 1;
-      else hi = mid;
-    }
-    cnt->compStart[comp] = lo;
-  }
-}
 
 // Write the new value of interior node (i,j,k) of component comp where the
 // fluid solver's halo refill puts it (FillGhostRegionForFluid,
@@ -1096,26 +1109,39 @@ Fields fields_of(Ctx& c) { return Fields{c.u, c.v, c.w, c.u0, c.v0, c.w0, c.fx, 
 
 }  // namespace
 
+static size_t touch_bytes(const Ctx& c) { return (size_t)((3 * c.g.nint + 127) / 128) * 16; }
+
 void launch_weights(Ctx& c, bool locals) {
   int n = locals ? c.capLocal : c.capImg;
   if (n <= 0) return;
+  // the locals' launch starts the touched-node bits afresh, the images' adds
+  // to them; a plan built after exactly that pair uses them as they are
+  unsigned* touch = reinterpret_cast<unsigned*>(c.touch);
+  if (locals) cudaMemsetAsync(c.touch, 0, touch_bytes(c), c.stream);
   if (c.g.unit_h)
-    k_weights<1><<<nblocks(n), kBlock, 0, c.stream>>>(c.rec(), c.g, c.dCnt, locals, c.W, c.win, c.cntInt);
+    k_weights<1><<<nblocks(n), kBlock, 0, c.stream>>>(c.rec(), c.g, c.dCnt, locals, c.W, c.win, c.cntInt, touch);
   else
-    k_weights<0><<<nblocks(n), kBlock, 0, c.stream>>>(c.rec(), c.g, c.dCnt, locals, c.W, c.win, c.cntInt);
+    k_weights<0><<<nblocks(n), kBlock, 0, c.stream>>>(c.rec(), c.g, c.dCnt, locals, c.W, c.win, c.cntInt, touch);
   c.launches++;
+  c.touchState = locals ? 1 : (c.touchState == 1 ? 2 : 0);
 }
 
 // touched-node flags, their per-block counts (iTmpA, scanned) and the total (dTotal)
 static void flag_touched_nodes(Ctx& c, cudaStream_t s) {
   const long long nvec = (3 * c.g.nint + 127) / 128;
-  cudaMemsetAsync(c.touch, 0, nvec * 16, s);
   k_win_by_cell<<<nblocks(c.cap), kBlock, 0, s>>>(c.dCnt, c.cellItems, c.win, c.winC);
-  k_touch<<<nblocks(c.cap), kBlock, 0, s>>>(c.g, c.dCnt, c.winC, reinterpret_cast<unsigned*>(c.touch));
+  c.launches++;
+  if (c.touchState != 2) {
+    // the weights were not made as a locals-then-images pair since the bits
+    // were last cleared: mark every window again
+    cudaMemsetAsync(c.touch, 0, touch_bytes(c), s);
+    k_touch<<<nblocks(c.cap), kBlock, 0, s>>>(c.g, c.dCnt, c.winC, reinterpret_cast<unsigned*>(c.touch));
+    c.launches++;
+  }
   const long long nb = nblocks(nvec);
   k_flag_count<<<(unsigned)nb, kBlock, 0, s>>>(reinterpret_cast<const uint4*>(c.touch), nvec, c.iTmpA);
   scan_exclusive(c.iTmpA, c.iTmpA, nb, nullptr, c.dTotal, c.scanScratch, s, &c.launches);
-  c.launches += 3;
+  c.launches++;
 }
 
 long long count_touched_nodes(Ctx& c) {
@@ -1146,10 +1172,9 @@ void build_spread_plan(Ctx& c) {
   const uint4* fv4 = reinterpret_cast<const uint4*>(c.touch);
   const long long nb = nblocks(nvec);
   k_set_runs<<<1, 1, 0, s>>>(c.dCnt, c.dTotal, c.capRuns);
-  k_flag_emit<<<(unsigned)nb, kBlock, 0, s>>>(fv4, nvec, nflags, c.iTmpA, c.runKey, c.capRuns);
+  k_flag_emit<<<(unsigned)nb, kBlock, 0, s>>>(fv4, nvec, nflags, c.iTmpA, c.runKey, c.capRuns, c.dCnt, c.g.nint);
   cudaMemsetAsync(c.planAlloc, 0, sizeof(unsigned long long), s);
-  k_comp_bounds<<<1, 1, 0, s>>>(c.dCnt, c.runKey, c.g.nint);
-  c.launches += 3;
+  c.launches += 2;
   k_plan_fill<<<run_blocks(c), kBlock, 0, s>>>(c.g, c.dCnt, c.runKey, c.cellStart, c.cellItems, c.winC, c.W,
                                                    c.imgSrc, c.runStart, c.runCnt, c.planRoot, c.planW, c.planAlloc,
                                                    c.capContrib);

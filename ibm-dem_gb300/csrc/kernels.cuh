@@ -161,6 +161,9 @@ struct Ctx {
   // state flags
   bool haveFluid = false, haveParcels = false, listsBuilt = false;
   bool weightsLocal = false, weightsGhost = false, planReady = false;
+  // the touched-node bits: 1 after the locals' weights cleared and marked
+  // them, 2 once the images' weights added theirs (complete), 0 otherwise
+  int touchState = 0;
   bool spreadValid = false;  // fCur matches the current plan
 };
 
