@@ -176,6 +176,7 @@ void init_geom(Geom& g, const ibmdem_params* p) {
     g.start[d] = (1 - 1) * hh[d];
     g.end[d] = (g.n[d] - 1 + 1) * hh[d];
     g.len[d] = hh[d] * g.n[d];
+    g.halfLen[d] = 0.5 * g.len[d];
     g.halfh[d] = 0.5 * hh[d];
     g.err[d] = hh[d] * 1e-20;
   }

@@ -102,6 +102,7 @@ struct Geom {
   long long nint;   // nx*ny*nz
   double h[3];      // dx, dy, dz
   double start[3], end[3], len[3];
+  double halfLen[3];  // 0.5*len (exact)
   double halfh[3];  // 0.5*di etc. (GetWeight)
   double err[3];    // di*1e-20 (AdjustParcelPosition)
   double hprod;     // dx*dy*dz
@@ -183,8 +184,8 @@ __device__ inline void set_err(Counters* c, int bit, int info) {
 __device__ inline double body_ref(const Geom& g, int d, double xm, double X) {
   double L = g.len[d];
   double diff = xm - X;
-  if (diff > 0.5 * L) return X + L;
-  if (diff < -0.5 * L) return X - L;
+  if (diff > g.halfLen[d]) return X + L;
+  if (diff < -g.halfLen[d]) return X - L;
   return X;
 }
 
