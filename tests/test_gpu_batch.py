@@ -111,6 +111,49 @@ def test_batch_shared_forcing_launches_match_alone(gpu_lib, lanes, interp_block)
         case.close()
 
 
+def test_batch_shared_launches_nonunit_spacing_and_substeps(gpu_lib):
+    """Shared forcing launches over members with physical units (the cylinder
+    fixture, dx = 3.75e-5 m), three DEM sub-steps and periodic spheres: each
+    member exactly as alone."""
+    import golden_util
+
+    _, cyl = golden_util.load("cylinders")
+    cs = [cyl, cases.contact_case(seed=11, coupleInterval=3), mixed_cases()[1]]
+    assert len({int(np.asarray(c[0])["Ns"]) for c in cs}) == 1
+    steps = 2
+    ref = [alone(c, steps) for c in cs]
+    members = [make_case(c) for c in cs]
+    b = api.Batch(members, lanes=2)
+    b.set_fused(True, 128)
+    b.step(steps)
+    b.synchronize()
+    for case, r in zip(members, ref):
+        assert_same(snapshot(case), r)
+    b.close()
+    for case in members:
+        case.close()
+
+
+def test_batch_shared_launches_fall_back_for_unequal_iterations(gpu_lib):
+    """Members with different forcing iteration counts cannot share the
+    launches: the batch keeps each member's own and the results stay exact."""
+    cs = mixed_cases()[:2]
+    p, parts, bodies, field = scenario.resolved_case(32, 32, 32, 5, 8.0, seed=9, n_modes=8, Ns=3)
+    cs.append((p, parts, bodies, field))
+    steps = 2
+    ref = [alone(c, steps) for c in cs]
+    members = [make_case(c) for c in cs]
+    b = api.Batch(members)
+    b.set_fused(True)
+    b.step(steps)
+    b.synchronize()
+    for case, r in zip(members, ref):
+        assert_same(snapshot(case), r)
+    b.close()
+    for case in members:
+        case.close()
+
+
 def test_batch_autotune_and_recapture(gpu_lib):
     cs = mixed_cases()[:3]
     members = [make_case(c) for c in cs]
