@@ -75,7 +75,12 @@ __device__ inline double min_image(double d, double L, double halfL) {
   return d;
 }
 
-// cell keys for both sorts; positions outside [0, L) are flagged
+// Cell keys for both cell lists, and each particle's slot in its cells from
+// the count atomics; positions outside [0, L) are flagged.  The lists are
+// built without a sort: the scans of the counts give the cells' starts, every
+// particle goes to start + slot, and the particle that took slot 0 puts its
+// cell's few items back in index order -- the order a stable sort by cell
+// gives.
 __global__ void k_u_keys(UGeom g, UPtr P, int np, uint32_t* kd, uint32_t* vd, int* cntD, uint32_t* kf,
                          uint32_t* vf, int* cntF, int* err, int* info) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -93,11 +98,41 @@ __global__ void k_u_keys(UGeom g, UPtr P, int np, uint32_t* kd, uint32_t* vd, in
   uint32_t keyD = (uint32_t)(((long long)cd[2] * g.nc[1] + cd[1]) * g.nc[0] + cd[0]);
   uint32_t keyF = (uint32_t)(((long long)cf[2] * g.n[1] + cf[1]) * g.n[0] + cf[0]);
   kd[i] = keyD;
-  vd[i] = (uint32_t)i;
   kf[i] = keyF;
-  vf[i] = (uint32_t)i;
-  atomicAdd(&cntD[keyD], 1);
-  atomicAdd(&cntF[keyF], 1);
+  vd[i] = (uint32_t)atomicAdd(&cntD[keyD], 1);
+  vf[i] = (uint32_t)atomicAdd(&cntF[keyF], 1);
+}
+
+// particle i to its cell's start + slot
+__global__ void k_u_place(int np, const uint32_t* __restrict__ key, const uint32_t* __restrict__ slot,
+                          const int* __restrict__ start, int* items) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < np) items[start[key[i]] + (int)slot[i]] = i;
+}
+
+// the slot-0 particle of each cell sorts the cell's items by index (Shell sort
+// with Ciura's gaps: an insertion sort for the usual handful)
+__global__ void k_u_order(int np, const uint32_t* __restrict__ key, const uint32_t* __restrict__ slot,
+                          const int* __restrict__ start, int* items) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= np || slot[i] != 0) return;
+  const uint32_t c = key[i];
+  const int s0 = start[c], n = start[c + 1] - s0;
+  if (n < 2) return;
+  int* a = items + s0;
+  constexpr int kGaps[8] = {701, 301, 132, 57, 23, 10, 4, 1};
+  for (int gi = 0; gi < 8; ++gi) {
+    const int gap = kGaps[gi];
+    for (int q = gap; q < n; ++q) {
+      const int v = a[q];
+      int j = q;
+      while (j >= gap && a[j - gap] > v) {
+        a[j] = a[j - gap];
+        j -= gap;
+      }
+      a[j] = v;
+    }
+  }
 }
 
 // Positions and radii in DEM-cell order, rounded to FP32, for the search.
@@ -541,16 +576,7 @@ __global__ void k_u_drag_move(UGeom g, UPtr P, int np, const double* __restrict_
   P.D(U_ALPHA, i) = af;
 }
 
-__global__ void k_copy_items(int np, const uint32_t* sorted, int* items) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < np) items[i] = (int)sorted[i];
-}
 
-int bits_of(long long n) {
-  int b = 1;
-  while ((1ll << b) < n) ++b;
-  return b;
-}
 
 double eta_of(double e) {
   // ZJS_COLLISION_DEM.F90:30: 3.1415926536 is a single-precision literal
@@ -574,8 +600,8 @@ struct ibmdem_ucase {
   int np = 0, cap = 0;
   double* pd = nullptr;
   int* gidx = nullptr;
-  uint32_t *kA = nullptr, *vA = nullptr, *kB = nullptr, *vB = nullptr;
-  uint32_t *kC = nullptr, *vC = nullptr, *kD = nullptr, *vD = nullptr;
+  uint32_t *kA = nullptr, *vA = nullptr;  // DEM cell of each particle, its slot in the cell
+  uint32_t *kC = nullptr, *vC = nullptr;  // fluid cell of each particle, its slot in the cell
   int *demStart = nullptr, *demItems = nullptr, *flStart = nullptr, *flItems = nullptr;
   int* nc[2] = {nullptr, nullptr};
   int* partner[2] = {nullptr, nullptr};
@@ -602,7 +628,6 @@ struct ibmdem_ucase {
   double phaseMs[8] = {};
   long long phaseCount[8] = {};
   int* scan = nullptr;
-  int* hist = nullptr;
   bool haveFluid = false, stepped = false;
 };
 
@@ -631,14 +656,14 @@ cudaError_t ualloc(ibmdem_ucase* u, T*& p, size_t n) {
 }
 
 void ufree_particles(ibmdem_ucase* u) {
-  void* ps[] = {u->pd, u->gidx, u->kA, u->vA, u->kB, u->vB, u->kC, u->vC, u->kD, u->vD, u->demItems, u->flItems,
-                u->nc[0], u->nc[1], u->partner[0], u->partner[1], u->xi[0], u->xi[1], u->st, u->pos, u->scan, u->hist, u->cstart, u->owner,
+  void* ps[] = {u->pd, u->gidx, u->kA, u->vA, u->kC, u->vC, u->demItems, u->flItems,
+                u->nc[0], u->nc[1], u->partner[0], u->partner[1], u->xi[0], u->xi[1], u->st, u->pos, u->scan, u->cstart, u->owner,
                 u->fterm, u->tterm, u->occFlag, u->occ, u->nOcc, u->T};
   for (void* q : ps)
     if (q) cudaFreeAsync(q, u->stream);
   u->pd = nullptr;
   u->gidx = u->demItems = u->flItems = nullptr;
-  u->kA = u->vA = u->kB = u->vB = u->kC = u->vC = u->kD = u->vD = nullptr;
+  u->kA = u->vA = u->kC = u->vC = nullptr;
   u->nc[0] = u->nc[1] = u->partner[0] = u->partner[1] = nullptr;
   u->xi[0] = u->xi[1] = nullptr;
   u->st = nullptr;
@@ -647,7 +672,7 @@ void ufree_particles(ibmdem_ucase* u) {
   u->fterm = u->tterm = nullptr;
   u->occFlag = u->occ = u->nOcc = nullptr;
   u->T = nullptr;
-  u->scan = u->hist = nullptr;
+  u->scan = nullptr;
   u->cap = u->np = 0;
 }
 
@@ -723,14 +748,13 @@ int one_step(ibmdem_ucase* u) {
   k_u_keys<<<nb, kBlock, 0, s>>>(g, P, np, u->kA, u->vA, u->demStart, u->kC, u->vC, u->flStart, u->dErr,
                                  u->dErr + 1);
   u->launches++;
-  uint32_t *k0 = u->kA, *v0 = u->vA, *k1 = u->kB, *v1 = u->vB;
-  radix_sort_pairs(k0, v0, k1, v1, np, nullptr, bits_of(g.ncd), u->hist, u->scan, s, &u->launches);
-  k_copy_items<<<nb, kBlock, 0, s>>>(np, v0, u->demItems);
   scan_exclusive(u->demStart, u->demStart, g.ncd, nullptr, u->demStart + g.ncd, u->scan, s, &u->launches);
-  k0 = u->kC, v0 = u->vC, k1 = u->kD, v1 = u->vD;
-  radix_sort_pairs(k0, v0, k1, v1, np, nullptr, bits_of(g.nint), u->hist, u->scan, s, &u->launches);
-  k_copy_items<<<nb, kBlock, 0, s>>>(np, v0, u->flItems);
   scan_exclusive(u->flStart, u->flStart, g.nint, nullptr, u->flStart + g.nint, u->scan, s, &u->launches);
+  k_u_place<<<nb, kBlock, 0, s>>>(np, u->kA, u->vA, u->demStart, u->demItems);
+  k_u_place<<<nb, kBlock, 0, s>>>(np, u->kC, u->vC, u->flStart, u->flItems);
+  k_u_order<<<nb, kBlock, 0, s>>>(np, u->kA, u->vA, u->demStart, u->demItems);
+  k_u_order<<<nb, kBlock, 0, s>>>(np, u->kC, u->vC, u->flStart, u->flItems);
+  u->launches += 4;
   }
   const int o = u->hcur, n = u->hcur ^ 1;
   {
@@ -906,7 +930,7 @@ int ibmdem_unresolved_set_particles(ibmdem_ucase* u, int32_t np, const ibmdem_pa
   };
   A(u->pd, (size_t)U_ND * cap);
   A(u->gidx, (size_t)cap);
-  for (auto* q : {&u->kA, &u->vA, &u->kB, &u->vB, &u->kC, &u->vC, &u->kD, &u->vD}) A(*q, (size_t)cap);
+  for (auto* q : {&u->kA, &u->vA, &u->kC, &u->vC}) A(*q, (size_t)cap);
   A(u->demItems, (size_t)cap);
   A(u->flItems, (size_t)cap);
   for (int b = 0; b < 2; ++b) {
@@ -925,9 +949,8 @@ int ibmdem_unresolved_set_particles(ibmdem_ucase* u, int32_t np, const ibmdem_pa
   A(u->owner, K * cap);
   A(u->fterm, 3 * K * cap);
   A(u->tterm, 3 * K * cap);
-  const long long scanN = std::max<long long>(std::max(g.ncd, g.nint) + 1, sort_hist_ints(cap));
-  A(u->scan, (size_t)std::max(scan_scratch_ints(scanN), scan_scratch_ints(sort_hist_ints(cap))));
-  A(u->hist, (size_t)sort_hist_ints(cap));
+  const long long scanN = std::max<long long>(std::max(g.ncd, g.nint), cap) + 1;
+  A(u->scan, (size_t)scan_scratch_ints(scanN));
   if (e != cudaSuccess) {
     ufree_particles(u);
     return uerr(u, IBMDEM_ENOMEM, "particle buffers: %s", cudaGetErrorString(e));
