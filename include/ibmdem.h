@@ -261,11 +261,11 @@ int ibmdem_step(ibmdem_ctx* ctx, int32_t nsteps);
  * That array (about 11.3 MB) is part of the library's device module, so every
  * device on which the library's kernels are loaded holds it until the process
  * exits, whether or not this function is ever called.  Each call waits for its
- * result (it synchronises the context's stream) and returns IBMDEM_ERANGE when
- * a point lies outside the box.  Calls that overlap in time on one device (from
- * several threads or contexts) share that array and race.  The first call on a
- * device looks the array up (which may load the module): make it before any
- * stream capture.  No counterpart in the reference. */
+ * result (it synchronises the context's stream), so no call may be made while
+ * that stream is being captured into a graph; it returns IBMDEM_ERANGE when a
+ * point lies outside the box.  Calls that overlap in time on one device (from
+ * several threads or contexts) share that array and race.  No counterpart in
+ * the reference. */
 #define IBMDEM_PROBE_MAX_POINTS 16384
 int ibmdem_interpolate_velocity_noalloc(ibmdem_ctx* ctx, int32_t n, const double* x, double* ulp);
 
