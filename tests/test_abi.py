@@ -103,3 +103,12 @@ def test_null_handles_are_rejected(gpu_lib):
         assert rc == -1, name
     lib.ibmdem_last_error.restype = ctypes.c_char_p
     assert lib.ibmdem_last_error(None) == b"null context"
+
+
+def test_compiled_caller_builds_against_the_header():
+    """The compiled coupled caller (run on the GPU by test_gpu_c_caller.py)
+    compiles against the header without warnings."""
+    src = os.path.join(os.path.dirname(os.path.abspath(__file__)), "c_caller", "coupled_step.c")
+    with tempfile.TemporaryDirectory() as d:
+        subprocess.run(["gcc", "-Wall", "-Wextra", "-Werror", "-I", os.path.dirname(HEADER), "-c", src, "-o",
+                        os.path.join(d, "coupled_step.o")], check=True)
