@@ -496,6 +496,7 @@ int create_on_stream(const ibmdem_params* p, int device, cudaStream_t stream, ib
   for (double** q : f)
     if (rc == IBMDEM_OK && dalloc(c, *q, nf) != cudaSuccess) rc = IBMDEM_ENOMEM;
   if (rc == IBMDEM_OK && dalloc(c, c.cellStart, nf + 1) != cudaSuccess) rc = IBMDEM_ENOMEM;
+  if (rc == IBMDEM_OK && dalloc(c, c.cellCount, nf + 1) != cudaSuccess) rc = IBMDEM_ENOMEM;
   if (rc == IBMDEM_OK && dalloc(c, c.dCnt, 1) != cudaSuccess) rc = IBMDEM_ENOMEM;
   if (rc == IBMDEM_OK && dalloc(c, c.dTotal, 4) != cudaSuccess) rc = IBMDEM_ENOMEM;
   if (rc == IBMDEM_OK && !(c.hCnt = pinned_counters())) rc = IBMDEM_ENOMEM;
@@ -503,6 +504,7 @@ int create_on_stream(const ibmdem_params* p, int device, cudaStream_t stream, ib
     for (double** q : f) cudaMemsetAsync(*q, 0, nf * sizeof(double), c.stream);
     cudaMemsetAsync(c.dCnt, 0, sizeof(Counters), c.stream);
     cudaMemsetAsync(c.cellStart, 0, sizeof(int) * (nf + 1), c.stream);
+    cudaMemsetAsync(c.cellCount, 0, sizeof(int) * (nf + 1), c.stream);
     if (cudaStreamSynchronize(c.stream) != cudaSuccess) rc = IBMDEM_ECUDA;
   }
   if (rc != IBMDEM_OK) {
@@ -525,7 +527,7 @@ int ibmdem_destroy(ibmdem_ctx* h) {
   poisson_release(c);
   cudaStreamSynchronize(c.stream);
   free_parcel_buffers(c);
-  void* ps[] = {c.u, c.v, c.w, c.u0, c.v0, c.w0, c.fx, c.fy, c.fz, c.cellStart, c.dCnt, c.dTotal, c.dBodies,
+  void* ps[] = {c.u, c.v, c.w, c.u0, c.v0, c.w0, c.fx, c.fy, c.fz, c.cellStart, c.cellCount, c.dCnt, c.dTotal, c.dBodies,
                 c.bodyStart, c.bodyR2, c.partnerCnt, c.partners, c.dProbes};
   for (void* p : ps) dfree(c, p);
   // the frees are ordered on the context's stream; let them complete before
@@ -764,6 +766,9 @@ int ibmdem_set_parcels(ibmdem_ctx* h, int32_t np, const ibmdem_parcel* parts) {
   Counters hc{};
   hc.npLocal = hc.np = np;
   CU(cudaMemcpyAsync(c.dCnt, &hc, sizeof hc, cudaMemcpyHostToDevice, c.stream));
+  // new parcels start from clean cell counts (a rebuild stopped by an error
+  // may have left some behind)
+  CU(cudaMemsetAsync(c.cellCount, 0, sizeof(int) * (c.g.ncell + 1), c.stream));
   CU(cudaStreamSynchronize(c.stream));
   c.haveParcels = true;
   c.listsBuilt = c.weightsLocal = c.weightsGhost = c.planReady = c.spreadValid = false;

@@ -45,6 +45,9 @@ struct Ctx {
   int* imgSrc = nullptr;    // [capImg] root local of each image
   int* imgShift = nullptr;  // [capImg] 2-bit shift code per axis
   int* cellStart = nullptr; // [ncell+1]
+  // per-cell parcel counts of the cell-list rebuild; all zero between rebuilds
+  // (the scatter zeroes the cells it used), so no sweep clears them
+  int* cellCount = nullptr;  // [ncell+1]
   int* cellItems = nullptr; // [cap] part indices sorted by cell (stable)
   int* bodyStart = nullptr; // [nMS+1]
   int* bodyItems = nullptr; // [capLocal] locals grouped by body (stable)

@@ -299,11 +299,15 @@ __global__ void k_cell_keys(Recs R, Geom g, Counters* cnt, uint32_t* cellOf, int
   slot[e] = atomicAdd(&cellCount[id - 1], 1);
 }
 
+// parcel e to its cell's start + slot; the cell's count goes back to zero
+// for the next rebuild
 __global__ void k_cell_scatter(const Counters* cnt, const uint32_t* __restrict__ cellOf, const int* __restrict__ slot,
-                               const int* __restrict__ cellStart, int* cellItems) {
+                               const int* __restrict__ cellStart, int* cellItems, int* cellCount) {
   int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= cnt->np) return;
-  cellItems[cellStart[cellOf[e]] + slot[e]] = e;
+  const uint32_t c = cellOf[e];
+  cellItems[cellStart[c] + slot[e]] = e;
+  if (slot[e] == 0) cellCount[c] = 0;
 }
 
 // Shell sort (Ciura's gaps) of a cell's items: an insertion sort for the usual
@@ -378,13 +382,12 @@ void rebuild_cell_lists(Ctx& c) {
   k_set_image_counts<<<1, 1, 0, s>>>(c.dCnt, c.dTotal, c.capImg);
   c.launches += 3;
   // cell lists: stable sort of part indices by cell (npPartInCell/partIdxInCell)
-  cudaMemsetAsync(c.cellStart, 0, sizeof(int) * (c.g.ncell + 1), s);
-  k_cell_keys<<<nblocks(c.cap), kBlock, 0, s>>>(c.rec(), c.g, c.dCnt, c.kA, c.iTmpA, c.cellStart);
+  k_cell_keys<<<nblocks(c.cap), kBlock, 0, s>>>(c.rec(), c.g, c.dCnt, c.kA, c.iTmpA, c.cellCount);
   c.launches++;
   c.planReady = false;  // the plan is rebuilt after new weights
-  scan_exclusive(c.cellStart, c.cellStart, c.g.ncell, nullptr, c.cellStart + c.g.ncell, c.scanScratch, s,
+  scan_exclusive(c.cellCount, c.cellStart, c.g.ncell, nullptr, c.cellStart + c.g.ncell, c.scanScratch, s,
                  &c.launches);
-  k_cell_scatter<<<nblocks(c.cap), kBlock, 0, s>>>(c.dCnt, c.kA, c.iTmpA, c.cellStart, c.cellItems);
+  k_cell_scatter<<<nblocks(c.cap), kBlock, 0, s>>>(c.dCnt, c.kA, c.iTmpA, c.cellStart, c.cellItems, c.cellCount);
   k_cell_order<<<nblocks(c.cap), kBlock, 0, s>>>(c.dCnt, c.kA, c.iTmpA, c.cellStart, c.cellItems);
   c.launches += 2;
   uint32_t *k0, *v0, *k1, *v1;

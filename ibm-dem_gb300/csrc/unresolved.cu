@@ -103,11 +103,14 @@ __global__ void k_u_keys(UGeom g, UPtr P, int np, uint32_t* kd, uint32_t* vd, in
   vf[i] = (uint32_t)atomicAdd(&cntF[keyF], 1);
 }
 
-// particle i to its cell's start + slot
+// particle i to its cell's start + slot; the cell's count goes back to zero
+// for the next step
 __global__ void k_u_place(int np, const uint32_t* __restrict__ key, const uint32_t* __restrict__ slot,
-                          const int* __restrict__ start, int* items) {
+                          const int* __restrict__ start, int* items, int* count) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < np) items[start[key[i]] + (int)slot[i]] = i;
+  if (i >= np) return;
+  items[start[key[i]] + (int)slot[i]] = i;
+  if (slot[i] == 0) count[key[i]] = 0;
 }
 
 // the slot-0 particle of each cell sorts the cell's items by index (Shell sort
@@ -603,6 +606,9 @@ struct ibmdem_ucase {
   uint32_t *kA = nullptr, *vA = nullptr;  // DEM cell of each particle, its slot in the cell
   uint32_t *kC = nullptr, *vC = nullptr;  // fluid cell of each particle, its slot in the cell
   int *demStart = nullptr, *demItems = nullptr, *flStart = nullptr, *flItems = nullptr;
+  // per-cell counts of the two cell lists; all zero between steps (the
+  // placement zeroes the cells it used), so no sweep clears them
+  int *demCount = nullptr, *flCount = nullptr;
   int* nc[2] = {nullptr, nullptr};
   int* partner[2] = {nullptr, nullptr};
   double* xi[2] = {nullptr, nullptr};
@@ -743,15 +749,13 @@ int one_step(ibmdem_ucase* u) {
   UPtr P = uptr(u);
   {
   UScope ts(u, UP_LISTS);
-  cudaMemsetAsync(u->demStart, 0, sizeof(int) * (g.ncd + 1), s);
-  cudaMemsetAsync(u->flStart, 0, sizeof(int) * (g.nint + 1), s);
-  k_u_keys<<<nb, kBlock, 0, s>>>(g, P, np, u->kA, u->vA, u->demStart, u->kC, u->vC, u->flStart, u->dErr,
+  k_u_keys<<<nb, kBlock, 0, s>>>(g, P, np, u->kA, u->vA, u->demCount, u->kC, u->vC, u->flCount, u->dErr,
                                  u->dErr + 1);
   u->launches++;
-  scan_exclusive(u->demStart, u->demStart, g.ncd, nullptr, u->demStart + g.ncd, u->scan, s, &u->launches);
-  scan_exclusive(u->flStart, u->flStart, g.nint, nullptr, u->flStart + g.nint, u->scan, s, &u->launches);
-  k_u_place<<<nb, kBlock, 0, s>>>(np, u->kA, u->vA, u->demStart, u->demItems);
-  k_u_place<<<nb, kBlock, 0, s>>>(np, u->kC, u->vC, u->flStart, u->flItems);
+  scan_exclusive(u->demCount, u->demStart, g.ncd, nullptr, u->demStart + g.ncd, u->scan, s, &u->launches);
+  scan_exclusive(u->flCount, u->flStart, g.nint, nullptr, u->flStart + g.nint, u->scan, s, &u->launches);
+  k_u_place<<<nb, kBlock, 0, s>>>(np, u->kA, u->vA, u->demStart, u->demItems, u->demCount);
+  k_u_place<<<nb, kBlock, 0, s>>>(np, u->kC, u->vC, u->flStart, u->flItems, u->flCount);
   k_u_order<<<nb, kBlock, 0, s>>>(np, u->kA, u->vA, u->demStart, u->demItems);
   k_u_order<<<nb, kBlock, 0, s>>>(np, u->kC, u->vC, u->flStart, u->flItems);
   u->launches += 4;
@@ -855,6 +859,8 @@ int ibmdem_unresolved_create(const ibmdem_uparams* p, int32_t device, ibmdem_uca
   A(u->alphaf, (size_t)g.nint);
   A(u->demStart, (size_t)g.ncd + 1);
   A(u->flStart, (size_t)g.nint + 1);
+  A(u->demCount, (size_t)g.ncd + 1);
+  A(u->flCount, (size_t)g.nint + 1);
   A(u->dErr, 2);
   A(u->dTotal, 1);
   if (e == cudaSuccess) {
@@ -862,6 +868,8 @@ int ibmdem_unresolved_create(const ibmdem_uparams* p, int32_t device, ibmdem_uca
     cudaMemsetAsync(u->vf, 0, nf * sizeof(double), u->stream);
     cudaMemsetAsync(u->wf, 0, nf * sizeof(double), u->stream);
     cudaMemsetAsync(u->dErr, 0, 2 * sizeof(int), u->stream);
+    cudaMemsetAsync(u->demCount, 0, ((size_t)g.ncd + 1) * sizeof(int), u->stream);
+    cudaMemsetAsync(u->flCount, 0, ((size_t)g.nint + 1) * sizeof(int), u->stream);
     e = cudaStreamSynchronize(u->stream);
   }
   if (e != cudaSuccess) {
@@ -877,7 +885,7 @@ int ibmdem_unresolved_destroy(ibmdem_ucase* u) {
   cudaSetDevice(u->device);
   cudaStreamSynchronize(u->stream);
   ufree_particles(u);
-  void* ps[] = {u->uf, u->vf, u->wf, u->alphaf, u->demStart, u->flStart, u->dErr, u->dTotal};
+  void* ps[] = {u->uf, u->vf, u->wf, u->alphaf, u->demStart, u->flStart, u->demCount, u->flCount, u->dErr, u->dTotal};
   for (void* q : ps)
     if (q) cudaFreeAsync(q, u->stream);
   cudaStreamSynchronize(u->stream);
@@ -922,6 +930,9 @@ int ibmdem_unresolved_set_particles(ibmdem_ucase* u, int32_t np, const ibmdem_pa
       if (!(parts[i].x[d] >= 0.0 && parts[i].x[d] < g.L[d]))
         return uerr(u, IBMDEM_ERANGE, "particle %d is outside the periodic box", i);
   ufree_particles(u);
+  // new particles start from clean cell counts
+  UCU(cudaMemsetAsync(u->demCount, 0, ((size_t)g.ncd + 1) * sizeof(int), u->stream));
+  UCU(cudaMemsetAsync(u->flCount, 0, ((size_t)g.nint + 1) * sizeof(int), u->stream));
   const int cap = std::max(np, 1);
   const size_t K = (size_t)g.K;
   cudaError_t e = cudaSuccess;
