@@ -303,8 +303,10 @@ def algorithmic(counters):
     }
 
 
-# FP64 instructions per parcel of the delta-weight kernel (ncu count, 512-sphere case)
-FP64_WEIGHTS_PER_PARCEL = 516
+# FP64 instructions per parcel of the delta-weight kernel (ncu's
+# sm__sass_thread_inst_executed_op_fp64_pred_on over the two launches of a step
+# of the 64-sphere case, divided by its 57,216 parcels)
+FP64_WEIGHTS_PER_PARCEL = 506
 
 
 def kernel_rows(alg, phases, hbm_peak, fp64_peak, npLocal):
@@ -543,7 +545,15 @@ FLUID_BYTES = {
 # products (2 adds, 3 multiplies), 9 differences, 9 Laplacians (2 adds, 2
 # multiplies), 3 gradients (a subtraction and a division), 3 right-hand sides
 # (7 adds) and 3 updates (7 operations)
-FLUID_GUESS_FP64 = 18 * 5 + 9 + 9 * 4 + 3 * 2 + 3 * 7 + 3 * 7
+FLUID_GUESS_FP64_REF = 18 * 5 + 9 + 9 * 4 + 3 * 2 + 3 * 7 + 3 * 7
+# FP64 instructions the guess kernel issues per interior node (ncu's
+# sm__sass_thread_inst_executed_op_fp64_pred_on on the 128^3 grid: 371.2 M over
+# 2,097,152 nodes; fewer than the statements' FLUID_GUESS_FP64_REF because exact
+# scalings and identity coefficients are not issued, compares included)
+FLUID_GUESS_FP64 = 177
+# the Poisson kernels issue this many FP64 instructions per operation that
+# poisson_counts counts (ncu on the 128^3 grid: 187.0 M issued against 155.8 M)
+POISSON_ISSUED_PER_COUNTED = 1.2006
 
 
 def poisson_counts(n, walls):
@@ -710,9 +720,8 @@ def run_fluid(args, device, stream, cpu=True):
                         "hbm_achieved_gbs": nint * FLUID_BYTES["guess"] / (guess_ms / 1e3) / 1e9,
                         "hbm_peak_gbs": hbm_peak, "hbm_peak_kind": peak_kind,
                         "fp64_ops_per_node": FLUID_GUESS_FP64,
-                        "fp64_ops_note": "the reference statement's FP64 operations; the kernel issues about 160 "
-                                         "(exact quarter scalings of the flux products, identity coefficients, "
-                                         "split-reciprocal divisions)",
+                        "fp64_ops_note": "FP64 instructions the kernel issues (ncu count); the reference's "
+                                         "statements have %d" % FLUID_GUESS_FP64_REF,
                         "fp64_achieved_gops": nint * FLUID_GUESS_FP64 / (guess_ms / 1e3) / 1e9,
                         "fp64_peak_gops": fp64_peak,
                         "fp64_frac": nint * FLUID_GUESS_FP64 / (guess_ms / 1e3) / 1e9 / fp64_peak if fp64_peak else None},
@@ -729,6 +738,11 @@ def run_fluid(args, device, stream, cpu=True):
         "roofline": {"bound": "fp64", "fp64_ops_per_solve": pops,
                      "fp64_achieved_gops": pops / (pois_ms / 1e3) / 1e9, "fp64_peak_gops": fp64_peak,
                      "fp64_frac": pops / (pois_ms / 1e3) / 1e9 / fp64_peak if fp64_peak else None,
+                     "fp64_issued_frac": pops * POISSON_ISSUED_PER_COUNTED / (pois_ms / 1e3) / 1e9 / fp64_peak
+                     if fp64_peak else None,
+                     "fp64_note": "fp64_frac counts the transforms' operations (poisson_counts); the kernels issue "
+                                  "%.2f times as many FP64 instructions (ncu, 128^3), fp64_issued_frac" %
+                                  POISSON_ISSUED_PER_COUNTED,
                      "hbm_bytes_per_solve": pb, "hbm_achieved_gbs": pb / (pois_ms / 1e3) / 1e9,
                      "hbm_peak_gbs": hbm_peak},
         "cpu_baseline": None,
