@@ -134,6 +134,33 @@ def test_batch_shared_launches_nonunit_spacing_and_substeps(gpu_lib):
         case.close()
 
 
+@pytest.mark.parametrize("fused", [False, True])
+def test_batch_with_an_empty_member(gpu_lib, fused):
+    """A member without parcels or bodies steps in a batch (with each member's
+    own forcing launches and with shared ones) and leaves its fluid as it was;
+    the other members are exactly as alone."""
+    from ibmdem.records import MULTISPHERE, PARCEL, make_params
+
+    p = make_params(16, 16, 16)
+    z = [np.zeros((20, 20, 20)) for _ in range(3)]
+    empty = (p, np.zeros(0, PARCEL), np.zeros(0, MULTISPHERE), z)
+    cs = [mixed_cases()[1], empty, mixed_cases()[2]]
+    steps = 2
+    ref = [alone(c, steps) for c in cs]
+    members = [make_case(c) for c in cs]
+    b = api.Batch(members)
+    b.set_fused(fused)
+    b.step(steps)
+    b.synchronize()
+    for case, r in zip(members, ref):
+        assert_same(snapshot(case), r)
+    parts, nl = members[1].get_parcels()
+    assert len(parts) == 0 and nl == 0
+    b.close()
+    for case in members:
+        case.close()
+
+
 def test_batch_shared_launches_fall_back_for_unequal_iterations(gpu_lib):
     """Members with different forcing iteration counts cannot share the
     launches: the batch keeps each member's own and the results stay exact."""
