@@ -48,7 +48,7 @@ def compare_parcels(a, b, nl, exact=True, fields_local=("x", "v", "fcol", "fdrag
 
 
 def rel_close(a, b, rtol=1e-9):
-    """max |a-b| <= rtol * max(|b|) per field (the spec relative tolerance)."""
+    """max |a-b| <= rtol * max(|b|) per field (the trajectory tolerance, 1e-9 by default)."""
     a = np.asarray(a, dtype=float)
     b = np.asarray(b, dtype=float)
     scale = max(np.abs(b).max(), 1e-300)

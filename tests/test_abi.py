@@ -83,7 +83,7 @@ def test_create_rejects_unsupported_parameters(oracle_mod):
     from ibmdem.records import make_params
 
     p = make_params(16, 16, 16)
-    p["bType"][2] = 1  # walls are not part of this build
+    p["bType"][2] = 1  # a wall on one face of an axis whose other face is periodic
     with pytest.raises(ValueError):
         oracle_mod.OracleCase(p)
     p = make_params(2, 16, 16)
