@@ -123,27 +123,87 @@ def config_of(workload, nparts):
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    """SM clock, power and clock-event reasons sampled during the timed region:
+    NVML through ctypes every 10 ms on the device whose PCI bus id CUDA reports
+    (so a short timed region still gets samples), or nvidia-smi every 200 ms
+    where NVML cannot be loaded.  Only reads; no setting is changed."""
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    # clock-event reason bits of nvml.h
+    REASONS = {"sw_power_cap": 0x4, "hw_slowdown": 0x8, "sw_thermal_slowdown": 0x20, "hw_thermal_slowdown": 0x40}
 
     def __init__(self, gpu_index):
         self.idx = gpu_index
         self.p = None
+        self.nvml = None
+        self.rows = []
+        self.source = None
+
+    def _nvml_open(self):
+        import ctypes
+        import threading
+
+        lib = ctypes.CDLL("libnvidia-ml.so.1")
+        if lib.nvmlInit_v2() != 0:
+            raise RuntimeError("nvmlInit failed")
+        dev = ctypes.c_void_p()
+        bus = None
+        try:
+            import torch
+
+            pr = torch.cuda.get_device_properties(self.idx)
+            bus = "%08x:%02x:%02x.0" % (pr.pci_domain_id, pr.pci_bus_id, pr.pci_device_id)
+        except Exception:
+            bus = None
+        if bus is None or lib.nvmlDeviceGetHandleByPciBusId_v2(bus.encode(), ctypes.byref(dev)) != 0:
+            if lib.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(self.idx), ctypes.byref(dev)) != 0:
+                lib.nvmlShutdown()
+                raise RuntimeError("no NVML handle")
+        reasons_fn = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            lib.nvmlDeviceGetCurrentClocksThrottleReasons
+        cmax = ctypes.c_uint()
+        lib.nvmlDeviceGetMaxClockInfo(dev, ctypes.c_int(1), ctypes.byref(cmax))
+        self.max_mhz = float(cmax.value)
+        self.stop = threading.Event()
+
+        def run():
+            clk, rs, pw = ctypes.c_uint(), ctypes.c_ulonglong(), ctypes.c_uint()
+            while not self.stop.is_set():
+                ok = lib.nvmlDeviceGetClockInfo(dev, ctypes.c_int(1), ctypes.byref(clk)) == 0
+                ok = ok and reasons_fn(dev, ctypes.byref(rs)) == 0
+                if lib.nvmlDeviceGetPowerUsage(dev, ctypes.byref(pw)) != 0:
+                    pw.value = 0
+                if ok:
+                    self.rows.append((float(clk.value), int(rs.value), pw.value / 1000.0))
+                self.stop.wait(0.01)
+
+        self.nvml = (lib, threading.Thread(target=run, daemon=True))
+        self.nvml[1].start()
+        self.source = "nvml, 10 ms"
 
     def __enter__(self):
         try:
-            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), "--query-gpu=" + self.Q,
-                                       "--format=csv,noheader,nounits", "-lms", "200"],
-                                      stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._nvml_open()
         except Exception:
-            self.p = None
+            self.nvml = None
+            try:
+                self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), "--query-gpu=" + self.Q,
+                                           "--format=csv,noheader,nounits", "-lms", "200"],
+                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                self.source = "nvidia-smi, 200 ms"
+            except Exception:
+                self.p = None
         return self
 
     def __exit__(self, *a):
         self.out = ""
+        if self.nvml:
+            lib, th = self.nvml
+            self.stop.set()
+            th.join(timeout=5)
+            lib.nvmlShutdown()
         if self.p:
             self.p.terminate()
             try:
@@ -152,6 +212,14 @@ class ClockSampler:
                 self.p.kill()
 
     def summary(self):
+        if self.nvml is not None:
+            if not self.rows:
+                return {"sm_mhz": None, "sm_max_mhz": self.max_mhz, "reasons": ["unsampled"], "samples": 0,
+                        "source": self.source}
+            reasons = sorted(n for n, bit in self.REASONS.items() if any(r[1] & bit for r in self.rows))
+            return {"sm_mhz": statistics.median(r[0] for r in self.rows), "sm_max_mhz": self.max_mhz,
+                    "sm_min_mhz": min(r[0] for r in self.rows), "reasons": reasons, "samples": len(self.rows),
+                    "power_w_max": max(r[2] for r in self.rows), "source": self.source}
         rows = []
         for line in (self.out or "").splitlines():
             f = [x.strip() for x in line.split(",")]
@@ -168,7 +236,8 @@ class ClockSampler:
                     reasons.add(n)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": float(rows[0][2]),
                 "reasons": sorted(reasons), "samples": len(rows),
-                "power_w_max": max(float(r[3]) for r in rows if r[3].replace(".", "").isdigit())}
+                "power_w_max": max(float(r[3]) for r in rows if r[3].replace(".", "").isdigit()),
+                "source": self.source}
 
 
 def cpu_baseline(case_data, steps):
@@ -954,6 +1023,8 @@ def run_ours(args):
             case.step(1)
         e1.record(stream)
         torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
     case.synchronize()
     ms = e0.elapsed_time(e1)
     launches = case.launches - launches0
