@@ -22,8 +22,11 @@ measured on, so that the code paths only large cases reach are compared too:
   within 1e-12; after the second step lists exact (or flips at the cut-off)
   and state within 1e-9.
 * 16 cases of the 256-case batched mix (grids up to 128^3, up to 512 bodies):
-  each member of a batch bit-identical to the case run alone, and each case's
-  first step against the restatement as above.
+  each member of a batch bit-identical to the case run alone, with each
+  member's own forcing launches and with shared ones, and each case's first
+  step against the restatement as above.
+* 128^3 between solid walls in z, 64 spheres of d = 16h with 4 against the low
+  wall, 20 steps, the same two checks.
 """
 import numpy as np
 import pytest
@@ -226,19 +229,38 @@ def test_config_batched_mix_16_cases(gpu_lib, oracle_mod):
         m = api.Case(p, parts, bodies, field, device=0)
         m.InitializationDEM()
         members.append(m)
-    b = api.Batch(members)
-    b.step(2)
-    b.synchronize()
-    for m, ((rp, rnl), rb, rf) in zip(members, ref):
-        gp, gnl = m.get_parcels()
-        assert gnl == rnl and len(gp) == len(rp)
-        for f in ("x", "v", "fcol", "fdrag", "vgap", "globalIdx", "MSIdx", "cellIdx"):
-            assert np.array_equal(gp[f], rp[f]), f
-        gb = m.get_bodies()
-        for f in ("x", "v", "omega", "AngMom", "rotMatGlo", "fcol", "fdrag", "fmom", "fmomCol"):
-            assert np.array_equal(gb[f], rb[f]), f
-        for x, y in zip(m.get_fluid(), rf):
-            assert np.array_equal(x, y)
-    b.close()
-    for m in members:
-        m.close()
+    # the batch with each member's own forcing launches, then with shared ones
+    for fused in (False, True):
+        if fused:
+            members = []
+            for p, parts, bodies, field in mix:
+                m = api.Case(p, parts, bodies, field, device=0)
+                m.InitializationDEM()
+                members.append(m)
+        b = api.Batch(members)
+        b.set_fused(fused)
+        b.step(2)
+        b.synchronize()
+        for m, ((rp, rnl), rb, rf) in zip(members, ref):
+            gp, gnl = m.get_parcels()
+            assert gnl == rnl and len(gp) == len(rp)
+            for f in ("x", "v", "fcol", "fdrag", "vgap", "globalIdx", "MSIdx", "cellIdx"):
+                assert np.array_equal(gp[f], rp[f]), (fused, f)
+            gb = m.get_bodies()
+            for f in ("x", "v", "omega", "AngMom", "rotMatGlo", "fcol", "fdrag", "fmom", "fmomCol"):
+                assert np.array_equal(gb[f], rb[f]), (fused, f)
+            for x, y in zip(m.get_fluid(), rf):
+                assert np.array_equal(x, y)
+        b.close()
+        for m in members:
+            m.close()
+
+
+def test_config_128cube_walled_64_spheres_20_steps(gpu_lib, oracle_mod):
+    """The 128^3 case between solid walls in z (x and y periodic), 4 of the 64
+    spheres resting against the low wall: wall contacts, mirror images across
+    the wall and the wall halo rules at the benchmark's grid size, lockstep and
+    free-running as above."""
+    case = scenario.walled_case(128, 128, 128, 64, 16.0, seed=1, walls="z", n_modes=32, touching=4)
+    stats = _run_resolved(gpu_lib, oracle_mod, case, 20)
+    assert stats["pairs"] > 0
