@@ -500,9 +500,23 @@ def run_served(args, device, stream):
         done = max(done, r["arrival"]) + sv
         plain_lat.append(done - r["arrival"])
     plain_span = done - plain_reqs[0]["arrival"]
+    # the same one-at-a-time service with the served arm's admission order:
+    # at each completion the arrived request with the fewest marker-steps
+    work = [len(r["case"][1]) * steps for r in plain_reqs]
+    t, left, plain_lat_lw = 0.0, list(range(len(plain_reqs))), []
+    while left:
+        arrived = [q for q in left if plain_reqs[q]["arrival"] <= t]
+        if not arrived:
+            t = min(plain_reqs[q]["arrival"] for q in left)
+            continue
+        q = min(arrived, key=lambda x: (work[x], x))
+        t += service[q]
+        plain_lat_lw.append(t - plain_reqs[q]["arrival"])
+        left.remove(q)
     plain_body_steps = sum(len(r["case"][2]) for r in plain_reqs) * steps
     # served
     srv = api.Server(budget, max_active=64, device=device, work_limit=args.serve_work_limit)
+    srv.set_policy(api.Server.LEAST_WORK)
     ids = []
     t0 = time.perf_counter()
     i = 0
@@ -534,6 +548,9 @@ def run_served(args, device, stream):
     return {"value": value, "unit": "particle-steps/s", "p50_s": percentile(lat, 50),
             "p99_s": percentile(lat, 99), "plain_value": plain_value,
             "plain_p50_s": percentile(plain_lat, 50), "plain_p99_s": percentile(plain_lat, 99),
+            "plain_least_work_p50_s": percentile(plain_lat_lw, 50), "plain_least_work_p99_s": percentile(plain_lat_lw, 99),
+            "policy": "least work (marker-steps) first among the queued requests that fit; plain_p50_s/p99 in "
+                      "arrival order, plain_least_work_* with the same order as the served arm",
             "ratio_vs_plain": value / plain_value, "requests": len(reqs), "plain_requests": len(plain_reqs),
             "plain_note": "plain value and latencies over the first plain_requests requests of the same stream",
             "failed": failed,

@@ -19,9 +19,10 @@
 // for the images and CloudEvolutionMS.  The autotuner also decides between the
 // two and picks the interpolation's block size.
 //
-// Server.  Requests wait in a first-in first-out queue and are admitted while
-// the summed device footprint of the running cases (ibmdem_case_bytes) stays
-// within the budget and fewer than max_active run.  An admitted case gets its
+// Server.  Requests wait in a queue and are admitted, in arrival order or
+// least work first (ibmdem_server_set_policy), while the summed device
+// footprint of the running cases (ibmdem_case_bytes) stays within the budget
+// and fewer than max_active run.  An admitted case gets its
 // own stream, its step captured once as a graph, and all of its steps queued
 // at admission; the device interleaves the running cases.  A case whose last
 // step has completed is read back and its memory returned to the pool in
@@ -345,6 +346,8 @@ struct ibmdem_server {
   long long inUse = 0;
   long long workLimit = 0;  // parcels in flight (0: no limit)
   long long workInUse = 0;
+  int policy = 0;          // 0: arrival order, 1: least work first
+  double ageLimit = 0.0;   // policy 1: a request queued this long (s) goes first (0: never)
   long long nextId = 1;
   std::deque<Request*> queue;
   std::vector<Request*> running;
@@ -730,13 +733,25 @@ int ibmdem_server_poll(ibmdem_server* s, int32_t* pending) {
     s->running[i] = s->running.back();
     s->running.pop_back();
   }
-  // admit in arrival order while the budget, the slots and the work limit
-  // allow (the work limit always lets one case run)
-  while (!s->queue.empty() && (int)s->running.size() < s->maxActive &&
-         s->inUse + s->queue.front()->bytes <= s->budget &&
-         (s->workLimit <= 0 || s->running.empty() || s->workInUse + s->queue.front()->np <= s->workLimit)) {
-    Request* r = s->queue.front();
-    s->queue.pop_front();
+  // admit while the budget, the slots and the work limit allow (the work
+  // limit always lets one case run): the oldest request, or under the
+  // least-work policy the one with the fewest marker-steps unless one has
+  // waited past the age limit (then the oldest of those)
+  while (!s->queue.empty() && (int)s->running.size() < s->maxActive) {
+    size_t pick = 0;
+    if (s->policy == 1) {
+      const double t = now_s();
+      const bool aged = s->ageLimit > 0.0 && t - s->queue.front()->tSubmit > s->ageLimit;
+      if (!aged)
+        for (size_t q = 1; q < s->queue.size(); ++q)
+          if ((long long)s->queue[q]->np * s->queue[q]->nsteps < (long long)s->queue[pick]->np * s->queue[pick]->nsteps)
+            pick = q;
+    }
+    Request* r = s->queue[pick];
+    if (s->inUse + r->bytes > s->budget ||
+        (s->workLimit > 0 && !s->running.empty() && s->workInUse + r->np > s->workLimit))
+      break;
+    s->queue.erase(s->queue.begin() + (long)pick);
     admit(s, r);
   }
   if (pending) *pending = (int32_t)(s->queue.size() + s->running.size());
@@ -791,6 +806,13 @@ int ibmdem_server_release(ibmdem_server* s, int64_t id) {
   }
   s->all.erase(it);
   delete r;
+  return IBMDEM_OK;
+}
+
+int ibmdem_server_set_policy(ibmdem_server* s, int32_t policy, double age_limit_s) {
+  if (!s || (policy != 0 && policy != 1) || !(age_limit_s >= 0.0)) return IBMDEM_EINVAL;
+  s->policy = policy;
+  s->ageLimit = age_limit_s;
   return IBMDEM_OK;
 }
 

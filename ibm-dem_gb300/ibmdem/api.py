@@ -37,7 +37,7 @@ EXPORTS = [
     "ibmdem_batch_set_lanes", "ibmdem_batch_step", "ibmdem_batch_synchronize", "ibmdem_batch_autotune",
     "ibmdem_server_create", "ibmdem_server_destroy", "ibmdem_server_last_error", "ibmdem_server_submit",
     "ibmdem_server_poll", "ibmdem_server_status", "ibmdem_server_result", "ibmdem_server_release",
-    "ibmdem_server_memory", "ibmdem_server_set_work_limit",
+    "ibmdem_server_memory", "ibmdem_server_set_work_limit", "ibmdem_server_set_policy",
     "ibmdem_unresolved_create", "ibmdem_unresolved_destroy", "ibmdem_unresolved_last_error",
     "ibmdem_unresolved_set_stream", "ibmdem_unresolved_set_fluid", "ibmdem_unresolved_set_particles",
     "ibmdem_unresolved_get_particles", "ibmdem_unresolved_get_volume_fraction", "ibmdem_unresolved_get_contacts",
@@ -147,6 +147,7 @@ def load(path=LIB_PATH):
     lib.ibmdem_server_release.argtypes = [vp, i64]
     lib.ibmdem_server_memory.argtypes = [vp, P(i64), P(i64)]
     lib.ibmdem_server_set_work_limit.argtypes = [vp, i64]
+    lib.ibmdem_server_set_policy.argtypes = [vp, i32, ctypes.c_double]
     lib.ibmdem_unresolved_create.argtypes = [vp, i32, P(vp)]
     lib.ibmdem_unresolved_destroy.argtypes = [vp]
     lib.ibmdem_unresolved_last_error.restype = ctypes.c_char_p
@@ -513,6 +514,7 @@ class Server:
     completion.  Input arrays are kept referenced until the request is admitted."""
 
     QUEUED, RUNNING, DONE = 0, 1, 2
+    ARRIVAL, LEAST_WORK = 0, 1
 
     def __init__(self, hbm_budget, max_active=64, device=0, work_limit=0):
         self.lib = load()
@@ -528,6 +530,11 @@ class Server:
     def _chk(self, rc, what):
         if rc != 0:
             raise IbmDemError(rc, f"{what}: {self.lib.ibmdem_server_last_error(self.h).decode()}")
+
+    def set_policy(self, policy, age_limit_s=0.0):
+        """Admission order: Server.ARRIVAL or Server.LEAST_WORK (fewest marker-steps
+        first, the oldest first again once one has waited age_limit_s > 0)."""
+        self._chk(self.lib.ibmdem_server_set_policy(self.h, int(policy), float(age_limit_s)), "server_set_policy")
 
     def submit(self, params, parcels, bodies, field=None, nsteps=100, keep_parcels=False):
         p = np.array(params, dtype=PARAMS, copy=True)

@@ -394,8 +394,9 @@ int ibmdem_batch_get_config(const ibmdem_batch* b, int32_t* lanes, int32_t* fuse
  * *lanes_out.  The trials advance every member. */
 int ibmdem_batch_autotune(ibmdem_batch* b, int32_t trial_steps, int32_t* lanes_out);
 
-/* A request server on one device.  Requests wait first-in first-out and are
- * admitted while the running cases' summed ibmdem_case_bytes stays within
+/* A request server on one device.  Requests wait in a queue (arrival order by
+ * default, ibmdem_server_set_policy) and are admitted while the running
+ * cases' summed ibmdem_case_bytes stays within
  * hbm_budget and fewer than max_active run.  An admitted case is created on
  * its own stream, initialised, its step captured as a graph and all of its
  * nsteps frozen-fluid steps queued at once, so requests admitted at different
@@ -425,6 +426,12 @@ int ibmdem_server_memory(const ibmdem_server* s, int64_t* in_use, int64_t* budge
  * total (one case always runs; 0 = no limit): bounds the work that shares the
  * device, so that early requests finish early under load. */
 int ibmdem_server_set_work_limit(ibmdem_server* s, int64_t parcels);
+/* Admission order: policy 0 = arrival order (the default), 1 = least work first
+ * (the queued request with the fewest marker-steps, np * nsteps, that fits),
+ * except that once the oldest queued request has waited more than age_limit_s
+ * seconds (> 0) the oldest go first again, so no request starves.  Either way
+ * a request is admitted only when it fits the budget and the work limit. */
+int ibmdem_server_set_policy(ibmdem_server* s, int32_t policy, double age_limit_s);
 
 /* ---- output files ------------------------------------------------------ */
 /* OutputCloudTecplot (ZJS_IO_DEM.F90:82-121): the header lines

@@ -211,6 +211,33 @@ def test_batch_autotune_and_recapture(gpu_lib):
         case.close()
 
 
+@pytest.mark.parametrize("policy", ["arrival", "least_work"])
+def test_server_admission_order(gpu_lib, policy):
+    """One case at a time (max_active 1), requests submitted largest first:
+    in arrival order they run in that order, under the least-work policy the
+    smallest runs first; the results are exactly as alone either way."""
+    cs = mixed_cases()
+    steps = 2
+    ref = [alone(c, steps) for c in cs]
+    order = sorted(range(len(cs)), key=lambda i: -len(cs[i][1]))
+    srv = api.Server(10 ** 11, max_active=1)
+    if policy == "least_work":
+        srv.set_policy(api.Server.LEAST_WORK)
+    ids = {i: srv.submit(cs[i][0], cs[i][1], cs[i][2], cs[i][3], nsteps=steps, keep_parcels=True) for i in order}
+    for _ in range(200000):
+        if srv.poll() == 0:
+            break
+    queued = {i: srv.state(ids[i])[2] for i in order}
+    run_order = sorted(order, key=lambda i: queued[i])
+    expect = order if policy == "arrival" else sorted(order, key=lambda i: len(cs[i][1]))
+    assert run_order == expect
+    for i in order:
+        parts, nl, bodies = srv.result(ids[i])
+        assert_same((parts, nl, bodies, None), ref[i], fields=False)
+        srv.release(ids[i])
+    srv.close()
+
+
 def test_server_results_match_alone_under_overlap(gpu_lib):
     cs = mixed_cases()
     steps = 4
