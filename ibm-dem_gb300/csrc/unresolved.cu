@@ -5,9 +5,11 @@
 //
 // Data layout: particle state is field-major (one array per scalar field,
 // np long); contact history is particle-major with maxContacts slots per
-// particle, double-buffered between steps.  Two stable radix sorts per step
-// give the DEM cell lists (contacts) and the fluid cell lists (volume
-// fraction); both gathers then walk particles in part order within a cell.
+// particle, double-buffered between steps.  Two cell lists per step, the DEM
+// cells (contacts) and the fluid cells (volume fraction), each in part order
+// within a cell (slots from the count atomics, a scatter and a per-cell order
+// fix-up: the order a stable sort gives); both gathers then walk particles in
+// part order within a cell.
 //
 // Every sum has a fixed order, so results do not depend on scheduling:
 //   fcol, tcol  over the 27 neighbour DEM cells (z outermost, periodic) and,
