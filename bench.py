@@ -52,7 +52,7 @@ METRIC = "particle-steps/s (contact+IBM) on 1 GB300, batched vs plain; p50/p99 s
 # DRAM bytes (read + write) per local marker and launch of the main kernels, from
 # one ncu capture of the 512-sphere 256^3 case; the benchmark workload has the
 # same per-marker structure, so traffic scales with markers.
-DRAM_BYTES_PER_MARKER = {"interp": 1189.0, "spread": 1781.0, "weights": 477.0}
+DRAM_BYTES_PER_MARKER = {"interp": 1189.0, "spread": 1781.0, "weights": 530.0}
 
 
 def max_over_ranks(x):
