@@ -521,6 +521,8 @@ int ibmdem_destroy(ibmdem_ctx* h) {
   if (!h) return IBMDEM_EINVAL;
   Ctx& c = h->c;
   cudaSetDevice(c.device);
+  if (c.stepBatch) ibmdem_batch_destroy(static_cast<ibmdem_batch*>(c.stepBatch));
+  c.stepBatch = nullptr;
   output_release(c);
   fluid_update_release(c);
   fluid_release(c);
@@ -1364,8 +1366,39 @@ int ibmdem_CloudEvolutionMS(ibmdem_ctx* h) {
   return launch_status(h);
 }
 
+int ibmdem_set_step_graphs(ibmdem_ctx* h, int32_t on) {
+  CHECK_CTX();
+  if (on != 0 && on != 1) return set_error(h, IBMDEM_EINVAL, "step graphs: 0 or 1");
+  h->c.stepGraphs = on != 0;
+  return IBMDEM_OK;
+}
+
 int ibmdem_step(ibmdem_ctx* h, int32_t nsteps) {
   CHECK_CTX();
+  Ctx& c = h->c;
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  cudaStreamIsCapturing(c.stream, &cap);
+  if (nsteps > 0 && c.stepGraphs && !c.timing && cap == cudaStreamCaptureStatusNone) {
+    // the steps as replays of one captured graph (a batch of this case alone):
+    // the same kernels, one launch per step instead of some eighty; a step
+    // captured inside someone else's capture, or with phase timing on, takes
+    // the stream path below
+    ibmdem_batch* b = static_cast<ibmdem_batch*>(c.stepBatch);
+    if (!b) {
+      int rc = ibmdem_batch_create(c.device, &b);
+      if (rc) return set_error(h, rc, "step graph: no batch");
+      rc = ibmdem_batch_add(b, h);
+      if (!rc) rc = ibmdem_batch_set_lanes(b, 1);
+      if (rc) {
+        ibmdem_batch_destroy(b);
+        return set_error(h, rc, "step graph: batch set-up failed");
+      }
+      c.stepBatch = b;
+    }
+    const int rc = ibmdem_batch_step(b, nsteps);
+    if (rc) return set_error(h, rc, "step graph: %s", ibmdem_batch_last_error(b));
+    return launch_status(h);
+  }
   for (int s = 0; s < nsteps; ++s) {
     int rc = mdf(h, true);
     if (rc) return rc;

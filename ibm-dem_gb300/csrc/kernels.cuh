@@ -127,6 +127,10 @@ struct Ctx {
 
   // per-phase CUDA-event timing (ibmdem_timing_enable)
   bool timing = false;
+  // ibmdem_step replays one captured graph per step (a one-member batch,
+  // created on first use) unless stepGraphs is off or phases are being timed
+  bool stepGraphs = true;
+  void* stepBatch = nullptr;  // ibmdem_batch*
   struct Span {
     int phase;
     cudaEvent_t a, b;

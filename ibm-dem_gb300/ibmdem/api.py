@@ -47,7 +47,7 @@ EXPORTS = [
     "ibmdem_set_fluid_async", "ibmdem_set_fluid_params", "ibmdem_set_fluid_field", "ibmdem_get_fluid_field", "ibmdem_StoreOldVelocity",
     "ibmdem_VelocityGuess", "ibmdem_FillGhostRegionForFluid", "ibmdem_Boundary", "ibmdem_ModifyBulkVelocity",
     "ibmdem_VelocityDivergence", "ibmdem_PressureCorrection", "ibmdem_VelocityCorrection", "ibmdem_PoissonSolver",
-    "ibmdem_set_friction", "ibmdem_get_friction_history", "ibmdem_batch_set_fused", "ibmdem_batch_get_config",
+    "ibmdem_set_friction", "ibmdem_get_friction_history", "ibmdem_batch_set_fused", "ibmdem_batch_get_config", "ibmdem_set_step_graphs",
 ]
 
 SUBROUTINES = [
@@ -135,6 +135,7 @@ def load(path=LIB_PATH):
     lib.ibmdem_batch_synchronize.argtypes = [vp, P(i32)]
     lib.ibmdem_batch_autotune.argtypes = [vp, i32, P(i32)]
     lib.ibmdem_batch_set_fused.argtypes = [vp, i32, i32]
+    lib.ibmdem_set_step_graphs.argtypes = [vp, i32]
     lib.ibmdem_batch_get_config.argtypes = [vp, P(i32), P(i32), P(i32)]
     lib.ibmdem_server_create.argtypes = [i32, i64, i32, P(vp)]
     lib.ibmdem_server_destroy.argtypes = [vp]
@@ -398,6 +399,10 @@ class Case:
 
     def step(self, n=1):
         self._chk(self.lib.ibmdem_step(self.h, int(n)), "step")
+
+    def set_step_graphs(self, on):
+        """ibmdem_step as replays of a captured graph (True, the default) or kernel by kernel."""
+        self._chk(self.lib.ibmdem_set_step_graphs(self.h, int(bool(on))), "set_step_graphs")
 
 
 def _make_method(name):

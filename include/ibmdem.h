@@ -248,8 +248,17 @@ int ibmdem_CloudEvolutionStepMS(ibmdem_ctx* ctx);
 /* couplesolverCylinder.F90:189-217. */
 int ibmdem_CloudEvolutionMS(ibmdem_ctx* ctx);
 /* `nsteps` frozen-fluid steps: restore the fluid set by ibmdem_set_fluid,
- * then ibmdem_MultiDirectForcing + ibmdem_CloudEvolutionMS. */
+ * then ibmdem_MultiDirectForcing + ibmdem_CloudEvolutionMS.  The step's
+ * kernels are captured once into a CUDA graph that every step replays (one
+ * launch instead of about eighty; captured again when the case's state
+ * changes), ordered after the work already on the context's stream and before
+ * the work issued on it later; results are the same as issuing the kernels one
+ * by one, which happens when step graphs are off, with phase timing on, or
+ * when the context's stream is itself being captured. */
 int ibmdem_step(ibmdem_ctx* ctx, int32_t nsteps);
+/* on = 1 (the default): ibmdem_step replays a captured graph; 0: it issues each
+ * kernel on the context's stream.  No counterpart in the reference. */
+int ibmdem_set_step_graphs(ibmdem_ctx* ctx, int32_t on);
 
 /* Fluid velocity interpolated at n caller-given points from the context's
  * resident u, v, w: for each point the ulp that

@@ -140,3 +140,33 @@ def test_async_fluid_readout_matches_sync(gpu_lib):
     for a, b in zip(out, ref):
         assert np.array_equal(a, b)
     case.close()
+
+
+def test_step_graph_matches_kernel_by_kernel(gpu_lib):
+    """ibmdem_step as replays of its captured graph (the default) and kernel by
+    kernel on the context's stream give the same parcels, bodies and fields; a
+    change of the parcels between steps makes the graph be captured again."""
+    out = []
+    for graphs in (True, False):
+        p, parts, bodies, field = cases.contact_case(seed=9, coupleInterval=2)
+        c = gpu_lib.Case(p, parts, bodies, field, device=0)
+        c.set_step_graphs(graphs)
+        c.InitializationDEM()
+        c.step(3)
+        # new parcels (the same ones again) in the middle of the run
+        gp, nl = c.get_parcels()
+        c.set_parcels(gp[:nl].copy())
+        c.InitializationDEM()
+        c.step(2)
+        out.append((c.get_parcels(), c.get_bodies(), c.get_fluid(), c.launches))
+        c.close()
+    (pa, nla), ba, fa, la = out[0]
+    (pb, nlb), bb, fb, lb = out[1]
+    assert nla == nlb and len(pa) == len(pb)
+    for f in ("x", "v", "fcol", "fdrag", "vgap", "globalIdx", "MSIdx", "cellIdx"):
+        assert np.array_equal(pa[f], pb[f]), f
+    for f in ("x", "v", "omega", "AngMom", "rotMatGlo", "fcol", "fdrag", "fmom", "fmomCol"):
+        assert np.array_equal(ba[f], bb[f]), f
+    for x, y in zip(fa, fb):
+        assert np.array_equal(x, y)
+    assert la == lb  # the graph counts the kernels it replays
