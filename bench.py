@@ -412,10 +412,12 @@ def percentile(xs, q):
 
 def run_batched(args, device, stream):
     """Batched mix (256 independent cases of uneven size): the plain path
-    advances the cases one after another, kernel by kernel, on one stream; the
-    batched path advances all of them with one CUDA graph launch per step, the
-    chain count picked by the autotuner.  Both time the same steps of the same
-    cases, host launch overhead included (wall clock, synchronised)."""
+    advances the cases one after another with ibmdem_step (each case's step a
+    replay of its own captured graph, the library's default); the batched path
+    advances all of them with one CUDA graph launch per step, its shape picked
+    by the autotuner.  Both time the same steps of the same cases, host launch
+    overhead included (wall clock, synchronised).  The plain path kernel by
+    kernel (step graphs off) is timed too, over batch_steps // 5 steps."""
     import torch
     from ibmdem import api, scenario
 
@@ -439,7 +441,18 @@ def run_batched(args, device, stream):
     torch.cuda.synchronize()
     plain_s = time.perf_counter() - t0
     plain_launch = sum(c.launches for c in cases) - l0
+    # the same cases kernel by kernel on their stream (step graphs off)
+    kk = max(1, k // 5)
     for c in cases:
+        c.set_step_graphs(False)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for c in cases:
+        c.step(kk)
+    torch.cuda.synchronize()
+    plain_kbk_s = time.perf_counter() - t0
+    for c in cases:
+        c.set_step_graphs(True)
         c.synchronize()
     b = api.Batch(cases, device=device)
     lanes = b.autotune(trial_steps=2)
@@ -459,6 +472,8 @@ def run_batched(args, device, stream):
         c.close()
     return {"value": nbodies * k / batch_s, "unit": "particle-steps/s", "plain_value": nbodies * k / plain_s,
             "ratio_vs_plain": plain_s / batch_s, "steps": k, "cases": len(cases), "bodies": nbodies,
+            "plain_kernel_by_kernel_value": nbodies * kk / plain_kbk_s,
+            "ratio_vs_plain_kernel_by_kernel": (plain_kbk_s / kk) / (batch_s / k),
             "markers": nmark, "lanes": lanes, "shared_forcing_launches": bool(fused), "interp_block": interp_block,
             "ms_per_step": batch_s / k * 1e3, "plain_ms_per_step": plain_s / k * 1e3,
             "gpu_launches": batch_launch, "plain_gpu_launches": plain_launch, "graph_launches": k,
