@@ -1,0 +1,447 @@
+"""Golden fixtures from the reference's own subroutines (tests/golden/ref_*.npz).
+
+The reference's Fortran is read from the source directory given on the command
+line and executed through fortran_subset.py on one MPI rank.  Each case is
+advanced by the reference's particle-side subroutines, and the state after
+every stage is stored: parcels, bodies, the fluid fields, the per-cell parcel
+lists and the contact lists.  tests/test_reference_pins.py replays the same
+stages on the C restatement in oracle/ (bit for bit) and
+tests/test_gpu_reference_pins.py on the CUDA library.
+
+What the harness supplies instead of the reference (each a configuration the
+reference hard-codes or a step it takes on several ranks only):
+  * the case: grid size, boundary types (SetBoundaryType,
+    initialization.F90:317-351, fixes them), dt and rhof (GridInitialization),
+    knCoeff, ResistCoeff and coupleInterval (InitParameters), collisionDist,
+    the parcels, bodies and wall probes (InitCylinderParcelsDEM and
+    SetWallProbe, ZJS_INIT_DEM.F90:369-509), all set in the reference's module
+    variables after the routine that would have set them;
+  * the multi-rank body exchange: on one rank CloudEvolutionStepMS integrates
+    only body 1 (couplesolverCylinder.F90:114-121,130), so the harness runs its
+    multi-rank branch, with the two steps that ranks exchange for replaced by
+    their one-rank result: AssembleForceMS is AssembleLocalForceMS followed by
+    its own copy from MSGlo into MS (ZJS_MS_DEM.F90:417-422), and
+    UpdateMSInfoInGhostRegion is its own copy from MS into MSGlo
+    (ZJS_MS_DEM.F90:165-167);
+  * the frozen fluid: each step starts from the case's u, v, w (halo refilled
+    by FillGhostRegionForFluid and Boundary), then runs the forcing loop of
+    FirstOrderForwardEuler (fluid.F90:256-280) and CloudEvolutionMS.
+Bodies never straddle a periodic face in these cases: there the reference's
+raw body-relative vector and the nearest-image one of the library agree.
+
+Usage: python tests/golden/make_reference_golden.py <reference source dir>
+"""
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(HERE)), "ibm-dem_gb300"))
+
+import fortran_subset as fs  # noqa: E402
+from ibmdem import scenario  # noqa: E402
+from ibmdem.records import MULTISPHERE, PARCEL, WALL_PROBE, field_shape, make_params  # noqa: E402
+
+# the makefile's sources, less the main program, the PETSc Poisson solve and the output routines
+SOURCES = ["vars.F90", "ZJS_VARS.F90", "boundary.F90", "initialization.F90", "allocate.F90", "fluid.F90",
+           "interpolation.F90", "ZJS_AUXILIARY_DEM.F90", "ZJS_COLLISION_DEM.F90", "ZJS_DRAGFORCE_DEM.F90",
+           "ZJS_EVOLUTION_DEM.F90", "ZJS_INIT_DEM.F90", "ZJS_INTERPOLATE_DEM.F90", "ZJS_MPI_DEM.F90",
+           "ZJS_UPDATE_LIST_DEM.F90", "ZJS_VOLUMEFRACTION_DEM.F90", "ZJS_MS_DEM.F90",
+           "couplesolverCylinder.F90"]
+# maxPartNo sizes neighCellWeight(125, maxPartNo, 3): 100000 would take 300 MB for cases of a few thousand
+CAPACITIES = {"maxpartno": 8000}
+
+
+def load_sources(ref_dir):
+    return [(f, open(os.path.join(ref_dir, f)).read()) for f in SOURCES]
+
+
+class ReferenceCase:
+    """One case held by the reference's translated subroutines."""
+
+    def __init__(self, sources, p, parts, bodies, field, probes=None):
+        self.p = p
+        self.T = fs.Translator(sources, CAPACITIES)
+        self.T.build(overrides={"setboundarytype": self._set_boundary_type,
+                                "assembleforcems": self._assemble_force_ms,
+                                "cloudevolutionstepms": self._cloud_evolution_step_ms})
+        self.G = G = self.T.new_state()
+        c = self.call
+        n = [int(p["nx"]), int(p["ny"]), int(p["nz"])]
+        h = [float(p["dx"]), float(p["dy"]), float(p["dz"])]
+        assert float(p["collisionBuffer"]) == 0.1, "collisionBuffer is a parameter of the reference"
+        assert list(p["gravity"]) == [0.0, 0.0, -9.81], "the reference's gravity"
+        c("PartitionInitialization", 1, 1, 1, n[0], n[1], n[2], n[0] * h[0], n[1] * h[1], n[2] * h[2])
+        assert (G.m_dx, G.m_dy, G.m_dz) == tuple(h), "grid spacing"
+        c("GridInitialization")
+        G.m_dt, G.m_rhof = float(p["dt"]), float(p["rhof"])
+        c("SetCellIndexMap")
+        c("BuildMPIRecvAndSendIndexForFluid")
+        # InitializationDEM (ZJS_INIT_DEM.F90:2-37), the case in place of InitCylinderParcelsDEM
+        c("InitParameters")
+        G.m_kncoeff, G.m_resistcoeff = float(p["knCoeff"]), float(p["ResistCoeff"])
+        G.m_coupleinterval = int(p["coupleInterval"])
+        G.m_dtdem = G.m_dt / G.m_coupleinterval
+        for name in ("CopyGridInformationDEM", "AllocateDEM", "SetCellType", "SetCellIndexMapDEM",
+                     "SetNeighCellIndexForCellsDEM", "SetBoundaryNormsAndPoints", "SetMirrorAndShiftCoords"):
+            c(name)
+        G.m_collisiondist = float(p["collisionDist"])
+        self._load_parcels(parts)
+        self._load_bodies(bodies)
+        G.m_nppartincell.a[:] = 0
+        c("PutParcelsIntoCellsDEM", 1, G.m_np, 0)
+        self._load_probes(probes)
+        self.set_field(field)
+        self.u0 = [G.m_u.a.copy(), G.m_v.a.copy(), G.m_w.a.copy()]
+        for name in ("RebuildParcelInCellListDEM", "RebuildParcelCollisionListDEM",
+                     "RebuildNeighborCellListForParcelsDEM", "UpdateLocalCellWeightListDEM",
+                     "UpdateParcelInfoInGhostRegion", "UpdateGhostCellWeightListDEM"):
+            c(name)
+
+    def call(self, name, *args):
+        return self.T.call(self.G, name, *args)
+
+    # harness replacements ---------------------------------------------------
+    def _set_boundary_type(self, G):
+        bt = [int(b) for b in self.p["bType"]]
+        G.m_bw, G.m_be, G.m_bb, G.m_bf, G.m_bs, G.m_bn = bt
+        G.m_bwg, G.m_beg, G.m_bbg, G.m_bfg, G.m_bsg, G.m_bng = bt
+        G.m_btype.a[:] = bt
+        return ()
+
+    def _assemble_force_ms(self, G):
+        self.call("AssembleLocalForceMS")
+        for i in range(G.m_nmslocal):
+            g = int(G.m_ms.a["globalidx"][i]) - 1
+            for f in ("fcol", "fmom", "fmomcol", "fdrag"):
+                G.m_ms.a[f][i] = G.m_msglo.a[f][g]
+        return ()
+
+    def _cloud_evolution_step_ms(self, G):
+        c = self.call
+        c("CalculateCollisionForce")
+        c("CalculateSolidBoundaryCollisionForce")
+        c("AssembleForceMS")
+        c("EvolutionMS")
+        for i in range(G.m_nms):
+            G.m_msglo.a[int(G.m_ms.a["globalidx"][i]) - 1] = G.m_ms.a[i]
+        for name in ("ResetVelocityAndPositionLagrangianPoints", "AdjustParcelPosition",
+                     "UpdateParcelInfoInGhostRegion", "RebuildAllListOrNot", "UpdateLocalCellWeightListDEM",
+                     "UpdateParcelInfoInGhostRegion", "UpdateGhostCellWeightListDEM"):
+            c(name)
+        return ()
+
+    # state in and out -------------------------------------------------------
+    def _load_parcels(self, parts):
+        G = self.G
+        n = len(parts)
+        for f in PARCEL.names:
+            if f != "pad_":
+                G.m_part.a[f.lower()][:n] = parts[f]
+        G.m_np = G.m_nplocal = n
+
+    def _load_bodies(self, bodies):
+        G = self.G
+        n = len(bodies)
+        for f in MULTISPHERE.names:
+            G.m_ms.a[f.lower()][:n] = bodies[f]
+            G.m_msglo.a[f.lower()][:n] = bodies[f]
+        G.m_nms = G.m_nmslocal = G.m_nmsglo = n
+
+    def _load_probes(self, probes):
+        G = self.G
+        G.m_numwallprobe.a[:] = 0
+        if probes is None:
+            return
+        for pr in probes:
+            face = int(pr["face"])
+            G.m_numwallprobe.a[face - 1] += 1
+            k = int(G.m_numwallprobe.a[face - 1]) - 1
+            G.m_wallprobe.a["points"][k, face - 1] = np.asarray(pr["points"]).T
+            G.m_wallprobe.a["force"][k, face - 1] = 0.0
+
+    def set_field(self, field):
+        G = self.G
+        for arr, f in zip((G.m_u, G.m_v, G.m_w), field):
+            arr.a[...] = np.asarray(f, dtype=np.float64).reshape(field_shape(self.p)).T
+        self.call("FillGhostRegionForFluid")
+        self.call("Boundary")
+
+    def parcels(self):
+        G = self.G
+        out = np.zeros(G.m_np, PARCEL)
+        for f in PARCEL.names:
+            if f != "pad_":
+                out[f] = G.m_part.a[f.lower()][:G.m_np]
+        return out
+
+    def bodies(self):
+        G = self.G
+        out = np.zeros(G.m_nms, MULTISPHERE)
+        for f in MULTISPHERE.names:
+            out[f] = G.m_ms.a[f.lower()][:G.m_nms]
+        return out
+
+    def fields(self):
+        G = self.G
+        return [a.a.T.copy() for a in (G.m_u, G.m_v, G.m_w, G.m_fx, G.m_fy, G.m_fz)]
+
+    def cell_lists(self):
+        """CSR over the haloed grid's cells in 1D index order; 1-based parcel indices."""
+        G = self.G
+        cnt = G.m_nppartincell.a.astype(np.int64)
+        start = np.zeros(len(cnt) + 1, np.int64)
+        np.cumsum(cnt, out=start[1:])
+        items = np.concatenate([G.m_partidxincell.a[:c, k] for k, c in enumerate(cnt)]) if cnt.sum() else \
+            np.zeros(0, np.int32)
+        return start.astype(np.int32), items.astype(np.int32)
+
+    def collision_lists(self):
+        G = self.G
+        nl = G.m_nplocal
+        cnt = G.m_neighpartno.a[:nl].astype(np.int64)
+        start = np.zeros(nl + 1, np.int64)
+        np.cumsum(cnt, out=start[1:])
+        items = np.concatenate([G.m_neighpartidx.a[:c, k] for k, c in enumerate(cnt)]) if cnt.sum() else \
+            np.zeros(0, np.int32)
+        return start.astype(np.int32), items.astype(np.int32)
+
+    def probe_forces(self):
+        G = self.G
+        out = []
+        for face in range(6):
+            for k in range(int(G.m_numwallprobe.a[face])):
+                out.append(G.m_wallprobe.a["force"][k, face].copy())
+        return np.array(out).reshape(-1, 3)
+
+    # the coupled step on a frozen fluid ----------------------------------------
+    def multi_direct_forcing(self):
+        """The forcing loop of FirstOrderForwardEuler (fluid.F90:258-280)."""
+        G = self.G
+        for a, a0 in zip((G.m_u, G.m_v, G.m_w), self.u0):
+            a.a[...] = a0
+        G.m_part.a["fdrag"][:G.m_nplocal] = 0.0
+        G.m_fx.a[...] = 0.0
+        G.m_fy.a[...] = 0.0
+        G.m_fz.a[...] = 0.0
+        for _ in range(int(self.p["Ns"])):
+            for name in ("UpdateFluidVelocityOnLagrangianPoints", "UpdateParcelInfoInGhostRegion",
+                         "UpdateMomentumSourceTerm", "VelocityPostGuess", "FillGhostRegionForFluid", "Boundary"):
+                self.call(name)
+
+    def cloud_evolution(self):
+        self.call("CloudEvolutionMS")
+
+    def weights(self):
+        """Every parcel's window cells and delta weights, as (np, 125[, 3]),
+        zero past its neighCellNo entries."""
+        G = self.G
+        n = G.m_np
+        cnt = G.m_neighcellno.a[:n]
+        used = np.arange(125)[None, :] < cnt[:, None]
+        cells = np.where(used, G.m_neighcellidx.a[:, :n].T, 0).astype(np.int32)
+        w = np.where(used[..., None], G.m_neighcellweight.a[:, :n, :].transpose(1, 0, 2), 0.0)
+        return cnt.astype(np.int32), cells, np.ascontiguousarray(w)
+
+    def snapshot(self):
+        s = {"parcels": self.parcels(), "nlocal": np.int32(self.G.m_nplocal), "bodies": self.bodies()}
+        s["cell_start"], s["cell_items"] = self.cell_lists()
+        s["pair_start"], s["pair_items"] = self.collision_lists()
+        s["probe_force"] = self.probe_forces()
+        cnt, cells, w = self.weights()
+        s["window_count"] = cnt
+        s["window_digest"] = digest(cells, w)
+        return s
+
+
+class ReferenceFluid:
+    """The reference's fluid stencils on one rank (fluid.F90, boundary.F90)."""
+
+    def __init__(self, sources, p, visc):
+        self.p = p
+        self.T = fs.Translator(sources, CAPACITIES)
+        self.T.build(overrides={"setboundarytype": lambda G: ReferenceCase._set_boundary_type(self, G)})
+        self.G = G = self.T.new_state()
+        n = [int(p["nx"]), int(p["ny"]), int(p["nz"])]
+        h = [float(p["dx"]), float(p["dy"]), float(p["dz"])]
+        self.call("PartitionInitialization", 1, 1, 1, n[0], n[1], n[2], n[0] * h[0], n[1] * h[1], n[2] * h[2])
+        self.call("GridInitialization")
+        G.m_dt, G.m_rhof, G.m_visc = float(p["dt"]), float(p["rhof"]), float(visc)
+        self.call("SetCellIndexMap")
+        self.call("BuildMPIRecvAndSendIndexForFluid")
+
+    def call(self, name, *args):
+        return self.T.call(self.G, name, *args)
+
+    def set(self, name, a):
+        getattr(self.G, "m_" + name.lower()).a[...] = np.asarray(a, dtype=np.float64).reshape(
+            field_shape(self.p)).T
+
+    def get(self, name):
+        return getattr(self.G, "m_" + name.lower()).a.T.copy()
+
+
+# the fluid step of FirstOrderForwardEuler after the forcing loop (fluid.F90:256,281-324), the Poisson
+# solve (SetPressureVector, PoissonSolver) replaced by a given pressure correction; each stage with the
+# fields it writes
+FLUID_STAGES = [
+    ("guess", [("StoreOldVelocity",), ("VelocityGuess", 1.0, 0.0, 1.0), ("FillGhostRegionForFluid",),
+               ("Boundary",)], ["u", "v", "w", "uold", "vold", "wold", "RHSul", "RHSvl", "RHSwl", "Px", "Py", "Pz"]),
+    ("bulk", [("ModifyBulkVelocity",), ("FillGhostRegionForFluid",), ("Boundary",)], ["u", "v", "w"]),
+    ("divergence", [("VelocityDivergence", 1.0), ("FillGhostRegionForFluid",), ("Boundary",)], ["velDiv"]),
+    ("pressure", [("PressureCorrection",), ("FillGhostRegionForFluid",), ("Boundary",)], ["P", "Pcorr"]),
+    ("correction", [("VelocityCorrection", 1.0), ("FillGhostRegionForFluid",), ("Boundary",)],
+     ["u", "v", "w", "omegaX", "omegaY", "omegaZ"]),
+]
+FLUID_INPUTS = ["u", "v", "w", "fx", "fy", "fz", "P", "Pcorr", "RHSul", "RHSvl", "RHSwl"]
+
+
+def run_fluid(sources, name, p, visc, seed):
+    """Random fields through FLUID_STAGES; the digest of every written field after every stage."""
+    import hashlib
+    rng = np.random.default_rng(seed)
+    R = ReferenceFluid(sources, p, visc)
+    out = {"params": np.asarray(p), "visc": np.float64(visc)}
+    for f in FLUID_INPUTS:
+        a = rng.standard_normal(field_shape(p)) * (1e3 if f in ("P", "Pcorr") else 0.1)
+        out["in_" + f] = a
+        R.set(f, a)
+    # the bulk-velocity switches and targets GridInitialization sets (initialization.F90:262-264)
+    G = R.G
+    out["bulk"] = np.array([G.m_defavebulkuswitch, G.m_defavebulkvswitch, G.m_defavebulkwswitch,
+                            G.m_bulku, G.m_bulkv, G.m_bulkw], dtype=np.float64)
+    for stage, calls, written in FLUID_STAGES:
+        for c in calls:
+            if c[0] == "StoreOldVelocity":
+                for a in "uvw":
+                    getattr(G, f"m_{a}old").a[...] = getattr(G, f"m_{a}").a
+                continue
+            R.call(*c)
+        for f in written:
+            out[f"{stage}_{f}"] = np.frombuffer(hashlib.sha256(R.get(f).tobytes()).digest(), np.uint8)
+    print(f"{name}: fluid stages done", flush=True)
+    return out
+
+
+def digest(*arrays):
+    """SHA-256 of the arrays' bytes, in order."""
+    import hashlib
+    h = hashlib.sha256()
+    for a in arrays:
+        h.update(np.ascontiguousarray(a).tobytes())
+    return np.frombuffer(h.digest(), np.uint8)
+
+
+def run_drag(sources, seed, n=400):
+    """CalculateDragForce (ZJS_DRAGFORCE_DEM.F90:2-35) on random parcels and
+    fluid states covering both Reynolds-number branches, the Rep >= 1 clamp and
+    both voidage branches."""
+    rng = np.random.default_rng(seed)
+    T = fs.Translator(sources, CAPACITIES)
+    T.build()
+    G = T.new_state()
+    rho = rng.uniform(500.0, 3000.0, n)
+    rad = 10.0 ** rng.uniform(-5.0, -2.0, n)
+    vp = rng.standard_normal((n, 3)) * 10.0 ** rng.uniform(-4.0, 0.5, (n, 1))
+    denf = rng.uniform(800.0, 1200.0, n)
+    alphaf = rng.uniform(0.3, 1.0, n)
+    alphaf[:20] = np.float32(0.8)  # at the single-precision literal of the voidage branch
+    velf = vp + rng.standard_normal((n, 3)) * 10.0 ** rng.uniform(-6.0, 0.5, (n, 1))
+    beta = np.zeros((n, 3))
+    for i in range(n):
+        G.m_part.a["rho"][0], G.m_part.a["rad"][0] = rho[i], rad[i]
+        G.m_part.a["v"][0] = vp[i]
+        b = np.zeros(3)
+        T.call(G, "CalculateDragForce", 1, float(denf[i]), float(alphaf[i]), velf[i].copy(), b)
+        beta[i] = b
+    return {"rho": rho, "rad": rad, "v": vp, "denf": denf, "alphaf": alphaf, "velf": velf, "beta": beta}
+
+
+# ----------------------------------------------------------------------------
+# the cases
+
+
+def _interior(p, a):
+    return np.asarray(a)[2:-2, 2:-2, 2:-2]
+
+
+def periodic_case():
+    """Three spheres of 6 cells on 16^3, periodic: bodies 1 and 2 in contact,
+    markers within the two-cell image band of four faces, no body straddling
+    a face."""
+    n, d = 16, 6.0
+    p, parts, bodies, field = scenario.resolved_case(n, n, n, 1, d, seed=11, n_modes=6, vel_std=0.02,
+                                                    coupleInterval=2, knCoeff=1e4, ResistCoeff=0.9)
+    X = np.array([[4.4, 5.0, 6.5], [4.4 + d + 0.35, 5.4, 6.2], [8.2, 11.6, 12.1]])
+    V = np.array([[0.02, -0.01, 0.005], [-0.02, 0.01, 0.0], [0.0, 0.015, -0.01]])
+    parts, bodies = scenario.sphere_bodies(X, d, 1.0, 1.14e3, V)
+    return "periodic", p, parts, bodies, field, None
+
+
+def walled_case():
+    """Two spheres of 6 cells on 14x14x16 with solid walls in z: body 1 a
+    quarter cell from the low wall (wall contact, one probe covering its
+    footprint and one beside it), body 2 touching body 1."""
+    n, d = 14, 6.0
+    p, parts, bodies, field = scenario.resolved_case(n, n, 16, 1, d, seed=5, n_modes=6, vel_std=0.02,
+                                                    coupleInterval=2, knCoeff=1e4, ResistCoeff=0.9, walls="z")
+    scenario.fill_halo(p, field)
+    X = np.array([[6.6, 7.1, 3.2], [6.6 + d + 0.3, 7.3, 3.5]])
+    V = np.array([[0.0, 0.01, -0.03], [-0.01, 0.0, 0.0]])
+    parts, bodies = scenario.sphere_bodies(X, d, 1.0, 1.14e3, V)
+    probes = np.zeros(2, WALL_PROBE)
+    probes["face"] = 5
+    probes[0]["points"] = [[4, 5, 0], [9, 5, 0], [9, 9, 0], [4, 9, 0]]
+    probes[1]["points"] = [[10, 1, 0], [13, 1, 0], [13, 4, 0], [10, 4, 0]]
+    return "walled", p, parts, bodies, field, probes
+
+
+def run_case(sources, name, p, parts, bodies, field, probes, steps):
+    t0 = time.time()
+    R = ReferenceCase(sources, p, parts, bodies, field, probes)
+    # the fields as the reference holds them: halo refilled by FillGhostRegionForFluid and Boundary
+    u0 = [a.T.copy() for a in R.u0]
+    out = {"params": np.asarray(p), "in_parcels": parts, "in_bodies": bodies,
+           "in_u": u0[0], "in_v": u0[1], "in_w": u0[2],
+           "in_probes": probes if probes is not None else np.zeros(0, WALL_PROBE), "steps": np.int32(steps)}
+    for k, v in R.snapshot().items():
+        out["init_" + k] = v
+    for s in range(steps):
+        R.multi_direct_forcing()
+        for k, v in R.snapshot().items():
+            out[f"mdf{s}_" + k] = v
+        for k, v in zip(("u", "v", "w", "fx", "fy", "fz"), R.fields()):
+            out[f"mdf{s}_" + k] = _interior(p, v)
+        R.cloud_evolution()
+        for k, v in R.snapshot().items():
+            out[f"step{s}_" + k] = v
+        print(f"{name}: step {s + 1}/{steps} after {time.time() - t0:.0f} s", flush=True)
+    return out
+
+
+def main(ref_dir):
+    sources = load_sources(ref_dir)
+    path = os.path.join(HERE, "ref_drag.npz")
+    np.savez_compressed(path, **run_drag(sources, 9))
+    print(f"wrote {path} ({os.path.getsize(path) // 1024} KB)")
+    for name, walls, n, seed in (("fluid_walls_y", "y", (10, 8, 12), 3), ("fluid_periodic", "", (8, 10, 6), 4)):
+        p = make_params(*n, walls=walls, dt=1e-3, rhof=1e3)
+        out = run_fluid(sources, name, p, 1e-3, seed)
+        path = os.path.join(HERE, f"ref_{name}.npz")
+        np.savez_compressed(path, **out)
+        print(f"wrote {path} ({os.path.getsize(path) // 1024} KB)")
+    for maker, steps in ((periodic_case, 3), (walled_case, 3)):
+        name, p, parts, bodies, field, probes = maker()
+        out = run_case(sources, name, p, parts, bodies, field, probes, steps)
+        path = os.path.join(HERE, f"ref_{name}.npz")
+        np.savez_compressed(path, **out)
+        print(f"wrote {path} ({os.path.getsize(path) // 1024} KB)")
+
+
+if __name__ == "__main__":
+    if len(sys.argv) != 2:
+        sys.exit(__doc__)
+    main(sys.argv[1])

@@ -1,0 +1,84 @@
+"""The CUDA library against the reference's own subroutines, through the C ABI.
+
+The fixtures tests/golden/ref_{periodic,walled}.npz hold the state of the
+reference's Fortran statements (run by tests/golden/make_reference_golden.py)
+after InitializationDEM and after each forcing loop and CloudEvolutionMS of
+three coupled steps.  The library replays the same stages from the same
+inputs.  Up to and including the first forcing loop it must agree bit for bit:
+cell lists, contact lists, every parcel field (images included), the fields
+u, v, w with their halo and fx, fy, fz, the bodies.  From the first
+CloudEvolutionMS on, the body rotation goes through CUDA's cos and sin instead
+of the host's: bodies, parcels and fields then agree to 1e-9 of each field's
+largest value, and the cell and contact lists stay identical.
+"""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+import cases
+
+pytestmark = pytest.mark.gpu
+
+sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+from test_reference_pins import IMAGE_FIELDS, load  # noqa: E402
+
+BODY_FIELDS = ("x", "v", "omega", "AngMom", "rotMat", "rotMatGlo", "fdrag", "fcol", "fmom", "fmomCol", "fhydro",
+               "fmomHydro", "vold", "AngMomOld")
+
+
+def same_or_close(a, b, exact, what):
+    if exact:
+        assert np.array_equal(a, b), what
+    else:
+        assert cases.rel_close(a, b, 1e-9), what
+
+
+def check(ref, tag, c, exact, fields=False):
+    s, i = c.get_cell_lists()
+    assert np.array_equal(s, ref[tag + "_cell_start"]) and np.array_equal(i, ref[tag + "_cell_items"]), \
+        f"{tag}: cell lists"
+    s, i = c.get_collision_lists()
+    assert np.array_equal(s, ref[tag + "_pair_start"]) and np.array_equal(i, ref[tag + "_pair_items"]), \
+        f"{tag}: contact lists"
+    parts, nl = c.get_parcels()
+    want = ref[tag + "_parcels"]
+    assert nl == int(ref[tag + "_nlocal"]) and len(parts) == len(want), tag
+    for f in ("globalIdx", "cellIdx", "MSIdx", "pType"):
+        assert np.array_equal(parts[f], want[f]), f"{tag}: parcel {f}"
+    for f in ("x", "v", "fdrag", "vol", "m", "radeff"):
+        same_or_close(parts[f], want[f], exact, f"{tag}: parcel {f}")
+    for f in ("fcol", "vgap"):
+        same_or_close(parts[f][:nl], want[f][:nl], exact, f"{tag}: local parcel {f}")
+    assert set(IMAGE_FIELDS) >= {"x", "v", "fdrag"}
+    bodies, wb = c.get_bodies(), ref[tag + "_bodies"]
+    for f in BODY_FIELDS:
+        same_or_close(bodies[f], wb[f], exact, f"{tag}: body {f}")
+    if len(ref[tag + "_probe_force"]):
+        got = np.array([p["force"] for p in c.get_wall_probes()])
+        same_or_close(got, ref[tag + "_probe_force"], exact, f"{tag}: probe forces")
+    if fields:
+        for name, a in zip(("u", "v", "w", "fx", "fy", "fz"), c.get_fluid()):
+            same_or_close(a[2:-2, 2:-2, 2:-2], ref[f"{tag}_{name}"], exact, f"{tag}: {name}")
+
+
+@pytest.mark.parametrize("name", ["periodic", "walled"])
+def test_library_matches_the_reference(gpu_lib, name):
+    ref = load(name)
+    field = (ref["in_u"], ref["in_v"], ref["in_w"])
+    c = gpu_lib.Case(ref["params"], ref["in_parcels"], ref["in_bodies"], field, device=0)
+    try:
+        if len(ref["in_probes"]):
+            c.set_wall_probes(ref["in_probes"])
+        c.InitializationDEM()
+        check(ref, "init", c, exact=True)
+        for s in range(int(ref["steps"])):
+            c.set_fluid(*field)
+            c.MultiDirectForcing()
+            check(ref, f"mdf{s}", c, exact=(s == 0), fields=True)
+            c.CloudEvolutionMS()
+            check(ref, f"step{s}", c, exact=False)
+    finally:
+        c.close()
+

@@ -1,0 +1,138 @@
+"""The CPU restatement in oracle/ against the reference's own subroutines.
+
+The fixtures tests/golden/ref_*.npz were made by make_reference_golden.py, which
+runs the reference's Fortran statements (through fortran_subset.py, on one
+rank) on seeded cases.  Here the restatement replays the same stages from the
+same inputs and must agree bit for bit at every one of them:
+
+* two coupled cases (periodic; walls in z with wall contact and probes), three
+  steps of two DEM sub-steps each: after InitializationDEM, after each forcing
+  loop (fluid.F90:258-280) and after each CloudEvolutionMS
+  (couplesolverCylinder.F90:189-217) -- every parcel field the reference
+  defines (images included), every body field, the per-cell parcel lists, the
+  contact lists, the interpolation windows and weights, the fields u, v, w
+  (halo included) and fx, fy, fz, the wall-probe forces;
+* the fluid step's stencils (fluid.F90:2-250, boundary.F90:122-245) on random
+  fields, periodic and between walls;
+* the drag law CalculateDragForce (ZJS_DRAGFORCE_DEM.F90:2-35).
+"""
+import hashlib
+import os
+import sys
+
+import numpy as np
+import pytest
+
+from ibmdem import records
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+if GOLDEN not in sys.path:
+    sys.path.insert(0, GOLDEN)
+# image slots hold only what MyMPIUpdateVelocityAndPosition sends (ZJS_MPI_DEM.F90:102-170)
+IMAGE_FIELDS = ("globalIdx", "cellIdx", "pType", "MSIdx", "radeff", "rad", "rho", "vol", "m", "x", "v", "fdrag")
+
+
+def load(name):
+    with np.load(os.path.join(GOLDEN, f"ref_{name}.npz"), allow_pickle=False) as z:
+        return {k: z[k] for k in z.files}
+
+
+def digest(*arrays):
+    h = hashlib.sha256()
+    for a in arrays:
+        h.update(np.ascontiguousarray(a).tobytes())
+    return np.frombuffer(h.digest(), np.uint8)
+
+
+def check_stage(ref, tag, c):
+    """State of the restatement `c` against the reference's at stage `tag`."""
+    parts, nl = c.get_parcels()
+    want = ref[tag + "_parcels"]
+    assert nl == int(ref[tag + "_nlocal"]), tag
+    assert len(parts) == len(want), tag
+    for f in records.PARCEL.names:
+        if f == "pad_":
+            continue
+        assert np.array_equal(parts[f][:nl], want[f][:nl]), f"{tag}: local parcel {f}"
+        if f in IMAGE_FIELDS:
+            assert np.array_equal(parts[f][nl:], want[f][nl:]), f"{tag}: image parcel {f}"
+    bodies, wb = c.get_bodies(), ref[tag + "_bodies"]
+    for f in records.MULTISPHERE.names:
+        assert np.array_equal(bodies[f], wb[f]), f"{tag}: body {f}"
+    s, i = c.get_cell_lists()
+    assert np.array_equal(s, ref[tag + "_cell_start"]) and np.array_equal(i, ref[tag + "_cell_items"]), \
+        f"{tag}: cell lists"
+    s, i = c.get_collision_lists()
+    assert np.array_equal(s, ref[tag + "_pair_start"]) and np.array_equal(i, ref[tag + "_pair_items"]), \
+        f"{tag}: contact lists"
+    n = len(parts)
+    w, cells = c.get_weights(n)
+    cnt = ref[tag + "_window_count"]
+    used = np.arange(125)[None, :] < cnt[:, None]
+    assert np.array_equal(digest(np.where(used, cells, 0).astype(np.int32), np.where(used[..., None], w, 0.0)),
+                          ref[tag + "_window_digest"]), f"{tag}: interpolation windows"
+    if len(ref[tag + "_probe_force"]):
+        got = np.array([p["force"] for p in c.get_wall_probes()])
+        assert np.array_equal(got, ref[tag + "_probe_force"]), f"{tag}: probe forces"
+
+
+def check_fields(ref, tag, c):
+    for name, a in zip(("u", "v", "w", "fx", "fy", "fz"), c.get_fluid()):
+        assert np.array_equal(a[2:-2, 2:-2, 2:-2], ref[f"{tag}_{name}"]), f"{tag}: {name}"
+
+
+@pytest.mark.parametrize("name", ["periodic", "walled"])
+def test_coupled_steps_match_the_reference(oracle_mod, name):
+    ref = load(name)
+    field = (ref["in_u"], ref["in_v"], ref["in_w"])
+    c = oracle_mod.OracleCase(ref["params"], ref["in_parcels"], ref["in_bodies"], field)
+    if len(ref["in_probes"]):
+        c.set_wall_probes(ref["in_probes"])
+    c.InitializationDEM()
+    check_stage(ref, "init", c)
+    assert len(ref["init_pair_items"]) > 0, "the case has contacts"
+    assert len(ref["init_parcels"]) > int(ref["init_nlocal"]), "the case has images"
+    for s in range(int(ref["steps"])):
+        c.set_fluid(*field)
+        c.MultiDirectForcing()
+        check_stage(ref, f"mdf{s}", c)
+        check_fields(ref, f"mdf{s}", c)
+        c.CloudEvolutionMS()
+        check_stage(ref, f"step{s}", c)
+    c.close()
+
+
+def test_walled_case_exercises_wall_contact():
+    ref = load("walled")
+    f = ref["step0_probe_force"]
+    assert f[0][2] > 0 and not f[1].any(), "one probe under the body, one beside it"
+    assert list(ref["params"]["bType"]) == [0, 0, 0, 0, 1, 1]
+
+
+@pytest.mark.parametrize("name", ["fluid_walls_y", "fluid_periodic"])
+def test_fluid_stencils_match_the_reference(oracle_mod, name):
+    import make_reference_golden as mrg
+
+    ref = load(name)
+    F = oracle_mod.OracleFluid(ref["params"])
+    for f in mrg.FLUID_INPUTS:
+        F.set_field(records.FLUID[f], ref["in_" + f])
+    F.set_fluid_params(float(ref["visc"]))
+    b = ref["bulk"]
+    for stage, calls, written in mrg.FLUID_STAGES:
+        for call in calls:
+            if call[0] == "ModifyBulkVelocity":
+                F.ModifyBulkVelocity(int(b[0]), int(b[1]), int(b[2]), b[3], b[4], b[5])
+            else:
+                getattr(F, call[0])(*call[1:])
+        for f in written:
+            assert np.array_equal(digest(F.get_field(records.FLUID[f])), ref[f"{stage}_{f}"]), f"{stage}: {f}"
+    F.close()
+
+
+def test_drag_law_matches_the_reference(oracle_mod):
+    ref = load("drag")
+    for i in range(len(ref["rho"])):
+        beta = oracle_mod.drag_beta(ref["rho"][i], ref["rad"][i], ref["v"][i], ref["denf"][i], ref["alphaf"][i],
+                                    ref["velf"][i])
+        assert np.array_equal(beta, ref["beta"][i]), i
