@@ -2,10 +2,12 @@
  * fluid halo fill of boundary.F90:122-247), test infrastructure only: the
  * parity checker for the GPU fluid kernels and their timed CPU baseline.
  *
- * Parity unpinned: there is no Fortran compiler here to run the reference, so
- * each statement is restated with the reference's operations in the
+ * Each statement is restated with the reference's operations in the
  * reference's order (gfortran -O3 on x86-64 without -march: left-to-right,
- * no FMA contraction; this file is built with -ffp-contract=off).
+ * no FMA contraction; this file is built with -ffp-contract=off).  Parity
+ * pinned: every field each stencil writes agrees bit for bit with the
+ * reference's own subroutines run through tests/golden/fortran_subset.py
+ * (tests/test_reference_pins.py::test_fluid_stencils_match_the_reference).
  *
  * One rank: the MPI exchanges of FillGhostRegionForFluid become the periodic
  * copies and wall mirrors of DealWithBoundaryFluid, face by face in the

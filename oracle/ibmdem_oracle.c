@@ -2,10 +2,13 @@
  * ibmdem_oracle.c — CPU restatement of the IBM-DEM particle-side hot path.
  *
  * TEST INFRASTRUCTURE ONLY (parity checker and timed CPU baseline); the
- * product never links or calls it.  PARITY UNPINNED: the Fortran reference
- * cannot be built or run here and has no tests or golden vectors for this
- * path; this file restates its source, citing file:line for each routine, and
- * is pinned by the analytic checks in tests/test_oracle_*.py.
+ * product never links or calls it.  PARITY PINNED: the Fortran reference
+ * cannot be compiled here and has no tests or golden vectors for this path;
+ * this file restates its source, citing file:line for each routine, and
+ * agrees bit for bit with the reference's own subroutines run through the
+ * Fortran-subset translator of tests/golden/fortran_subset.py
+ * (tests/test_reference_pins.py), besides the analytic checks in
+ * tests/test_oracle_*.py.
  *
  * Scope: one MPI rank owning the whole domain; each axis either periodic
  * (bType = 0 on both faces) or bounded by two solid walls (bType = 1).  On one

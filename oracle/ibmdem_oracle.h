@@ -6,11 +6,14 @@
  * or calls it.  Only tests/, __graft_entry__.smoke() and bench.py's CPU legs
  * load it.
  *
- * PARITY UNPINNED: the reference (Fortran 90 + MPI + PETSc) cannot be compiled
- * or run here (no Fortran compiler, no MPI) and ships no tests, golden vectors
- * or known-answer fixtures for this path.  The restatement follows the
- * reference source line by line (file:line cited at each function) and is
- * pinned only by analytic and self-consistency checks (tests/test_oracle_*.py).
+ * PARITY PINNED to the reference's own subroutines: the reference (Fortran 90
+ * + MPI + PETSc) cannot be compiled here and ships no tests or golden vectors,
+ * so tests/golden/fortran_subset.py runs its Fortran statements through a
+ * translator on one rank, and tests/test_reference_pins.py checks this
+ * restatement against what they produce (tests/golden/ref_*.npz), bit for bit
+ * at every stage of two coupled cases.  The restatement follows the reference
+ * source line by line (file:line cited at each function); analytic checks
+ * (tests/test_oracle_*.py) cover what the reference does not have.
  *
  * The entry points mirror the reference subroutines one-for-one and operate on
  * one single-rank case, each axis periodic or between two solid walls.  Record layouts are the C-ABI ones

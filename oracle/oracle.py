@@ -1,8 +1,8 @@
 """ctypes binding of the CPU restatement (oracle/libibmdem_oracle.so).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
-CPU legs of bench.py, never by the product.  PARITY UNPINNED: the Fortran
-reference cannot be built here; see ibmdem_oracle.c.
+CPU legs of bench.py, never by the product.  Parity pinned to the reference's
+own subroutines, run by tests/golden/fortran_subset.py; see ibmdem_oracle.c.
 """
 import ctypes
 import os

@@ -4,9 +4,10 @@
  * TEST INFRASTRUCTURE ONLY (parity checker and timed CPU baseline); the
  * product never links or calls it.
  *
- * PARITY UNPINNED: the reference holds only the drag law of this path
- * (CalculateDragForce, ZJS_DRAGFORCE_DEM.F90:2-35, restated in
- * orc_CalculateDragForce), the normal contact law it shares with the resolved
+ * PARITY UNPINNED beyond the drag law: the reference holds only the drag law
+ * of this path (CalculateDragForce, ZJS_DRAGFORCE_DEM.F90:2-35, restated in
+ * orc_CalculateDragForce and pinned bit for bit to the reference's own
+ * subroutine by tests/test_reference_pins.py), the normal contact law it shares with the resolved
  * path (ZJS_COLLISION_DEM.F90:30-57) and an empty LogVolumeFraction
  * (ZJS_EVOLUTION_DEM.F90:27-32).  The rest -- tangential friction with history,
  * the Gaussian volume fraction, interpolation at the particle and the
