@@ -17,7 +17,8 @@ reference hard-codes or a step it takes on several ranks only):
     SetWallProbe, ZJS_INIT_DEM.F90:369-509), all set in the reference's module
     variables after the routine that would have set them;
   * the multi-rank body exchange: on one rank CloudEvolutionStepMS integrates
-    only body 1 (couplesolverCylinder.F90:114-121,130), so the harness runs its
+    only body 1 (couplesolverCylinder.F90:114-121,130), so for more than one
+    body (the single-body case runs that one-rank path unchanged) the harness runs its
     multi-rank branch, with the two steps that ranks exchange for replaced by
     their one-rank result: AssembleForceMS is AssembleLocalForceMS followed by
     its own copy from MSGlo into MS (ZJS_MS_DEM.F90:417-422), and
@@ -62,12 +63,18 @@ def load_sources(ref_dir):
 class ReferenceCase:
     """One case held by the reference's translated subroutines."""
 
-    def __init__(self, sources, p, parts, bodies, field, probes=None):
+    def __init__(self, sources, p, parts, bodies, field, probes=None, one_rank_bodies=False):
+        """`one_rank_bodies` keeps the reference's own one-rank body update
+        (defined for a single body) instead of its multi-rank branch."""
         self.p = p
         self.T = fs.Translator(sources, CAPACITIES)
-        self.T.build(overrides={"setboundarytype": self._set_boundary_type,
-                                "assembleforcems": self._assemble_force_ms,
-                                "cloudevolutionstepms": self._cloud_evolution_step_ms})
+        overrides = {"setboundarytype": self._set_boundary_type}
+        if not one_rank_bodies:
+            overrides.update({"assembleforcems": self._assemble_force_ms,
+                              "cloudevolutionstepms": self._cloud_evolution_step_ms})
+        else:
+            assert len(bodies) == 1, "the one-rank body update integrates body 1 only"
+        self.T.build(overrides=overrides)
         self.G = G = self.T.new_state()
         c = self.call
         n = [int(p["nx"]), int(p["ny"]), int(p["nz"])]
@@ -399,9 +406,22 @@ def walled_case():
     return "walled", p, parts, bodies, field, probes
 
 
+def single_case():
+    """One sphere of 8 cells on 16x14x18, periodic, markers in the image band of
+    three faces: the reference's own one-rank CloudEvolutionStepMS
+    (couplesolverCylinder.F90:99-187, ncputot == 1) runs unchanged."""
+    d = 8.0
+    p, parts, bodies, field = scenario.resolved_case(16, 14, 18, 1, d, seed=17, n_modes=6, vel_std=0.02,
+                                                    coupleInterval=3, knCoeff=1e4, ResistCoeff=0.9)
+    X = np.array([[5.2, 6.9, 13.4]])
+    V = np.array([[0.01, -0.02, 0.015]])
+    parts, bodies = scenario.sphere_bodies(X, d, 1.0, 1.14e3, V)
+    return "single", p, parts, bodies, field, None
+
+
 def run_case(sources, name, p, parts, bodies, field, probes, steps):
     t0 = time.time()
-    R = ReferenceCase(sources, p, parts, bodies, field, probes)
+    R = ReferenceCase(sources, p, parts, bodies, field, probes, one_rank_bodies=(name == "single"))
     # the fields as the reference holds them: halo refilled by FillGhostRegionForFluid and Boundary
     u0 = [a.T.copy() for a in R.u0]
     out = {"params": np.asarray(p), "in_parcels": parts, "in_bodies": bodies,
@@ -433,7 +453,7 @@ def main(ref_dir):
         path = os.path.join(HERE, f"ref_{name}.npz")
         np.savez_compressed(path, **out)
         print(f"wrote {path} ({os.path.getsize(path) // 1024} KB)")
-    for maker, steps in ((periodic_case, 3), (walled_case, 3)):
+    for maker, steps in ((periodic_case, 3), (walled_case, 3), (single_case, 3)):
         name, p, parts, bodies, field, probes = maker()
         out = run_case(sources, name, p, parts, bodies, field, probes, steps)
         path = os.path.join(HERE, f"ref_{name}.npz")

@@ -63,7 +63,7 @@ def check(ref, tag, c, exact, fields=False):
             same_or_close(a[2:-2, 2:-2, 2:-2], ref[f"{tag}_{name}"], exact, f"{tag}: {name}")
 
 
-@pytest.mark.parametrize("name", ["periodic", "walled"])
+@pytest.mark.parametrize("name", ["periodic", "walled", "single"])
 def test_library_matches_the_reference(gpu_lib, name):
     ref = load(name)
     field = (ref["in_u"], ref["in_v"], ref["in_w"])
