@@ -49,7 +49,10 @@ def rotate_matrix(theta):
                      (1 - c) * uz * ux - s * uy, (1 - c) * uz * uy + s * ux, (1 - c) * uz * uz + c])
 
 
-def cylinder_case(template):
+CYLINDER_CENTRES = [[0.55e-3, 0.45e-3, 0.9e-3], [1.42e-3, 0.46e-3, 0.62e-3], [0.95e-3, 0.44e-3, 1.55e-3]]
+
+
+def cylinder_case(template, centres=CYLINDER_CENTRES):
     n = (48, 24, 48)
     dx = 9e-3 / 240  # PartitionInitialization(4,1,4,240,32,240,9d-3,1.2d-3,9d-3)
     p = make_params(*n, h=dx, dt=5e-5, coupleInterval=2, knCoeff=4e4, ResistCoeff=0.9)
@@ -62,7 +65,7 @@ def cylinder_case(template):
     pi = math.acos(-1.0)
     rho = 2.65e3
     L = np.array(n) * dx
-    centres = np.array([[0.55e-3, 0.45e-3, 0.9e-3], [1.42e-3, 0.46e-3, 0.62e-3], [0.95e-3, 0.44e-3, 1.55e-3]])
+    centres = np.array(centres)
     rnd = [0.2, 0.7, 0.45]
     vel = np.array([[1e-3, 0.0, -5e-4], [-1e-3, 2e-4, 0.0], [0.0, -3e-4, 8e-4]])
     parts = np.zeros(3 * nl, PARCEL)

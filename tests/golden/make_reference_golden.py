@@ -30,7 +30,7 @@ reference hard-codes or a step it takes on several ranks only):
 Bodies never straddle a periodic face in these cases: there the reference's
 raw body-relative vector and the nearest-image one of the library agree.
 
-Usage: python tests/golden/make_reference_golden.py <reference source dir>
+Usage: python tests/golden/make_reference_golden.py <reference source dir> [fixture names]
 """
 import os
 import sys
@@ -342,6 +342,21 @@ def digest(*arrays):
     return np.frombuffer(h.digest(), np.uint8)
 
 
+# image slots hold only what MyMPIUpdateVelocityAndPosition sends (ZJS_MPI_DEM.F90:102-170)
+IMAGE_FIELDS = ("globalIdx", "cellIdx", "pType", "MSIdx", "radeff", "rad", "rho", "vol", "m", "x", "v", "fdrag")
+
+
+def parcel_digest(parts, nl):
+    """Every parcel field the reference defines: all of a local's, an image's IMAGE_FIELDS."""
+    cols = [parts[f][:nl] for f in PARCEL.names if f != "pad_"] + [parts[f][nl:] for f in IMAGE_FIELDS]
+    return digest(*cols)
+
+
+def field_digest(fields):
+    """u, v, w with their halo; fx, fy, fz on the interior (the reference discards their halo)."""
+    return digest(*fields[:3], *[f[2:-2, 2:-2, 2:-2] for f in fields[3:]])
+
+
 def run_drag(sources, seed, n=400):
     """CalculateDragForce (ZJS_DRAGFORCE_DEM.F90:2-35) on random parcels and
     fluid states covering both Reynolds-number branches, the Rep >= 1 clamp and
@@ -442,26 +457,74 @@ def run_case(sources, name, p, parts, bodies, field, probes, steps):
     return out
 
 
-def main(ref_dir):
+def cylinder_case(ref_dir):
+    """Three cylinders from the reference's marker template CYLINDER_LP1125.dat in
+    its own units (dx = 3.75e-5 m, dt = 5e-5 s), built as InitCylinderParcelsDEM
+    builds them (tests/golden/make_golden.py), on 48x24x48, periodic, two in contact,
+    none straddling a face."""
+    import make_golden
+    p, parts, bodies, field = make_golden.cylinder_case(
+        os.path.join(ref_dir, "CYLINDER_LP1125.dat"), centres=[[0.52e-3, 0.45e-3, 0.6e-3], [1.16e-3, 0.46e-3, 0.63e-3], [0.9e-3, 0.44e-3, 1.25e-3]])
+    return "cylinders", p, parts, bodies, field, None
+
+
+def run_compact(sources, name, p, parts, bodies, field, probes, steps):
+    """As run_case, but stages stored as digests, with the bodies in full and the
+    final parcel positions and velocities."""
+    t0 = time.time()
+    R = ReferenceCase(sources, p, parts, bodies, field, probes)
+    # the case's field is single-precision exact: stored as float32
+    u0 = [a.T.astype(np.float32) for a in R.u0]
+    assert all(np.array_equal(a.astype(np.float64), b.T) for a, b in zip(u0, R.u0))
+    out = {"params": np.asarray(p), "in_parcels": parts, "in_bodies": bodies,
+           "in_u": u0[0], "in_v": u0[1], "in_w": u0[2], "steps": np.int32(steps)}
+
+    def stage(tag, fields=False):
+        parts_now, nl = R.parcels(), R.G.m_nplocal
+        out[tag + "_nlocal"] = np.int32(nl)
+        out[tag + "_np"] = np.int32(len(parts_now))
+        out[tag + "_parcel_digest"] = parcel_digest(parts_now, nl)
+        out[tag + "_bodies"] = R.bodies()
+        out[tag + "_cell_digest"] = digest(*R.cell_lists())
+        out[tag + "_pair_digest"] = digest(*R.collision_lists())
+        out[tag + "_npairs"] = np.int32(len(R.collision_lists()[1]))
+        cnt, cells, w = R.weights()
+        out[tag + "_window_digest"] = digest(cells, w)
+        if fields:
+            out[tag + "_field_digest"] = field_digest(R.fields())
+
+    stage("init")
+    for s in range(steps):
+        R.multi_direct_forcing()
+        stage(f"mdf{s}", fields=True)
+        R.cloud_evolution()
+        stage(f"step{s}")
+        print(f"{name}: step {s + 1}/{steps} after {time.time() - t0:.0f} s", flush=True)
+    final = R.parcels()
+    out["final_x"], out["final_v"] = final["x"], final["v"]
+    return out
+
+
+def main(ref_dir, only=None):
     sources = load_sources(ref_dir)
-    path = os.path.join(HERE, "ref_drag.npz")
-    np.savez_compressed(path, **run_drag(sources, 9))
-    print(f"wrote {path} ({os.path.getsize(path) // 1024} KB)")
-    for name, walls, n, seed in (("fluid_walls_y", "y", (10, 8, 12), 3), ("fluid_periodic", "", (8, 10, 6), 4)):
-        p = make_params(*n, walls=walls, dt=1e-3, rhof=1e3)
-        out = run_fluid(sources, name, p, 1e-3, seed)
+    jobs = {
+        "drag": lambda: run_drag(sources, 9),
+        "fluid_walls_y": lambda: run_fluid(sources, "fluid_walls_y", make_params(10, 8, 12, walls="y"), 1e-3, 3),
+        "fluid_periodic": lambda: run_fluid(sources, "fluid_periodic", make_params(8, 10, 6), 1e-3, 4),
+        "periodic": lambda: run_case(sources, *periodic_case(), 3),
+        "walled": lambda: run_case(sources, *walled_case(), 3),
+        "single": lambda: run_case(sources, *single_case(), 3),
+        "cylinders": lambda: run_compact(sources, *cylinder_case(ref_dir), 2),
+    }
+    for name, job in jobs.items():
+        if only and name not in only:
+            continue
         path = os.path.join(HERE, f"ref_{name}.npz")
-        np.savez_compressed(path, **out)
-        print(f"wrote {path} ({os.path.getsize(path) // 1024} KB)")
-    for maker, steps in ((periodic_case, 3), (walled_case, 3), (single_case, 3)):
-        name, p, parts, bodies, field, probes = maker()
-        out = run_case(sources, name, p, parts, bodies, field, probes, steps)
-        path = os.path.join(HERE, f"ref_{name}.npz")
-        np.savez_compressed(path, **out)
-        print(f"wrote {path} ({os.path.getsize(path) // 1024} KB)")
+        np.savez_compressed(path, **job())
+        print(f"wrote {path} ({os.path.getsize(path) // 1024} KB)", flush=True)
 
 
 if __name__ == "__main__":
-    if len(sys.argv) != 2:
+    if len(sys.argv) < 2:
         sys.exit(__doc__)
-    main(sys.argv[1])
+    main(sys.argv[1], sys.argv[2:])

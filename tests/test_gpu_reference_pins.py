@@ -22,7 +22,7 @@ import cases
 pytestmark = pytest.mark.gpu
 
 sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
-from test_reference_pins import IMAGE_FIELDS, load  # noqa: E402
+from test_reference_pins import IMAGE_FIELDS, load, mrg  # noqa: E402
 
 BODY_FIELDS = ("x", "v", "omega", "AngMom", "rotMat", "rotMatGlo", "fdrag", "fcol", "fmom", "fmomCol", "fhydro",
                "fmomHydro", "vold", "AngMomOld")
@@ -82,3 +82,30 @@ def test_library_matches_the_reference(gpu_lib, name):
     finally:
         c.close()
 
+
+
+def test_cylinders_in_physical_units(gpu_lib):
+    """The reference's own units and marker template (tests/golden/ref_cylinders.npz,
+    stored as digests): after InitializationDEM the parcels, cell lists, contact
+    lists and bodies are bit-identical; after each coupled step the bodies, and at
+    the end every parcel position and velocity, agree to 1e-9."""
+    ref = load("cylinders")
+    field = tuple(ref[f"in_{a}"].astype(np.float64) for a in "uvw")
+    c = gpu_lib.Case(ref["params"], ref["in_parcels"], ref["in_bodies"], field, device=0)
+    try:
+        c.InitializationDEM()
+        parts, nl = c.get_parcels()
+        assert np.array_equal(mrg.parcel_digest(parts, nl), ref["init_parcel_digest"]), "parcels"
+        assert np.array_equal(mrg.digest(*c.get_cell_lists()), ref["init_cell_digest"]), "cell lists"
+        assert np.array_equal(mrg.digest(*c.get_collision_lists()), ref["init_pair_digest"]), "contact lists"
+        for s in range(int(ref["steps"])):
+            c.set_fluid(*field)
+            c.MultiDirectForcing()
+            c.CloudEvolutionMS()
+            bodies, wb = c.get_bodies(), ref[f"step{s}_bodies"]
+            for f in BODY_FIELDS:
+                assert cases.rel_close(bodies[f], wb[f], 1e-9), f"step {s}: body {f}"
+        parts, _ = c.get_parcels()
+        assert cases.rel_close(parts["x"], ref["final_x"], 1e-9) and cases.rel_close(parts["v"], ref["final_v"], 1e-9)
+    finally:
+        c.close()

@@ -30,8 +30,9 @@ from ibmdem import records
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 if GOLDEN not in sys.path:
     sys.path.insert(0, GOLDEN)
-# image slots hold only what MyMPIUpdateVelocityAndPosition sends (ZJS_MPI_DEM.F90:102-170)
-IMAGE_FIELDS = ("globalIdx", "cellIdx", "pType", "MSIdx", "radeff", "rad", "rho", "vol", "m", "x", "v", "fdrag")
+import make_reference_golden as mrg  # noqa: E402
+
+IMAGE_FIELDS = mrg.IMAGE_FIELDS
 
 
 def load(name):
@@ -105,6 +106,43 @@ def test_coupled_steps_match_the_reference(oracle_mod, name):
     c.close()
 
 
+def compact_stage(ref, tag, c, fields=False):
+    """A stage of a fixture stored as digests (bodies in full)."""
+    parts, nl = c.get_parcels()
+    assert nl == int(ref[tag + "_nlocal"]) and len(parts) == int(ref[tag + "_np"]), tag
+    assert np.array_equal(mrg.parcel_digest(parts, nl), ref[tag + "_parcel_digest"]), f"{tag}: parcels"
+    bodies, wb = c.get_bodies(), ref[tag + "_bodies"]
+    for f in records.MULTISPHERE.names:
+        assert np.array_equal(bodies[f], wb[f]), f"{tag}: body {f}"
+    assert np.array_equal(mrg.digest(*c.get_cell_lists()), ref[tag + "_cell_digest"]), f"{tag}: cell lists"
+    assert np.array_equal(mrg.digest(*c.get_collision_lists()), ref[tag + "_pair_digest"]), f"{tag}: contact lists"
+    w, cells = c.get_weights(len(parts))
+    assert np.array_equal(mrg.digest(cells, w), ref[tag + "_window_digest"]), f"{tag}: interpolation windows"
+    if fields:
+        assert np.array_equal(mrg.field_digest(c.get_fluid()), ref[tag + "_field_digest"]), f"{tag}: fields"
+
+
+def test_cylinders_in_physical_units_match_the_reference(oracle_mod):
+    """Three cylinders from the reference's marker template in its own units
+    (dx = 3.75e-5 m, dt = 5e-5 s), two of them in contact, two coupled steps of
+    two sub-steps."""
+    ref = load("cylinders")
+    field = tuple(ref[f"in_{a}"].astype(np.float64) for a in "uvw")
+    c = oracle_mod.OracleCase(ref["params"], ref["in_parcels"], ref["in_bodies"], field)
+    c.InitializationDEM()
+    compact_stage(ref, "init", c)
+    assert int(ref["init_npairs"]) > 0
+    for s in range(int(ref["steps"])):
+        c.set_fluid(*field)
+        c.MultiDirectForcing()
+        compact_stage(ref, f"mdf{s}", c, fields=True)
+        c.CloudEvolutionMS()
+        compact_stage(ref, f"step{s}", c)
+    parts, _ = c.get_parcels()
+    assert np.array_equal(parts["x"], ref["final_x"]) and np.array_equal(parts["v"], ref["final_v"])
+    c.close()
+
+
 def test_walled_case_exercises_wall_contact():
     ref = load("walled")
     f = ref["step0_probe_force"]
@@ -114,8 +152,6 @@ def test_walled_case_exercises_wall_contact():
 
 @pytest.mark.parametrize("name", ["fluid_walls_y", "fluid_periodic"])
 def test_fluid_stencils_match_the_reference(oracle_mod, name):
-    import make_reference_golden as mrg
-
     ref = load(name)
     F = oracle_mod.OracleFluid(ref["params"])
     for f in mrg.FLUID_INPUTS:
