@@ -468,6 +468,74 @@ def cylinder_case(ref_dir):
     return "cylinders", p, parts, bodies, field, None
 
 
+def _f32(field):
+    """A field rounded to single precision, so that a fixture can store it as float32."""
+    return [np.asarray(f, dtype=np.float32).astype(np.float64) for f in field]
+
+
+def corner_case():
+    """Two spheres (d = 4h) on 12x10x12 between walls in x and in z, periodic in
+    y: body 1 in the corner of the low x and low z walls (wall contact on both,
+    mirror images across each wall and across the corner, periodic images across
+    the low y face), body 2 touching it; a probe on each of the two walls."""
+    p = make_params(12, 10, 12, walls="xz", knCoeff=1e4, ResistCoeff=0.9, coupleInterval=2)
+    field = _f32(scenario.fourier_field(p, 4, 0.02, seed=21))
+    scenario.fill_halo(p, field)
+    X = np.array([[2.3, 2.6, 2.4], [2.3 + 4.0 + 0.3, 2.8, 2.6]])
+    V = np.array([[-0.02, 0.01, -0.02], [-0.01, 0.0, 0.0]])
+    parts, bodies = scenario.sphere_bodies(X, 4.0, 1.0, 1.14e3, V)
+    probes = np.zeros(2, WALL_PROBE)
+    probes[0]["face"], probes[1]["face"] = 1, 5
+    probes[0]["points"] = [[0, 1, 1], [0, 4, 1], [0, 4, 4], [0, 1, 4]]
+    probes[1]["points"] = [[1, 1, 0], [4, 1, 0], [4, 4, 0], [1, 4, 0]]
+    return "corner", p, parts, bodies, field, probes
+
+
+def edge_case():
+    """Markers placed by hand on exact boundaries, 12^3 periodic: body 1's on
+    cell corners and cell centres (so window offsets of exactly 0.5 and 1.5
+    cells meet the delta kernel's branch points), body 2's at the contact
+    cut-off distance collisionDist*(1+collisionBuffer) from them, one ulp either
+    side of it and exactly as the sum rounds, plus one overlapping pair."""
+    p = make_params(12, 12, 12, knCoeff=1e4, ResistCoeff=0.9, coupleInterval=2)
+    field = _f32(scenario.fourier_field(p, 4, 0.02, seed=23))
+    cut = float(p["collisionDist"]) * (1.0 + float(p["collisionBuffer"]))
+    up, down = np.inf, -np.inf
+    a = [(4.0, 4.0, 4.0), (4.5, 4.5, 4.5), (7.0, 5.0, 4.0), (4.0, 7.5, 6.5), (8.0, 8.0, 8.0)]
+    b = [(4.0 + cut, 4.0, 4.0), (4.5, np.nextafter(4.5 + cut, down), 4.5), (7.0, 5.0, np.nextafter(4.0 - cut, up)),
+         (np.nextafter(4.0 - cut, down), 7.5, 6.5), (8.0 + 1.2, 8.0, 8.0)]
+    n = len(a) + len(b)
+    parts = np.zeros(n, PARCEL)
+    parts["x"] = np.array(a + b)
+    parts["MSIdx"] = [1] * len(a) + [2] * len(b)
+    parts["globalIdx"] = list(range(1, len(a) + 1)) + list(range(1, len(b) + 1))
+    parts["radeff"], parts["rho"], parts["vol"], parts["pType"] = 0.75, 1.14e3, 0.5, -1
+    parts["m"] = parts["rho"] * parts["vol"]
+    parts["v"] = [[0.01, 0.0, 0.0]] * len(a) + [[-0.01, 0.005, 0.0]] * len(b)
+    bodies = np.zeros(2, MULTISPHERE)
+    for k, pts in enumerate((a, b)):
+        B = bodies[k:k + 1]
+        B["globalIdx"] = k + 1
+        B["x"] = np.mean(pts, axis=0)
+        B["v"] = B["vold"] = parts["v"][0 if k == 0 else len(a)]
+        B["rad"], B["rho"], B["vol"] = 2.0, 1.14e3, 5.0
+        B["m"] = B["rho"] * B["vol"]
+        B["I"] = 0.4 * B["m"] * 4.0
+        B["InertiaTensor"] = np.diag([B["I"][0]] * 3).reshape(9)
+        B["rotMat"] = B["rotMatGlo"] = B["rotMatGloOld"] = np.eye(3).reshape(9)
+    return "edge", p, parts, bodies, field, None
+
+
+def empty_case():
+    """Two bodies and no markers, 10^3 periodic: the lists are empty, the
+    forcing loop leaves the fluid as it was and the bodies fall under gravity."""
+    p = make_params(10, 10, 10, coupleInterval=2)
+    field = _f32(scenario.fourier_field(p, 4, 0.02, seed=25))
+    _, bodies = scenario.sphere_bodies(np.array([[3.0, 4.0, 5.0], [7.0, 6.0, 5.0]]), 4.0, 1.0, 1.14e3,
+                                       np.array([[0.01, 0.0, 0.0], [0.0, -0.01, 0.02]]))
+    return "empty", p, np.zeros(0, PARCEL), bodies, field, None
+
+
 def run_compact(sources, name, p, parts, bodies, field, probes, steps):
     """As run_case, but stages stored as digests, with the bodies in full and the
     final parcel positions and velocities."""
@@ -477,7 +545,8 @@ def run_compact(sources, name, p, parts, bodies, field, probes, steps):
     u0 = [a.T.astype(np.float32) for a in R.u0]
     assert all(np.array_equal(a.astype(np.float64), b.T) for a, b in zip(u0, R.u0))
     out = {"params": np.asarray(p), "in_parcels": parts, "in_bodies": bodies,
-           "in_u": u0[0], "in_v": u0[1], "in_w": u0[2], "steps": np.int32(steps)}
+           "in_u": u0[0], "in_v": u0[1], "in_w": u0[2], "steps": np.int32(steps),
+           "in_probes": probes if probes is not None else np.zeros(0, WALL_PROBE)}
 
     def stage(tag, fields=False):
         parts_now, nl = R.parcels(), R.G.m_nplocal
@@ -492,6 +561,7 @@ def run_compact(sources, name, p, parts, bodies, field, probes, steps):
         out[tag + "_window_digest"] = digest(cells, w)
         if fields:
             out[tag + "_field_digest"] = field_digest(R.fields())
+        out[tag + "_probe_force"] = R.probe_forces()
 
     stage("init")
     for s in range(steps):
@@ -515,6 +585,9 @@ def main(ref_dir, only=None):
         "walled": lambda: run_case(sources, *walled_case(), 3),
         "single": lambda: run_case(sources, *single_case(), 3),
         "cylinders": lambda: run_compact(sources, *cylinder_case(ref_dir), 2),
+        "corner": lambda: run_compact(sources, *corner_case(), 3),
+        "edge": lambda: run_compact(sources, *edge_case(), 3),
+        "empty": lambda: run_compact(sources, *empty_case(), 2),
     }
     for name, job in jobs.items():
         if only and name not in only:

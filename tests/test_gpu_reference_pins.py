@@ -84,15 +84,19 @@ def test_library_matches_the_reference(gpu_lib, name):
 
 
 
-def test_cylinders_in_physical_units(gpu_lib):
-    """The reference's own units and marker template (tests/golden/ref_cylinders.npz,
-    stored as digests): after InitializationDEM the parcels, cell lists, contact
-    lists and bodies are bit-identical; after each coupled step the bodies, and at
-    the end every parcel position and velocity, agree to 1e-9."""
-    ref = load("cylinders")
+@pytest.mark.parametrize("name", ["corner", "edge", "empty", "cylinders"])
+def test_compact_cases(gpu_lib, name):
+    """Fixtures stored as digests (tests/golden/ref_{corner,edge,empty,cylinders}.npz):
+    after InitializationDEM the parcels, cell lists, contact lists and bodies are
+    bit-identical, and for the unit-spacing cases the parcels and fields after
+    the first forcing loop too; after each coupled step the bodies, and at the
+    end every parcel position and velocity, agree to 1e-9."""
+    ref = load(name)
     field = tuple(ref[f"in_{a}"].astype(np.float64) for a in "uvw")
     c = gpu_lib.Case(ref["params"], ref["in_parcels"], ref["in_bodies"], field, device=0)
     try:
+        if len(ref["in_probes"]):
+            c.set_wall_probes(ref["in_probes"])
         c.InitializationDEM()
         parts, nl = c.get_parcels()
         assert np.array_equal(mrg.parcel_digest(parts, nl), ref["init_parcel_digest"]), "parcels"
@@ -101,11 +105,17 @@ def test_cylinders_in_physical_units(gpu_lib):
         for s in range(int(ref["steps"])):
             c.set_fluid(*field)
             c.MultiDirectForcing()
+            if s == 0 and float(ref["params"]["dx"]) == 1.0:
+                parts, nl = c.get_parcels()
+                assert np.array_equal(mrg.parcel_digest(parts, nl), ref["mdf0_parcel_digest"]), "mdf0 parcels"
+                assert np.array_equal(mrg.field_digest(c.get_fluid()), ref["mdf0_field_digest"]), "mdf0 fields"
             c.CloudEvolutionMS()
             bodies, wb = c.get_bodies(), ref[f"step{s}_bodies"]
             for f in BODY_FIELDS:
                 assert cases.rel_close(bodies[f], wb[f], 1e-9), f"step {s}: body {f}"
         parts, _ = c.get_parcels()
-        assert cases.rel_close(parts["x"], ref["final_x"], 1e-9) and cases.rel_close(parts["v"], ref["final_v"], 1e-9)
+        if len(parts):
+            assert cases.rel_close(parts["x"], ref["final_x"], 1e-9)
+            assert cases.rel_close(parts["v"], ref["final_v"], 1e-9)
     finally:
         c.close()

@@ -107,7 +107,7 @@ def test_coupled_steps_match_the_reference(oracle_mod, name):
 
 
 def compact_stage(ref, tag, c, fields=False):
-    """A stage of a fixture stored as digests (bodies in full)."""
+    """A stage of a fixture stored as digests (bodies and probe forces in full)."""
     parts, nl = c.get_parcels()
     assert nl == int(ref[tag + "_nlocal"]) and len(parts) == int(ref[tag + "_np"]), tag
     assert np.array_equal(mrg.parcel_digest(parts, nl), ref[tag + "_parcel_digest"]), f"{tag}: parcels"
@@ -120,18 +120,32 @@ def compact_stage(ref, tag, c, fields=False):
     assert np.array_equal(mrg.digest(cells, w), ref[tag + "_window_digest"]), f"{tag}: interpolation windows"
     if fields:
         assert np.array_equal(mrg.field_digest(c.get_fluid()), ref[tag + "_field_digest"]), f"{tag}: fields"
+    if len(ref[tag + "_probe_force"]):
+        got = np.array([p["force"] for p in c.get_wall_probes()])
+        assert np.array_equal(got, ref[tag + "_probe_force"]), f"{tag}: probe forces"
 
 
-def test_cylinders_in_physical_units_match_the_reference(oracle_mod):
-    """Three cylinders from the reference's marker template in its own units
-    (dx = 3.75e-5 m, dt = 5e-5 s), two of them in contact, two coupled steps of
-    two sub-steps."""
-    ref = load("cylinders")
+COMPACT = {
+    "cylinders": "three cylinders from the reference's marker template in its own units (dx = 3.75e-5 m, "
+                 "dt = 5e-5 s), two of them in contact",
+    "corner": "two spheres between walls in x and z, one in the corner: wall contact on both walls, mirror "
+              "images across each wall and across the corner, periodic images in y, a probe on each wall",
+    "edge": "markers on cell corners and centres (the delta kernel's branch points) and at the contact "
+            "cut-off distance, one ulp either side of it",
+    "empty": "bodies without markers",
+}
+
+
+@pytest.mark.parametrize("name", sorted(COMPACT))
+def test_compact_cases_match_the_reference(oracle_mod, name):
+    """Fixtures stored as SHA-256 digests of every stage (bodies in full)."""
+    ref = load(name)
     field = tuple(ref[f"in_{a}"].astype(np.float64) for a in "uvw")
     c = oracle_mod.OracleCase(ref["params"], ref["in_parcels"], ref["in_bodies"], field)
+    if len(ref["in_probes"]):
+        c.set_wall_probes(ref["in_probes"])
     c.InitializationDEM()
     compact_stage(ref, "init", c)
-    assert int(ref["init_npairs"]) > 0
     for s in range(int(ref["steps"])):
         c.set_fluid(*field)
         c.MultiDirectForcing()
@@ -141,6 +155,15 @@ def test_cylinders_in_physical_units_match_the_reference(oracle_mod):
     parts, _ = c.get_parcels()
     assert np.array_equal(parts["x"], ref["final_x"]) and np.array_equal(parts["v"], ref["final_v"])
     c.close()
+
+
+def test_compact_cases_exercise_what_they_claim():
+    cyl, corner, edge, empty = (load(n) for n in ("cylinders", "corner", "edge", "empty"))
+    assert int(cyl["init_npairs"]) > 0 and float(cyl["params"]["dx"]) == 9e-3 / 240
+    assert int(corner["init_np"]) > int(corner["init_nlocal"]), "mirror and periodic images"
+    assert (corner["step0_probe_force"][:, 0] > 0).any() or (corner["step0_probe_force"][:, 2] > 0).any()
+    assert int(edge["init_npairs"]) >= 4, "the pairs at the cut-off"
+    assert int(empty["init_np"]) == 0 and len(empty["init_bodies"]) == 2
 
 
 def test_walled_case_exercises_wall_contact():
