@@ -27,7 +27,7 @@ reassociation):
     the receive buffer, MPI_REDUCE copies, barriers and broadcasts do nothing.
 Statements for files and the terminal (open, write, read, close, print) do
 nothing.  A subroutine the sources call but do not define (PETSc) raises when
-it is reached.
+it is reached, unless the caller supplies it.
 """
 import math
 import re
@@ -883,6 +883,8 @@ class Translator:
         exec(compile(self.source, "<reference translation>", "exec"), ns)
         for k, f in (overrides or {}).items():
             ns["f_" + k.lower()] = f
+        # a subroutine the sources call but do not define: one supplied as an override, else an error
+        ns["_ext"] = lambda n: ns["f_" + n] if "f_" + n in ns else _missing(n)
         self.ns = ns
         return ns
 
@@ -1099,8 +1101,7 @@ class Translator:
             callee = self.subs[name]
             if len(args) != len(callee.args):
                 raise SyntaxError(f"call {name}: {len(args)} arguments for {len(callee.args)}")
-        elif name not in BUILTIN_CALLS:
-            return [f"_missing('{name}')"]
+        fn = f"f_{name}" if (name in self.subs or name in BUILTIN_CALLS) else f"_ext('{name}')"
         outs = self.outs[name] if name in self.subs else set(range(len(args)))
         codes, backs = [], []
         for k, a in enumerate(args):
@@ -1117,7 +1118,7 @@ class Translator:
             codes.append(X.code)
         self.tmp += 1
         r = f"_r{self.tmp}"
-        out = [f"{r} = f_{name}(G{''.join(', ' + c for c in codes)})"]
+        out = [f"{r} = {fn}(G{''.join(', ' + c for c in codes)})"]
         for k, code, kind in backs:
             out.append(f"{code} = {r}[{k}]")
         return out

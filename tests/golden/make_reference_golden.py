@@ -267,10 +267,12 @@ class ReferenceCase:
 class ReferenceFluid:
     """The reference's fluid stencils on one rank (fluid.F90, boundary.F90)."""
 
-    def __init__(self, sources, p, visc):
+    def __init__(self, sources, p, visc, extra=None):
         self.p = p
         self.T = fs.Translator(sources, CAPACITIES)
-        self.T.build(overrides={"setboundarytype": lambda G: ReferenceCase._set_boundary_type(self, G)})
+        overrides = {"setboundarytype": lambda G: ReferenceCase._set_boundary_type(self, G)}
+        overrides.update(extra or {})
+        self.T.build(overrides=overrides)
         self.G = G = self.T.new_state()
         n = [int(p["nx"]), int(p["ny"]), int(p["nz"])]
         h = [float(p["dx"]), float(p["dy"]), float(p["dz"])]
@@ -380,6 +382,45 @@ def run_drag(sources, seed, n=400):
         T.call(G, "CalculateDragForce", 1, float(denf[i]), float(alphaf[i]), velf[i].copy(), b)
         beta[i] = b
     return {"rho": rho, "rad": rad, "v": vp, "denf": denf, "alphaf": alphaf, "velf": velf, "beta": beta}
+
+
+RK3_WRITTEN = ["u", "v", "w", "RHSul", "RHSvl", "RHSwl", "Px", "Py", "Pz", "velDiv", "P", "Pcorr", "omegaX",
+               "omegaY", "omegaZ"]
+
+
+def run_fluid_rk3(sources, name, p, visc, seed):
+    """The reference's ThirdOrderLowStorageRungeKutta (fluid.F90:329-366) as it
+    stands, its Poisson solve (SetPressureVector, PoissonSolver) replaced by a
+    given pressure correction per stage; digests of the velocity and the
+    divergence where each stage's solve would start, and of every written
+    field at the end."""
+    rng = np.random.default_rng(seed)
+    pcorr = [rng.standard_normal(field_shape(p)) * 1e3 for _ in range(3)]
+    out = {"params": np.asarray(p), "visc": np.float64(visc)}
+    hook = {"stage": 0}
+    R = None
+
+    def poisson(G):
+        k = hook["stage"]
+        for f in ("u", "v", "w", "velDiv"):
+            out[f"rk{k}_{f}"] = digest(R.get(f))
+        R.set("Pcorr", pcorr[k])
+        hook["stage"] += 1
+        return ()
+
+    R = ReferenceFluid(sources, p, visc, extra={"setpressurevector": lambda G: (), "poissonsolver": poisson})
+    for f in FLUID_INPUTS:
+        a = rng.standard_normal(field_shape(p)) * (1e3 if f in ("P", "Pcorr") else 0.1)
+        out["in_" + f] = a
+        R.set(f, a)
+    for k in range(3):
+        out[f"in_pcorr{k}"] = pcorr[k]
+    R.call("ThirdOrderLowStorageRungeKutta")
+    assert hook["stage"] == 3
+    for f in RK3_WRITTEN:
+        out[f"end_{f}"] = digest(R.get(f))
+    print(f"{name}: three Runge-Kutta stages done", flush=True)
+    return out
 
 
 # ----------------------------------------------------------------------------
@@ -581,6 +622,8 @@ def main(ref_dir, only=None):
         "drag": lambda: run_drag(sources, 9),
         "fluid_walls_y": lambda: run_fluid(sources, "fluid_walls_y", make_params(10, 8, 12, walls="y"), 1e-3, 3),
         "fluid_periodic": lambda: run_fluid(sources, "fluid_periodic", make_params(8, 10, 6), 1e-3, 4),
+        "fluid_rk3_walls_z": lambda: run_fluid_rk3(sources, "fluid_rk3_walls_z", make_params(8, 6, 10, walls="z"),
+                                                   2e-3, 6),
         "periodic": lambda: run_case(sources, *periodic_case(), 3),
         "walled": lambda: run_case(sources, *walled_case(), 3),
         "single": lambda: run_case(sources, *single_case(), 3),

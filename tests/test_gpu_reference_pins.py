@@ -119,3 +119,41 @@ def test_compact_cases(gpu_lib, name):
             assert cases.rel_close(parts["v"], ref["final_v"], 1e-9)
     finally:
         c.close()
+
+
+def test_runge_kutta_fluid_step(gpu_lib):
+    """The reference's ThirdOrderLowStorageRungeKutta (fluid.F90:329-366) between
+    walls in z, each stage's Poisson solve replaced by the fixture's correction:
+    the velocity and divergence where each solve starts and every field written
+    by the end are bit-identical (tests/golden/ref_fluid_rk3_walls_z.npz)."""
+    from test_reference_pins import digest
+
+    ref = load("fluid_rk3_walls_z")
+    c = gpu_lib.Case(ref["params"], device=0)
+    try:
+        for f in mrg.FLUID_INPUTS:
+            c.set_fluid_field(f, ref["in_" + f])
+        c.set_fluid_params(float(ref["visc"]))
+        aRK = [32.0 / 60.0, 25.0 / 60.0, 45.0 / 60.0]
+        bRK = [0.0, -17.0 / 60.0, -25.0 / 60.0]
+        for k in range(3):
+            cRK = aRK[k] + bRK[k]
+            c.VelocityGuess(aRK[k], bRK[k], cRK)
+            c.FillGhostRegionForFluid()
+            c.Boundary()
+            c.VelocityDivergence(cRK)
+            c.FillGhostRegionForFluid()
+            c.Boundary()
+            for f in ("u", "v", "w", "velDiv"):
+                assert np.array_equal(digest(c.get_fluid_field(f)), ref[f"rk{k}_{f}"]), f"stage {k}: {f}"
+            c.set_fluid_field("Pcorr", ref[f"in_pcorr{k}"])
+            c.PressureCorrection()
+            c.FillGhostRegionForFluid()
+            c.Boundary()
+            c.VelocityCorrection(cRK)
+            c.FillGhostRegionForFluid()
+            c.Boundary()
+        for f in mrg.RK3_WRITTEN:
+            assert np.array_equal(digest(c.get_fluid_field(f)), ref[f"end_{f}"]), f
+    finally:
+        c.close()

@@ -192,6 +192,40 @@ def test_fluid_stencils_match_the_reference(oracle_mod, name):
     F.close()
 
 
+def test_runge_kutta_fluid_step_matches_the_reference(oracle_mod):
+    """The reference's ThirdOrderLowStorageRungeKutta (fluid.F90:329-366), walls
+    in z: VelocityGuess with the kept right-hand side (bRK != 0), the divergence
+    and the corrections scaled by cRK = aRK + bRK, each stage's Poisson solve
+    replaced by a given correction."""
+    ref = load("fluid_rk3_walls_z")
+    F = oracle_mod.OracleFluid(ref["params"])
+    for f in mrg.FLUID_INPUTS:
+        F.set_field(records.FLUID[f], ref["in_" + f])
+    F.set_fluid_params(float(ref["visc"]))
+    aRK = [32.0 / 60.0, 25.0 / 60.0, 45.0 / 60.0]
+    bRK = [0.0, -17.0 / 60.0, -25.0 / 60.0]
+    for k in range(3):
+        cRK = aRK[k] + bRK[k]
+        F.VelocityGuess(aRK[k], bRK[k], cRK)
+        F.FillGhostRegionForFluid()
+        F.Boundary()
+        F.VelocityDivergence(cRK)
+        F.FillGhostRegionForFluid()
+        F.Boundary()
+        for f in ("u", "v", "w", "velDiv"):
+            assert np.array_equal(digest(F.get_field(records.FLUID[f])), ref[f"rk{k}_{f}"]), f"stage {k}: {f}"
+        F.set_field(records.FLUID["Pcorr"], ref[f"in_pcorr{k}"])
+        F.PressureCorrection()
+        F.FillGhostRegionForFluid()
+        F.Boundary()
+        F.VelocityCorrection(cRK)
+        F.FillGhostRegionForFluid()
+        F.Boundary()
+    for f in mrg.RK3_WRITTEN:
+        assert np.array_equal(digest(F.get_field(records.FLUID[f])), ref[f"end_{f}"]), f
+    F.close()
+
+
 def test_drag_law_matches_the_reference(oracle_mod):
     ref = load("drag")
     for i in range(len(ref["rho"])):
