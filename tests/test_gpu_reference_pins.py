@@ -129,7 +129,8 @@ def test_runge_kutta_fluid_step(gpu_lib):
     from test_reference_pins import digest
 
     ref = load("fluid_rk3_walls_z")
-    c = gpu_lib.Case(ref["params"], device=0)
+    # the fluid stencils work on the fields ibmdem_set_fluid installs
+    c = gpu_lib.Case(ref["params"], field=(ref["in_u"], ref["in_v"], ref["in_w"]), device=0)
     try:
         for f in mrg.FLUID_INPUTS:
             c.set_fluid_field(f, ref["in_" + f])
