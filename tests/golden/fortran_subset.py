@@ -18,7 +18,11 @@ reassociation):
   * integer division truncates toward zero; mod takes the dividend's sign;
     assignment of a real to an integer truncates;
   * x**2 is x*x and x**3 is (x*x)*x (gfortran's expansion of small constant
-    integer powers); a real power calls pow();
+    integer powers, each product rounded to the operand's precision); a real
+    power calls pow();
+  * a single-precision sqrt or exp is the double result rounded once to
+    single (exact for sqrt; the reference's path takes none of the others in
+    single precision);
   * sqrt, exp, log, log10, cos, sin and acos come from this host's C library
     (Python's math module), as the C restatement's do;
   * sum() adds in array element order from 0;
@@ -75,6 +79,19 @@ def _powi(x, n):
     if n == 0:
         return 1.0
     return math.pow(x, n)
+
+
+def _powi4(x, n):
+    """A single-precision value to a small integer power, every product rounded to single."""
+    if n == 2:
+        return f32(x * x)
+    if n == 3:
+        return f32(f32(x * x) * x)
+    if n == 1:
+        return x
+    if n == 0:
+        return 1.0
+    return f32(math.pow(x, n))
 
 
 def _fsum(a):
@@ -874,8 +891,8 @@ class Translator:
             src.append(self._translate(u))
         self.source = "\n".join(src)
         ns = {"FArr": FArr, "_dummy": _dummy, "_recview": _recview, "_idiv": _idiv, "_imod": _imod,
-              "_powi": _powi, "_fsum": _fsum, "_floor": _floor, "_trunc": _trunc, "_nint": _nint, "f32": f32,
-              "_flat": _flat, "_missing": _missing}
+              "_powi": _powi, "_powi4": _powi4, "_fsum": _fsum, "_floor": _floor, "_trunc": _trunc,
+              "_nint": _nint, "f32": f32, "_flat": _flat, "_missing": _missing}
         for tn, dt in self.dtypes.items():
             ns["_DT_" + tn] = dt
         for k, f in BUILTIN_CALLS.items():
@@ -1073,8 +1090,7 @@ class Translator:
         raise SyntaxError(f"statement {st}")
 
     def _cond(self, e):
-        x = self._ex(e)
-        return x.code
+        return self._ex(e).code
 
     def _assign(self, lhs, rhs):
         L = self._des(lhs, lvalue=True)
@@ -1171,10 +1187,12 @@ class Translator:
             return E(f"_idiv({a.code}, {b.code})", "i")
         if rank > 0 and kind == "i" and op == "/":
             raise SyntaxError("integer array division")
-        code = f"({a.code} {op} {b.code})"
         if kind == "r4" and rank == 0:
-            code = f"f32{code}"
-        return E(code, kind, rank)
+            # an integer operand is converted to single precision first
+            ac = f"f32({a.code})" if a.kind == "i" else a.code
+            bc = f"f32({b.code})" if b.kind == "i" else b.code
+            return E(f"f32({ac} {op} {bc})", kind)
+        return E(f"({a.code} {op} {b.code})", kind, rank)
 
     def _pow(self, b, east):
         if east[0] == "num" and re.match(r"^\d+$", east[1]):
@@ -1183,8 +1201,7 @@ class Translator:
                 raise SyntaxError("array power")
             if b.kind == "i":
                 return E(f"(({b.code}) ** {n})", "i")
-            code = f"_powi({b.code}, {n})"
-            return E(f"f32({code})" if b.kind == "r4" else code, b.kind)
+            return E(f"_powi4({b.code}, {n})" if b.kind == "r4" else f"_powi({b.code}, {n})", b.kind)
         x = self._ex(east)
         if b.rank or x.rank:
             raise SyntaxError("array power")
@@ -1227,10 +1244,10 @@ class Translator:
                 raise SyntaxError(f"{name} of an array")
             arg = x.code if real(x.kind) else f"float({x.code})"
             code = f"math.{fn}({arg})"
-            kind = "r8" if x.kind in ("r8", "i") and name != "real" else x.kind
-            if name.startswith("d"):
-                kind = "r8"
-            return E(f"f32({code})" if kind == "r4" else code, kind)
+            # a single-precision argument gives a single-precision result (the double result rounded once)
+            if x.kind == "r4" and not name.startswith("d"):
+                return E(f"f32({code})", "r4")
+            return E(code, "r8")
         if name == "floor":
             return E(f"_floor({x.code})", "i")
         if name == "int":

@@ -41,10 +41,12 @@ implicit none
     z = 0.1*3.0
     w = 0.1*3d0 ! mixed: promoted
 endsubroutine
-subroutine powers(x,y2,y3)
+subroutine powers(x,y2,y3,z3,zi)
 implicit none
-    real*8::x,y2,y3
+    real*8::x,y2,y3,z3,zi
     y2 = x**2; y3 = x**3
+    z3 = 1.1**3
+    zi = 16777217*1.0
 endsubroutine
 subroutine loops(s)
 implicit none
@@ -128,8 +130,11 @@ def test_default_real_literals_are_single_precision():
 def test_small_integer_powers_are_products():
     T, G = build()
     x = 1.0 / 3.0
-    _, y2, y3 = T.call(G, "powers", x, 0.0, 0.0)
+    _, y2, y3, z3, zi = T.call(G, "powers", x, 0.0, 0.0, 0.0, 0.0)
     assert y2 == x * x and y3 == (x * x) * x
+    f = np.float32
+    assert z3 == float(f(f(f(1.1) * f(1.1)) * f(1.1)))  # every single-precision product rounded
+    assert zi == float(f(16777217))  # the integer operand converted to single first
 
 
 def test_loop_with_negative_stride():
