@@ -504,8 +504,8 @@ def cylinder_case(ref_dir):
     builds them (tests/golden/make_golden.py), on 48x24x48, periodic, two in contact,
     none straddling a face."""
     import make_golden
-    p, parts, bodies, field = make_golden.cylinder_case(
-        os.path.join(ref_dir, "CYLINDER_LP1125.dat"), centres=[[0.52e-3, 0.45e-3, 0.6e-3], [1.16e-3, 0.46e-3, 0.63e-3], [0.9e-3, 0.44e-3, 1.25e-3]])
+    centres = [[0.52e-3, 0.45e-3, 0.6e-3], [1.16e-3, 0.46e-3, 0.63e-3], [0.9e-3, 0.44e-3, 1.25e-3]]
+    p, parts, bodies, field = make_golden.cylinder_case(os.path.join(ref_dir, "CYLINDER_LP1125.dat"), centres)
     return "cylinders", p, parts, bodies, field, None
 
 
