@@ -63,11 +63,11 @@ def load_sources(ref_dir):
 class ReferenceCase:
     """One case held by the reference's translated subroutines."""
 
-    def __init__(self, sources, p, parts, bodies, field, probes=None, one_rank_bodies=False):
+    def __init__(self, sources, p, parts, bodies, field, probes=None, one_rank_bodies=False, capacities=None):
         """`one_rank_bodies` keeps the reference's own one-rank body update
         (defined for a single body) instead of its multi-rank branch."""
         self.p = p
-        self.T = fs.Translator(sources, CAPACITIES)
+        self.T = fs.Translator(sources, capacities or CAPACITIES)
         overrides = {"setboundarytype": self._set_boundary_type}
         if not one_rank_bodies:
             overrides.update({"assembleforcems": self._assemble_force_ms,
@@ -616,6 +616,70 @@ def run_compact(sources, name, p, parts, bodies, field, probes, steps):
     return out
 
 
+CONFIG_SEED = 1
+
+
+def config_case():
+    """The plain resolved configuration the benchmark's CPU-runnable case names:
+    128^3 periodic, 64 spheres of d = 16h (about 800 markers each), seeded
+    random sequential addition, 32 Fourier modes of amplitude 0.05, velocities
+    N(0, 0.01).  Regenerated by the tests from the seed (the fixture holds
+    digests of the inputs)."""
+    p, parts, bodies, field = scenario.resolved_case(128, 128, 128, 64, 16.0, seed=CONFIG_SEED, n_modes=32, amp=0.05,
+                                                    vel_std=0.01)
+    scenario.fill_halo(p, field)
+    return p, parts, bodies, field
+
+
+def straddlers(p, parts, bodies):
+    """Bodies with a marker more than half a box length from the centre along an
+    axis: the ones whose torque arms the reference takes across the box."""
+    L = np.array([int(p["nx"]) * float(p["dx"]), int(p["ny"]) * float(p["dy"]), int(p["nz"]) * float(p["dz"])])
+    d = np.abs(parts["x"] - bodies["x"][parts["MSIdx"] - 1])
+    far = (d > 0.5 * L[None, :]).any(1)
+    mask = np.zeros(len(bodies), bool)
+    mask[parts["MSIdx"][far] - 1] = True
+    return mask
+
+
+def run_config(sources):
+    """config_case through InitializationDEM, one forcing loop and one
+    CloudEvolutionMS: digests of the init and forcing stages, the bodies after
+    the step in full.  Bodies that straddle a face take the raw torque arm in
+    the reference (the library's deviation 2), so only their translation is
+    comparable after the step."""
+    t0 = time.time()
+    p, parts, bodies, field = config_case()
+    R = ReferenceCase(sources, p, parts, bodies, field, None, capacities={"maxpartno": 2 * len(parts)})
+    print(f"config: initialised after {time.time() - t0:.0f} s", flush=True)
+    u0 = [a.T.copy() for a in R.u0]
+    out = {"params": np.asarray(p), "seed": np.int32(CONFIG_SEED), "in_parcel_digest": parcel_digest(parts, len(parts)),
+           "in_body_digest": digest(*[bodies[f] for f in MULTISPHERE.names]), "in_field_digest": digest(*u0),
+           "straddlers": straddlers(p, parts, bodies)}
+
+    def stage(tag, fields=False):
+        parts_now, nl = R.parcels(), R.G.m_nplocal
+        out[tag + "_nlocal"] = np.int32(nl)
+        out[tag + "_np"] = np.int32(len(parts_now))
+        out[tag + "_parcel_digest"] = parcel_digest(parts_now, nl)
+        out[tag + "_cell_digest"] = digest(*R.cell_lists())
+        out[tag + "_pair_digest"] = digest(*R.collision_lists())
+        out[tag + "_npairs"] = np.int32(len(R.collision_lists()[1]))
+        cnt, cells, w = R.weights()
+        out[tag + "_window_digest"] = digest(cells, w)
+        if fields:
+            out[tag + "_field_digest"] = field_digest(R.fields())
+
+    stage("init")
+    R.multi_direct_forcing()
+    stage("mdf0", fields=True)
+    print(f"config: forcing loop after {time.time() - t0:.0f} s", flush=True)
+    R.cloud_evolution()
+    out["step0_bodies"] = R.bodies()
+    print(f"config: step after {time.time() - t0:.0f} s", flush=True)
+    return out
+
+
 def main(ref_dir, only=None):
     sources = load_sources(ref_dir)
     jobs = {
@@ -628,6 +692,7 @@ def main(ref_dir, only=None):
         "walled": lambda: run_case(sources, *walled_case(), 3),
         "single": lambda: run_case(sources, *single_case(), 3),
         "cylinders": lambda: run_compact(sources, *cylinder_case(ref_dir), 2),
+        "config": lambda: run_config(sources),
         "corner": lambda: run_compact(sources, *corner_case(), 3),
         "edge": lambda: run_compact(sources, *edge_case(), 3),
         "empty": lambda: run_compact(sources, *empty_case(), 2),
