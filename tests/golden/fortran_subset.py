@@ -29,11 +29,13 @@ reassociation):
   * local variables start at zero (Fortran leaves them undefined);
   * MPI is one rank: MPI_SENDRECV to and from rank 0 copies the message into
     the receive buffer, MPI_REDUCE copies, barriers and broadcasts do nothing.
-Statements for files and the terminal (open, write, read, close, print) do
+List-directed reads (read(unit,*)) take the next record of the file the unit
+was opened on; other statements for files and the terminal (write, print) do
 nothing.  A subroutine the sources call but do not define (PETSc) raises when
 it is reached, unless the caller supplies it.
 """
 import math
+import os
 import re
 from fractions import Fraction
 
@@ -160,6 +162,34 @@ def _flat(buf):
     if not np.shares_memory(f, a):
         raise ValueError("message buffer is not contiguous")
     return f
+
+
+# ----------------------------------------------------------------------------
+# list-directed reads from files (the marker templates); writes do nothing
+
+
+def _io_open(G, unit, name):
+    """Remember the file a unit names; it is read only if a read asks for it."""
+    G.io_units[unit] = {"name": name, "lines": None}
+
+
+def _io_read(G, unit, n):
+    """The next record of `unit`: its first n whitespace-separated values."""
+    u = G.io_units[unit]
+    if u["lines"] is None:
+        with open(G.io_path(u["name"])) as f:
+            u["lines"] = iter(f.read().split("\n"))
+    for line in u["lines"]:
+        vals = line.replace(",", " ").split()
+        if vals:
+            if len(vals) < n:
+                raise ValueError(f"record of {len(vals)} values for {n} items")
+            return vals[:n]
+    raise EOFError(u["name"])
+
+
+def _io_close(G, unit):
+    G.io_units.pop(unit, None)
 
 
 # ----------------------------------------------------------------------------
@@ -862,9 +892,12 @@ class Translator:
         raise KeyError(f"{tn}%{name}")
 
     # state -----------------------------------------------------------------
-    def new_state(self):
-        """Module variables of one rank: fixed arrays allocated, scalars zero."""
+    def new_state(self, io_dir="."):
+        """Module variables of one rank: fixed arrays allocated, scalars zero.
+        Files the sources read are looked up in `io_dir`."""
         G = type("RankState", (), {})()
+        G.io_units = {}
+        G.io_path = lambda name: os.path.join(io_dir, name.strip())
         for name, s in self.msyms.items():
             if s.param is not None:
                 continue
@@ -892,7 +925,8 @@ class Translator:
         self.source = "\n".join(src)
         ns = {"FArr": FArr, "_dummy": _dummy, "_recview": _recview, "_idiv": _idiv, "_imod": _imod,
               "_powi": _powi, "_powi4": _powi4, "_fsum": _fsum, "_floor": _floor, "_trunc": _trunc,
-              "_nint": _nint, "f32": f32, "_flat": _flat, "_missing": _missing}
+              "_nint": _nint, "f32": f32, "_flat": _flat, "_missing": _missing, "_io_open": _io_open,
+              "_io_read": _io_read, "_io_close": _io_close}
         for tn, dt in self.dtypes.items():
             ns["_DT_" + tn] = dt
         for k, f in BUILTIN_CALLS.items():
@@ -1062,7 +1096,10 @@ class Translator:
         if t == "cycle":
             out.append(pad + "continue")
             return ind
-        if t in ("continue", "io"):
+        if t == "io":
+            out.extend(pad + l for l in self._io(st[1]))
+            return ind
+        if t == "continue":
             out.append(pad + "pass")
             return ind
         if t == "stop":
@@ -1088,6 +1125,37 @@ class Translator:
                 out.append(pad + f"{self._ref(self._sym(a[1][0][0]))} = None")
             return ind
         raise SyntaxError(f"statement {st}")
+
+    def _io(self, s):
+        """open(unit, file=...), read(unit, *) items and close(unit); anything
+        else (writes, formats, prints) does nothing."""
+        m = re.match(r"^(open|read|close)\s*\(", s)
+        if not m:
+            return ["pass"]
+        j = _match_paren(s, m.end() - 1)
+        ctl = _split_top(s[m.end():j], ",")
+        unit = self._ex(parse_expr(ctl[0])).code
+        if m.group(1) == "open":
+            files = [c.split("=", 1)[1] for c in ctl[1:] if re.match(r"^\s*file\s*=", c)]
+            if not files:
+                return ["pass"]
+            return [f"_io_open(G, {unit}, {self._ex(parse_expr(files[0])).code})"]
+        if m.group(1) == "close":
+            return [f"_io_close(G, {unit})"]
+        if len(ctl) != 2 or ctl[1].strip() != "*":
+            raise SyntaxError(f"read other than list-directed: {s!r}")
+        items = [parse_expr(x) for x in _split_top(s[j + 1:], ",") if x.strip()]
+        self.tmp += 1
+        v = f"_v{self.tmp}"
+        out = [f"{v} = _io_read(G, {unit}, {len(items)})"]
+        for k, it in enumerate(items):
+            L = self._des(it, lvalue=True)
+            conv = {"i": "int", "r8": "float", "r4": "f32"}.get(L.kind)
+            if conv is None or L.rank:
+                raise SyntaxError(f"read into {L.kind} of rank {L.rank}")
+            val = f"float({v}[{k}].replace('d', 'e').replace('D', 'E'))" if conv != "int" else f"int({v}[{k}])"
+            out.append(f"{L.code} = {val if conv != 'f32' else 'f32(' + val + ')'}")
+        return out
 
     def _cond(self, e):
         return self._ex(e).code
@@ -1121,7 +1189,9 @@ class Translator:
         outs = self.outs[name] if name in self.subs else set(range(len(args)))
         codes, backs = [], []
         for k, a in enumerate(args):
-            if a[0] == "des" and a[1][0][0] not in self.pvals:
+            an = a[1][0][0] if a[0] == "des" else None
+            if an is not None and (an not in self.pvals or (an in self.u.syms and self.u.syms[an].param is None)) \
+                    and not (an in self.u.syms and self.u.syms[an].param is not None):
                 s = self._sym(a[1][0][0])
                 if s is not None:
                     D = self._des(a, lvalue=False, for_arg=True)
@@ -1215,7 +1285,12 @@ class Translator:
         parts = e[1]
         name, args = parts[0]
         s = self._sym(name) if (name in self.u.syms or name in self.msyms) else None
-        if name in self.pvals and len(parts) == 1 and args is None:
+        local = name in self.u.syms and self.u.syms[name].param is None
+        if name in self.u.syms and self.u.syms[name].param is not None and args is None:
+            ls = self.u.syms[name]
+            v = self._const(ls.param, ls.kind)
+            return E(repr(v), ls.kind, const=v)
+        if name in self.pvals and not local and len(parts) == 1 and args is None:
             v = self.pvals[name]
             if name in self.msyms:
                 kind = self.msyms[name].kind

@@ -94,6 +94,22 @@ implicit none
     enddo
     enddo
 endsubroutine
+subroutine readfile(a,n)
+implicit none
+    integer::n,i
+    real*8::a(1:3,1:2)
+    character(len=20)::name
+    name = "  pts.dat"
+    open(10,file=adjustl(trim(name)))
+    read(10,*) n
+    do i=1,n
+        read(10,*) a(1,i), a(2,i), a(3,i)
+    enddo
+    close(10)
+    open(11,file="log.txt",access="append")
+    write(11,*) "ignored", n
+    close(11)
+endsubroutine
 subroutine sendself(out)
 implicit none
     integer::out(1:2),buf(1:2),st(MPI_STATUS_SIZE),ierr
@@ -175,3 +191,15 @@ def test_single_precision_literal_rounding_is_from_the_decimal():
     # 0.1 and 2.08e-4 rounded once from the decimal agree with numpy's float32 parse
     for text in ("0.1", "2.08e-4", "3.1415926536", "0.0183", "8.33"):
         assert fs._dec_to_f32(text) == float(np.float32(text))
+
+
+def test_list_directed_reads(tmp_path):
+    (tmp_path / "pts.dat").write_text("2\n 0.1 -2.5e-3  7\n\n1d-3, 4.0 5\n")
+    T = fs.Translator([("t.F90", SRC)])
+    T.build()
+    G = T.new_state(io_dir=str(tmp_path))
+    a = np.zeros((3, 2), order="F")
+    r = T.call(G, "readfile", a, 0)
+    assert r[1] == 2
+    assert a[:, 0].tolist() == [0.1, -2.5e-3, 7.0] and a[:, 1].tolist() == [1e-3, 4.0, 5.0]
+    assert not (tmp_path / "log.txt").exists()
