@@ -263,3 +263,18 @@ def test_drag_law_matches_the_reference(oracle_mod):
         beta = oracle_mod.drag_beta(ref["rho"][i], ref["rad"][i], ref["v"][i], ref["denf"][i], ref["alphaf"][i],
                                     ref["velf"][i])
         assert np.array_equal(beta, ref["beta"][i]), i
+
+
+@pytest.mark.skipif(not os.environ.get("IBMDEM_REFERENCE_DIR"), reason="IBMDEM_REFERENCE_DIR (the reference's "
+                    "Fortran sources) not set")
+def test_fixtures_reproduce_from_the_reference_sources():
+    """With the reference's sources at hand, the translator reproduces the stored
+    fixtures byte for byte (the edge, empty and drag ones, which take seconds)."""
+    sources = mrg.load_sources(os.environ["IBMDEM_REFERENCE_DIR"])
+    for name, job in (("edge", lambda: mrg.run_compact(sources, *mrg.edge_case(), 3)),
+                      ("empty", lambda: mrg.run_compact(sources, *mrg.empty_case(), 2)),
+                      ("drag", lambda: mrg.run_drag(sources, 9))):
+        new, old = job(), load(name)
+        assert sorted(new) == sorted(old), name
+        for k in old:
+            assert np.array_equal(np.asarray(new[k]), old[k]), f"{name}: {k}"
