@@ -52,49 +52,32 @@ def rotate_matrix(theta):
 CYLINDER_CENTRES = [[0.55e-3, 0.45e-3, 0.9e-3], [1.42e-3, 0.46e-3, 0.62e-3], [0.95e-3, 0.44e-3, 1.55e-3]]
 
 
-def cylinder_case(template, centres=CYLINDER_CENTRES):
-    n = (48, 24, 48)
-    dx = 9e-3 / 240  # PartitionInitialization(4,1,4,240,32,240,9d-3,1.2d-3,9d-3)
-    p = make_params(*n, h=dx, dt=5e-5, coupleInterval=2, knCoeff=4e4, ResistCoeff=0.9)
-    tpl = np.loadtxt(template)
-    nl = len(tpl)
+def cylinder_geometry(dx):
+    """InitCylinderParcelsDEM's shape constants (ZJS_INIT_DEM.F90:370-381): radius
+    2.08e-4 (a single-precision literal), height 4x radius, the template scaled by
+    (rad-0.3dx)*height/rad and height-0.6dx, rho = 2650."""
     rad = float(np.float32(2.08e-4))
     height = rad * 4
-    radratio = (rad - 0.3 * dx) * height / rad
-    heightratio = height - 0.3 * 2 * dx
-    pi = math.acos(-1.0)
-    rho = 2.65e3
-    L = np.array(n) * dx
-    centres = np.array(centres)
-    rnd = [0.2, 0.7, 0.45]
-    vel = np.array([[1e-3, 0.0, -5e-4], [-1e-3, 2e-4, 0.0], [0.0, -3e-4, 8e-4]])
-    parts = np.zeros(3 * nl, PARCEL)
-    bodies = np.zeros(3, MULTISPHERE)
-    for j in range(3):
+    return {"rad": rad, "height": height, "radratio": (rad - 0.3 * dx) * height / rad,
+            "heightratio": height - 0.3 * 2 * dx, "pi": math.acos(-1.0), "rho": 2.65e3}
+
+
+def cylinder_bodies(centres, rnd, vel, dx):
+    """The cylinders' body records as InitCylinderParcelsDEM fills them: mass
+    properties, the cylinder inertia tensor and a rotation by pi/2*rnd about y."""
+    g = cylinder_geometry(dx)
+    rad, height, pi = g["rad"], g["height"], g["pi"]
+    centres, vel = np.asarray(centres, dtype=np.float64), np.asarray(vel, dtype=np.float64)
+    bodies = np.zeros(len(centres), MULTISPHERE)
+    for j in range(len(centres)):
         rot = rotate_matrix([0.0, pi / 2.0 * rnd[j], 0.0])
-        R = rot.reshape(3, 3)
-        x = np.stack([radratio * tpl[:, 0] + centres[j, 0], radratio * tpl[:, 1] + centres[j, 1],
-                      heightratio * tpl[:, 2] + centres[j, 2]], axis=1)
-        xt = x - centres[j]
-        x = np.stack([R[0, 0] * xt[:, 0] + R[0, 1] * xt[:, 1] + R[0, 2] * xt[:, 2],
-                      R[1, 0] * xt[:, 0] + R[1, 1] * xt[:, 1] + R[1, 2] * xt[:, 2],
-                      R[2, 0] * xt[:, 0] + R[2, 1] * xt[:, 1] + R[2, 2] * xt[:, 2]], axis=1) + centres[j]
-        sl = slice(j * nl, (j + 1) * nl)
-        parts["x"][sl] = scenario.wrap_coord(x, L)
-        parts["v"][sl] = vel[j]
-        parts["radeff"][sl] = dx * 0.75
-        parts["vol"][sl] = pi * dx / nl * (rad ** 2 + 2 * rad * height + 0.25 * dx ** 2)
-        parts["rho"][sl] = rho
-        parts["m"][sl] = parts["rho"][sl] * parts["vol"][sl]
-        parts["MSIdx"][sl] = j + 1
-        parts["globalIdx"][sl] = np.arange(1, nl + 1)
         B = bodies[j:j + 1]
         B["globalIdx"] = j + 1
         B["x"] = centres[j]
         B["v"] = vel[j]
         B["vold"] = vel[j]
         B["rad"] = rad
-        B["rho"] = rho
+        B["rho"] = g["rho"]
         B["vol"] = (pi * rad ** 2) * height
         B["m"] = B["vol"] * B["rho"]
         it = np.zeros(9)
@@ -105,6 +88,45 @@ def cylinder_case(template, centres=CYLINDER_CENTRES):
         B["rotMat"] = rot
         B["rotMatGlo"] = rot
         B["rotMatGloOld"] = rot
+    return bodies
+
+
+def cylinder_markers(tpl, bodies, dx, L=None):
+    """Every body's template markers, scaled, rotated about the body centre and
+    (with a box length L) wrapped into the box, body by body."""
+    g = cylinder_geometry(dx)
+    nl = len(tpl)
+    parts = np.zeros(len(bodies) * nl, PARCEL)
+    for j in range(len(bodies)):
+        c = bodies["x"][j]
+        R = bodies["rotMat"][j].reshape(3, 3)
+        x = np.stack([g["radratio"] * tpl[:, 0] + c[0], g["radratio"] * tpl[:, 1] + c[1],
+                      g["heightratio"] * tpl[:, 2] + c[2]], axis=1)
+        xt = x - c
+        x = np.stack([R[0, 0] * xt[:, 0] + R[0, 1] * xt[:, 1] + R[0, 2] * xt[:, 2],
+                      R[1, 0] * xt[:, 0] + R[1, 1] * xt[:, 1] + R[1, 2] * xt[:, 2],
+                      R[2, 0] * xt[:, 0] + R[2, 1] * xt[:, 1] + R[2, 2] * xt[:, 2]], axis=1) + c
+        sl = slice(j * nl, (j + 1) * nl)
+        parts["x"][sl] = x if L is None else scenario.wrap_coord(x, L)
+        parts["v"][sl] = bodies["v"][j]
+        parts["radeff"][sl] = dx * 0.75
+        parts["vol"][sl] = g["pi"] * dx / nl * (g["rad"] ** 2 + 2 * g["rad"] * g["height"] + 0.25 * dx ** 2)
+        parts["rho"][sl] = g["rho"]
+        parts["m"][sl] = parts["rho"][sl] * parts["vol"][sl]
+        parts["MSIdx"][sl] = j + 1
+        parts["globalIdx"][sl] = np.arange(1, nl + 1)
+    return parts
+
+
+def cylinder_case(template, centres=CYLINDER_CENTRES):
+    n = (48, 24, 48)
+    dx = 9e-3 / 240  # PartitionInitialization(4,1,4,240,32,240,9d-3,1.2d-3,9d-3)
+    p = make_params(*n, h=dx, dt=5e-5, coupleInterval=2, knCoeff=4e4, ResistCoeff=0.9)
+    tpl = np.loadtxt(template)
+    rnd = [0.2, 0.7, 0.45]
+    vel = np.array([[1e-3, 0.0, -5e-4], [-1e-3, 2e-4, 0.0], [0.0, -3e-4, 8e-4]])
+    bodies = cylinder_bodies(centres, rnd, vel, dx)
+    parts = cylinder_markers(tpl, bodies, dx, np.array(n) * dx)
     field = scenario.fourier_field(p, 6, 0.02, seed=5)
     return p, parts, bodies, f32_field(field)
 

@@ -680,6 +680,57 @@ def run_config(sources):
     return out
 
 
+GENERATION_FIELDS = ("x", "v", "radeff", "rho", "vol", "m", "MSIdx", "globalIdx")
+
+
+def run_generation(sources, ref_dir, seed):
+    """The reference's InitCylinderParcelsDEM (ZJS_INIT_DEM.F90:351-505) as it
+    stands, on the grid of its own run (PartitionInitialization(.,.,.,240,32,240,
+    9d-3,1.2d-3,9d-3), here one rank holding the whole box): 86 cylinders from
+    CYLINDER_LP1125.dat, rotated by pi/2 times a random number each.  The random
+    numbers (gfortran's random_number) are supplied, and SetNeighCellIndex (the
+    fluid's global neighbour table, which the generation does not read) is
+    skipped.  tests/golden/make_golden.py's cylinder generator, given the
+    reference's centres and random numbers, must produce the same records: its
+    bodies are compared in the tests, its markers here (their digests are
+    stored side by side)."""
+    import make_golden
+
+    rnd = list(np.random.default_rng(seed).random(86))
+    supply = iter(rnd)
+
+    def random_number(G, x):
+        return (next(supply),)
+
+    T = fs.Translator(sources)
+    T.build(overrides={"random_number": random_number, "setneighcellindex": lambda G: ()})
+    G = T.new_state(io_dir=ref_dir)
+    c = lambda name, *a: T.call(G, name, *a)  # noqa: E731
+    c("PartitionInitialization", 1, 1, 1, 240, 32, 240, 9e-3, 1.2e-3, 9e-3)
+    c("GridInitialization")
+    for name in ("InitParameters", "CopyGridInformationDEM", "AllocateDEM", "SetCellIndexMapDEM",
+                 "InitCylinderParcelsDEM"):
+        c(name)
+    n = G.m_np
+    parts = np.zeros(n, PARCEL)
+    for f in PARCEL.names:
+        if f != "pad_":
+            parts[f] = G.m_part.a[f.lower()][:n]
+    bodies = np.zeros(G.m_nmsglo, MULTISPHERE)
+    for f in MULTISPHERE.names:
+        bodies[f] = G.m_msglo.a[f.lower()][:G.m_nmsglo]
+    tpl = np.loadtxt(os.path.join(ref_dir, "CYLINDER_LP1125.dat"))
+    dx = 9e-3 / 240
+    assert G.m_dx == dx
+    mine = make_golden.cylinder_markers(tpl, make_golden.cylinder_bodies(bodies["x"], rnd, bodies["v"], dx), dx)
+    ref_digest = digest(*[parts[f] for f in GENERATION_FIELDS])
+    my_digest = digest(*[mine[f] for f in GENERATION_FIELDS])
+    print(f"generation: {n} markers of {len(bodies)} cylinders, generator "
+          f"{'identical' if np.array_equal(ref_digest, my_digest) else 'DIFFERENT'}", flush=True)
+    return {"rnd": np.array(rnd), "bodies": bodies, "np": np.int32(n), "marker_digest": ref_digest,
+            "generator_marker_digest": my_digest, "dx": np.float64(dx)}
+
+
 def main(ref_dir, only=None):
     sources = load_sources(ref_dir)
     jobs = {
@@ -693,6 +744,7 @@ def main(ref_dir, only=None):
         "single": lambda: run_case(sources, *single_case(), 3),
         "cylinders": lambda: run_compact(sources, *cylinder_case(ref_dir), 2),
         "config": lambda: run_config(sources),
+        "generation": lambda: run_generation(sources, ref_dir, 27),
         "corner": lambda: run_compact(sources, *corner_case(), 3),
         "edge": lambda: run_compact(sources, *edge_case(), 3),
         "empty": lambda: run_compact(sources, *empty_case(), 2),

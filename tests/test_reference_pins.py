@@ -197,6 +197,23 @@ def test_benchmark_configuration_matches_the_reference(oracle_mod):
     c.close()
 
 
+def test_cylinder_generation_matches_the_reference():
+    """The reference's own InitCylinderParcelsDEM on the grid of its run (86
+    cylinders, 96,750 markers from CYLINDER_LP1125.dat) against the cylinder
+    generator of tests/golden/make_golden.py, which built the cylinder cases:
+    every body record bit-identical here, the markers by their digests (the
+    template is the reference's data, compared when the fixture was made)."""
+    import make_golden
+
+    ref = load("generation")
+    want = ref["bodies"]
+    got = make_golden.cylinder_bodies(want["x"], ref["rnd"], want["v"], float(ref["dx"]))
+    for f in records.MULTISPHERE.names:
+        assert np.array_equal(got[f], want[f]), f"body {f}"
+    assert int(ref["np"]) == 86 * 1125
+    assert np.array_equal(ref["generator_marker_digest"], ref["marker_digest"]), "markers"
+
+
 def test_walled_case_exercises_wall_contact():
     ref = load("walled")
     f = ref["step0_probe_force"]
