@@ -1,6 +1,6 @@
 /* CPU restatement of the reference's fluid stencils (fluid.F90:2-249 and the
  * fluid halo fill of boundary.F90:122-247), test infrastructure only: the
- * parity checker for the GPU fluid kernels and their timed CPU baseline.
+ * parity reference for the GPU fluid kernels and their timed CPU baseline.
  *
  * Each statement is restated with the reference's operations in the
  * reference's order (gfortran -O3 on x86-64 without -march: left-to-right,

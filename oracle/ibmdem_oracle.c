@@ -1,7 +1,7 @@
 /*
  * ibmdem_oracle.c — CPU restatement of the IBM-DEM particle-side hot path.
  *
- * TEST INFRASTRUCTURE ONLY (parity checker and timed CPU baseline); the
+ * TEST INFRASTRUCTURE ONLY (parity reference and timed CPU baseline); the
  * product never links or calls it.  PARITY PINNED: the Fortran reference
  * cannot be compiled here and has no tests or golden vectors for this path;
  * this file restates its source, citing file:line for each routine, and

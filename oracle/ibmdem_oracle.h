@@ -1,7 +1,7 @@
 /*
  * ibmdem_oracle.h — CPU restatement of the IBM-DEM particle-side hot path.
  *
- * TEST INFRASTRUCTURE ONLY.  This library is the parity checker for the GPU
+ * TEST INFRASTRUCTURE ONLY.  This library is the parity reference for the GPU
  * library (libibmdem) and the timed CPU baseline; nothing in the product links
  * or calls it.  Only tests/, __graft_entry__.smoke() and bench.py's CPU legs
  * load it.

@@ -1,7 +1,7 @@
 /*
  * unresolved_oracle.c — CPU restatement of the unresolved CFD-DEM path.
  *
- * TEST INFRASTRUCTURE ONLY (parity checker and timed CPU baseline); the
+ * TEST INFRASTRUCTURE ONLY (parity reference and timed CPU baseline); the
  * product never links or calls it.
  *
  * PARITY UNPINNED beyond the drag law: the reference holds only the drag law
