@@ -40,6 +40,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
+sys.path.insert(0, os.path.dirname(HERE))
 sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(HERE)), "ibm-dem_gb300"))
 
 import fortran_subset as fs  # noqa: E402
@@ -680,6 +681,68 @@ def run_config(sources):
     return out
 
 
+COUPLED_FIELDS = ["u", "v", "w", "fx", "fy", "fz", "P", "Pcorr", "velDiv", "omegaX", "omegaY", "omegaZ"]
+
+
+def coupled_case():
+    """Two spheres (d = 6h) in contact on 16x12x16 between walls in y (the
+    reference's own boundary set-up, initialization.F90:317-351), a Fourier
+    field, 2 DEM sub-steps per fluid step."""
+    p = make_params(16, 12, 16, walls="y", knCoeff=1e4, ResistCoeff=0.9, coupleInterval=2)
+    field = _f32(scenario.fourier_field(p, 4, 0.02, seed=29))
+    scenario.fill_halo(p, field)
+    X = np.array([[5.1, 5.8, 7.9], [5.1 + 6.0 + 0.3, 6.1, 8.2]])
+    V = np.array([[0.02, -0.01, 0.0], [-0.02, 0.01, 0.005]])
+    parts, bodies = scenario.sphere_bodies(X, 6.0, 1.0, 1.14e3, V)
+    return "coupled", p, parts, bodies, field, None
+
+
+def pressure_solve(G, walls):
+    """SetPressureVector + PoissonSolver (poisson.F90:107-158) supplied: the pinned
+    pressure-correction system solved by the numpy FFT of tests/fft_poisson.py,
+    the interior of Pcorr written as GetLocalArray writes it."""
+    import fft_poisson
+
+    b = G.m_veldiv.a[2:-2, 2:-2, 2:-2].T
+    G.m_pcorr.a[2:-2, 2:-2, 2:-2] = fft_poisson.solve(b, (G.m_dx, G.m_dy, G.m_dz), walls).T
+    return ()
+
+
+def run_coupled(sources, steps):
+    """The reference's whole time step, FirstOrderForwardEuler (fluid.F90:252-327)
+    as it stands: uold, the forcing loop, VelocityGuess, ModifyBulkVelocity,
+    VelocityDivergence, the Poisson solve (supplied), PressureCorrection,
+    VelocityCorrection, each with its halo refill, then CloudEvolutionMS; the
+    fluid is not frozen.  Digests of the fields, the parcels and the bodies
+    (in full) after every step."""
+    t0 = time.time()
+    name, p, parts, bodies, field, probes = coupled_case()
+    walls = "".join(a for a, f in zip("xyz", range(0, 6, 2)) if int(p["bType"][f]) == 1)
+    R = ReferenceCase(sources, p, parts, bodies, field, probes)
+    R.T.ns["f_setpressurevector"] = lambda G: ()
+    R.T.ns["f_poissonsolver"] = lambda G: pressure_solve(G, walls)
+    G = R.G
+    G.m_visc = 1e-3
+    u0 = [a.T.astype(np.float32) for a in R.u0]
+    assert all(np.array_equal(a.astype(np.float64), b.T) for a, b in zip(u0, R.u0))
+    out = {"params": np.asarray(p), "in_parcels": parts, "in_bodies": bodies, "in_u": u0[0], "in_v": u0[1],
+           "in_w": u0[2], "steps": np.int32(steps), "visc": np.float64(G.m_visc),
+           "bulk": np.array([G.m_defavebulkuswitch, G.m_defavebulkvswitch, G.m_defavebulkwswitch, G.m_bulku,
+                             G.m_bulkv, G.m_bulkw], dtype=np.float64), "walls": np.array(walls)}
+    for s in range(steps):
+        R.call("FirstOrderForwardEuler")
+        parts_now, nl = R.parcels(), G.m_nplocal
+        out[f"step{s}_nlocal"] = np.int32(nl)
+        out[f"step{s}_parcel_digest"] = parcel_digest(parts_now, nl)
+        out[f"step{s}_bodies"] = R.bodies()
+        for f in COUPLED_FIELDS:
+            a = getattr(G, "m_" + f.lower()).a.T.copy()
+            # the reference accumulates fx, fy, fz into halo cells it then ignores
+            out[f"step{s}_{f}"] = digest(a[2:-2, 2:-2, 2:-2] if f in ("fx", "fy", "fz") else a)
+        print(f"coupled: step {s + 1}/{steps} after {time.time() - t0:.0f} s", flush=True)
+    return out
+
+
 GENERATION_FIELDS = ("x", "v", "radeff", "rho", "vol", "m", "MSIdx", "globalIdx")
 
 
@@ -745,6 +808,7 @@ def main(ref_dir, only=None):
         "cylinders": lambda: run_compact(sources, *cylinder_case(ref_dir), 2),
         "config": lambda: run_config(sources),
         "generation": lambda: run_generation(sources, ref_dir, 27),
+        "coupled": lambda: run_coupled(sources, 3),
         "corner": lambda: run_compact(sources, *corner_case(), 3),
         "edge": lambda: run_compact(sources, *edge_case(), 3),
         "empty": lambda: run_compact(sources, *empty_case(), 2),

@@ -214,6 +214,71 @@ def test_cylinder_generation_matches_the_reference():
     assert np.array_equal(ref["generator_marker_digest"], ref["marker_digest"]), "markers"
 
 
+def test_whole_time_step_matches_the_reference(oracle_mod):
+    """The reference's FirstOrderForwardEuler (fluid.F90:252-327) as it stands,
+    three steps on 16x12x16 between walls in y with two spheres in contact: the
+    forcing loop, VelocityGuess, ModifyBulkVelocity, VelocityDivergence, the
+    Poisson solve, PressureCorrection, VelocityCorrection (each with its halo
+    refill) and CloudEvolutionMS, the fluid evolving.  The restatement's
+    particle and fluid halves, chained in the same order with the same supplied
+    Poisson solve (tests/fft_poisson.py), agree bit for bit after every step."""
+    import fft_poisson
+
+    ref = load("coupled")
+    p = ref["params"]
+    h = (float(p["dx"]), float(p["dy"]), float(p["dz"]))
+    walls = str(ref["walls"])
+    field = [ref[f"in_{a}"].astype(np.float64) for a in "uvw"]
+    c = oracle_mod.OracleCase(p, ref["in_parcels"], ref["in_bodies"], field)
+    F = oracle_mod.OracleFluid(p)
+    F.set_fluid_params(float(ref["visc"]))
+    b = ref["bulk"]
+    FL = records.FLUID
+    c.InitializationDEM()
+    for s in range(int(ref["steps"])):
+        u0 = field
+        c.set_fluid(*u0)
+        c.MultiDirectForcing()
+        after = c.get_fluid()
+        for k, name in enumerate(("u", "v", "w", "fx", "fy", "fz")):
+            F.set_field(FL[name], after[k])
+        for k, name in enumerate(("uold", "vold", "wold")):
+            F.set_field(FL[name], u0[k])
+        F.VelocityGuess(1.0, 0.0, 1.0)
+        F.FillGhostRegionForFluid()
+        F.Boundary()
+        F.ModifyBulkVelocity(int(b[0]), int(b[1]), int(b[2]), b[3], b[4], b[5])
+        F.FillGhostRegionForFluid()
+        F.Boundary()
+        F.VelocityDivergence(1.0)
+        F.FillGhostRegionForFluid()
+        F.Boundary()
+        pc = F.get_field(FL["Pcorr"])
+        pc[2:-2, 2:-2, 2:-2] = fft_poisson.solve(F.get_field(FL["velDiv"])[2:-2, 2:-2, 2:-2], h, walls)
+        F.set_field(FL["Pcorr"], pc)
+        F.PressureCorrection()
+        F.FillGhostRegionForFluid()
+        F.Boundary()
+        F.VelocityCorrection(1.0)
+        F.FillGhostRegionForFluid()
+        F.Boundary()
+        c.CloudEvolutionMS()
+        parts, nl = c.get_parcels()
+        assert nl == int(ref[f"step{s}_nlocal"]), s
+        assert np.array_equal(mrg.parcel_digest(parts, nl), ref[f"step{s}_parcel_digest"]), f"step {s}: parcels"
+        got, want = c.get_bodies(), ref[f"step{s}_bodies"]
+        for f in records.MULTISPHERE.names:
+            assert np.array_equal(got[f], want[f]), f"step {s}: body {f}"
+        for f in mrg.COUPLED_FIELDS:
+            a = F.get_field(FL[f])
+            if f in ("fx", "fy", "fz"):
+                a = a[2:-2, 2:-2, 2:-2]
+            assert np.array_equal(digest(a), ref[f"step{s}_{f}"]), f"step {s}: {f}"
+        field = [F.get_field(FL[a]) for a in "uvw"]
+    c.close()
+    F.close()
+
+
 def test_walled_case_exercises_wall_contact():
     ref = load("walled")
     f = ref["step0_probe_force"]
