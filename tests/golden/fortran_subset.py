@@ -30,8 +30,9 @@ reassociation):
   * MPI is one rank: MPI_SENDRECV to and from rank 0 copies the message into
     the receive buffer, MPI_REDUCE copies, barriers and broadcasts do nothing.
 List-directed reads (read(unit,*)) take the next record of the file the unit
-was opened on; other statements for files and the terminal (write, print) do
-nothing.  A subroutine the sources call but do not define (PETSc) raises when
+was opened on; list-directed writes to a file unit keep each record's values,
+unformatted, under the file's name (nothing reaches the disk); writes to the
+terminal and print statements do nothing.  A subroutine the sources call but do not define (PETSc) raises when
 it is reached, unless the caller supplies it.
 """
 import math
@@ -190,6 +191,36 @@ def _io_read(G, unit, n):
 
 def _io_close(G, unit):
     G.io_units.pop(unit, None)
+
+
+def _io_write(G, unit, items):
+    """A list-directed record written to a file unit: its values are kept, in
+    order and unformatted, under the file's name (G.io_written); nothing is
+    written to disk."""
+    u = G.io_units.get(unit)
+    if u is None:
+        raise RuntimeError(f"write to unit {unit}, which no open names")
+    rec = []
+    for x in items:
+        if isinstance(x, np.ndarray):
+            rec.extend(v.item() for v in x.ravel(order="F"))
+        elif isinstance(x, np.generic):
+            rec.append(x.item())
+        else:
+            rec.append(x)
+    G.io_written.setdefault(u["name"].strip(), []).append(rec)
+
+
+def _io_internal(fmt, items):
+    """An internal write of integers (and strings) into a character variable:
+    list-directed (a blank and 11 columns for each default integer, a string
+    as it stands) or with one Iw edit descriptor."""
+    if fmt is None:
+        return "".join(x if isinstance(x, str) else f" {int(x):11d}" for x in items)
+    m = re.match(r"^\(\s*i(\d+)\s*\)$", fmt.strip().lower())
+    if not m or len(items) != 1:
+        raise NotImplementedError(f"internal write with format {fmt!r}")
+    return f"{int(items[0]):{int(m.group(1))}d}"
 
 
 # ----------------------------------------------------------------------------
@@ -551,7 +582,7 @@ class Sym:
 
 
 _TYPESPEC = re.compile(r"^(integer|real\s*\*\s*8|real\s*\*\s*4|real|double\s+precision|logical|"
-                       r"character\s*\(\s*len\s*=\s*\d+\s*\)|character\s*\*\s*\d+|character|"
+                       r"character\s*\(\s*len\s*=\s*(?:\d+|\*)\s*\)|character\s*\*\s*\d+|character|"
                        r"type\s*\(\s*\w+\s*\)|petscint|petscscalar|petscerrorcode)(?=\s|,|::|$)")
 _OPAQUE = re.compile(r"^(ksp|mat|vec|is|vecscatter)\s+[a-z_]\w*(\s*,\s*[a-z_]\w*)*$")
 
@@ -897,6 +928,7 @@ class Translator:
         Files the sources read are looked up in `io_dir`."""
         G = type("RankState", (), {})()
         G.io_units = {}
+        G.io_written = {}
         G.io_path = lambda name: os.path.join(io_dir, name.strip())
         for name, s in self.msyms.items():
             if s.param is not None:
@@ -926,7 +958,7 @@ class Translator:
         ns = {"FArr": FArr, "_dummy": _dummy, "_recview": _recview, "_idiv": _idiv, "_imod": _imod,
               "_powi": _powi, "_powi4": _powi4, "_fsum": _fsum, "_floor": _floor, "_trunc": _trunc,
               "_nint": _nint, "f32": f32, "_flat": _flat, "_missing": _missing, "_io_open": _io_open,
-              "_io_read": _io_read, "_io_close": _io_close}
+              "_io_read": _io_read, "_io_close": _io_close, "_io_write": _io_write, "_io_internal": _io_internal}
         for tn, dt in self.dtypes.items():
             ns["_DT_" + tn] = dt
         for k, f in BUILTIN_CALLS.items():
@@ -1127,11 +1159,14 @@ class Translator:
         raise SyntaxError(f"statement {st}")
 
     def _io(self, s):
-        """open(unit, file=...), read(unit, *) items and close(unit); anything
-        else (writes, formats, prints) does nothing."""
-        m = re.match(r"^(open|read|close)\s*\(", s)
+        """open(unit, file=...), read(unit, *) items, write(unit, *) items,
+        internal writes of integers and close(unit); writes to the terminal,
+        print and format statements do nothing."""
+        m = re.match(r"^(open|read|close|write)\s*\(", s)
         if not m:
             return ["pass"]
+        if m.group(1) == "write":
+            return self._write(s, m)
         j = _match_paren(s, m.end() - 1)
         ctl = _split_top(s[m.end():j], ",")
         unit = self._ex(parse_expr(ctl[0])).code
@@ -1156,6 +1191,31 @@ class Translator:
             val = f"float({v}[{k}].replace('d', 'e').replace('D', 'E'))" if conv != "int" else f"int({v}[{k}])"
             out.append(f"{L.code} = {val if conv != 'f32' else 'f32(' + val + ')'}")
         return out
+
+    def _write(self, s, m):
+        j = _match_paren(s, m.end() - 1)
+        ctl = [c.strip() for c in _split_top(s[m.end():j], ",")]
+        items = [parse_expr(x) for x in _split_top(s[j + 1:], ",") if x.strip()]
+        if ctl[0] == "*":
+            return ["pass"]
+        fmt = None if len(ctl) < 2 or ctl[1] == "*" else ctl[1]
+        U = self._ex(parse_expr(ctl[0]))
+        if U.kind == "c":
+            if fmt is not None and fmt.startswith(("'", '"')):
+                fmt = self._ex(parse_expr(fmt)).code
+            elif fmt is not None:
+                return [f"raise NotImplementedError({('internal write: ' + s)!r})"]
+            L = self._des(parse_expr(ctl[0]), lvalue=True)
+            vals = ", ".join(self._ex(x).code for x in items)
+            return [f"{L.code} = _io_internal({fmt}, [{vals}])"]
+        if fmt is not None:
+            # a formatted record to a file: an error if it is ever reached
+            return [f"raise NotImplementedError({('formatted write: ' + s)!r})"]
+        vals = []
+        for x in items:
+            X = self._ex(x)
+            vals.append(X.code if X.rank == 0 else f"np.array({X.code})")
+        return [f"_io_write(G, {U.code}, [{', '.join(vals)}])"]
 
     def _cond(self, e):
         return self._ex(e).code

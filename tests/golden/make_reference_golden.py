@@ -47,12 +47,12 @@ import fortran_subset as fs  # noqa: E402
 from ibmdem import scenario  # noqa: E402
 from ibmdem.records import MULTISPHERE, PARCEL, WALL_PROBE, field_shape, make_params  # noqa: E402
 
-# the makefile's sources, less the main program, the PETSc Poisson solve and the output routines
+# the makefile's sources, less the main program, the PETSc Poisson solve and the fluid's file output
 SOURCES = ["vars.F90", "ZJS_VARS.F90", "boundary.F90", "initialization.F90", "allocate.F90", "fluid.F90",
            "interpolation.F90", "ZJS_AUXILIARY_DEM.F90", "ZJS_COLLISION_DEM.F90", "ZJS_DRAGFORCE_DEM.F90",
            "ZJS_EVOLUTION_DEM.F90", "ZJS_INIT_DEM.F90", "ZJS_INTERPOLATE_DEM.F90", "ZJS_MPI_DEM.F90",
            "ZJS_UPDATE_LIST_DEM.F90", "ZJS_VOLUMEFRACTION_DEM.F90", "ZJS_MS_DEM.F90",
-           "couplesolverCylinder.F90"]
+           "couplesolverCylinder.F90", "ZJS_IO_DEM.F90"]
 # maxPartNo sizes neighCellWeight(125, maxPartNo, 3): 100000 would take 300 MB for cases of a few thousand
 CAPACITIES = {"maxpartno": 8000}
 
@@ -743,6 +743,32 @@ def run_coupled(sources, steps):
     return out
 
 
+def run_output(sources):
+    """The reference's output routines after one coupled step of the periodic
+    case: OutputCloudTecplot (ZJS_IO_DEM.F90:82-121, the marker file) and
+    PostProcessing (fluid.F90:368-404, one probe line per body), their records'
+    values as the translator keeps them, beside the parcels and bodies they were
+    written from."""
+    name, p, parts, bodies, field, probes = periodic_case()
+    R = ReferenceCase(sources, p, parts, bodies, field, probes)
+    R.multi_direct_forcing()
+    R.cloud_evolution()
+    G = R.G
+    G.m_step = 7
+    R.call("OutputCloudTecplot", "1")
+    R.call("PostProcessing")
+    out = {"params": np.asarray(p), "parcels": R.parcels()[:G.m_nplocal], "bodies": R.bodies(),
+           "step": np.int32(G.m_step), "rhof": np.float64(G.m_rhof)}
+    recs = G.io_written["Results/Particle_1_0.dat"]
+    out["marker_header"] = np.array([" ".join(str(x) for x in recs[0]), " ".join(str(x) for x in recs[1])])
+    out["marker_rows"] = np.array(recs[2:], dtype=np.float64)
+    ids = sorted(int(k.split("/")[-1].split(".")[0]) for k in G.io_written if k.endswith(".probe"))
+    out["probe_ids"] = np.array(ids, np.int32)
+    out["probe_rows"] = np.array([G.io_written[f"./DEM/{i}.probe"][0] for i in ids], dtype=np.float64)
+    print(f"output: {len(recs) - 2} marker records, {len(ids)} probe lines", flush=True)
+    return out
+
+
 GENERATION_FIELDS = ("x", "v", "radeff", "rho", "vol", "m", "MSIdx", "globalIdx")
 
 
@@ -809,6 +835,7 @@ def main(ref_dir, only=None):
         "config": lambda: run_config(sources),
         "generation": lambda: run_generation(sources, ref_dir, 27),
         "coupled": lambda: run_coupled(sources, 3),
+        "output": lambda: run_output(sources),
         "corner": lambda: run_compact(sources, *corner_case(), 3),
         "edge": lambda: run_compact(sources, *edge_case(), 3),
         "empty": lambda: run_compact(sources, *empty_case(), 2),

@@ -279,6 +279,30 @@ def test_whole_time_step_matches_the_reference(oracle_mod):
     F.close()
 
 
+def test_output_files_hold_the_reference_values(tmp_path):
+    """The library's host writers against the reference's own output routines
+    after one coupled step: the marker file of OutputCloudTecplot
+    (ZJS_IO_DEM.F90:82-121) and the per-body probe lines of PostProcessing
+    (fluid.F90:392-397) hold the same records and, read back from their 17
+    significant digits, exactly the values the reference writes (the body
+    accelerations fdrag/m*rhof, fmom/I*rhof and fcol/m formed as it forms
+    them)."""
+    from ibmdem import api
+
+    ref = load("output")
+    path = tmp_path / "Particle_1_0.dat"
+    api.write_tecplot_markers(path, ref["parcels"])
+    lines = path.read_text().splitlines()
+    assert [" ".join(x.split()) for x in lines[:2]] == list(ref["marker_header"])
+    rows = np.array([[float(t) for t in x.split()] for x in lines[2:]])
+    assert np.array_equal(rows, ref["marker_rows"])
+    api.write_body_probes(tmp_path, int(ref["step"]), ref["bodies"], float(ref["rhof"]))
+    for k, i in enumerate(ref["probe_ids"]):
+        line = (tmp_path / f"{i}.probe").read_text().splitlines()
+        assert len(line) == 1
+        assert np.array_equal(np.array([float(t) for t in line[0].split()]), ref["probe_rows"][k]), i
+
+
 def test_walled_case_exercises_wall_contact():
     ref = load("walled")
     f = ref["step0_probe_force"]
