@@ -272,7 +272,11 @@ BUILTIN_CALLS = {
 }
 
 MPI_CONSTANTS = {"mpi_comm_world": 0, "mpi_integer": 1, "mpi_double_precision": 2, "mpi_double": 2,
-                 "mpi_sum": 3, "mpi_max": 4, "mpi_status_size": 6, "petsc_null_character": 0}
+                 "mpi_sum": 3, "mpi_max": 4, "mpi_status_size": 6, "petsc_null_character": 0,
+                 # names PETSc's Fortran headers define, for calls the caller supplies
+                 "petsc_comm_world": 0, "petsc_decide": -1, "petsc_null_integer": 0, "petsc_copy_values": 0,
+                 "matmpiaij": 0, "mat_final_assembly": 0, "insert_values": 1, "add_values": 2,
+                 "scatter_forward": 0, "petsc_viewer_stdout_world": 0}
 
 # ----------------------------------------------------------------------------
 # source lines
@@ -624,7 +628,8 @@ def _parse_dims(text):
 def parse_decl(stmt):
     """A declaration statement -> list of (Sym, init_ast); None when `stmt` is not one."""
     if _OPAQUE.match(stmt):
-        return []
+        names = re.split(r"\s*,\s*", stmt.split(None, 1)[1].strip())
+        return [(Sym(n, "o"), None) for n in names]
     m = _TYPESPEC.match(stmt)
     if not m:
         return None
@@ -942,7 +947,7 @@ class Translator:
             elif s.kind == "t":
                 val = np.zeros((), dtype=self.dtypes[s.tname])
             else:
-                val = {"i": 0, "r8": 0.0, "r4": 0.0, "l": False, "c": ""}[s.kind]
+                val = {"i": 0, "r8": 0.0, "r4": 0.0, "l": False, "c": "", "o": None}[s.kind]
             setattr(G, "m_" + name, val)
         return G
 
@@ -1043,7 +1048,7 @@ class Translator:
 
     @staticmethod
     def _zero(kind):
-        return {"i": "0", "r8": "0.0", "r4": "0.0", "l": "False", "c": "''"}[kind]
+        return {"i": "0", "r8": "0.0", "r4": "0.0", "l": "False", "c": "''", "o": "None"}[kind]
 
     def _sym(self, name):
         u = self.u

@@ -769,6 +769,51 @@ def run_output(sources):
     return out
 
 
+PETSC_CALLS = ("MatCreate", "MatSetSizes", "MatSetType", "MatMPIAIJSetPreallocation", "MatSetFromOptions",
+               "MatSetup", "VecCreateMPI", "VecSetFromOptions", "ISCreateGeneral", "VecScatterCreate",
+               "MatAssemblyBegin", "MatAssemblyEnd", "VecAssemblyBegin", "VecAssemblyEnd")
+
+
+def run_poisson(ref_dir, name, p, seed):
+    """The reference's pressure-correction system as poisson.F90 assembles it
+    (InitPressureCorrectionMatrix, SetPressureCorrectionJacobian and
+    SetPressureVector, poisson.F90:2-131): the translator runs them with
+    PETSc's MatSetValues and VecSetValues supplied as recorders (ADD_VALUES
+    accumulating, INSERT_VALUES replacing) and the rest of PETSc's calls as
+    nothing; the matrix in coordinate form and the right-hand side of a random
+    divergence are stored."""
+    sources = load_sources(ref_dir) + [("poisson.F90", open(os.path.join(ref_dir, "poisson.F90")).read())]
+    entries, rhs = {}, {}
+
+    def mat_set_values(G, mat, m, idxm, n, idxn, v, mode, ierr):
+        assert m == 1 and n == 1
+        key = (int(idxm), int(idxn))
+        entries[key] = (entries.get(key, 0.0) + v) if mode == fs.MPI_CONSTANTS["add_values"] else v
+        return (mat, m, idxm, n, idxn, v, mode, 0)
+
+    def vec_set_values(G, vec, n, idx, v, mode, ierr):
+        assert n == 1
+        rhs[int(idx)] = v
+        return (vec, n, idx, v, mode, 0)
+
+    noop = lambda G, *a: a  # noqa: E731
+    extra = {c.lower(): noop for c in PETSC_CALLS}
+    extra.update({"matsetvalues": mat_set_values, "vecsetvalues": vec_set_values})
+    R = ReferenceFluid(sources, p, 1e-3, extra=extra)
+    R.call("InitPressureCorrectionMatrix")
+    R.call("SetPressureCorrectionJacobian")
+    div = np.random.default_rng(seed).standard_normal(field_shape(p))
+    R.set("velDiv", div)
+    R.call("SetPressureVector")
+    keys = sorted(entries)
+    n = int(p["nx"]) * int(p["ny"]) * int(p["nz"])
+    assert sorted(rhs) == list(range(n))
+    print(f"{name}: {len(keys)} matrix entries on {n} rows", flush=True)
+    return {"params": np.asarray(p), "rows": np.array([k[0] for k in keys], np.int32),
+            "cols": np.array([k[1] for k in keys], np.int32), "vals": np.array([entries[k] for k in keys]),
+            "velDiv": div, "rhs": np.array([rhs[i] for i in range(n)])}
+
+
 GENERATION_FIELDS = ("x", "v", "radeff", "rho", "vol", "m", "MSIdx", "globalIdx")
 
 
@@ -836,6 +881,9 @@ def main(ref_dir, only=None):
         "generation": lambda: run_generation(sources, ref_dir, 27),
         "coupled": lambda: run_coupled(sources, 3),
         "output": lambda: run_output(sources),
+        "poisson_walls_y": lambda: run_poisson(ref_dir, "poisson_walls_y", make_params(6, 5, 4, walls="y", h=0.5),
+                                               31),
+        "poisson_periodic": lambda: run_poisson(ref_dir, "poisson_periodic", make_params(5, 4, 6), 32),
         "corner": lambda: run_compact(sources, *corner_case(), 3),
         "edge": lambda: run_compact(sources, *edge_case(), 3),
         "empty": lambda: run_compact(sources, *empty_case(), 2),

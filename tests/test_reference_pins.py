@@ -303,6 +303,35 @@ def test_output_files_hold_the_reference_values(tmp_path):
         assert np.array_equal(np.array([float(t) for t in line[0].split()]), ref["probe_rows"][k]), i
 
 
+@pytest.mark.parametrize("name", ["poisson_walls_y", "poisson_periodic"])
+def test_pressure_system_matches_the_reference(oracle_mod, name):
+    """The pressure-correction matrix the restatement applies (the system the
+    library's Poisson solve is checked against) equals, entry for entry, the
+    one the reference's SetPressureCorrectionJacobian assembles through
+    MatSetValues (poisson.F90:46-105), pinned row included; and the reference's
+    SetPressureVector right-hand side is the divergence with the pinned entry
+    set to zero."""
+    ref = load(name)
+    p = ref["params"]
+    n = int(p["nx"]) * int(p["ny"]) * int(p["nz"])
+    A = np.zeros((n, n))
+    A[ref["rows"], ref["cols"]] = ref["vals"]
+    F = oracle_mod.OracleFluid(p)
+    got = np.zeros((n, n))
+    inner = (int(p["nz"]), int(p["ny"]), int(p["nx"]))
+    for c in range(n):
+        unit = np.zeros(n)
+        unit[c] = 1.0
+        e = np.zeros(F.shape)
+        e[2:-2, 2:-2, 2:-2] = unit.reshape(inner)
+        got[:, c] = F.PressureOperator(e)[2:-2, 2:-2, 2:-2].reshape(-1)
+    F.close()
+    assert np.array_equal(got, A)
+    want = ref["velDiv"][2:-2, 2:-2, 2:-2].reshape(-1).copy()
+    want[0] = 0.0
+    assert np.array_equal(ref["rhs"], want)
+
+
 def test_walled_case_exercises_wall_contact():
     ref = load("walled")
     f = ref["step0_probe_force"]
