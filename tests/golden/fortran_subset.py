@@ -137,6 +137,22 @@ class FArr:
         return FArr(np.zeros(shape, dtype=dtype, order="F"), [int(lo) for lo, _ in bounds])
 
 
+def _ck(i, n):
+    """A subscript checked against its dimension's extent."""
+    if 0 <= i < n:
+        return i
+    raise IndexError(f"subscript {i} outside the extent {n} (counted from 0)")
+
+
+def _cks(lo, hi, n):
+    """A section lo:hi checked against its dimension's extent (empty sections pass)."""
+    lo = 0 if lo is None else lo
+    hi = n if hi is None else hi
+    if hi > lo and (lo < 0 or hi > n):
+        raise IndexError(f"section {lo}:{hi} outside the extent {n} (counted from 0)")
+    return slice(lo, hi)
+
+
 def _dummy(arg, lbounds, shape):
     """An explicit-shape dummy argument over the actual argument's storage."""
     a = arg.a if isinstance(arg, FArr) else arg
@@ -853,7 +869,10 @@ class E:
 
 
 class Translator:
-    def __init__(self, files, param_overrides=None):
+    def __init__(self, files, param_overrides=None, check_bounds=False):
+        """`check_bounds` checks every subscript and section against its
+        dimension's extent (slower)."""
+        self.check_bounds = check_bounds
         self.modules, self.subs = parse_sources(files)
         self.param_overrides = {k.lower(): v for k, v in (param_overrides or {}).items()}
         self.msyms, self.types, self.pvals = {}, {}, dict(MPI_CONSTANTS)
@@ -963,7 +982,8 @@ class Translator:
         ns = {"FArr": FArr, "_dummy": _dummy, "_recview": _recview, "_idiv": _idiv, "_imod": _imod,
               "_powi": _powi, "_powi4": _powi4, "_fsum": _fsum, "_floor": _floor, "_trunc": _trunc,
               "_nint": _nint, "f32": f32, "_flat": _flat, "_missing": _missing, "_io_open": _io_open,
-              "_io_read": _io_read, "_io_close": _io_close, "_io_write": _io_write, "_io_internal": _io_internal}
+              "_io_read": _io_read, "_io_close": _io_close, "_io_write": _io_write, "_io_internal": _io_internal,
+              "_ck": _ck, "_cks": _cks}
         for tn, dt in self.dtypes.items():
             ns["_DT_" + tn] = dt
         for k, f in BUILTIN_CALLS.items():
@@ -1421,13 +1441,18 @@ class Translator:
             return E(f"({x.code}).size", "i")
         raise SyntaxError(name)
 
-    def _index(self, s, k, a, static_lb, base):
-        """Code of one subscript of dimension k: (code, is_slice)."""
+    def _index(self, s, k, a, static_lb, base, extent=None):
+        """Code of one subscript of dimension k: (code, is_slice); `extent` is
+        the code of the dimension's length, for the bounds checks."""
         off = str(static_lb) if static_lb is not None else f"{base}.o{k}"
         if a[0] == "range":
-            lo = "" if a[1] is None else f"({self._iexpr(a[1])})-{off}"
-            hi = "" if a[2] is None else f"({self._iexpr(a[2])})-{off}+1"
-            return f"{lo}:{hi}", True
+            lo = None if a[1] is None else f"({self._iexpr(a[1])})-{off}"
+            hi = None if a[2] is None else f"({self._iexpr(a[2])})-{off}+1"
+            if self.check_bounds and extent is not None:
+                return f"_cks({lo}, {hi}, {extent})", True
+            return f"{lo or ''}:{hi or ''}", True
+        if self.check_bounds and extent is not None:
+            return f"_ck(({self._iexpr(a)})-{off}, {extent})", False
         return f"({self._iexpr(a)})-{off}", False
 
     def _iexpr(self, a):
@@ -1463,7 +1488,7 @@ class Translator:
                 lbs = self._static_lbs(s, s.dims)
                 sub = args if args is not None else [("range", None, None)] * len(s.dims)
                 for k, a in enumerate(sub):
-                    c, sl = self._index(s, k, a, lbs[k], base)
+                    c, sl = self._index(s, k, a, lbs[k], base, f"{base}.a.shape[{k}]")
                     idx.append(c)
                     rank += sl
                 arr = f"{base}.a['{comp}']"
@@ -1474,8 +1499,9 @@ class Translator:
             if f.dims:
                 flbs = [self._const(lo, "i") for lo, _ in f.dims]
                 sub = cargs if cargs is not None else [("range", None, None)] * len(f.dims)
+                fext = [self._const(hi, "i") - self._const(lo, "i") + 1 for lo, hi in f.dims]
                 for k, a in enumerate(sub):
-                    c, sl = self._index(f, k, a, flbs[k], None)
+                    c, sl = self._index(f, k, a, flbs[k], None, str(fext[k]))
                     idx.append(c)
                     rank += sl
             elif cargs is not None:
@@ -1497,7 +1523,7 @@ class Translator:
         lbs = self._static_lbs(s, s.dims)
         idx, rank = [], 0
         for k, a in enumerate(args):
-            c, sl = self._index(s, k, a, lbs[k], base)
+            c, sl = self._index(s, k, a, lbs[k], base, f"{base}.a.shape[{k}]")
             idx.append(c)
             rank += sl
         code = f"{base}.a[{', '.join(idx)}]"

@@ -30,7 +30,7 @@ reference hard-codes or a step it takes on several ranks only):
 Bodies never straddle a periodic face in these cases: there the reference's
 raw body-relative vector and the nearest-image one of the library agree.
 
-Usage: python tests/golden/make_reference_golden.py <reference source dir> [fixture names]
+Usage: python tests/golden/make_reference_golden.py <reference source dir> [fixture names] [--check-bounds]
 """
 import os
 import sys
@@ -55,6 +55,8 @@ SOURCES = ["vars.F90", "ZJS_VARS.F90", "boundary.F90", "initialization.F90", "al
            "couplesolverCylinder.F90", "ZJS_IO_DEM.F90"]
 # maxPartNo sizes neighCellWeight(125, maxPartNo, 3): 100000 would take 300 MB for cases of a few thousand
 CAPACITIES = {"maxpartno": 8000}
+# --check-bounds on the command line checks every subscript of the reference's statements against its extent
+CHECK_BOUNDS = False
 
 
 def load_sources(ref_dir):
@@ -68,7 +70,7 @@ class ReferenceCase:
         """`one_rank_bodies` keeps the reference's own one-rank body update
         (defined for a single body) instead of its multi-rank branch."""
         self.p = p
-        self.T = fs.Translator(sources, capacities or CAPACITIES)
+        self.T = fs.Translator(sources, capacities or CAPACITIES, CHECK_BOUNDS)
         overrides = {"setboundarytype": self._set_boundary_type}
         if not one_rank_bodies:
             overrides.update({"assembleforcems": self._assemble_force_ms,
@@ -270,7 +272,7 @@ class ReferenceFluid:
 
     def __init__(self, sources, p, visc, extra=None):
         self.p = p
-        self.T = fs.Translator(sources, CAPACITIES)
+        self.T = fs.Translator(sources, CAPACITIES, CHECK_BOUNDS)
         overrides = {"setboundarytype": lambda G: ReferenceCase._set_boundary_type(self, G)}
         overrides.update(extra or {})
         self.T.build(overrides=overrides)
@@ -365,7 +367,7 @@ def run_drag(sources, seed, n=400):
     fluid states covering both Reynolds-number branches, the Rep >= 1 clamp and
     both voidage branches."""
     rng = np.random.default_rng(seed)
-    T = fs.Translator(sources, CAPACITIES)
+    T = fs.Translator(sources, CAPACITIES, CHECK_BOUNDS)
     T.build()
     G = T.new_state()
     rho = rng.uniform(500.0, 3000.0, n)
@@ -836,7 +838,7 @@ def run_generation(sources, ref_dir, seed):
     def random_number(G, x):
         return (next(supply),)
 
-    T = fs.Translator(sources)
+    T = fs.Translator(sources, None, CHECK_BOUNDS)
     T.build(overrides={"random_number": random_number, "setneighcellindex": lambda G: ()})
     G = T.new_state(io_dir=ref_dir)
     c = lambda name, *a: T.call(G, name, *a)  # noqa: E731
@@ -897,6 +899,8 @@ def main(ref_dir, only=None):
 
 
 if __name__ == "__main__":
-    if len(sys.argv) < 2:
+    args = [a for a in sys.argv[1:] if a != "--check-bounds"]
+    CHECK_BOUNDS = len(args) < len(sys.argv) - 1
+    if not args:
         sys.exit(__doc__)
-    main(sys.argv[1], sys.argv[2:])
+    main(args[0], args[1:])

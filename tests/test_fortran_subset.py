@@ -110,6 +110,13 @@ implicit none
     write(11,*) "ignored", n
     close(11)
 endsubroutine
+subroutine oob(k,x)
+implicit none
+    integer::k
+    real*8::x,a(1:3)
+    a(:) = 1d0
+    x = a(k)
+endsubroutine
 subroutine sendself(out)
 implicit none
     integer::out(1:2),buf(1:2),st(MPI_STATUS_SIZE),ierr
@@ -203,3 +210,16 @@ def test_list_directed_reads(tmp_path):
     assert r[1] == 2
     assert a[:, 0].tolist() == [0.1, -2.5e-3, 7.0] and a[:, 1].tolist() == [1e-3, 4.0, 5.0]
     assert not (tmp_path / "log.txt").exists()
+
+
+def test_bounds_checks():
+    import pytest
+
+    T = fs.Translator([("t.F90", SRC)], check_bounds=True)
+    T.build()
+    G = T.new_state()
+    assert T.call(G, "oob", 3, 0.0)[1] == 1.0
+    for k in (0, 4):
+        with pytest.raises(IndexError):
+            T.call(G, "oob", k, 0.0)
+    T.call(G, "sections", -1, 2)  # sections inside their bounds pass
