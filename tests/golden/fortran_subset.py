@@ -27,6 +27,10 @@ reassociation):
     (Python's math module), as the C restatement's do;
   * sum() adds in array element order from 0;
   * local variables start at zero (Fortran leaves them undefined);
+  * subscripts are not checked unless the translator is built with
+    check_bounds, which checks every subscript and section against its
+    dimension's extent (numpy would otherwise take a negative index from the
+    end without complaint);
   * MPI is one rank: MPI_SENDRECV to and from rank 0 copies the message into
     the receive buffer, MPI_REDUCE copies, barriers and broadcasts do nothing.
 List-directed reads (read(unit,*)) take the next record of the file the unit
