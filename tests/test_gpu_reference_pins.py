@@ -1,15 +1,14 @@
 """The CUDA library against the reference's own subroutines, through the C ABI.
 
-The fixtures tests/golden/ref_{periodic,walled}.npz hold the state of the
-reference's Fortran statements (run by tests/golden/make_reference_golden.py)
-after InitializationDEM and after each forcing loop and CloudEvolutionMS of
-three coupled steps.  The library replays the same stages from the same
-inputs.  Up to and including the first forcing loop it must agree bit for bit:
-cell lists, contact lists, every parcel field (images included), the fields
-u, v, w with their halo and fx, fy, fz, the bodies.  From the first
-CloudEvolutionMS on, the body rotation goes through CUDA's cos and sin instead
-of the host's: bodies, parcels and fields then agree to 1e-9 of each field's
-largest value, and the cell and contact lists stay identical.
+The fixtures tests/golden/ref_*.npz hold the state of the reference's Fortran
+statements (run by tests/golden/make_reference_golden.py) after
+InitializationDEM and after each forcing loop and CloudEvolutionMS of two or
+three coupled steps.  The library replays the same stages from the same inputs
+and agrees bit for bit at every one of them: cell lists, contact lists, every
+parcel field the reference defines (images included), the fields u, v, w with
+their halo and fx, fy, fz, the bodies, the wall-probe forces.  (The body
+rotation goes through CUDA's cos and sin, the reference's through the host's;
+on these cases they agree to the last bit.)
 """
 import os
 import sys
@@ -17,7 +16,6 @@ import sys
 import numpy as np
 import pytest
 
-import cases
 
 pytestmark = pytest.mark.gpu
 
@@ -28,14 +26,11 @@ BODY_FIELDS = ("x", "v", "omega", "AngMom", "rotMat", "rotMatGlo", "fdrag", "fco
                "fmomHydro", "vold", "AngMomOld")
 
 
-def same_or_close(a, b, exact, what):
-    if exact:
-        assert np.array_equal(a, b), what
-    else:
-        assert cases.rel_close(a, b, 1e-9), what
+def same(a, b, what):
+    assert np.array_equal(a, b), what
 
 
-def check(ref, tag, c, exact, fields=False):
+def check(ref, tag, c, fields=False):
     s, i = c.get_cell_lists()
     assert np.array_equal(s, ref[tag + "_cell_start"]) and np.array_equal(i, ref[tag + "_cell_items"]), \
         f"{tag}: cell lists"
@@ -48,19 +43,19 @@ def check(ref, tag, c, exact, fields=False):
     for f in ("globalIdx", "cellIdx", "MSIdx", "pType"):
         assert np.array_equal(parts[f], want[f]), f"{tag}: parcel {f}"
     for f in ("x", "v", "fdrag", "vol", "m", "radeff"):
-        same_or_close(parts[f], want[f], exact, f"{tag}: parcel {f}")
+        same(parts[f], want[f], f"{tag}: parcel {f}")
     for f in ("fcol", "vgap"):
-        same_or_close(parts[f][:nl], want[f][:nl], exact, f"{tag}: local parcel {f}")
+        same(parts[f][:nl], want[f][:nl], f"{tag}: local parcel {f}")
     assert set(IMAGE_FIELDS) >= {"x", "v", "fdrag"}
     bodies, wb = c.get_bodies(), ref[tag + "_bodies"]
     for f in BODY_FIELDS:
-        same_or_close(bodies[f], wb[f], exact, f"{tag}: body {f}")
+        same(bodies[f], wb[f], f"{tag}: body {f}")
     if len(ref[tag + "_probe_force"]):
         got = np.array([p["force"] for p in c.get_wall_probes()])
-        same_or_close(got, ref[tag + "_probe_force"], exact, f"{tag}: probe forces")
+        same(got, ref[tag + "_probe_force"], f"{tag}: probe forces")
     if fields:
         for name, a in zip(("u", "v", "w", "fx", "fy", "fz"), c.get_fluid()):
-            same_or_close(a[2:-2, 2:-2, 2:-2], ref[f"{tag}_{name}"], exact, f"{tag}: {name}")
+            same(a[2:-2, 2:-2, 2:-2], ref[f"{tag}_{name}"], f"{tag}: {name}")
 
 
 @pytest.mark.parametrize("name", ["periodic", "walled", "single"])
@@ -72,13 +67,13 @@ def test_library_matches_the_reference(gpu_lib, name):
         if len(ref["in_probes"]):
             c.set_wall_probes(ref["in_probes"])
         c.InitializationDEM()
-        check(ref, "init", c, exact=True)
+        check(ref, "init", c)
         for s in range(int(ref["steps"])):
             c.set_fluid(*field)
             c.MultiDirectForcing()
-            check(ref, f"mdf{s}", c, exact=(s == 0), fields=True)
+            check(ref, f"mdf{s}", c, fields=True)
             c.CloudEvolutionMS()
-            check(ref, f"step{s}", c, exact=False)
+            check(ref, f"step{s}", c)
     finally:
         c.close()
 
@@ -87,10 +82,11 @@ def test_library_matches_the_reference(gpu_lib, name):
 @pytest.mark.parametrize("name", ["corner", "edge", "empty", "cylinders"])
 def test_compact_cases(gpu_lib, name):
     """Fixtures stored as digests (tests/golden/ref_{corner,edge,empty,cylinders}.npz):
-    after InitializationDEM the parcels, cell lists, contact lists and bodies are
-    bit-identical, and for the unit-spacing cases the parcels and fields after
-    the first forcing loop too; after each coupled step the bodies, and at the
-    end every parcel position and velocity, agree to 1e-9."""
+    every stage's parcels, cell lists, contact lists, fields and probe forces
+    match the reference's digests, the bodies and the final parcel positions and
+    velocities are bit-identical."""
+    from test_reference_pins import compact_stage
+
     ref = load(name)
     field = tuple(ref[f"in_{a}"].astype(np.float64) for a in "uvw")
     c = gpu_lib.Case(ref["params"], ref["in_parcels"], ref["in_bodies"], field, device=0)
@@ -98,25 +94,15 @@ def test_compact_cases(gpu_lib, name):
         if len(ref["in_probes"]):
             c.set_wall_probes(ref["in_probes"])
         c.InitializationDEM()
-        parts, nl = c.get_parcels()
-        assert np.array_equal(mrg.parcel_digest(parts, nl), ref["init_parcel_digest"]), "parcels"
-        assert np.array_equal(mrg.digest(*c.get_cell_lists()), ref["init_cell_digest"]), "cell lists"
-        assert np.array_equal(mrg.digest(*c.get_collision_lists()), ref["init_pair_digest"]), "contact lists"
+        compact_stage(ref, "init", c, windows=False)
         for s in range(int(ref["steps"])):
             c.set_fluid(*field)
             c.MultiDirectForcing()
-            if s == 0 and float(ref["params"]["dx"]) == 1.0:
-                parts, nl = c.get_parcels()
-                assert np.array_equal(mrg.parcel_digest(parts, nl), ref["mdf0_parcel_digest"]), "mdf0 parcels"
-                assert np.array_equal(mrg.field_digest(c.get_fluid()), ref["mdf0_field_digest"]), "mdf0 fields"
+            compact_stage(ref, f"mdf{s}", c, fields=True, windows=False)
             c.CloudEvolutionMS()
-            bodies, wb = c.get_bodies(), ref[f"step{s}_bodies"]
-            for f in BODY_FIELDS:
-                assert cases.rel_close(bodies[f], wb[f], 1e-9), f"step {s}: body {f}"
+            compact_stage(ref, f"step{s}", c, windows=False)
         parts, _ = c.get_parcels()
-        if len(parts):
-            assert cases.rel_close(parts["x"], ref["final_x"], 1e-9)
-            assert cases.rel_close(parts["v"], ref["final_v"], 1e-9)
+        assert np.array_equal(parts["x"], ref["final_x"]) and np.array_equal(parts["v"], ref["final_v"])
     finally:
         c.close()
 

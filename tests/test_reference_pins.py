@@ -106,8 +106,9 @@ def test_coupled_steps_match_the_reference(oracle_mod, name):
     c.close()
 
 
-def compact_stage(ref, tag, c, fields=False, bodies=True):
-    """A stage of a fixture stored as digests (bodies and probe forces in full)."""
+def compact_stage(ref, tag, c, fields=False, bodies=True, windows=True):
+    """A stage of a fixture stored as digests (bodies and probe forces in full);
+    `windows` off for a case without get_weights."""
     parts, nl = c.get_parcels()
     assert nl == int(ref[tag + "_nlocal"]) and len(parts) == int(ref[tag + "_np"]), tag
     assert np.array_equal(mrg.parcel_digest(parts, nl), ref[tag + "_parcel_digest"]), f"{tag}: parcels"
@@ -117,8 +118,9 @@ def compact_stage(ref, tag, c, fields=False, bodies=True):
             assert np.array_equal(got[f], wb[f]), f"{tag}: body {f}"
     assert np.array_equal(mrg.digest(*c.get_cell_lists()), ref[tag + "_cell_digest"]), f"{tag}: cell lists"
     assert np.array_equal(mrg.digest(*c.get_collision_lists()), ref[tag + "_pair_digest"]), f"{tag}: contact lists"
-    w, cells = c.get_weights(len(parts))
-    assert np.array_equal(mrg.digest(cells, w), ref[tag + "_window_digest"]), f"{tag}: interpolation windows"
+    if windows:
+        w, cells = c.get_weights(len(parts))
+        assert np.array_equal(mrg.digest(cells, w), ref[tag + "_window_digest"]), f"{tag}: interpolation windows"
     if fields:
         assert np.array_equal(mrg.field_digest(c.get_fluid()), ref[tag + "_field_digest"]), f"{tag}: fields"
     if tag + "_probe_force" in ref and len(ref[tag + "_probe_force"]):
