@@ -625,11 +625,19 @@ CONFIG_SEED = 1
 def config_case():
     """The plain resolved configuration the benchmark's CPU-runnable case names:
     128^3 periodic, 64 spheres of d = 16h (about 800 markers each), seeded
-    random sequential addition, 32 Fourier modes of amplitude 0.05, velocities
-    N(0, 0.01).  Regenerated by the tests from the seed (the fixture holds
-    digests of the inputs)."""
-    p, parts, bodies, field = scenario.resolved_case(128, 128, 128, 64, 16.0, seed=CONFIG_SEED, n_modes=32, amp=0.05,
-                                                    vel_std=0.01)
+    random sequential addition, velocities N(0, 0.01).  The fluid is seeded
+    integers times 2^-25 (|u| < 0.032) instead of Fourier modes, so that any
+    host regenerates it bit for bit; the tests regenerate the whole case from
+    the seed (the fixture holds digests of the inputs)."""
+    p, parts, bodies, _ = scenario.resolved_case(128, 128, 128, 64, 16.0, seed=CONFIG_SEED, n_modes=0,
+                                                vel_std=0.01)
+    rng = np.random.default_rng(CONFIG_SEED + 100)
+    shape = field_shape(p)
+    field = []
+    for _ in range(3):
+        a = np.zeros(shape)
+        a[2:-2, 2:-2, 2:-2] = rng.integers(-2 ** 20, 2 ** 20, size=(128, 128, 128)) * 2.0 ** -25
+        field.append(a)
     scenario.fill_halo(p, field)
     return p, parts, bodies, field
 

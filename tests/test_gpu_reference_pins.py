@@ -107,6 +107,42 @@ def test_compact_cases(gpu_lib, name):
         c.close()
 
 
+def test_benchmark_configuration(gpu_lib):
+    """The benchmark's CPU-runnable configuration (128^3 periodic, 64 spheres of
+    d = 16h, 51,456 markers), regenerated from its seed: after
+    InitializationDEM and the first forcing loop the parcels, cell lists,
+    contact lists and fields equal the reference's; after CloudEvolutionMS every
+    body's translation does, and the rotation of each body that does not
+    straddle a periodic face (tests/golden/ref_config.npz)."""
+    from ibmdem import records
+
+    ref = load("config")
+    p, parts, bodies, field = mrg.config_case()
+    same(mrg.parcel_digest(parts, len(parts)), ref["in_parcel_digest"], "regenerated parcels")
+    same(mrg.digest(*[bodies[f] for f in records.MULTISPHERE.names]), ref["in_body_digest"], "regenerated bodies")
+    same(mrg.digest(*field), ref["in_field_digest"], "regenerated field")
+    c = gpu_lib.Case(p, parts, bodies, field, device=0)
+    try:
+        c.InitializationDEM()
+        for tag in ("init", "mdf0"):
+            if tag == "mdf0":
+                c.set_fluid(*field)
+                c.MultiDirectForcing()
+                same(mrg.field_digest(c.get_fluid()), ref["mdf0_field_digest"], "mdf0: fields")
+            got, nl = c.get_parcels()
+            same(mrg.parcel_digest(got, nl), ref[tag + "_parcel_digest"], f"{tag}: parcels")
+            same(mrg.digest(*c.get_cell_lists()), ref[tag + "_cell_digest"], f"{tag}: cell lists")
+            same(mrg.digest(*c.get_collision_lists()), ref[tag + "_pair_digest"], f"{tag}: contact lists")
+        c.CloudEvolutionMS()
+        got, want, far = c.get_bodies(), ref["step0_bodies"], ref["straddlers"]
+        for f in ("x", "v", "vold", "fdrag", "fcol", "fhydro"):
+            same(got[f], want[f], f"body {f}")
+        for f in ("omega", "AngMom", "rotMat", "rotMatGlo", "fmom", "fmomCol", "fmomHydro"):
+            same(got[f][~far], want[f][~far], f"body {f} (bodies inside the box)")
+    finally:
+        c.close()
+
+
 def test_runge_kutta_fluid_step(gpu_lib):
     """The reference's ThirdOrderLowStorageRungeKutta (fluid.F90:329-366) between
     walls in z, each stage's Poisson solve replaced by the fixture's correction:
