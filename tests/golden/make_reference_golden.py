@@ -824,6 +824,32 @@ def run_poisson(ref_dir, name, p, seed):
             "velDiv": div, "rhs": np.array([rhs[i] for i in range(n)])}
 
 
+def run_trajectory(sources, steps):
+    """The periodic case over `steps` coupled steps (each the forcing loop on the
+    frozen fluid, then CloudEvolutionMS with its 2 sub-steps): after every step
+    the bodies in full and digests of the parcels and of the fields the forcing
+    loop left."""
+    t0 = time.time()
+    name, p, parts, bodies, field, probes = periodic_case()
+    R = ReferenceCase(sources, p, parts, bodies, field, probes)
+    u0 = [a.T.copy() for a in R.u0]
+    out = {"params": np.asarray(p), "in_parcels": parts, "in_bodies": bodies, "in_u": u0[0], "in_v": u0[1],
+           "in_w": u0[2], "steps": np.int32(steps), "bodies": [], "parcel_digest": [], "field_digest": [],
+           "npairs": []}
+    for s in range(steps):
+        R.multi_direct_forcing()
+        out["field_digest"].append(field_digest(R.fields()))
+        R.cloud_evolution()
+        out["bodies"].append(R.bodies())
+        out["parcel_digest"].append(parcel_digest(R.parcels(), R.G.m_nplocal))
+        out["npairs"].append(len(R.collision_lists()[1]))
+        if (s + 1) % 10 == 0:
+            print(f"trajectory: step {s + 1}/{steps} after {time.time() - t0:.0f} s", flush=True)
+    for k in ("bodies", "parcel_digest", "field_digest", "npairs"):
+        out[k] = np.array(out[k])
+    return out
+
+
 GENERATION_FIELDS = ("x", "v", "radeff", "rho", "vol", "m", "MSIdx", "globalIdx")
 
 
@@ -891,6 +917,7 @@ def main(ref_dir, only=None):
         "generation": lambda: run_generation(sources, ref_dir, 27),
         "coupled": lambda: run_coupled(sources, 3),
         "output": lambda: run_output(sources),
+        "trajectory": lambda: run_trajectory(sources, 100),
         "poisson_walls_y": lambda: run_poisson(ref_dir, "poisson_walls_y", make_params(6, 5, 4, walls="y", h=0.5),
                                                31),
         "poisson_periodic": lambda: run_poisson(ref_dir, "poisson_periodic", make_params(5, 4, 6), 32),

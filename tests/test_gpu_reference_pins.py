@@ -107,6 +107,31 @@ def test_compact_cases(gpu_lib, name):
         c.close()
 
 
+def test_hundred_step_trajectory(gpu_lib):
+    """One hundred coupled steps of the periodic case (tests/golden/ref_trajectory.npz):
+    after every step the bodies, the parcels and the forcing loop's fields are
+    bit-identical to the reference's."""
+    from ibmdem import records
+
+    ref = load("trajectory")
+    field = (ref["in_u"], ref["in_v"], ref["in_w"])
+    c = gpu_lib.Case(ref["params"], ref["in_parcels"], ref["in_bodies"], field, device=0)
+    try:
+        c.InitializationDEM()
+        for s in range(int(ref["steps"])):
+            c.set_fluid(*field)
+            c.MultiDirectForcing()
+            same(mrg.field_digest(c.get_fluid()), ref["field_digest"][s], f"step {s}: fields")
+            c.CloudEvolutionMS()
+            parts, nl = c.get_parcels()
+            same(mrg.parcel_digest(parts, nl), ref["parcel_digest"][s], f"step {s}: parcels")
+            got = c.get_bodies()
+            for f in records.MULTISPHERE.names:
+                same(got[f], ref["bodies"][s][f], f"step {s}: body {f}")
+    finally:
+        c.close()
+
+
 def test_benchmark_configuration(gpu_lib):
     """The benchmark's CPU-runnable configuration (128^3 periodic, 64 spheres of
     d = 16h, 51,456 markers), regenerated from its seed: after

@@ -334,6 +334,29 @@ def test_pressure_system_matches_the_reference(oracle_mod, name):
     assert np.array_equal(ref["rhs"], want)
 
 
+def test_hundred_step_trajectory_matches_the_reference(oracle_mod):
+    """One hundred coupled steps of the periodic case (three spheres, one
+    contact, images on four faces; two DEM sub-steps a step): after every step
+    the bodies, the parcels and the forcing loop's fields are bit-identical to
+    the reference's."""
+    ref = load("trajectory")
+    field = (ref["in_u"], ref["in_v"], ref["in_w"])
+    c = oracle_mod.OracleCase(ref["params"], ref["in_parcels"], ref["in_bodies"], field)
+    c.InitializationDEM()
+    for s in range(int(ref["steps"])):
+        c.set_fluid(*field)
+        c.MultiDirectForcing()
+        assert np.array_equal(mrg.field_digest(c.get_fluid()), ref["field_digest"][s]), f"step {s}: fields"
+        c.CloudEvolutionMS()
+        parts, nl = c.get_parcels()
+        assert np.array_equal(mrg.parcel_digest(parts, nl), ref["parcel_digest"][s]), f"step {s}: parcels"
+        got = c.get_bodies()
+        for f in records.MULTISPHERE.names:
+            assert np.array_equal(got[f], ref["bodies"][s][f]), f"step {s}: body {f}"
+    assert ref["npairs"].min() > 0
+    c.close()
+
+
 def test_walled_case_exercises_wall_contact():
     ref = load("walled")
     f = ref["step0_probe_force"]
