@@ -749,6 +749,8 @@ def run_coupled(sources, steps):
             a = getattr(G, "m_" + f.lower()).a.T.copy()
             # the reference accumulates fx, fy, fz into halo cells it then ignores
             out[f"step{s}_{f}"] = digest(a[2:-2, 2:-2, 2:-2] if f in ("fx", "fy", "fz") else a)
+            if s == 0 and f in ("u", "v", "w", "P"):
+                out[f"step0_{f}_values"] = a
         print(f"coupled: step {s + 1}/{steps} after {time.time() - t0:.0f} s", flush=True)
     return out
 

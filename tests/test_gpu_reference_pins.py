@@ -132,6 +132,57 @@ def test_hundred_step_trajectory(gpu_lib):
         c.close()
 
 
+def test_whole_time_step(gpu_lib):
+    """The reference's FirstOrderForwardEuler (fluid.F90:252-327) on the library:
+    StoreOldVelocity, the forcing loop, VelocityGuess, ModifyBulkVelocity,
+    VelocityDivergence, PressureCorrection with the fixture's supplied Poisson
+    solve (tests/fft_poisson.py), VelocityCorrection, each with its halo refill,
+    and CloudEvolutionMS (tests/golden/ref_coupled.npz, first step).  The
+    library forms ModifyBulkVelocity's sums in an order of its own, so u, v, w
+    and P agree to 1e-10 of their largest value; the bodies, which the forcing
+    loop before it sets, bit for bit."""
+    import cases
+    import fft_poisson
+    from ibmdem import records
+
+    ref = load("coupled")
+    p = ref["params"]
+    h = (float(p["dx"]), float(p["dy"]), float(p["dz"]))
+    field = tuple(ref[f"in_{a}"].astype(np.float64) for a in "uvw")
+    b = ref["bulk"]
+    c = gpu_lib.Case(p, ref["in_parcels"], ref["in_bodies"], field, device=0)
+    try:
+        c.set_fluid_params(float(ref["visc"]))
+        c.InitializationDEM()
+        c.StoreOldVelocity()
+        c.MultiDirectForcing()
+        c.VelocityGuess(1.0, 0.0, 1.0)
+        c.FillGhostRegionForFluid()
+        c.Boundary()
+        c.ModifyBulkVelocity(int(b[0]), int(b[1]), int(b[2]), b[3], b[4], b[5])
+        c.FillGhostRegionForFluid()
+        c.Boundary()
+        c.VelocityDivergence(1.0)
+        c.FillGhostRegionForFluid()
+        c.Boundary()
+        pc = c.get_fluid_field("Pcorr")
+        pc[2:-2, 2:-2, 2:-2] = fft_poisson.solve(c.get_fluid_field("velDiv")[2:-2, 2:-2, 2:-2], h, str(ref["walls"]))
+        c.PressureCorrection(pc)
+        c.FillGhostRegionForFluid()
+        c.Boundary()
+        c.VelocityCorrection(1.0)
+        c.FillGhostRegionForFluid()
+        c.Boundary()
+        c.CloudEvolutionMS()
+        for f in ("u", "v", "w", "P"):
+            assert cases.rel_close(c.get_fluid_field(f), ref[f"step0_{f}_values"], 1e-10), f
+        got = c.get_bodies()
+        for f in records.MULTISPHERE.names:
+            same(got[f], ref["step0_bodies"][f], f"body {f}")
+    finally:
+        c.close()
+
+
 def test_benchmark_configuration(gpu_lib):
     """The benchmark's CPU-runnable configuration (128^3 periodic, 64 spheres of
     d = 16h, 51,456 markers), regenerated from its seed: after
