@@ -357,6 +357,30 @@ def test_hundred_step_trajectory_matches_the_reference(oracle_mod):
     c.close()
 
 
+def test_pins_catch_planted_mistakes(oracle_mod):
+    """The comparisons are not vacuous: a restatement with ModifyBulkVelocity
+    left out fails the whole-time-step pin, and one parcel moved by one ulp
+    fails the periodic case at its first stage."""
+    import types
+
+    class NoBulk(oracle_mod.OracleFluid):
+        def ModifyBulkVelocity(self, *args):
+            pass
+
+    with pytest.raises(AssertionError):
+        test_whole_time_step_matches_the_reference(types.SimpleNamespace(OracleCase=oracle_mod.OracleCase,
+                                                                         OracleFluid=NoBulk))
+
+    class Nudged(oracle_mod.OracleCase):
+        def __init__(self, params, parcels=None, bodies=None, field=None):
+            parcels = np.array(parcels, copy=True)
+            parcels["x"][5, 0] = np.nextafter(parcels["x"][5, 0], np.inf)
+            super().__init__(params, parcels, bodies, field)
+
+    with pytest.raises(AssertionError, match="init"):
+        test_coupled_steps_match_the_reference(types.SimpleNamespace(OracleCase=Nudged), "periodic")
+
+
 def test_walled_case_exercises_wall_contact():
     ref = load("walled")
     f = ref["step0_probe_force"]
