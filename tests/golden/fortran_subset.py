@@ -31,8 +31,11 @@ reassociation):
     check_bounds, which checks every subscript and section against its
     dimension's extent (numpy would otherwise take a negative index from the
     end without complaint);
-  * MPI is one rank: MPI_SENDRECV to and from rank 0 copies the message into
-    the receive buffer, MPI_REDUCE copies, barriers and broadcasts do nothing.
+  * MPI is one rank (MPI_SENDRECV to and from rank 0 copies the message into
+    the receive buffer, MPI_REDUCE copies, barriers and broadcasts do nothing),
+    or several ranks run as threads that share a World: messages go through
+    mailboxes, reductions add in rank order at the root, every wait is
+    bounded.
 List-directed reads (read(unit,*)) take the next record of the file the unit
 was opened on; list-directed writes to a file unit keep each record's values,
 unformatted, under the file's name (nothing reaches the disk); writes to the
@@ -244,43 +247,103 @@ def _io_internal(fmt, items):
 
 
 # ----------------------------------------------------------------------------
-# one MPI rank
+# MPI: one rank (a state without a world), or several ranks run as threads of
+# one process (states that share a World)
+
+
+class World:
+    """The communicator of ranks run as threads: mailboxes for point-to-point
+    messages and slots for the collectives.  Every wait has a time limit."""
+
+    def __init__(self, n, timeout=120.0):
+        import threading
+        self.n, self.timeout = n, timeout
+        self.cv = threading.Condition()
+        self.box = {}
+        self.barrier = threading.Barrier(n, timeout=timeout)
+        self.slots = [None] * n
+
+    def post(self, src, dest, tag, data):
+        with self.cv:
+            self.box.setdefault((src, dest, tag), []).append(data)
+            self.cv.notify_all()
+
+    def take(self, src, dest, tag):
+        with self.cv:
+            if not self.cv.wait_for(lambda: self.box.get((src, dest, tag)), timeout=self.timeout):
+                raise TimeoutError(f"rank {dest} waited for a message {tag} from rank {src}")
+            return self.box[(src, dest, tag)].pop(0)
+
+
+def _payload(buf, count):
+    if isinstance(buf, (np.ndarray, FArr)):
+        return _flat(buf)[:count].copy()
+    return np.array([buf])[:count]
+
+
+def _deliver(buf, data):
+    if isinstance(buf, (np.ndarray, FArr)):
+        _flat(buf)[:len(data)] = data
+        return buf
+    if len(data):
+        return type(buf)(data[0]) if not isinstance(buf, np.generic) else data[0]
+    return buf
 
 
 def _mpi_sendrecv(G, sbuf, scount, stype, dest, stag, rbuf, rcount, rtype, src, rtag, comm, status, ierr):
-    if dest != 0 or src != 0:
-        raise RuntimeError(f"MPI_SENDRECV to {dest} from {src} on one rank")
-    if scount > rcount:
-        raise RuntimeError(f"MPI_SENDRECV message of {scount} truncated to {rcount}")
-    if isinstance(sbuf, (np.ndarray, FArr)):
-        data = _flat(sbuf)[:scount].copy()
+    W = getattr(G, "world", None)
+    data = _payload(sbuf, scount)
+    if W is None:
+        if dest != 0 or src != 0:
+            raise RuntimeError(f"MPI_SENDRECV to {dest} from {src} on one rank")
+        got = data
     else:
-        data = np.array([sbuf])[:scount]
-    if isinstance(rbuf, (np.ndarray, FArr)):
-        _flat(rbuf)[:scount] = data
-    elif scount >= 1:
-        rbuf = type(rbuf)(data[0]) if not isinstance(rbuf, np.generic) else data[0]
+        W.post(G.rank, dest, stag, data)
+        got = W.take(src, G.rank, rtag)
+    if len(got) > rcount:
+        raise RuntimeError(f"MPI_SENDRECV message of {len(got)} truncated to {rcount}")
+    rbuf = _deliver(rbuf, got)
     return (sbuf, scount, stype, dest, stag, rbuf, rcount, rtype, src, rtag, comm, status, 0)
 
 
 def _mpi_reduce(G, sbuf, rbuf, count, dtype, op, root, comm, ierr):
-    if isinstance(rbuf, (np.ndarray, FArr)):
-        _flat(rbuf)[:count] = _flat(sbuf)[:count]
-    else:
-        rbuf = sbuf
+    """Sum or maximum over the ranks in rank order, at the root."""
+    W = getattr(G, "world", None)
+    if W is None:
+        return (sbuf, _deliver(rbuf, _payload(sbuf, count)), count, dtype, op, root, comm, 0)
+    W.slots[G.rank] = _payload(sbuf, count)
+    W.barrier.wait()
+    if G.rank == root:
+        acc = W.slots[0].copy()
+        for r in range(1, W.n):
+            acc = acc + W.slots[r] if op == MPI_CONSTANTS["mpi_sum"] else np.maximum(acc, W.slots[r])
+        rbuf = _deliver(rbuf, acc)
+    W.barrier.wait()
     return (sbuf, rbuf, count, dtype, op, root, comm, 0)
 
 
 def _mpi_bcast(G, buf, count, dtype, root, comm, ierr):
+    W = getattr(G, "world", None)
+    if W is None:
+        return (buf, count, dtype, root, comm, 0)
+    if G.rank == root:
+        W.slots[root] = _payload(buf, count)
+    W.barrier.wait()
+    if G.rank != root:
+        buf = _deliver(buf, W.slots[root])
+    W.barrier.wait()
     return (buf, count, dtype, root, comm, 0)
 
 
 def _mpi_barrier(G, comm, ierr):
+    W = getattr(G, "world", None)
+    if W is not None:
+        W.barrier.wait()
     return (comm, 0)
 
 
 def _mpi_comm_rank(G, comm, rank, ierr):
-    return (comm, 0, 0)
+    return (comm, getattr(G, "rank", 0), 0)
 
 
 BUILTIN_CALLS = {

@@ -852,6 +852,162 @@ def run_trajectory(sources, steps):
     return out
 
 
+def multirank_case():
+    """Three spheres (d = 6h) on 24x16x16, periodic in x, walls in y and z, for
+    two ranks along x: body 1 straddles the ranks' seam at x = 12, body 2
+    touches it from the other rank, body 3 lies in the image band of the
+    periodic x face."""
+    p = make_params(24, 16, 16, walls="yz", knCoeff=1e4, ResistCoeff=0.9, coupleInterval=2)
+    field = _f32(scenario.fourier_field(p, 4, 0.02, seed=41))
+    scenario.fill_halo(p, field)
+    X = np.array([[11.2, 7.9, 8.1], [11.2 + 6.0 + 0.3, 8.2, 7.8], [3.6, 8.0, 8.3]])
+    V = np.array([[0.02, -0.01, 0.0], [-0.02, 0.01, 0.005], [0.0, 0.01, -0.01]])
+    parts, bodies = scenario.sphere_bodies(X, 6.0, 1.0, 1.14e3, V)
+    return p, parts, bodies, field
+
+
+def run_multirank(sources, steps, cpus=(2, 1, 1)):
+    """The reference as it runs in production, on several MPI ranks (threads of
+    this process sharing a fortran_subset.World), its multi-rank code unchanged:
+    the bodies and parcels split by rank, their ghosts exchanged with the
+    periodic shift, AssembleForceMS, UpdateMSInfoInGhostRegion and RebuildListMS
+    as written.  The harness supplies SetBoundaryType with the case's global
+    types and each rank's share of the case (InitCylinderParcelsDEM's role: the
+    bodies centred in the rank's box, then RebuildListMS, then the markers of
+    the bodies it holds inside its box).  Stored after every coupled step: the
+    fields assembled from the ranks' slabs, the bodies and the parcels."""
+    import threading
+
+    p, parts, bodies, field = multirank_case()
+    nr = cpus[0] * cpus[1] * cpus[2]
+    bt_glo = [int(b) for b in p["bType"]]
+
+    def set_boundary_type(G):
+        G.m_bwg, G.m_beg, G.m_bbg, G.m_bfg, G.m_bsg, G.m_bng = bt_glo
+        b = [-1] * 6
+        for ax, (idx, ncpu) in enumerate(((G.m_cpuidxx, G.m_cpunx), (G.m_cpuidxy, G.m_cpuny),
+                                          (G.m_cpuidxz, G.m_cpunz))):
+            if idx == 0:
+                b[2 * ax] = bt_glo[2 * ax]
+            if idx == ncpu - 1:
+                b[2 * ax + 1] = bt_glo[2 * ax + 1]
+        G.m_bw, G.m_be, G.m_bb, G.m_bf, G.m_bs, G.m_bn = b
+        G.m_btype.a[:] = b
+        return ()
+
+    T = fs.Translator(sources, CAPACITIES, CHECK_BOUNDS)
+    T.build(overrides={"setboundarytype": set_boundary_type})
+    world = fs.World(nr)
+    n = [int(p["nx"]), int(p["ny"]), int(p["nz"])]
+    results, errors = [None] * nr, []
+
+    def rank(r):
+        G = T.new_state()
+        G.world, G.rank = world, r
+        c = lambda name, *a: T.call(G, name, *a)  # noqa: E731
+        try:
+            c("PartitionInitialization", *cpus, *n, *[float(k) for k in n])
+            c("GridInitialization")
+            G.m_dt, G.m_rhof = float(p["dt"]), float(p["rhof"])
+            c("SetCellIndexMap")
+            c("BuildMPIRecvAndSendIndexForFluid")
+            c("InitParameters")
+            G.m_kncoeff, G.m_resistcoeff = float(p["knCoeff"]), float(p["ResistCoeff"])
+            G.m_coupleinterval = int(p["coupleInterval"])
+            G.m_dtdem = G.m_dt / G.m_coupleinterval
+            for name in ("CopyGridInformationDEM", "AllocateDEM", "SetCellType", "SetCellIndexMapDEM",
+                         "SetNeighCellIndexForCellsDEM", "SetBoundaryNormsAndPoints", "SetMirrorAndShiftCoords"):
+                c(name)
+            G.m_collisiondist = float(p["collisionDist"])
+            lo = np.array([G.m_xstart, G.m_ystart, G.m_zstart])
+            hi = np.array([G.m_xend, G.m_yend, G.m_zend])
+            G.m_nmsglo = len(bodies)
+            inside = [j for j in range(len(bodies)) if np.all(bodies["x"][j] > lo) and np.all(bodies["x"][j] < hi)]
+            for k, j in enumerate(inside):
+                for f in MULTISPHERE.names:
+                    G.m_ms.a[f.lower()][k] = bodies[f][j]
+                    G.m_msglo.a[f.lower()][j] = bodies[f][j]
+            G.m_nms = G.m_nmslocal = len(inside)
+            c("RebuildListMS")
+            held = {int(G.m_ms.a["globalidx"][i]) for i in range(G.m_nms)}
+            mine = parts[[q for q in range(len(parts)) if int(parts["MSIdx"][q]) in held and
+                          np.all(parts["x"][q] > lo) and np.all(parts["x"][q] < hi)]]
+            for f in PARCEL.names:
+                if f != "pad_":
+                    G.m_part.a[f.lower()][:len(mine)] = mine[f]
+            G.m_np = G.m_nplocal = len(mine)
+            G.m_nmslocal = G.m_nms
+            G.m_nppartincell.a[:] = 0
+            c("PutParcelsIntoCellsDEM", 1, G.m_np, 0)
+            sl = (slice(G.m_sg1 - 1, G.m_eg1), slice(G.m_sg2 - 1, G.m_eg2), slice(G.m_sg3 - 1, G.m_eg3))
+            for arr, f in zip((G.m_u, G.m_v, G.m_w), field):
+                arr.a[2:-2, 2:-2, 2:-2] = np.asarray(f)[2:-2, 2:-2, 2:-2].T[sl]
+            c("FillGhostRegionForFluid")
+            c("Boundary")
+            u0 = [G.m_u.a.copy(), G.m_v.a.copy(), G.m_w.a.copy()]
+            # the rest of InitializationDEM (ZJS_INIT_DEM.F90:24-35)
+            for name in ("RebuildListMS", "RebuildParcelInCellListDEM", "RebuildParcelCollisionListDEM",
+                         "RebuildNeighborCellListForParcelsDEM", "UpdateLocalCellWeightListDEM",
+                         "UpdateParcelInfoInGhostRegion", "UpdateGhostCellWeightListDEM"):
+                c(name)
+            out = []
+            for _ in range(steps):
+                for a, a0 in zip((G.m_u, G.m_v, G.m_w), u0):
+                    a.a[...] = a0
+                G.m_part.a["fdrag"][:G.m_nplocal] = 0.0
+                for a in (G.m_fx, G.m_fy, G.m_fz):
+                    a.a[...] = 0.0
+                for _ in range(int(p["Ns"])):
+                    for name in ("UpdateFluidVelocityOnLagrangianPoints", "UpdateParcelInfoInGhostRegion",
+                                 "UpdateMomentumSourceTerm", "VelocityPostGuess", "FillGhostRegionForFluid",
+                                 "Boundary"):
+                        c(name)
+                slab = [a.a[2:-2, 2:-2, 2:-2].copy() for a in (G.m_u, G.m_fx)]
+                c("CloudEvolutionMS")
+                loc = np.zeros(G.m_nplocal, PARCEL)
+                for f in PARCEL.names:
+                    if f != "pad_":
+                        loc[f] = G.m_part.a[f.lower()][:G.m_nplocal]
+                bl = np.zeros(G.m_nmslocal, MULTISPHERE)
+                for f in MULTISPHERE.names:
+                    bl[f] = G.m_ms.a[f.lower()][:G.m_nmslocal]
+                out.append((slab, sl, loc, bl))
+            results[r] = out
+        except BaseException:
+            import traceback
+            errors.append(traceback.format_exc())
+            world.barrier.abort()
+
+    threads = [threading.Thread(target=rank, args=(r,)) for r in range(nr)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    if errors:
+        raise RuntimeError(errors[0])
+    out = {"params": np.asarray(p), "in_parcels": parts, "in_bodies": bodies, "steps": np.int32(steps),
+           "cpus": np.array(cpus, np.int32)}
+    for a, f in zip("uvw", field):
+        out["in_" + a] = np.asarray(f, dtype=np.float32)
+    key = lambda a: a["MSIdx"].astype(np.int64) * 1000000 + a["globalIdx"]  # noqa: E731
+    for s in range(steps):
+        for k, name in enumerate(("u", "fx")):
+            glob = np.zeros(n)
+            for r in range(nr):
+                slab, sl, _, _ = results[r][s]
+                glob[sl] = slab[k]
+            out[f"step{s}_{name}"] = np.ascontiguousarray(glob.T)
+        b = np.concatenate([results[r][s][3] for r in range(nr)])
+        out[f"step{s}_bodies"] = b[np.argsort(b["globalIdx"])]
+        q = np.concatenate([results[r][s][2] for r in range(nr)])
+        q = q[np.argsort(key(q))]
+        for f in ("MSIdx", "globalIdx", "x", "v", "fdrag", "fcol"):
+            out[f"step{s}_parcel_{f}"] = q[f]
+        out[f"step{s}_ranks"] = np.array([len(results[r][s][2]) for r in range(nr)], np.int32)
+    print(f"multirank: {nr} ranks, parcels per rank {out['step0_ranks'].tolist()}", flush=True)
+    return out
+
+
 GENERATION_FIELDS = ("x", "v", "radeff", "rho", "vol", "m", "MSIdx", "globalIdx")
 
 
@@ -920,6 +1076,7 @@ def main(ref_dir, only=None):
         "coupled": lambda: run_coupled(sources, 3),
         "output": lambda: run_output(sources),
         "trajectory": lambda: run_trajectory(sources, 100),
+        "multirank": lambda: run_multirank(sources, 2),
         "poisson_walls_y": lambda: run_poisson(ref_dir, "poisson_walls_y", make_params(6, 5, 4, walls="y", h=0.5),
                                                31),
         "poisson_periodic": lambda: run_poisson(ref_dir, "poisson_periodic", make_params(5, 4, 6), 32),

@@ -117,6 +117,16 @@ implicit none
     a(:) = 1d0
     x = a(k)
 endsubroutine
+subroutine ring(me,got,total)
+implicit none
+    integer::me,got,total,mine,st(MPI_STATUS_SIZE),ierr,nr
+    nr = 3
+    mine = 10*(me+1)
+    call MPI_SENDRECV(mine,1,MPI_INTEGER,mod(me+1,nr),7,got,1,MPI_INTEGER,mod(me+nr-1,nr),7,MPI_COMM_WORLD,st,ierr)
+    call MPI_REDUCE(mine,total,1,MPI_INTEGER,MPI_SUM,0,MPI_COMM_WORLD,ierr)
+    call MPI_BCAST(total,1,MPI_INTEGER,0,MPI_COMM_WORLD,ierr)
+    call MPI_BARRIER(MPI_COMM_WORLD,ierr)
+endsubroutine
 subroutine sendself(out)
 implicit none
     integer::out(1:2),buf(1:2),st(MPI_STATUS_SIZE),ierr
@@ -223,3 +233,27 @@ def test_bounds_checks():
         with pytest.raises(IndexError):
             T.call(G, "oob", k, 0.0)
     T.call(G, "sections", -1, 2)  # sections inside their bounds pass
+
+
+def test_ranks_as_threads():
+    """Three ranks sharing a World: a ring exchange, a sum at the root and its
+    broadcast."""
+    import threading
+
+    T = fs.Translator([("t.F90", SRC)])
+    T.build()
+    world = fs.World(3, timeout=30.0)
+    out = [None] * 3
+
+    def rank(r):
+        G = T.new_state()
+        G.world, G.rank = world, r
+        out[r] = T.call(G, "ring", r, 0, 0)
+
+    threads = [threading.Thread(target=rank, args=(r,)) for r in range(3)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert [o[1] for o in out] == [30, 10, 20]
+    assert [o[2] for o in out] == [60, 60, 60]

@@ -381,6 +381,45 @@ def test_pins_catch_planted_mistakes(oracle_mod):
         test_coupled_steps_match_the_reference(types.SimpleNamespace(OracleCase=Nudged), "periodic")
 
 
+def test_one_rank_restatement_matches_the_reference_on_two_ranks(oracle_mod):
+    """The restatement keeps the reference's multi-rank body semantics on one
+    rank.  Against the reference's own multi-rank code on two ranks (threads
+    sharing a translated MPI; tests/golden/ref_multirank.npz: a body straddling
+    the ranks' seam, one touching it from the other rank, bodies and parcels
+    exchanged as ghosts with the periodic shift), two coupled steps agree to
+    1e-13 of each quantity's largest value: the ranks sum a node's forcing and
+    a body's forces in their own order (measured: 3e-15 at most), while
+    positions, rotations and contact forces come out bit-identical."""
+    import cases
+
+    ref = load("multirank")
+    field = [ref[f"in_{a}"].astype(np.float64) for a in "uvw"]
+    c = oracle_mod.OracleCase(ref["params"], ref["in_parcels"], ref["in_bodies"], field)
+    c.InitializationDEM()
+    key = lambda a: a["MSIdx"].astype(np.int64) * 1000000 + a["globalIdx"]  # noqa: E731
+    for s in range(int(ref["steps"])):
+        c.set_fluid(*field)
+        c.MultiDirectForcing()
+        got = c.get_fluid()
+        assert cases.rel_close(got[0][2:-2, 2:-2, 2:-2], ref[f"step{s}_u"], 1e-13), f"step {s}: u"
+        assert cases.rel_close(got[3][2:-2, 2:-2, 2:-2], ref[f"step{s}_fx"], 1e-13), f"step {s}: fx"
+        c.CloudEvolutionMS()
+        bodies, want = c.get_bodies(), ref[f"step{s}_bodies"]
+        assert np.array_equal(bodies["globalIdx"], want["globalIdx"])
+        for f in ("x", "v", "omega", "AngMom", "rotMatGlo", "fdrag", "fcol", "fmom", "fmomCol"):
+            assert cases.rel_close(bodies[f], want[f], 1e-13), f"step {s}: body {f}"
+        for f in ("x", "omega", "AngMom", "fcol", "fmomCol"):
+            assert np.array_equal(bodies[f], want[f]), f"step {s}: body {f} bit for bit"
+        parts, nl = c.get_parcels()
+        parts = parts[:nl][np.argsort(key(parts[:nl]))]
+        assert np.array_equal(parts["MSIdx"], ref[f"step{s}_parcel_MSIdx"])
+        assert np.array_equal(parts["globalIdx"], ref[f"step{s}_parcel_globalIdx"])
+        for f in ("x", "v", "fdrag", "fcol"):
+            assert cases.rel_close(parts[f], ref[f"step{s}_parcel_{f}"], 1e-13), f"step {s}: parcel {f}"
+    assert (ref["step0_ranks"] > 0).all() and len(ref["step0_ranks"]) == 2
+    c.close()
+
+
 def test_walled_case_exercises_wall_contact():
     ref = load("walled")
     f = ref["step0_probe_force"]
