@@ -866,7 +866,21 @@ def multirank_case():
     return p, parts, bodies, field
 
 
-def run_multirank(sources, steps, cpus=(2, 1, 1)):
+def multirank_straddle_case():
+    """multirank_case with body 1 straddling the periodic x face (centre 0.8
+    cells from it, its far markers local to the other rank), body 2 touching
+    it, body 3 in the middle of the second rank's box."""
+    p = make_params(24, 16, 16, walls="yz", knCoeff=1e4, ResistCoeff=0.9, coupleInterval=2)
+    field = _f32(scenario.fourier_field(p, 4, 0.02, seed=43))
+    scenario.fill_halo(p, field)
+    X = np.array([[0.8, 7.9, 8.1], [0.8 + 6.0 + 0.3, 8.2, 7.8], [15.5, 8.0, 8.3]])
+    V = np.array([[0.02, -0.01, 0.0], [-0.02, 0.01, 0.005], [0.0, 0.01, -0.01]])
+    parts, bodies = scenario.sphere_bodies(X, 6.0, 1.0, 1.14e3, V)
+    parts["x"] = scenario.wrap_coord(parts["x"], np.array([24.0, 16.0, 16.0]))
+    return p, parts, bodies, field
+
+
+def run_multirank(sources, steps, cpus=(2, 1, 1), make_case=None):
     """The reference as it runs in production, on several MPI ranks (threads of
     this process sharing a fortran_subset.World), its multi-rank code unchanged:
     the bodies and parcels split by rank, their ghosts exchanged with the
@@ -878,7 +892,7 @@ def run_multirank(sources, steps, cpus=(2, 1, 1)):
     fields assembled from the ranks' slabs, the bodies and the parcels."""
     import threading
 
-    p, parts, bodies, field = multirank_case()
+    p, parts, bodies, field = (make_case or multirank_case)()
     nr = cpus[0] * cpus[1] * cpus[2]
     bt_glo = [int(b) for b in p["bType"]]
 
@@ -1077,6 +1091,7 @@ def main(ref_dir, only=None):
         "output": lambda: run_output(sources),
         "trajectory": lambda: run_trajectory(sources, 100),
         "multirank": lambda: run_multirank(sources, 2),
+        "multirank_straddle": lambda: run_multirank(sources, 2, make_case=multirank_straddle_case),
         "poisson_walls_y": lambda: run_poisson(ref_dir, "poisson_walls_y", make_params(6, 5, 4, walls="y", h=0.5),
                                                31),
         "poisson_periodic": lambda: run_poisson(ref_dir, "poisson_periodic", make_params(5, 4, 6), 32),

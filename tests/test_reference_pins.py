@@ -381,7 +381,8 @@ def test_pins_catch_planted_mistakes(oracle_mod):
         test_coupled_steps_match_the_reference(types.SimpleNamespace(OracleCase=Nudged), "periodic")
 
 
-def test_one_rank_restatement_matches_the_reference_on_two_ranks(oracle_mod):
+@pytest.mark.parametrize("name", ["multirank", "multirank_straddle"])
+def test_one_rank_restatement_matches_the_reference_on_two_ranks(oracle_mod, name):
     """The restatement keeps the reference's multi-rank body semantics on one
     rank.  Against the reference's own multi-rank code on two ranks (threads
     sharing a translated MPI; tests/golden/ref_multirank.npz: a body straddling
@@ -389,10 +390,14 @@ def test_one_rank_restatement_matches_the_reference_on_two_ranks(oracle_mod):
     exchanged as ghosts with the periodic shift), two coupled steps agree to
     1e-13 of each quantity's largest value: the ranks sum a node's forcing and
     a body's forces in their own order (measured: 3e-15 at most), while
-    positions, rotations and contact forces come out bit-identical."""
+    positions, rotations and contact forces come out bit-identical.
+    ref_multirank_straddle.npz has a body straddling the periodic x face: there
+    the one-rank reference takes a torque arm a box length long, while on two
+    ranks the body reaches its far markers' rank as a ghost shifted by the box
+    length, which is the nearest-image arm the restatement uses."""
     import cases
 
-    ref = load("multirank")
+    ref = load(name)
     field = [ref[f"in_{a}"].astype(np.float64) for a in "uvw"]
     c = oracle_mod.OracleCase(ref["params"], ref["in_parcels"], ref["in_bodies"], field)
     c.InitializationDEM()
