@@ -880,6 +880,20 @@ def multirank_straddle_case():
     return p, parts, bodies, field
 
 
+def multirank_corner_case():
+    """Three spheres (d = 6h) on 24x16x24, periodic in x and z, walls in y, for
+    2x1x2 ranks (the reference's own run splits x and z, 4x1x4): body 1 on the
+    corner where the four ranks meet, body 2 touching it across the z seam,
+    body 3 in the image band of the periodic x and z faces."""
+    p = make_params(24, 16, 24, walls="y", knCoeff=1e4, ResistCoeff=0.9, coupleInterval=2)
+    field = _f32(scenario.fourier_field(p, 4, 0.02, seed=47))
+    scenario.fill_halo(p, field)
+    X = np.array([[12.3, 7.9, 11.6], [12.1, 8.2, 11.6 + 6.0 + 0.3], [3.4, 8.0, 3.6]])
+    V = np.array([[0.02, -0.01, 0.0], [-0.02, 0.01, 0.005], [0.0, 0.01, -0.01]])
+    parts, bodies = scenario.sphere_bodies(X, 6.0, 1.0, 1.14e3, V)
+    return p, parts, bodies, field
+
+
 def run_multirank(sources, steps, cpus=(2, 1, 1), make_case=None):
     """The reference as it runs in production, on several MPI ranks (threads of
     this process sharing a fortran_subset.World), its multi-rank code unchanged:
@@ -1092,6 +1106,7 @@ def main(ref_dir, only=None):
         "trajectory": lambda: run_trajectory(sources, 100),
         "multirank": lambda: run_multirank(sources, 2),
         "multirank_straddle": lambda: run_multirank(sources, 2, make_case=multirank_straddle_case),
+        "multirank_corner": lambda: run_multirank(sources, 2, cpus=(2, 1, 2), make_case=multirank_corner_case),
         "poisson_walls_y": lambda: run_poisson(ref_dir, "poisson_walls_y", make_params(6, 5, 4, walls="y", h=0.5),
                                                31),
         "poisson_periodic": lambda: run_poisson(ref_dir, "poisson_periodic", make_params(5, 4, 6), 32),

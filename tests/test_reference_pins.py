@@ -381,7 +381,7 @@ def test_pins_catch_planted_mistakes(oracle_mod):
         test_coupled_steps_match_the_reference(types.SimpleNamespace(OracleCase=Nudged), "periodic")
 
 
-@pytest.mark.parametrize("name", ["multirank", "multirank_straddle"])
+@pytest.mark.parametrize("name", ["multirank", "multirank_straddle", "multirank_corner"])
 def test_one_rank_restatement_matches_the_reference_on_two_ranks(oracle_mod, name):
     """The restatement keeps the reference's multi-rank body semantics on one
     rank.  Against the reference's own multi-rank code on two ranks (threads
@@ -389,8 +389,11 @@ def test_one_rank_restatement_matches_the_reference_on_two_ranks(oracle_mod, nam
     the ranks' seam, one touching it from the other rank, bodies and parcels
     exchanged as ghosts with the periodic shift), two coupled steps agree to
     1e-13 of each quantity's largest value: the ranks sum a node's forcing and
-    a body's forces in their own order (measured: 3e-15 at most), while
-    positions, rotations and contact forces come out bit-identical.
+    a body's forces in their own order (measured: 4e-15 at most), while the
+    body positions come out bit-identical (on two ranks the rotations and
+    contact forces too).  ref_multirank_corner.npz splits x and z over 2x1x2
+    ranks, as the reference's own run splits them 4x1x4, with a body on the
+    corner where the four ranks meet.
     ref_multirank_straddle.npz has a body straddling the periodic x face: there
     the one-rank reference takes a torque arm a box length long, while on two
     ranks the body reaches its far markers' rank as a ghost shifted by the box
@@ -413,7 +416,8 @@ def test_one_rank_restatement_matches_the_reference_on_two_ranks(oracle_mod, nam
         assert np.array_equal(bodies["globalIdx"], want["globalIdx"])
         for f in ("x", "v", "omega", "AngMom", "rotMatGlo", "fdrag", "fcol", "fmom", "fmomCol"):
             assert cases.rel_close(bodies[f], want[f], 1e-13), f"step {s}: body {f}"
-        for f in ("x", "omega", "AngMom", "fcol", "fmomCol"):
+        exact = ("x", "omega", "AngMom", "fcol", "fmomCol") if int(np.prod(ref["cpus"])) == 2 else ("x",)
+        for f in exact:
             assert np.array_equal(bodies[f], want[f]), f"step {s}: body {f} bit for bit"
         parts, nl = c.get_parcels()
         parts = parts[:nl][np.argsort(key(parts[:nl]))]
@@ -421,7 +425,7 @@ def test_one_rank_restatement_matches_the_reference_on_two_ranks(oracle_mod, nam
         assert np.array_equal(parts["globalIdx"], ref[f"step{s}_parcel_globalIdx"])
         for f in ("x", "v", "fdrag", "fcol"):
             assert cases.rel_close(parts[f], ref[f"step{s}_parcel_{f}"], 1e-13), f"step {s}: parcel {f}"
-    assert (ref["step0_ranks"] > 0).all() and len(ref["step0_ranks"]) == 2
+    assert (ref["step0_ranks"] > 0).all() and len(ref["step0_ranks"]) == int(np.prod(ref["cpus"]))
     c.close()
 
 
