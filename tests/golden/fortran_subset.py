@@ -957,7 +957,6 @@ class Translator:
             if s.param is not None:
                 self.pvals[name] = self.param_overrides.get(name, self._const(s.param, s.kind))
         self.dtypes = {tn: self._record_dtype(tn) for tn in self.types}
-        self.code = {}
         self.ns = None
 
     # constants -------------------------------------------------------------
@@ -980,10 +979,14 @@ class Translator:
         if t == "neg":
             return -self._cval(e[1])
         if t == "bin":
-            a, b = self._cval(e[2]), self._cval(e[3])
-            if e[1] == "/" and isinstance(a, int) and isinstance(b, int):
-                return _idiv(a, b)
-            return {"+": a + b, "-": a - b, "*": a * b, "/": a / b if e[1] == "/" else 0}[e[1]]
+            a, b, op = self._cval(e[2]), self._cval(e[3]), e[1]
+            if op == "+":
+                return a + b
+            if op == "-":
+                return a - b
+            if op == "*":
+                return a * b
+            return _idiv(a, b) if isinstance(a, int) and isinstance(b, int) else a / b
         if t == "des" and len(e[1]) == 1 and e[1][0][1] is None:
             name = e[1][0][0]
             if name in self.pvals and self.pvals[name] is not None:
